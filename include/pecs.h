@@ -1,0 +1,184 @@
+/*
+ * pecs.h -- C ABI of the GB300-native PECS drift-diffusion--Poisson time step.
+ *
+ * The reference (mdh266/PECS) is a single deal.II translation unit whose hot
+ * path is driven by SolarCellProblem::run_full_system (source/SolarCell.cpp:
+ * 1898-2095).  This header is the boundary that replaces, for that path:
+ *
+ *   - the class surface Poisson::PoissonData (include/Poisson.hpp:26-84),
+ *     ChargeCarrierSpace::Carrier (include/Carrier.hpp:38-101) and
+ *     ChargeCarrierSpace::CarrierPair (include/CarrierPair.hpp:30-110):
+ *     pecs_lu_factor / pecs_lu_solve are set_solver() / solve();
+ *   - the per-step stages of the IMEX loop (source/SolarCell.cpp:2055-2080):
+ *     pecs_assemble_carrier_rhs, pecs_solve_carriers, pecs_assemble_poisson_rhs,
+ *     pecs_solve_poisson, and pecs_step for the whole step;
+ *   - the setup that deal.II performs once (meshes, DoF maps, the LDG and
+ *     mixed matrices, UMFPACK factorisation): pecs_create.
+ *
+ * Conventions: every call returns 0 on success and a negative PECS_E* code on
+ * failure; pecs_last_error() returns the message of the last failure on the
+ * calling thread.  No call aborts the process.  Host buffers are owned by the
+ * caller and copied; device memory is owned by the library.  Contexts are
+ * independent; calls on one context must not overlap from several threads.
+ */
+#ifndef PECS_H
+#define PECS_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* error codes */
+#define PECS_OK 0
+#define PECS_E_ARG (-1)       /* invalid argument */
+#define PECS_E_CUDA (-2)      /* CUDA runtime error */
+#define PECS_E_SINGULAR (-3)  /* pivot below threshold during factorisation */
+#define PECS_E_NONFINITE (-4) /* NaN/Inf detected in a state vector */
+#define PECS_E_STATE (-5)     /* call out of sequence */
+#define PECS_E_NODEVICE (-6)  /* no CUDA device available */
+
+/* boundary ids, include/SolarCell.hpp:314-324 of the reference */
+#define PECS_INTERFACE 0
+#define PECS_DIRICHLET 1
+#define PECS_NEUMANN 2
+#define PECS_SCHOTTKY 3
+
+/* fields of an instance's state */
+#define PECS_FIELD_N 0       /* electrons  (semiconductor carrier_1) */
+#define PECS_FIELD_P 1       /* holes      (semiconductor carrier_2) */
+#define PECS_FIELD_R 2       /* reductants (electrolyte carrier_1)   */
+#define PECS_FIELD_O 3       /* oxidants   (electrolyte carrier_2)   */
+#define PECS_FIELD_POISSON 4 /* [D (RT) | Phi (DGQ_{k-1})]           */
+
+/* matrices exported by pecs_get_matrix */
+#define PECS_MAT_N 0
+#define PECS_MAT_P 1
+#define PECS_MAT_R 2
+#define PECS_MAT_O 3
+#define PECS_MAT_POISSON 4
+#define PECS_MAT_MASS_SEMI 5
+#define PECS_MAT_MASS_ELEC 6
+
+/* solver precision */
+#define PECS_PREC_FP64 0    /* FP64 factors, FP64 arithmetic */
+#define PECS_PREC_FP32_IR 1 /* FP32 factors + FP64-residual iterative refinement */
+
+/*
+ * Already-scaled parameters of one instance (the role of
+ * ParameterSpace::Parameters, include/Parameters.hpp:27-289).  Profiles:
+ * value[0] applies where x < junction_x, value[1] elsewhere.
+ */
+typedef struct pecs_params {
+  int degree;      /* LDG degree k (1 or 2); Poisson uses RT_{k-1} x DGQ_{k-1} */
+  int full_system; /* 1: semiconductor + electrolyte; 0: semiconductor only */
+  int nx_semi, nx_elec, ny;
+  double x_semi0, x_semi1, x_elec1, height;
+  int bc_semi[4], bc_elec[4], bc_poisson[4]; /* (left, right, bottom, top) */
+  double lambda2;  /* scaled Debye length squared */
+  double eps_semi, eps_elec;
+  double mu[4];    /* mobilities: electrons, holes, reductants, oxidants */
+  double dt, penalty;
+  double k_et, k_ht;
+  double junction_x;
+  double nd[2], na[2], n_eq[2], p_eq[2];
+  double r_eq, o_eq;
+  int ic_kind;  /* 0: equilibrium densities, 1: doping profile */
+  int gen_kind; /* 0 off, 1 alpha*G0*exp(alpha*(y-H)), 2 G0*exp(-alpha*(x_semi1-x)) */
+  double G0, alpha;
+  int srh;      /* 0: SRH returns 0 (reference), 1: documented SRH formula */
+  double tau_n, tau_p, n_i;
+  double phi_bi, phi_app; /* potential data phi_bi - phi_app where x == 0 */
+  double s_n, s_p;        /* Schottky recombination velocities */
+} pecs_params;
+
+typedef struct pecs_options {
+  int precision;     /* PECS_PREC_* */
+  int leaf_cells;    /* nested-dissection leaf size in cells (0 = default) */
+  int use_graphs;    /* capture a time step in a CUDA graph (1 = yes) */
+  int ir_max_iters;  /* FP32_IR: refinement sweeps per solve (0 = default) */
+  double ir_tol;     /* FP32_IR: target relative residual (0 = default 1e-12) */
+  int device;        /* CUDA device ordinal */
+  int host_setup_only; /* 1: build meshes, matrices and factors on the host only
+                          (no device work; for inspecting the setup) */
+} pecs_options;
+
+typedef struct pecs_info {
+  int n_inst;
+  int ndofs[5];            /* per field */
+  long long factor_entries[3]; /* stored entries: semi carriers, elec carriers, Poisson */
+  int factor_levels[3];
+  int factor_nodes[3];
+  long long factor_bytes;  /* device bytes of all factors */
+  double setup_seconds;    /* host assembly + factorisation */
+  int n_distinct_carrier_factors;
+} pecs_info;
+
+typedef struct pecs_ctx pecs_ctx;
+
+const char* pecs_last_error(void);
+void pecs_default_options(pecs_options* opt);
+
+/* Setup: meshes, DoF maps, LDG + mixed matrices, LU factors, upload.
+ * `params` holds n_inst instances; all must share the fields that enter the
+ * matrices (mesh, degree, boundary layout, lambda2, eps, mu, dt, penalty). */
+int pecs_create(const pecs_params* params, int n_inst, const pecs_options* opt, pecs_ctx** out);
+void pecs_destroy(pecs_ctx* ctx);
+int pecs_get_info(pecs_ctx* ctx, pecs_info* info);
+
+/* CSR export of a setup matrix (which = PECS_MAT_*).  Call with NULL arrays to
+ * query n and nnz. */
+int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowptr, int* col,
+                    double* val);
+
+/* Initial conditions (SolarCell.cpp:1996-2034): L2 projection of the initial
+ * profiles, then the initial Poisson solve. */
+int pecs_initialize(pecs_ctx* ctx);
+int pecs_set_state(pecs_ctx* ctx, int inst, int field, const double* host, size_t n);
+int pecs_get_state(pecs_ctx* ctx, int inst, int field, double* host, size_t n);
+/* right-hand side of the last assembly (field = PECS_FIELD_*) */
+int pecs_get_rhs(pecs_ctx* ctx, int inst, int field, double* host, size_t n);
+
+/* Stages of one IMEX step (SolarCell.cpp:2057-2075). */
+int pecs_assemble_carrier_rhs(pecs_ctx* ctx); /* assemble_semiconductor_rhs + assemble_electrolyte_rhs */
+int pecs_solve_carriers(pecs_ctx* ctx);       /* solve_full_system */
+int pecs_assemble_poisson_rhs(pecs_ctx* ctx); /* assemble_Poisson_rhs */
+int pecs_solve_poisson(pecs_ctx* ctx);        /* solve_Poisson */
+int pecs_step(pecs_ctx* ctx, int n_steps);    /* n full steps */
+
+/* March every instance until max over fields of ||u^{n+1}-u^n||/||u^{n+1}||
+ * <= tol or max_steps; converged instances stop updating.  steps and
+ * rel_change (n_inst entries each, may be NULL) receive per-instance results. */
+int pecs_run_to_steady_state(pecs_ctx* ctx, int max_steps, double tol, int check_every,
+                             int* steps, double* rel_change);
+/* I_Sigma = int_Sigma [k_et (n-n_e) o - k_ht (p-p_e) r] ds per instance. */
+int pecs_interface_current(pecs_ctx* ctx, double* out);
+/* One I-V sweep end to end: initial state from host (n_inst x ndofs per field,
+ * NULL = built-in initial conditions), run to steady state, copy back the
+ * interface currents and (optionally) the final densities. */
+int pecs_iv_sweep(pecs_ctx* ctx, const double* const* init_fields, int max_steps, double tol,
+                  int check_every, double* currents, int* steps, double* const* final_fields);
+int pecs_synchronize(pecs_ctx* ctx);
+
+/* ---- drop-in direct solver for an externally assembled matrix ------------
+ * Carrier::set_solver / PoissonData::set_solver (Carrier.cpp:26-32,
+ * Poisson.cpp:90-96) and their solve() (Carrier.cpp:34-40, Poisson.cpp:98-105).
+ * dof_cell[i] names the mesh cell that owns dof i (faces: either neighbour),
+ * cell_xy holds the cell centres (2 per cell) used by nested dissection,
+ * dof_class[i] = 0 marks dofs whose diagonal blocks are cell-local and
+ * mutually uncoupled across cells (the LDG current dofs), which are then
+ * eliminated first; NULL = all dofs class 1. */
+typedef struct pecs_lu pecs_lu;
+int pecs_lu_factor(int n, const int* rowptr, const int* col, const double* val,
+                   const int* dof_cell, const int* dof_class, int n_cells, const double* cell_xy,
+                   int precision, int leaf_cells, pecs_lu** out);
+int pecs_lu_solve(pecs_lu* lu, int nrhs, const double* b, double* x); /* host arrays, nrhs*n */
+int pecs_lu_solve_device(pecs_lu* lu, int nrhs, const double* b_dev, double* x_dev, void* stream);
+int pecs_lu_stats(pecs_lu* lu, long long* entries, int* levels, int* nodes, int* max_front);
+void pecs_lu_destroy(pecs_lu* lu);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PECS_H */

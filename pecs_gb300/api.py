@@ -1,0 +1,333 @@
+"""Python host API over the C ABI: parameters, problem contexts, the drop-in LU.
+
+``Params`` holds already-scaled parameters (the role of
+ParameterSpace::Parameters, include/Parameters.hpp:27-289 of the reference);
+``Context`` owns one GPU-resident group of instances that share meshes and
+matrices; ``LU`` is the externally-assembled direct solver
+(SparseDirectUMFPACK's initialize/vmult as used by Carrier/PoissonData).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _ffi as F
+from ._ffi import (DIRICHLET, INTERFACE, NEUMANN, SCHOTTKY, FIELD_N, FIELD_O, FIELD_P,
+                   FIELD_POISSON, FIELD_R, PREC_FP32_IR, PREC_FP64, check, lib)
+
+
+@dataclass
+class Params:
+    degree: int = 1
+    full_system: bool = True
+    nx_semi: int = 16
+    nx_elec: int = 16
+    ny: int = 16
+    x_semi0: float = 0.0
+    x_semi1: float = 1.0
+    x_elec1: float = 2.0
+    height: float = 1.0
+    bc_semi: tuple = (DIRICHLET, INTERFACE, NEUMANN, NEUMANN)
+    bc_elec: tuple = (INTERFACE, DIRICHLET, NEUMANN, NEUMANN)
+    bc_poisson: tuple = (DIRICHLET, DIRICHLET, NEUMANN, NEUMANN)
+    lambda2: float = 1e-2
+    eps_semi: float = 1.0
+    eps_elec: float = 1.5
+    mu: tuple = (1.0, 1.0, 1.0, 1.0)
+    dt: float = 1e-3
+    penalty: float = 1.0
+    k_et: float = 1e-2
+    k_ht: float = 1e-2
+    junction_x: float = 0.5
+    nd: tuple = (1.0, 1.0)
+    na: tuple = (0.0, 0.0)
+    n_eq: tuple = (1.0, 1.0)
+    p_eq: tuple = (1e-4, 1e-4)
+    r_eq: float = 1.0
+    o_eq: float = 1.0
+    ic_kind: int = 0
+    gen_kind: int = 2
+    G0: float = 1.0
+    alpha: float = 5.0
+    srh: bool = True
+    tau_n: float = 1.0
+    tau_p: float = 1.0
+    n_i: float = 1e-2
+    phi_bi: float = 0.0
+    phi_app: float = 0.0
+    s_n: float = 0.0
+    s_p: float = 0.0
+
+    def copy(self, **kw) -> "Params":
+        return dataclasses.replace(self, **kw)
+
+    def to_c(self) -> F.pecs_params:
+        p = F.pecs_params()
+        for f in dataclasses.fields(self):
+            v = getattr(self, f.name)
+            if isinstance(v, (tuple, list)):
+                arr = getattr(p, f.name)
+                for i, x in enumerate(v):
+                    arr[i] = x
+            else:
+                setattr(p, f.name, int(v) if isinstance(v, bool) else v)
+        return p
+
+
+def config1(**kw) -> Params:
+    """Semiconductor-only p-n junction on the unit square, 16x16 cells, k=1,
+    dt=1e-3, 100 steps, initial densities = doping."""
+    n_i = 1e-2
+    p = Params(degree=1, full_system=False, nx_semi=16, nx_elec=0, ny=16,
+               bc_semi=(DIRICHLET, DIRICHLET, NEUMANN, NEUMANN),
+               bc_poisson=(DIRICHLET, DIRICHLET, NEUMANN, NEUMANN),
+               lambda2=1e-2, eps_semi=1.0, dt=1e-3, junction_x=0.5, nd=(1.0, 0.0), na=(0.0, 1.0),
+               n_eq=(1.0, n_i * n_i), p_eq=(n_i * n_i, 1.0), ic_kind=1, gen_kind=0, srh=True,
+               tau_n=1.0, tau_p=1.0, n_i=n_i, phi_bi=math.log(1.0 / (n_i * n_i)), phi_app=0.0,
+               k_et=0.0, k_ht=0.0)
+    return p.copy(**kw)
+
+
+def config2(n_refine: int = 6, **kw) -> Params:
+    """Coupled half cell: semiconductor [0,1]^2 and electrolyte [1,2]x[0,1],
+    2^r x 2^r cells each, k=1, G = G0 exp(-alpha (1-x)), dt=1e-3."""
+    n_i = 1e-2
+    n = 2 ** n_refine
+    p = Params(degree=1, full_system=True, nx_semi=n, nx_elec=n, ny=n, lambda2=1e-2,
+               eps_semi=1.0, eps_elec=1.5, dt=1e-3, nd=(1.0, 1.0), na=(0.0, 0.0),
+               n_eq=(1.0, 1.0), p_eq=(n_i * n_i, n_i * n_i), r_eq=1.0, o_eq=1.0, ic_kind=0,
+               gen_kind=2, G0=1.0, alpha=5.0, srh=True, tau_n=1.0, tau_p=1.0, n_i=n_i,
+               k_et=1e-2, k_ht=1e-2, phi_bi=0.0, phi_app=0.0)
+    return p.copy(**kw)
+
+
+def reference_params(n_refine: int = 4, degree: int = 1, **kw) -> Params:
+    """Reference-faithful physics: constant equilibria 2, 0, 30, 29, SRH = 0,
+    generation alpha*G0*exp(alpha*(y-H)), Dirichlet on every outer side."""
+    n = 2 ** n_refine
+    p = Params(degree=degree, nx_semi=n, nx_elec=n, ny=n, nd=(2.0, 2.0), na=(0.0, 0.0),
+               n_eq=(2.0, 2.0), p_eq=(0.0, 0.0), r_eq=30.0, o_eq=29.0, ic_kind=0, gen_kind=1,
+               srh=False, bc_semi=(DIRICHLET, INTERFACE, DIRICHLET, DIRICHLET),
+               bc_elec=(INTERFACE, DIRICHLET, DIRICHLET, DIRICHLET),
+               bc_poisson=(DIRICHLET, DIRICHLET, DIRICHLET, DIRICHLET))
+    return p.copy(**kw)
+
+
+def default_options(precision: int = PREC_FP64, use_graphs: bool = True, leaf_cells: int = 8,
+                    ir_max_iters: int = 2, device: int = 0,
+                    host_setup_only: bool = False) -> F.pecs_options:
+    o = F.pecs_options()
+    lib().pecs_default_options(C.byref(o))
+    o.precision = precision
+    o.use_graphs = int(use_graphs)
+    o.leaf_cells = leaf_cells
+    o.ir_max_iters = ir_max_iters
+    o.device = device
+    o.host_setup_only = int(host_setup_only)
+    return o
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Context:
+    """A group of instances resident on one GPU (pecs_create)."""
+
+    def __init__(self, params: Sequence[Params] | Params, precision: int = PREC_FP64,
+                 use_graphs: bool = True, leaf_cells: int = 8, ir_max_iters: int = 2,
+                 device: int = 0, host_setup_only: bool = False):
+        if isinstance(params, Params):
+            params = [params]
+        self.params = list(params)
+        arr = (F.pecs_params * len(self.params))(*[p.to_c() for p in self.params])
+        opt = default_options(precision, use_graphs, leaf_cells, ir_max_iters, device,
+                              host_setup_only)
+        h = C.c_void_p()
+        check(lib().pecs_create(arr, len(self.params), C.byref(opt), C.byref(h)))
+        self._h = h
+        self.n_inst = len(self.params)
+        self.full = bool(self.params[0].full_system)
+        info = self.info()
+        self.ndofs = list(info.ndofs)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pecs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self) -> F.pecs_info:
+        i = F.pecs_info()
+        check(lib().pecs_get_info(self._h, C.byref(i)))
+        return i
+
+    def matrix(self, which: int):
+        import scipy.sparse as sp
+        n = C.c_int()
+        nnz = C.c_longlong()
+        check(lib().pecs_get_matrix(self._h, which, C.byref(n), C.byref(nnz), None, None, None))
+        rp = np.zeros(n.value + 1, dtype=np.int32)
+        ci = np.zeros(nnz.value, dtype=np.int32)
+        v = np.zeros(nnz.value)
+        check(lib().pecs_get_matrix(self._h, which, None, None,
+                                    rp.ctypes.data_as(C.POINTER(C.c_int)),
+                                    ci.ctypes.data_as(C.POINTER(C.c_int)), _dptr(v)))
+        return sp.csr_matrix((v, ci, rp), shape=(n.value, n.value))
+
+    def initialize(self):
+        check(lib().pecs_initialize(self._h))
+
+    def get_state(self, field: int, inst: int = 0) -> np.ndarray:
+        out = np.zeros(self.ndofs[field])
+        check(lib().pecs_get_state(self._h, inst, field, _dptr(out), out.size))
+        return out
+
+    def set_state(self, field: int, values: np.ndarray, inst: int = 0):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        check(lib().pecs_set_state(self._h, inst, field, _dptr(v), v.size))
+
+    def get_rhs(self, field: int, inst: int = 0) -> np.ndarray:
+        out = np.zeros(self.ndofs[field])
+        check(lib().pecs_get_rhs(self._h, inst, field, _dptr(out), out.size))
+        return out
+
+    def fields(self):
+        return (FIELD_N, FIELD_P, FIELD_R, FIELD_O, FIELD_POISSON) if self.full else \
+            (FIELD_N, FIELD_P, FIELD_POISSON)
+
+    def state(self, inst: int = 0) -> dict:
+        names = {FIELD_N: "n", FIELD_P: "p", FIELD_R: "r", FIELD_O: "o", FIELD_POISSON: "P"}
+        return {names[f]: self.get_state(f, inst) for f in self.fields()}
+
+    def assemble_carrier_rhs(self):
+        check(lib().pecs_assemble_carrier_rhs(self._h))
+
+    def solve_carriers(self):
+        check(lib().pecs_solve_carriers(self._h))
+
+    def assemble_poisson_rhs(self):
+        check(lib().pecs_assemble_poisson_rhs(self._h))
+
+    def solve_poisson(self):
+        check(lib().pecs_solve_poisson(self._h))
+
+    def step(self, n: int = 1):
+        check(lib().pecs_step(self._h, n))
+
+    def run_to_steady_state(self, max_steps: int, tol: float, check_every: int = 50):
+        steps = np.zeros(self.n_inst, dtype=np.int32)
+        rel = np.zeros(self.n_inst)
+        check(lib().pecs_run_to_steady_state(self._h, max_steps, tol, check_every,
+                                             steps.ctypes.data_as(C.POINTER(C.c_int)), _dptr(rel)))
+        return steps, rel
+
+    def interface_current(self) -> np.ndarray:
+        out = np.zeros(self.n_inst)
+        check(lib().pecs_interface_current(self._h, _dptr(out)))
+        return out
+
+    def iv_sweep(self, max_steps: int, tol: float, check_every: int = 50,
+                 init: Optional[dict] = None, want_fields: bool = False):
+        """End-to-end I-V sweep through the public API: host initial state in,
+        host currents (and optionally fields) out."""
+        init_arr = None
+        keep = []
+        if init is not None:
+            ptrs = (C.POINTER(C.c_double) * 5)()
+            for f in range(5):
+                if self.ndofs[f]:
+                    a = np.ascontiguousarray(init[f], dtype=np.float64).reshape(-1)
+                    keep.append(a)
+                    ptrs[f] = _dptr(a)
+            init_arr = ptrs
+        cur = np.zeros(self.n_inst)
+        steps = np.zeros(self.n_inst, dtype=np.int32)
+        finals = None
+        fptrs = None
+        if want_fields:
+            finals = {f: np.zeros(self.n_inst * self.ndofs[f]) for f in range(5) if self.ndofs[f]}
+            fptrs = (C.POINTER(C.c_double) * 5)()
+            for f, a in finals.items():
+                fptrs[f] = _dptr(a)
+        check(lib().pecs_iv_sweep(self._h, init_arr, max_steps, tol, check_every, _dptr(cur),
+                                  steps.ctypes.data_as(C.POINTER(C.c_int)), fptrs))
+        return cur, steps, finals
+
+
+class LU:
+    """Drop-in direct solver: factor(set_solver) once, solve() every step."""
+
+    def __init__(self, A, dof_cell: np.ndarray, cell_xy: np.ndarray,
+                 dof_class: Optional[np.ndarray] = None, precision: int = PREC_FP64,
+                 leaf_cells: int = 8):
+        import scipy.sparse as sp
+        A = sp.csr_matrix(A)
+        A.sort_indices()
+        self.n = A.shape[0]
+        rp = np.ascontiguousarray(A.indptr, dtype=np.int32)
+        ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+        v = np.ascontiguousarray(A.data, dtype=np.float64)
+        dc = np.ascontiguousarray(dof_cell, dtype=np.int32)
+        xy = np.ascontiguousarray(cell_xy, dtype=np.float64).reshape(-1)
+        cls = None if dof_class is None else np.ascontiguousarray(dof_class, dtype=np.int32)
+        h = C.c_void_p()
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
+        check(lib().pecs_lu_factor(self.n, ip(rp), ip(ci), _dptr(v), ip(dc),
+                                   None if cls is None else ip(cls), xy.size // 2, _dptr(xy),
+                                   precision, leaf_cells, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pecs_lu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, b: np.ndarray) -> np.ndarray:
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        nrhs = 1 if b.ndim == 1 else b.shape[0]
+        x = np.zeros_like(b)
+        check(lib().pecs_lu_solve(self._h, nrhs, _dptr(b), _dptr(x)))
+        return x
+
+    def solve_device(self, b, x, nrhs: int = 1, stream: int = 0):
+        """b, x: device pointers (e.g. torch.Tensor.data_ptr()) of nrhs*n doubles."""
+        check(lib().pecs_lu_solve_device(self._h, nrhs, C.c_void_p(b), C.c_void_p(x),
+                                         C.c_void_p(stream)))
+
+    def host_apply(self, b: np.ndarray) -> np.ndarray:
+        """Diagnostic host application of the factors (no GPU)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        check(lib().pecs_lu_host_apply(self._h, _dptr(b), _dptr(x)))
+        return x
+
+    def stats(self):
+        e = C.c_longlong()
+        lv = C.c_int()
+        nn = C.c_int()
+        mf = C.c_int()
+        check(lib().pecs_lu_stats(self._h, C.byref(e), C.byref(lv), C.byref(nn), C.byref(mf)))
+        return {"entries": e.value, "levels": lv.value, "nodes": nn.value, "max_front": mf.value}

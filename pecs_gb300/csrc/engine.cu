@@ -1,0 +1,1236 @@
+// GB300 engine for the PECS IMEX time step and the C ABI (include/pecs.h).
+//
+// Data layout in HBM (everything resident after pecs_create):
+//   state[2][field]  ping-pong state vectors, [instance][ndofs(field)] FP64,
+//                    field-major so a kernel reads one instance's vector
+//                    contiguously; carrier vectors are component-wise
+//                    [J_x | J_y | u] with the cell's dofs contiguous.
+//   rhs/y[field]     assembled right-hand sides / forward-sweep slots.
+//   bconst[field]    time-independent RHS parts (generation, Dirichlet data,
+//                    doping), per instance.
+//   carrier and Poisson FactorBanks (solve.cuh) + per-RHS update workspaces.
+// A step is: carrier RHS (1 launch) -> carrier solves (one launch per tree
+// level for all carriers and instances) -> Poisson RHS (1) -> Poisson solve
+// -> steady-state reduction (2) + snapshot (1).  pecs_run_to_steady_state
+// replays a CUDA graph of two steps (even/odd ping-pong).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.hpp"
+#include "mf.hpp"
+#include "problem.hpp"
+#include "rhs_kernels.cuh"
+#include "solve.cuh"
+
+namespace pecs {
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& m) { g_last_error = m; }
+
+// ---------------------------------------------------------------------------
+// small kernels: residual, axpy, steady-state test, interface current
+// ---------------------------------------------------------------------------
+
+struct VecList {  // up to 256 vectors of equal length per launch
+  const double* const* b;
+  const double* const* x;
+  double* const* out;
+  const int* mat;  // matrix index per vector
+};
+
+struct CsrDev {
+  const int* rp;
+  const int* ci;
+  const double* v;
+};
+
+struct CsrSet {
+  CsrDev m[5];
+};
+
+// out = b - A x   (one thread per row; grid.y = vector)
+__global__ void k_residual(CsrSet M, VecList L, int n, const int* __restrict__ active,
+                           const int* __restrict__ vec_inst) {
+  const int v = blockIdx.y;
+  if (active && !active[vec_inst[v]]) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const CsrDev A = M.m[L.mat[v]];
+  const double* x = L.x[v];
+  double s = 0.0;
+  for (int p = A.rp[i]; p < A.rp[i + 1]; ++p) s += A.v[p] * x[A.ci[p]];
+  L.out[v][i] = L.b[v][i] - s;
+}
+
+// x += d
+__global__ void k_axpy(double* const* x, const double* const* d, int n,
+                       const int* __restrict__ active, const int* __restrict__ vec_inst) {
+  const int v = blockIdx.y;
+  if (active && !active[vec_inst[v]]) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[v][i] += d[v][i];
+}
+
+constexpr int kRedThreads = 256;
+constexpr int kRedChunks = 16;
+
+// partial sums of |new-old|^2 and |new|^2: grid (kRedChunks, 5 fields, n_inst)
+__global__ void k_relchange_partial(FieldPtrs NEW, FieldPtrs OLD, int n_fields,
+                                    double2* __restrict__ partial) {
+  const int chunk = blockIdx.x, fld = blockIdx.y, i = blockIdx.z;
+  __shared__ double sd[kRedThreads], sn[kRedThreads];
+  double d2 = 0.0, n2 = 0.0;
+  if (fld < n_fields) {
+    const int f = fld == n_fields - 1 ? 4 : fld;
+    const int nd = NEW.nd[f];
+    const double* a = NEW.u[f] + (size_t)i * nd;
+    const double* b = OLD.u[f] + (size_t)i * nd;
+    const int per = (nd + kRedChunks - 1) / kRedChunks;
+    const int lo = chunk * per, hi = min(nd, lo + per);
+    for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+      const double x = a[t], y = b[t];
+      d2 += (x - y) * (x - y);
+      n2 += x * x;
+    }
+  }
+  sd[threadIdx.x] = d2;
+  sn[threadIdx.x] = n2;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sd[threadIdx.x] += sd[threadIdx.x + o];
+      sn[threadIdx.x] += sn[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    partial[((size_t)i * 5 + fld) * kRedChunks + chunk] = make_double2(sd[0], sn[0]);
+}
+
+// per instance: rel = max_f sqrt(d2/n2); record first step with rel <= tol.
+__global__ void k_converge(const double2* __restrict__ partial, int n_inst, int n_fields, double tol,
+                           int* __restrict__ conv_step, double* __restrict__ rel,
+                           int* __restrict__ step_ctr, int* __restrict__ active,
+                           int* __restrict__ n_active) {
+  const int step = *step_ctr + 1;
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n_inst; i += blockDim.x) {
+    double r = 0.0;
+    bool finite = true;
+    for (int fld = 0; fld < n_fields; ++fld) {
+      double d2 = 0.0, n2 = 0.0;
+      for (int c = 0; c < kRedChunks; ++c) {
+        const double2 v = partial[((size_t)i * 5 + fld) * kRedChunks + c];
+        d2 += v.x;
+        n2 += v.y;
+      }
+      finite = finite && isfinite(d2) && isfinite(n2);
+      const double q = n2 > 0.0 ? sqrt(d2 / n2) : sqrt(d2);
+      r = fmax(r, q);
+    }
+    if (active[i]) {
+      rel[i] = finite ? r : __longlong_as_double(0x7ff8000000000000LL);
+      if (!finite) {
+        active[i] = 0;
+        conv_step[i] = -step;  // non-finite state: stopped, reported as failure
+      } else if (r <= tol) {
+        active[i] = 0;
+        conv_step[i] = step;
+      }
+    }
+    if (active[i]) atomicAdd(&cnt, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *step_ctr = step;
+    *n_active = cnt;
+  }
+}
+
+// I_Sigma per instance: one block per instance, threads over interface faces
+__global__ void k_interface_current(Tables T, RegionDev semi, RegionDev elec, FieldPtrs F,
+                                    const InstDev* __restrict__ inst, const double* __restrict__ ne,
+                                    const double* __restrict__ pe, const int* __restrict__ isemi,
+                                    const int* __restrict__ ielec, int n_iface, int n1, int nq,
+                                    double* __restrict__ out) {
+  const int i = blockIdx.x;
+  const InstDev P = inst[i];
+  __shared__ double sacc[kRedThreads];
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < n_iface; t += blockDim.x) {
+    const int Ks = isemi[t], Ke = ielec[t];
+    const double* un = F.u[0] + (size_t)i * F.nd[0] + 2 * semi.nc * n1 + Ks * n1;
+    const double* up = F.u[1] + (size_t)i * F.nd[1] + 2 * semi.nc * n1 + Ks * n1;
+    const double* ur = F.u[2] + (size_t)i * F.nd[2] + 2 * elec.nc * n1 + Ke * n1;
+    const double* uo = F.u[3] + (size_t)i * F.nd[3] + 2 * elec.nc * n1 + Ke * n1;
+    const double hy = semi.h[Ks].y;
+    for (int q = 0; q < nq; ++q) {
+      double n = 0, p = 0, r = 0, o = 0;
+      for (int a = 0; a < n1; ++a) {
+        const double fs = T.fphi[(semi.iface_face * n1 + a) * nq + q];
+        const double fe = T.fphi[(elec.iface_face * n1 + a) * nq + q];
+        n += fs * un[a];
+        p += fs * up[a];
+        r += fe * ur[a];
+        o += fe * uo[a];
+      }
+      const size_t o2 = (size_t)i * n_iface * nq + (size_t)t * nq + q;
+      acc += (P.k_et * (n - ne[o2]) * o - P.k_ht * (p - pe[o2]) * r) * T.fw[q] * hy;
+    }
+  }
+  sacc[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sacc[threadIdx.x] += sacc[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[i] = sacc[0];
+}
+
+// copy state of instances that converged at this step into the snapshot
+__global__ void k_snapshot(FieldPtrs NEW, double* const* snap, const int* __restrict__ conv_step,
+                           const int* __restrict__ step_ctr, int n_fields_total) {
+  const int i = blockIdx.z, f = blockIdx.y;
+  if (f >= n_fields_total) return;
+  const int cs = conv_step[i];
+  const int step = *step_ctr;
+  if (cs != step && cs != -step) return;
+  const int nd = NEW.nd[f];
+  const double* a = NEW.u[f] + (size_t)i * nd;
+  double* b = snap[f] + (size_t)i * nd;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nd; t += gridDim.x * blockDim.x) b[t] = a[t];
+}
+
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Engine
+// ---------------------------------------------------------------------------
+
+struct SetTable {  // device pointer arrays of one SetsView
+  std::vector<DBuf<double*>> b, y, w, x;
+  SetsView view{};
+  int max_nrhs = 0;
+};
+
+struct Engine {
+  pecs_options opt{};
+  std::unique_ptr<Setup> S;
+  int n_inst = 0;
+  int n_fields = 5;  // fields in use (3 for semiconductor only: n, p, P)
+  bool host_only = false;
+  bool full = true;
+  int nd[5] = {0, 0, 0, 0, 0};
+  double setup_seconds = 0.0;
+  cudaStream_t st = nullptr;
+  // factors
+  MfFactor fs[2], fe[2], fp;
+  int n_fs = 0, n_fe = 0;
+  FactorBank bank_c, bank_p;
+  // device matrices (for refinement residuals)
+  DBuf<int> A_rp[5], A_ci[5];
+  DBuf<double> A_v[5];
+  CsrSet csr{};
+  // tables and regions
+  DBuf<double> t_phi, t_qw, t_fphi, t_fw, t_psix, t_psiy, t_phiP, t_mref;
+  Tables T{};
+  DBuf<double2> h_[2], ph_[2];
+  DBuf<int4> bid_[2];
+  DBuf<int> rt_[2], phid_[2], partner_[2], iface_[2];
+  RegionDev R[2]{};
+  DBuf<InstDev> inst;
+  DBuf<double> iface_ne, iface_pe, sch_ne, sch_pe;
+  DBuf<int> isemi, ielec;
+  // vectors
+  DBuf<double> state[2][5], rhs[5], bconst[5], yv[5], res[5], delta[5], snap[5];
+  std::vector<DBuf<double>> wbuf_c, wbuf_p;
+  int cur = 0;
+  bool carriers_advanced = false;
+  bool initialized = false;
+  // solve pointer tables: [nxt][0=main, 1=correction]
+  SetTable tab_c[2][2], tab_p[2][2];
+  DBuf<double*> snap_ptrs;
+  // steady state
+  DBuf<double2> partial;
+  DBuf<int> conv_step, step_ctr, active, n_active;
+  DBuf<double> rel;
+  // graphs
+  cudaGraphExec_t graph2[2] = {nullptr, nullptr};  // two steps starting from cur = 0 / 1
+  bool graph_valid = false;
+  int kernel_launches_per_step = 0;
+
+  ~Engine() {
+    for (auto& g : graph2)
+      if (g) cudaGraphExecDestroy(g);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  FieldPtrs fields(const DBuf<double>* u, DBuf<double>* out) const {
+    FieldPtrs F{};
+    for (int f = 0; f < 5; ++f) {
+      F.u[f] = u ? u[f].p : nullptr;
+      F.out[f] = out ? out[f].p : nullptr;
+      F.bc[f] = bconst[f].p;
+      F.nd[f] = nd[f];
+    }
+    return F;
+  }
+
+  void build_sets(const std::vector<std::vector<int>>& set_fields, const FactorBank& bank,
+                  DBuf<double>* bsrc, DBuf<double>* xdst, std::vector<DBuf<double>>& wbufs,
+                  int& wcount, SetTable& tab) {
+    const int ns = (int)set_fields.size();
+    tab.b.resize(ns);
+    tab.y.resize(ns);
+    tab.w.resize(ns);
+    tab.x.resize(ns);
+    tab.max_nrhs = 0;
+    int widx = 0;
+    for (int si = 0; si < ns; ++si) {
+      std::vector<double*> hb, hy, hw, hx;
+      for (int i = 0; i < n_inst; ++i)
+        for (int f : set_fields[si]) {
+          hb.push_back(bsrc[f].p + (size_t)i * nd[f]);
+          hy.push_back(yv[f].p + (size_t)i * nd[f]);
+          hx.push_back(xdst[f].p + (size_t)i * nd[f]);
+          if (widx >= (int)wbufs.size()) {
+            wbufs.emplace_back();
+            wbufs.back().alloc(bank.set_wtotal(si));
+            wbufs.back().zero();
+          }
+          if ((int)wbufs[widx].n < bank.set_wtotal(si)) {
+            wbufs[widx].alloc(bank.set_wtotal(si));
+            wbufs[widx].zero();
+          }
+          hw.push_back(wbufs[widx].p);
+          ++widx;
+        }
+      tab.b[si].upload(hb);
+      tab.y[si].upload(hy);
+      tab.w[si].upload(hw);
+      tab.x[si].upload(hx);
+      tab.view.set[si].nrhs = (int)hb.size();
+      tab.view.set[si].b = tab.b[si].p;
+      tab.view.set[si].y = tab.y[si].p;
+      tab.view.set[si].w = tab.w[si].p;
+      tab.view.set[si].x = tab.x[si].p;
+      tab.max_nrhs = std::max(tab.max_nrhs, (int)hb.size());
+    }
+    wcount = std::max(wcount, widx);
+  }
+
+  std::vector<std::vector<int>> carrier_set_fields() const {
+    std::vector<std::vector<int>> sf;
+    if (n_fs == 1)
+      sf.push_back({0, 1});
+    else {
+      sf.push_back({0});
+      sf.push_back({1});
+    }
+    if (full) {
+      if (n_fe == 1)
+        sf.push_back({2, 3});
+      else {
+        sf.push_back({2});
+        sf.push_back({3});
+      }
+    }
+    return sf;
+  }
+
+  void create(const std::vector<pecs_params>& P, const pecs_options& o) {
+    auto t0 = std::chrono::steady_clock::now();
+    opt = o;
+    n_inst = (int)P.size();
+    host_only = opt.host_setup_only != 0;
+    if (!host_only) {
+      int ndev = 0;
+      if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+        throw PecsError(PECS_E_NODEVICE, "no CUDA device available");
+      if (opt.device < 0 || opt.device >= ndev) throw PecsError(PECS_E_ARG, "bad device ordinal");
+      PECS_CUDA(cudaSetDevice(opt.device));
+      PECS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    }
+    S.reset(new Setup(P));
+    full = S->full;
+    n_fields = full ? 5 : 3;
+    nd[0] = nd[1] = S->semi.ndofs;
+    nd[2] = nd[3] = full ? S->elec.ndofs : 0;
+    nd[4] = S->pois.ndofs;
+    // factorisation (host, FP64); equal carrier matrices share one factor
+    const int leaf = opt.leaf_cells > 0 ? opt.leaf_cells : 8;
+    auto same = [](const Csr& a, const Csr& b) {
+      return a.rowptr == b.rowptr && a.col == b.col && a.val == b.val;
+    };
+    auto factor = [&](const Csr& A, const std::vector<int>& dc, const std::vector<int>* cls, int nc,
+                      const std::vector<double>& xy, MfFactor& F) {
+      F = mf_analyze(A, dc.data(), cls ? cls->data() : nullptr, nc, xy.data(), leaf);
+      try {
+        mf_factorize(F, A);
+      } catch (const std::exception& e) {
+        throw PecsError(PECS_E_SINGULAR, e.what());
+      }
+    };
+    n_fs = same(S->semi.A[0], S->semi.A[1]) ? 1 : 2;
+    for (int t = 0; t < n_fs; ++t)
+      factor(S->semi.A[t], S->semi.dof_cell, &S->semi.dof_class, S->semi.grid.nc(), S->semi.cell_xy, fs[t]);
+    if (full) {
+      n_fe = same(S->elec.A[0], S->elec.A[1]) ? 1 : 2;
+      for (int t = 0; t < n_fe; ++t)
+        factor(S->elec.A[t], S->elec.dof_cell, &S->elec.dof_class, S->elec.grid.nc(), S->elec.cell_xy, fe[t]);
+    }
+    factor(S->pois.A, S->pois.dof_cell, nullptr, S->pois.grid.nc(), S->pois.cell_xy, fp);
+    if (host_only) {
+      setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      return;
+    }
+    std::vector<const MfFactor*> cf;
+    for (int t = 0; t < n_fs; ++t) cf.push_back(&fs[t]);
+    for (int t = 0; t < n_fe; ++t) cf.push_back(&fe[t]);
+    bank_c.build(cf, opt.precision);
+    bank_p.build({&fp}, opt.precision);
+    // free host copies of the factor values (structure is kept for stats)
+    for (auto* F : {&fs[0], &fs[1], &fe[0], &fe[1], &fp}) {
+      std::vector<std::vector<double>>().swap(F->Gf);
+      std::vector<std::vector<double>>().swap(F->Hb);
+    }
+    // matrices for refinement residuals
+    const Csr* mats[5] = {&S->semi.A[0], &S->semi.A[1], full ? &S->elec.A[0] : nullptr,
+                          full ? &S->elec.A[1] : nullptr, &S->pois.A};
+    for (int f = 0; f < 5; ++f) {
+      if (!mats[f]) continue;
+      A_rp[f].upload(mats[f]->rowptr);
+      A_ci[f].upload(mats[f]->col);
+      A_v[f].upload(mats[f]->val);
+      csr.m[f] = CsrDev{A_rp[f].p, A_ci[f].p, A_v[f].p};
+    }
+    upload_tables();
+    upload_regions();
+    // vectors
+    for (int f = 0; f < 5; ++f) {
+      const size_t n = (size_t)n_inst * nd[f];
+      if (n == 0) continue;
+      for (int b = 0; b < 2; ++b) {
+        state[b][f].alloc(n);
+        state[b][f].zero();
+      }
+      rhs[f].alloc(n);
+      rhs[f].zero();
+      yv[f].alloc(n);
+      res[f].alloc(n);
+      delta[f].alloc(n);
+      snap[f].alloc(n);
+      std::vector<double> bc;
+      bc.reserve(n);
+      for (int i = 0; i < n_inst; ++i) bc.insert(bc.end(), S->bconst[f][i].begin(), S->bconst[f][i].end());
+      bconst[f].upload(bc);
+    }
+    // solve pointer tables
+    int wc = 0, wp = 0;
+    auto csf = carrier_set_fields();
+    for (int nx = 0; nx < 2; ++nx) {
+      build_sets(csf, bank_c, rhs, state[nx], wbuf_c, wc, tab_c[nx][0]);
+      build_sets(csf, bank_c, res, delta, wbuf_c, wc, tab_c[nx][1]);
+      build_sets({{4}}, bank_p, rhs, state[nx], wbuf_p, wp, tab_p[nx][0]);
+      build_sets({{4}}, bank_p, res, delta, wbuf_p, wp, tab_p[nx][1]);
+    }
+    prepare_ir();
+    // steady-state buffers
+    partial.alloc((size_t)n_inst * 5 * kRedChunks);
+    partial.zero();
+    conv_step.alloc(n_inst);
+    rel.alloc(n_inst);
+    step_ctr.alloc(1);
+    n_active.alloc(1);
+    active.alloc(n_inst);
+    std::vector<int> ones(n_inst, 1);
+    active.upload(ones);
+    std::vector<double*> sp(5, nullptr);
+    for (int f = 0; f < 5; ++f) sp[f] = snap[f].p;
+    snap_ptrs.upload(sp);
+    PECS_CUDA(cudaDeviceSynchronize());
+    setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+
+  void upload_tables() {
+    const CarrierTables& ct = S->ct;
+    const PoissonTables& pt = S->pt;
+    t_phi.upload(ct.phi);
+    t_qw.upload(ct.qw);
+    t_fphi.upload(ct.fphi);
+    t_fw.upload(ct.fw);
+    t_psix.upload(pt.psi_x);
+    t_psiy.upload(pt.psi_y);
+    t_phiP.upload(pt.phi);
+    std::vector<double> mref(ct.n1 * ct.n1, 0.0);
+    for (int a = 0; a < ct.n1; ++a)
+      for (int b = 0; b < ct.n1; ++b)
+        for (int q = 0; q < ct.Q; ++q) mref[a * ct.n1 + b] += ct.phi[a * ct.Q + q] * ct.phi[b * ct.Q + q] * ct.qw[q];
+    t_mref.upload(mref);
+    T = Tables{t_phi.p, t_qw.p, t_fphi.p, t_fw.p, t_psix.p, t_psiy.p, t_phiP.p, t_mref.p};
+  }
+
+  void upload_regions() {
+    const int nrt = S->n_rt, nphi = S->n_phi, nloc = nrt + nphi;
+    const pecs_params& P0 = S->inst[0];
+    for (int r = 0; r < (full ? 2 : 1); ++r) {
+      const CarrierSystem& CS = r == 0 ? S->semi : S->elec;
+      const Grid& g = CS.grid;
+      const std::vector<int>& c2p = r == 0 ? S->s2p : S->e2p;
+      const int nc = g.nc();
+      std::vector<double2> h(nc);
+      std::vector<int4> bid(nc);
+      std::vector<int> rt(nc * nrt), phid(nc * nphi), partner(nc, -1), ifc(nc, -1);
+      for (int K = 0; K < nc; ++K) {
+        double x0, y0, hx, hy;
+        g.geom(K, x0, y0, hx, hy);
+        h[K] = make_double2(hx, hy);
+        bid[K] = make_int4(g.face_bid(K, 0), g.face_bid(K, 1), g.face_bid(K, 2), g.face_bid(K, 3));
+        const int pc = c2p[K];
+        for (int b = 0; b < nrt; ++b) rt[K * nrt + b] = S->pois.l2g[pc * nloc + b];
+        for (int a = 0; a < nphi; ++a) phid[K * nphi + a] = S->pois.l2g[pc * nloc + nrt + a];
+      }
+      const std::vector<int>& mine = r == 0 ? S->iface_semi : S->iface_elec;
+      const std::vector<int>& other = r == 0 ? S->iface_elec : S->iface_semi;
+      for (size_t t = 0; t < mine.size(); ++t) {
+        partner[mine[t]] = other[t];
+        ifc[mine[t]] = (int)t;
+      }
+      h_[r].upload(h);
+      bid_[r].upload(bid);
+      rt_[r].upload(rt);
+      phid_[r].upload(phid);
+      partner_[r].upload(partner);
+      iface_[r].upload(ifc);
+      RegionDev& D = R[r];
+      D.nc = nc;
+      D.nd = CS.ndofs;
+      D.field1 = r == 0 ? 0 : 2;
+      D.is_semi = r == 0;
+      D.iface_face = r == 0 ? kRight : kLeft;
+      D.partner_face = r == 0 ? kLeft : kRight;
+      D.inv_eps = 1.0 / (r == 0 ? P0.eps_semi : P0.eps_elec);
+      D.inv_dt = 1.0 / P0.dt;
+      D.h = h_[r].p;
+      D.bid = bid_[r].p;
+      D.rt = rt_[r].p;
+      D.phid = phid_[r].p;
+      D.partner = partner_[r].p;
+      D.iface = iface_[r].p;
+    }
+    if (!full) R[1] = R[0];
+    std::vector<InstDev> ip(n_inst);
+    for (int i = 0; i < n_inst; ++i) {
+      const pecs_params& p = S->inst[i];
+      ip[i] = InstDev{p.k_et, p.k_ht, p.tau_n, p.tau_p, p.n_i, p.s_n, p.s_p, p.srh, 0};
+    }
+    inst.upload(ip);
+    std::vector<double> a, b, c, d;
+    for (int i = 0; i < n_inst; ++i) {
+      a.insert(a.end(), S->iface_ne[i].begin(), S->iface_ne[i].end());
+      b.insert(b.end(), S->iface_pe[i].begin(), S->iface_pe[i].end());
+      if (S->has_schottky) {
+        c.insert(c.end(), S->schottky_ne[i].begin(), S->schottky_ne[i].end());
+        d.insert(d.end(), S->schottky_pe[i].begin(), S->schottky_pe[i].end());
+      }
+    }
+    iface_ne.upload(a);
+    iface_pe.upload(b);
+    sch_ne.upload(c);
+    sch_pe.upload(d);
+    isemi.upload(S->iface_semi);
+    ielec.upload(S->iface_elec);
+  }
+
+  // ---- stages ------------------------------------------------------------
+  int nxt() const { return cur ^ 1; }
+
+  void launch_carrier_rhs(cudaStream_t s, const int* act) {
+    FieldPtrs F = fields(state[cur], rhs);
+    const int ntot = 2 * R[0].nc + (full ? 2 * R[1].nc : 0);
+    dim3 grid((ntot + 127) / 128, n_inst);
+    const int nif = (int)S->iface_semi.size();
+    const double* sne = S->has_schottky ? sch_ne.p : nullptr;
+    const double* spe = S->has_schottky ? sch_pe.p : nullptr;
+    if (S->k == 1)
+      k_carrier_rhs<1><<<grid, 128, 0, s>>>(T, R[0], R[1], full ? 2 : 1, F, inst.p, iface_ne.p,
+                                            iface_pe.p, nif, sne, spe, act);
+    else
+      k_carrier_rhs<2><<<grid, 128, 0, s>>>(T, R[0], R[1], full ? 2 : 1, F, inst.p, iface_ne.p,
+                                            iface_pe.p, nif, sne, spe, act);
+    PECS_CUDA(cudaGetLastError());
+  }
+
+  void launch_poisson_rhs(cudaStream_t s, const DBuf<double>* carriers, const int* act) {
+    FieldPtrs F = fields(carriers, rhs);
+    const int ncells = R[0].nc + (full ? R[1].nc : 0);
+    const int n = std::max(ncells, S->pois.n_rt_total);
+    dim3 grid((n + 127) / 128, n_inst);
+    if (S->k == 1)
+      k_poisson_rhs<1><<<grid, 128, 0, s>>>(T, R[0], R[1], full ? 2 : 1, F, S->pois.n_rt_total, act);
+    else
+      k_poisson_rhs<2><<<grid, 128, 0, s>>>(T, R[0], R[1], full ? 2 : 1, F, S->pois.n_rt_total, act);
+    PECS_CUDA(cudaGetLastError());
+  }
+
+  // Device vector lists for the refinement sweeps, key = target*8 + first field.
+  struct IrLists {
+    DBuf<const double*> b, x, d;
+    DBuf<double*> out, xw;
+    DBuf<int> mat, vin;
+    int nv = 0, n = 0;
+  };
+  IrLists ir[2][2];  // [target][0 carriers, 1 Poisson]
+
+  void prepare_ir() {
+    for (int target = 0; target < 2; ++target)
+      for (int which = 0; which < 2; ++which) {
+        std::vector<int> flds = which ? std::vector<int>{4} : carrier_fields();
+        std::vector<const double*> hb, hx, hd;
+        std::vector<double*> hout, hxw;
+        std::vector<int> hm, hi;
+        int n = 0;
+        for (int i = 0; i < n_inst; ++i)
+          for (int f : flds) {
+            hb.push_back(rhs[f].p + (size_t)i * nd[f]);
+            hx.push_back(state[target][f].p + (size_t)i * nd[f]);
+            hout.push_back(res[f].p + (size_t)i * nd[f]);
+            hxw.push_back(state[target][f].p + (size_t)i * nd[f]);
+            hd.push_back(delta[f].p + (size_t)i * nd[f]);
+            hm.push_back(f);
+            hi.push_back(i);
+            n = std::max(n, nd[f]);
+          }
+        IrLists& L = ir[target][which];
+        L.b.upload(hb);
+        L.x.upload(hx);
+        L.d.upload(hd);
+        L.out.upload(hout);
+        L.xw.upload(hxw);
+        L.mat.upload(hm);
+        L.vin.upload(hi);
+        L.nv = (int)hb.size();
+        L.n = n;
+      }
+  }
+
+  // x = A^-1 b into state[target]; FP32 factors add FP64-residual refinement sweeps.
+  void solve_bank(const FactorBank& bank, SetTable (&tab)[2][2], int target, int which,
+                  cudaStream_t s, const int* act) {
+    bank.solve(tab[target][0].view, tab[target][0].max_nrhs, s);
+    if (opt.precision != PECS_PREC_FP32_IR) return;
+    const int iters = opt.ir_max_iters > 0 ? opt.ir_max_iters : 2;
+    IrLists& L = ir[target][which];
+    VecList V{L.b.p, L.x.p, L.out.p, L.mat.p};
+    for (int it = 0; it < iters; ++it) {
+      k_residual<<<dim3((L.n + 127) / 128, L.nv), 128, 0, s>>>(csr, V, L.n, act, L.vin.p);
+      PECS_CUDA(cudaGetLastError());
+      bank.solve(tab[target][1].view, tab[target][1].max_nrhs, s);
+      k_axpy<<<dim3((L.n + 255) / 256, L.nv), 256, 0, s>>>(L.xw.p, L.d.p, L.n, act, L.vin.p);
+      PECS_CUDA(cudaGetLastError());
+    }
+  }
+
+  std::vector<int> carrier_fields() const {
+    return full ? std::vector<int>{0, 1, 2, 3} : std::vector<int>{0, 1};
+  }
+
+  void stage_carrier_rhs(cudaStream_t s, const int* act) { launch_carrier_rhs(s, act); }
+  void stage_solve_carriers(cudaStream_t s, const int* act) {
+    solve_bank(bank_c, tab_c, nxt(), 0, s, act);
+    carriers_advanced = true;
+  }
+  void stage_poisson_rhs(cudaStream_t s, const int* act) {
+    launch_poisson_rhs(s, carriers_advanced ? state[nxt()] : state[cur], act);
+  }
+  void stage_solve_poisson(cudaStream_t s, const int* act) {
+    const int target = carriers_advanced ? nxt() : cur;
+    solve_bank(bank_p, tab_p, target, 1, s, act);
+    if (carriers_advanced) {
+      cur = nxt();
+      carriers_advanced = false;
+    }
+  }
+
+  void full_step(cudaStream_t s, const int* act) {
+    stage_carrier_rhs(s, act);
+    stage_solve_carriers(s, act);
+    stage_poisson_rhs(s, act);
+    stage_solve_poisson(s, act);
+  }
+
+  // step + steady-state bookkeeping (state[cur] -> state[nxt], compares both)
+  void step_with_check(cudaStream_t s, double tol) {
+    const int old = cur;
+    full_step(s, active.p);
+    FieldPtrs NEW = fields(state[cur], nullptr), OLD = fields(state[old], nullptr);
+    k_relchange_partial<<<dim3(kRedChunks, 5, n_inst), kRedThreads, 0, s>>>(NEW, OLD, n_fields, partial.p);
+    PECS_CUDA(cudaGetLastError());
+    k_converge<<<1, 256, 0, s>>>(partial.p, n_inst, n_fields, tol, conv_step.p, rel.p, step_ctr.p,
+                                 active.p, n_active.p);
+    PECS_CUDA(cudaGetLastError());
+    k_snapshot<<<dim3(32, 5, n_inst), 256, 0, s>>>(NEW, snap_ptrs.p, conv_step.p, step_ctr.p, 5);
+    PECS_CUDA(cudaGetLastError());
+  }
+
+  void initialize() {
+    for (int f = 0; f < 4; ++f) {
+      if (nd[f] == 0) continue;
+      std::vector<double> v;
+      for (int i = 0; i < n_inst; ++i) v.insert(v.end(), S->init[f][i].begin(), S->init[f][i].end());
+      PECS_CUDA(cudaMemcpyAsync(state[cur][f].p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, st));
+      PECS_CUDA(cudaStreamSynchronize(st));
+    }
+    carriers_advanced = false;
+    stage_poisson_rhs(st, nullptr);
+    stage_solve_poisson(st, nullptr);
+    PECS_CUDA(cudaStreamSynchronize(st));
+    initialized = true;
+  }
+
+  void reset_convergence() {
+    std::vector<int> ones(n_inst, 1), zeros(n_inst, 0);
+    PECS_CUDA(cudaMemcpyAsync(active.p, ones.data(), n_inst * 4, cudaMemcpyHostToDevice, st));
+    PECS_CUDA(cudaMemcpyAsync(conv_step.p, zeros.data(), n_inst * 4, cudaMemcpyHostToDevice, st));
+    PECS_CUDA(cudaMemsetAsync(step_ctr.p, 0, 4, st));
+    PECS_CUDA(cudaStreamSynchronize(st));
+  }
+
+  void capture_graph(double tol) {
+    const int saved = cur;
+    for (int par = 0; par < 2; ++par) {
+      if (graph2[par]) {
+        cudaGraphExecDestroy(graph2[par]);
+        graph2[par] = nullptr;
+      }
+      cudaGraph_t g;
+      cur = par;
+      PECS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      try {
+        step_with_check(st, tol);
+        step_with_check(st, tol);
+      } catch (...) {
+        cudaStreamEndCapture(st, &g);
+        cur = saved;
+        throw;
+      }
+      PECS_CUDA(cudaStreamEndCapture(st, &g));
+      PECS_CUDA(cudaGraphInstantiate(&graph2[par], g, 0));
+      cudaGraphDestroy(g);
+    }
+    cur = saved;  // two steps return the ping-pong index to where it was
+    graph_tol = tol;
+    graph_valid = true;
+  }
+  double graph_tol = -1.0;
+
+  void run_to_steady(int max_steps, double tol, int check_every, int* steps, double* relc) {
+    if (!initialized) throw PecsError(PECS_E_STATE, "pecs_initialize must be called first");
+    if (max_steps < 0) throw PecsError(PECS_E_ARG, "max_steps < 0");
+    if (check_every <= 0) check_every = 50;
+    check_every += check_every & 1;
+    reset_convergence();
+    const bool use_graph = opt.use_graphs != 0;
+    if (use_graph && (!graph_valid || graph_tol != tol)) capture_graph(tol);
+    int done = 0;
+    int h_active = n_inst;
+    while (done < max_steps && h_active > 0) {
+      const int chunk = std::min(check_every, max_steps - done);
+      int k = 0;
+      for (; k + 2 <= chunk; k += 2) {
+        if (use_graph)
+          PECS_CUDA(cudaGraphLaunch(graph2[cur], st));
+        else {
+          step_with_check(st, tol);
+          step_with_check(st, tol);
+        }
+      }
+      if (k < chunk) {  // odd remainder
+        step_with_check(st, tol);
+        ++k;
+      }
+      done += k;
+      PECS_CUDA(cudaMemcpyAsync(&h_active, n_active.p, 4, cudaMemcpyDeviceToHost, st));
+      PECS_CUDA(cudaStreamSynchronize(st));
+    }
+    // instances that converged: restore their snapshot into the current state
+    std::vector<int> cs(n_inst);
+    std::vector<double> rl(n_inst);
+    PECS_CUDA(cudaMemcpy(cs.data(), conv_step.p, n_inst * 4, cudaMemcpyDeviceToHost));
+    PECS_CUDA(cudaMemcpy(rl.data(), rel.p, n_inst * 8, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n_inst; ++i) {
+      if (cs[i] != 0) {
+        for (int f = 0; f < 5; ++f)
+          if (nd[f])
+            PECS_CUDA(cudaMemcpyAsync(state[cur][f].p + (size_t)i * nd[f], snap[f].p + (size_t)i * nd[f],
+                                      (size_t)nd[f] * 8, cudaMemcpyDeviceToDevice, st));
+      }
+      if (steps) steps[i] = cs[i] > 0 ? cs[i] : (cs[i] < 0 ? cs[i] : done);
+      if (relc) relc[i] = rl[i];
+    }
+    PECS_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < n_inst; ++i)
+      if (cs[i] < 0)
+        throw PecsError(PECS_E_NONFINITE, "instance " + std::to_string(i) +
+                                              " produced a non-finite state at step " +
+                                              std::to_string(-cs[i]));
+  }
+
+  void interface_current(double* out) {
+    std::vector<double> h(n_inst, 0.0);
+    if (full && !S->iface_semi.empty()) {
+      DBuf<double> d;
+      d.alloc(n_inst);
+      FieldPtrs F = fields(carriers_advanced ? state[nxt()] : state[cur], nullptr);
+      k_interface_current<<<n_inst, kRedThreads, 0, st>>>(T, R[0], R[1], F, inst.p, iface_ne.p, iface_pe.p,
+                                                         isemi.p, ielec.p, (int)S->iface_semi.size(),
+                                                         S->n1, S->nq1, d.p);
+      PECS_CUDA(cudaGetLastError());
+      PECS_CUDA(cudaMemcpyAsync(h.data(), d.p, n_inst * 8, cudaMemcpyDeviceToHost, st));
+      PECS_CUDA(cudaStreamSynchronize(st));
+    }
+    std::copy(h.begin(), h.end(), out);
+  }
+
+  const DBuf<double>& latest(int f) const {
+    if (f < 4 && carriers_advanced) return state[nxt()][f];
+    return state[cur][f];
+  }
+};
+
+struct LuHandle {
+  MfFactor F;
+  int precision = PECS_PREC_FP64;
+  bool uploaded = false;
+  FactorBank bank;
+  int nrhs_cap = 0;
+  DBuf<double> b, y, x;
+  std::vector<DBuf<double>> w;
+  SetTable tab;
+  cudaStream_t st = nullptr;
+  ~LuHandle() {
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+}  // namespace pecs
+
+using namespace pecs;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct pecs_ctx {
+  Engine e;
+};
+struct pecs_lu {
+  LuHandle h;
+};
+
+#define PECS_TRY(...)                                   \
+  try {                                                 \
+    __VA_ARGS__;                                        \
+    return PECS_OK;                                     \
+  } catch (const PecsError& ex) {                       \
+    set_error(ex.what());                               \
+    return ex.code;                                     \
+  } catch (const std::bad_alloc&) {                     \
+    set_error("out of host memory");                    \
+    return PECS_E_ARG;                                  \
+  } catch (const std::exception& ex) {                  \
+    set_error(ex.what());                               \
+    return PECS_E_ARG;                                  \
+  }
+
+static void need_device(Engine& e) {
+  if (e.host_only) throw PecsError(PECS_E_STATE, "context was created with host_setup_only");
+}
+
+extern "C" {
+
+const char* pecs_last_error(void) { return g_last_error.c_str(); }
+
+void pecs_default_options(pecs_options* opt) {
+  if (!opt) return;
+  std::memset(opt, 0, sizeof(*opt));
+  opt->precision = PECS_PREC_FP64;
+  opt->leaf_cells = 8;
+  opt->use_graphs = 1;
+  opt->ir_max_iters = 2;
+  opt->ir_tol = 1e-12;
+  opt->device = 0;
+}
+
+int pecs_create(const pecs_params* params, int n_inst, const pecs_options* opt, pecs_ctx** out) {
+  PECS_TRY({
+    if (!out) throw PecsError(PECS_E_ARG, "out is NULL");
+    *out = nullptr;
+    std::string err = validate_params(params, n_inst);
+    if (!err.empty()) throw PecsError(PECS_E_ARG, err);
+    pecs_options o;
+    pecs_default_options(&o);
+    if (opt) o = *opt;
+    if (o.precision != PECS_PREC_FP64 && o.precision != PECS_PREC_FP32_IR)
+      throw PecsError(PECS_E_ARG, "unknown precision");
+    std::unique_ptr<pecs_ctx> c(new pecs_ctx());
+    c->e.create(std::vector<pecs_params>(params, params + n_inst), o);
+    *out = c.release();
+  })
+}
+
+void pecs_destroy(pecs_ctx* ctx) { delete ctx; }
+
+int pecs_get_info(pecs_ctx* ctx, pecs_info* info) {
+  PECS_TRY({
+    if (!ctx || !info) throw PecsError(PECS_E_ARG, "NULL argument");
+    Engine& e = ctx->e;
+    std::memset(info, 0, sizeof(*info));
+    info->n_inst = e.n_inst;
+    for (int f = 0; f < 5; ++f) info->ndofs[f] = e.nd[f];
+    long long es = 0, ee = 0;
+    int ls = 0, le = 0, ns = 0, ne = 0;
+    for (int t = 0; t < e.n_fs; ++t) {
+      es += e.fs[t].entries();
+      ls = std::max(ls, std::max(e.fs[t].n_heights, e.fs[t].n_depths));
+      ns += (int)e.fs[t].nodes.size();
+    }
+    for (int t = 0; t < e.n_fe; ++t) {
+      ee += e.fe[t].entries();
+      le = std::max(le, std::max(e.fe[t].n_heights, e.fe[t].n_depths));
+      ne += (int)e.fe[t].nodes.size();
+    }
+    info->factor_entries[0] = es;
+    info->factor_entries[1] = ee;
+    info->factor_entries[2] = e.fp.entries();
+    info->factor_levels[0] = ls;
+    info->factor_levels[1] = le;
+    info->factor_levels[2] = std::max(e.fp.n_heights, e.fp.n_depths);
+    info->factor_nodes[0] = ns;
+    info->factor_nodes[1] = ne;
+    info->factor_nodes[2] = (int)e.fp.nodes.size();
+    info->factor_bytes = e.bank_c.bytes() + e.bank_p.bytes();
+    info->setup_seconds = e.setup_seconds;
+    info->n_distinct_carrier_factors = e.n_fs + e.n_fe;
+  })
+}
+
+int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowptr, int* col,
+                    double* val) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    Setup& S = *ctx->e.S;
+    const Csr* A = nullptr;
+    switch (which) {
+      case PECS_MAT_N: A = &S.semi.A[0]; break;
+      case PECS_MAT_P: A = &S.semi.A[1]; break;
+      case PECS_MAT_R: A = S.full ? &S.elec.A[0] : nullptr; break;
+      case PECS_MAT_O: A = S.full ? &S.elec.A[1] : nullptr; break;
+      case PECS_MAT_POISSON: A = &S.pois.A; break;
+      case PECS_MAT_MASS_SEMI: A = &S.semi.M; break;
+      case PECS_MAT_MASS_ELEC: A = S.full ? &S.elec.M : nullptr; break;
+      default: break;
+    }
+    if (!A) throw PecsError(PECS_E_ARG, "no such matrix");
+    if (n) *n = A->n;
+    if (nnz) *nnz = A->nnz();
+    if (rowptr) std::copy(A->rowptr.begin(), A->rowptr.end(), rowptr);
+    if (col) std::copy(A->col.begin(), A->col.end(), col);
+    if (val) std::copy(A->val.begin(), A->val.end(), val);
+  })
+}
+
+int pecs_initialize(pecs_ctx* ctx) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    ctx->e.initialize();
+  })
+}
+
+static void check_field(Engine& e, int inst, int field, size_t n) {
+  need_device(e);
+  if (inst < 0 || inst >= e.n_inst) throw PecsError(PECS_E_ARG, "instance out of range");
+  if (field < 0 || field > 4 || e.nd[field] == 0) throw PecsError(PECS_E_ARG, "field out of range");
+  if (n != (size_t)e.nd[field]) throw PecsError(PECS_E_ARG, "length does not match the field size");
+}
+
+int pecs_set_state(pecs_ctx* ctx, int inst, int field, const double* host, size_t n) {
+  PECS_TRY({
+    if (!ctx || !host) throw PecsError(PECS_E_ARG, "NULL argument");
+    Engine& e = ctx->e;
+    check_field(e, inst, field, n);
+    if (e.carriers_advanced) throw PecsError(PECS_E_STATE, "step in progress");
+    PECS_CUDA(cudaMemcpyAsync(e.state[e.cur][field].p + (size_t)inst * e.nd[field], host, n * 8,
+                              cudaMemcpyHostToDevice, e.st));
+    PECS_CUDA(cudaStreamSynchronize(e.st));
+    e.initialized = true;
+  })
+}
+
+int pecs_get_state(pecs_ctx* ctx, int inst, int field, double* host, size_t n) {
+  PECS_TRY({
+    if (!ctx || !host) throw PecsError(PECS_E_ARG, "NULL argument");
+    Engine& e = ctx->e;
+    check_field(e, inst, field, n);
+    PECS_CUDA(cudaMemcpyAsync(host, e.latest(field).p + (size_t)inst * e.nd[field], n * 8,
+                              cudaMemcpyDeviceToHost, e.st));
+    PECS_CUDA(cudaStreamSynchronize(e.st));
+  })
+}
+
+int pecs_get_rhs(pecs_ctx* ctx, int inst, int field, double* host, size_t n) {
+  PECS_TRY({
+    if (!ctx || !host) throw PecsError(PECS_E_ARG, "NULL argument");
+    Engine& e = ctx->e;
+    check_field(e, inst, field, n);
+    PECS_CUDA(cudaMemcpyAsync(host, e.rhs[field].p + (size_t)inst * e.nd[field], n * 8,
+                              cudaMemcpyDeviceToHost, e.st));
+    PECS_CUDA(cudaStreamSynchronize(e.st));
+  })
+}
+
+int pecs_assemble_carrier_rhs(pecs_ctx* ctx) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    if (ctx->e.carriers_advanced) throw PecsError(PECS_E_STATE, "carriers already advanced");
+    ctx->e.stage_carrier_rhs(ctx->e.st, nullptr);
+    PECS_CUDA(cudaStreamSynchronize(ctx->e.st));
+  })
+}
+
+int pecs_solve_carriers(pecs_ctx* ctx) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    if (ctx->e.carriers_advanced) throw PecsError(PECS_E_STATE, "carriers already advanced");
+    ctx->e.stage_solve_carriers(ctx->e.st, nullptr);
+    PECS_CUDA(cudaStreamSynchronize(ctx->e.st));
+  })
+}
+
+int pecs_assemble_poisson_rhs(pecs_ctx* ctx) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    ctx->e.stage_poisson_rhs(ctx->e.st, nullptr);
+    PECS_CUDA(cudaStreamSynchronize(ctx->e.st));
+  })
+}
+
+int pecs_solve_poisson(pecs_ctx* ctx) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    ctx->e.stage_solve_poisson(ctx->e.st, nullptr);
+    PECS_CUDA(cudaStreamSynchronize(ctx->e.st));
+  })
+}
+
+int pecs_step(pecs_ctx* ctx, int n_steps) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    if (n_steps < 0) throw PecsError(PECS_E_ARG, "n_steps < 0");
+    Engine& e = ctx->e;
+    if (!e.initialized) throw PecsError(PECS_E_STATE, "pecs_initialize must be called first");
+    if (e.carriers_advanced) throw PecsError(PECS_E_STATE, "step in progress");
+    for (int s = 0; s < n_steps; ++s) e.full_step(e.st, nullptr);
+    PECS_CUDA(cudaStreamSynchronize(e.st));
+  })
+}
+
+int pecs_run_to_steady_state(pecs_ctx* ctx, int max_steps, double tol, int check_every, int* steps,
+                             double* rel_change) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    if (!(tol >= 0.0)) throw PecsError(PECS_E_ARG, "tol must be >= 0");
+    ctx->e.run_to_steady(max_steps, tol, check_every, steps, rel_change);
+  })
+}
+
+int pecs_interface_current(pecs_ctx* ctx, double* out) {
+  PECS_TRY({
+    if (!ctx || !out) throw PecsError(PECS_E_ARG, "NULL argument");
+    need_device(ctx->e);
+    ctx->e.interface_current(out);
+  })
+}
+
+int pecs_iv_sweep(pecs_ctx* ctx, const double* const* init_fields, int max_steps, double tol,
+                  int check_every, double* currents, int* steps, double* const* final_fields) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    Engine& e = ctx->e;
+    if (init_fields) {
+      e.carriers_advanced = false;
+      for (int f = 0; f < 5; ++f) {
+        if (!e.nd[f]) continue;
+        if (!init_fields[f]) throw PecsError(PECS_E_ARG, "init_fields entry is NULL");
+        PECS_CUDA(cudaMemcpyAsync(e.state[e.cur][f].p, init_fields[f], (size_t)e.n_inst * e.nd[f] * 8,
+                                  cudaMemcpyHostToDevice, e.st));
+      }
+      PECS_CUDA(cudaStreamSynchronize(e.st));
+      e.initialized = true;
+    } else {
+      e.initialize();
+    }
+    e.run_to_steady(max_steps, tol, check_every, steps, nullptr);
+    if (currents) e.interface_current(currents);
+    if (final_fields) {
+      for (int f = 0; f < 5; ++f) {
+        if (!e.nd[f] || !final_fields[f]) continue;
+        PECS_CUDA(cudaMemcpyAsync(final_fields[f], e.state[e.cur][f].p, (size_t)e.n_inst * e.nd[f] * 8,
+                                  cudaMemcpyDeviceToHost, e.st));
+      }
+      PECS_CUDA(cudaStreamSynchronize(e.st));
+    }
+  })
+}
+
+int pecs_synchronize(pecs_ctx* ctx) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    need_device(ctx->e);
+    PECS_CUDA(cudaStreamSynchronize(ctx->e.st));
+  })
+}
+
+// ---- drop-in direct solver -------------------------------------------------
+int pecs_lu_factor(int n, const int* rowptr, const int* col, const double* val, const int* dof_cell,
+                   const int* dof_class, int n_cells, const double* cell_xy, int precision,
+                   int leaf_cells, pecs_lu** out) {
+  PECS_TRY({
+    if (!out) throw PecsError(PECS_E_ARG, "out is NULL");
+    *out = nullptr;
+    if (n <= 0 || !rowptr || !col || !val || !dof_cell || n_cells <= 0 || !cell_xy)
+      throw PecsError(PECS_E_ARG, "invalid matrix arguments");
+    if (precision != PECS_PREC_FP64 && precision != PECS_PREC_FP32_IR)
+      throw PecsError(PECS_E_ARG, "unknown precision");
+    if (rowptr[0] != 0 || rowptr[n] < 0) throw PecsError(PECS_E_ARG, "bad rowptr");
+    Csr A;
+    A.n = n;
+    A.rowptr.assign(rowptr, rowptr + n + 1);
+    A.col.assign(col, col + rowptr[n]);
+    A.val.assign(val, val + rowptr[n]);
+    std::unique_ptr<pecs_lu> h(new pecs_lu());
+    h->h.precision = precision;
+    h->h.F = mf_analyze(A, dof_cell, dof_class, n_cells, cell_xy, leaf_cells);
+    try {
+      mf_factorize(h->h.F, A);
+    } catch (const std::exception& ex) {
+      throw PecsError(PECS_E_SINGULAR, ex.what());
+    }
+    *out = h.release();
+  })
+}
+
+static void lu_upload(LuHandle& h, int nrhs) {
+  if (!h.uploaded) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+      throw PecsError(PECS_E_NODEVICE, "no CUDA device available");
+    PECS_CUDA(cudaStreamCreateWithFlags(&h.st, cudaStreamNonBlocking));
+    h.bank.build({&h.F}, h.precision == PECS_PREC_FP64 ? PECS_PREC_FP64 : PECS_PREC_FP32_IR);
+    h.uploaded = true;
+  }
+  if (nrhs > h.nrhs_cap) {
+    const int n = h.F.n;
+    h.b.alloc((size_t)nrhs * n);
+    h.y.alloc((size_t)nrhs * n);
+    h.x.alloc((size_t)nrhs * n);
+    h.w.resize(nrhs);
+    for (auto& w : h.w) {
+      w.alloc(h.bank.set_wtotal(0));
+      w.zero();
+    }
+    h.nrhs_cap = nrhs;
+  }
+}
+
+static void lu_bind(LuHandle& h, int nrhs, const double* b, double* x) {
+  const int n = h.F.n;
+  std::vector<double*> hb(nrhs), hy(nrhs), hw(nrhs), hx(nrhs);
+  for (int r = 0; r < nrhs; ++r) {
+    hb[r] = const_cast<double*>(b) + (size_t)r * n;
+    hy[r] = h.y.p + (size_t)r * n;
+    hw[r] = h.w[r].p;
+    hx[r] = x + (size_t)r * n;
+  }
+  h.tab.b.resize(1);
+  h.tab.y.resize(1);
+  h.tab.w.resize(1);
+  h.tab.x.resize(1);
+  h.tab.b[0].upload(hb);
+  h.tab.y[0].upload(hy);
+  h.tab.w[0].upload(hw);
+  h.tab.x[0].upload(hx);
+  h.tab.view.set[0] = SetView{nrhs, h.tab.b[0].p, h.tab.y[0].p, h.tab.w[0].p, h.tab.x[0].p};
+  h.tab.max_nrhs = nrhs;
+}
+
+int pecs_lu_solve_device(pecs_lu* lu, int nrhs, const double* b_dev, double* x_dev, void* stream) {
+  PECS_TRY({
+    if (!lu || nrhs <= 0 || !b_dev || !x_dev) throw PecsError(PECS_E_ARG, "invalid arguments");
+    LuHandle& h = lu->h;
+    lu_upload(h, nrhs);
+    lu_bind(h, nrhs, b_dev, x_dev);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h.st;
+    h.bank.solve(h.tab.view, nrhs, s);
+    PECS_CUDA(cudaStreamSynchronize(s));
+  })
+}
+
+int pecs_lu_solve(pecs_lu* lu, int nrhs, const double* b, double* x) {
+  PECS_TRY({
+    if (!lu || nrhs <= 0 || !b || !x) throw PecsError(PECS_E_ARG, "invalid arguments");
+    LuHandle& h = lu->h;
+    lu_upload(h, nrhs);
+    const size_t bytes = (size_t)nrhs * h.F.n * 8;
+    PECS_CUDA(cudaMemcpyAsync(h.b.p, b, bytes, cudaMemcpyHostToDevice, h.st));
+    lu_bind(h, nrhs, h.b.p, h.x.p);
+    h.bank.solve(h.tab.view, nrhs, h.st);
+    PECS_CUDA(cudaMemcpyAsync(x, h.x.p, bytes, cudaMemcpyDeviceToHost, h.st));
+    PECS_CUDA(cudaStreamSynchronize(h.st));
+  })
+}
+
+int pecs_lu_stats(pecs_lu* lu, long long* entries, int* levels, int* nodes, int* max_front) {
+  PECS_TRY({
+    if (!lu) throw PecsError(PECS_E_ARG, "lu is NULL");
+    const MfFactor& F = lu->h.F;
+    if (entries) *entries = F.entries();
+    if (levels) *levels = std::max(F.n_heights, F.n_depths);
+    if (nodes) *nodes = (int)F.nodes.size();
+    if (max_front) *max_front = F.max_front();
+  })
+}
+
+void pecs_lu_destroy(pecs_lu* lu) { delete lu; }
+
+// diagnostic: apply the host copy of the factors (no GPU involved)
+int pecs_lu_host_apply(pecs_lu* lu, const double* b, double* x) {
+  PECS_TRY({
+    if (!lu || !b || !x) throw PecsError(PECS_E_ARG, "invalid arguments");
+    if (lu->h.F.Gf.empty()) throw PecsError(PECS_E_STATE, "host factors were released");
+    mf_apply_host(lu->h.F, b, x);
+  })
+}
+
+}  // extern "C"

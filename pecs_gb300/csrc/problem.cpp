@@ -1,0 +1,745 @@
+// Host-side setup of the PECS problem (see problem.hpp).
+#include "problem.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <sstream>
+#include <stdexcept>
+#include <tuple>
+
+namespace pecs {
+
+Csr coo_to_csr(int n, const std::vector<int>& r, const std::vector<int>& c,
+               const std::vector<double>& v) {
+  Csr A;
+  A.n = n;
+  std::vector<int> cnt(n + 1, 0);
+  for (int x : r) cnt[x + 1]++;
+  for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+  std::vector<int> cc(r.size());
+  std::vector<double> vv(r.size());
+  for (size_t t = 0; t < r.size(); ++t) {
+    int p = pos[r[t]]++;
+    cc[p] = c[t];
+    vv[p] = v[t];
+  }
+  A.rowptr.assign(n + 1, 0);
+  std::vector<std::pair<int, double>> row;
+  for (int i = 0; i < n; ++i) {
+    row.clear();
+    for (int p = cnt[i]; p < cnt[i + 1]; ++p) row.emplace_back(cc[p], vv[p]);
+    std::stable_sort(row.begin(), row.end(),
+                     [](const std::pair<int, double>& a, const std::pair<int, double>& b) {
+                       return a.first < b.first;
+                     });
+    for (size_t t = 0; t < row.size();) {
+      int col = row[t].first;
+      double s = 0.0;
+      while (t < row.size() && row[t].first == col) s += row[t++].second;
+      if (s == 0.0) continue;  // structural zeros of the flux pattern are not stored
+      A.col.push_back(col);
+      A.val.push_back(s);
+    }
+    A.rowptr[i + 1] = (int)A.col.size();
+  }
+  return A;
+}
+
+int Grid::face_bid(int K, int f) const {
+  int i = K % nx, j = K / nx;
+  if (f == kLeft && i == 0) return bc[0];
+  if (f == kRight && i == nx - 1) return bc[1];
+  if (f == kBottom && j == 0) return bc[2];
+  if (f == kTop && j == ny - 1) return bc[3];
+  return -1;
+}
+
+void Grid::geom(int K, double& x0, double& y0, double& hx, double& hy) const {
+  int i = K % nx, j = K / nx;
+  x0 = xs[i];
+  y0 = ys[j];
+  hx = xs[i + 1] - xs[i];
+  hy = ys[j + 1] - ys[j];
+}
+
+static Grid uniform(double x0, double x1, double y0, double y1, int nx, int ny, const int* bc,
+                    int material) {
+  Grid g;
+  g.nx = nx;
+  g.ny = ny;
+  g.xs.resize(nx + 1);
+  g.ys.resize(ny + 1);
+  // same arithmetic as numpy.linspace: x0 + i*step, last point exact
+  double sx = (x1 - x0) / nx, sy = (y1 - y0) / ny;
+  for (int i = 0; i <= nx; ++i) g.xs[i] = x0 + i * sx;
+  for (int j = 0; j <= ny; ++j) g.ys[j] = y0 + j * sy;
+  g.xs[nx] = x1;
+  g.ys[ny] = y1;
+  for (int f = 0; f < 4; ++f) g.bc[f] = bc[f];
+  g.material.assign(g.nc(), material);
+  return g;
+}
+
+// ---------------------------------------------------------------------------
+// Coefficient functions (reference: source/InitialConditions.cpp,
+// Generation.cpp:29-44, BiasValues.cpp:11-31,75-94, SolarCell.hpp:86-98)
+// ---------------------------------------------------------------------------
+static inline double pw(double x, const double v[2], double xj) { return x < xj ? v[0] : v[1]; }
+
+static double generation(const pecs_params& P, double x, double y) {
+  if (P.gen_kind == 0) return 0.0;
+  if (P.gen_kind == 1) return P.alpha * P.G0 * std::exp(P.alpha * (y - P.height));
+  return P.G0 * std::exp(-P.alpha * (P.x_semi1 - x));
+}
+
+static double potential_dirichlet(const pecs_params& P, double x, double /*y*/) {
+  return x == 0.0 ? (P.phi_bi - P.phi_app) : 0.0;
+}
+
+static double carrier_bc(const pecs_params& P, int field, double x, double /*y*/) {
+  switch (field) {
+    case 0: return pw(x, P.n_eq, P.junction_x);
+    case 1: return pw(x, P.p_eq, P.junction_x);
+    case 2: return P.r_eq;
+    default: return P.o_eq;
+  }
+}
+
+static double initial_profile(const pecs_params& P, int field, double x, double y) {
+  if (P.ic_kind == 1 && field == 0) return pw(x, P.nd, P.junction_x);
+  if (P.ic_kind == 1 && field == 1) return pw(x, P.na, P.junction_x);
+  return carrier_bc(P, field, x, y);
+}
+
+// ---------------------------------------------------------------------------
+// Local matrices
+// ---------------------------------------------------------------------------
+namespace {
+
+struct DofVals {  // values of one carrier local dof at points
+  const double *px, *py, *v;
+};
+
+// Carrier local dof i in [0, 3 n1): component and node.
+inline void carrier_comp(int i, int n1, int& comp, int& a) {
+  comp = i / n1;
+  a = i % n1;
+}
+
+// assemble_local_LDG_cell_and_bc_terms (source/LDG.cpp:85-281) on an
+// axis-aligned hx*hy cell.
+std::vector<double> ldg_cell_matrix(const CarrierTables& ct, double hx, double hy, double mu,
+                                    double dt, double tos, double pen_h, const int bids[4]) {
+  const int n1 = ct.n1, nd = 3 * n1, Q = ct.Q, nq = ct.nq1;
+  std::vector<double> A(nd * nd, 0.0);
+  for (int i = 0; i < nd; ++i) {
+    int ci, a;
+    carrier_comp(i, n1, ci, a);
+    for (int j = 0; j < nd; ++j) {
+      int cj, b;
+      carrier_comp(j, n1, cj, b);
+      double s = 0.0;
+      for (int q = 0; q < Q; ++q) {
+        double JxW = ct.qw[q] * hx * hy;
+        double phia = ct.phi[a * Q + q], phib = ct.phi[b * Q + q];
+        double dxa = ct.dphi_x[a * Q + q] / hx, dya = ct.dphi_y[a * Q + q] / hy;
+        double t = 0.0;
+        // (tos/dt) v u
+        if (ci == 2 && cj == 2) t += (tos / dt) * phia * phib;
+        // (1/mu) p . q
+        if (ci == cj && ci < 2) t += (1.0 / mu) * phia * phib;
+        // - div(p) u
+        if (cj == 2) {
+          if (ci == 0) t -= dxa * phib;
+          if (ci == 1) t -= dya * phib;
+        }
+        // - grad(v) . q
+        if (ci == 2) {
+          if (cj == 0) t -= dxa * phib;
+          if (cj == 1) t -= dya * phib;
+        }
+        s += t * JxW;
+      }
+      A[i * nd + j] = s;
+    }
+  }
+  for (int f = 0; f < 4; ++f) {
+    int bid = bids[f];
+    if (bid < 0) continue;
+    double flen = (f == kLeft || f == kRight) ? hy : hx;
+    const double nx_ = kFaceNormal[f][0], ny_ = kFaceNormal[f][1];
+    for (int i = 0; i < nd; ++i) {
+      int ci, a;
+      carrier_comp(i, n1, ci, a);
+      for (int j = 0; j < nd; ++j) {
+        int cj, b;
+        carrier_comp(j, n1, cj, b);
+        double s = 0.0;
+        for (int q = 0; q < nq; ++q) {
+          double Jf = ct.fw[q] * flen;
+          double fa = ct.fphi[(f * n1 + a) * nq + q], fb = ct.fphi[(f * n1 + b) * nq + q];
+          if (bid == kDirichlet) {
+            // v (n.q + pen/h u)
+            if (ci != 2) continue;
+            double nq_ = (cj == 0 ? nx_ * fb : 0.0) + (cj == 1 ? ny_ * fb : 0.0);
+            double uj = (cj == 2) ? fb : 0.0;
+            s += fa * (nq_ + pen_h * uj) * Jf;
+          } else {
+            // (p.n) u
+            if (cj != 2) continue;
+            double pn = (ci == 0 ? nx_ * fa : 0.0) + (ci == 1 ? ny_ * fa : 0.0);
+            s += pn * fb * Jf;
+          }
+        }
+        A[i * nd + j] += s;
+      }
+    }
+  }
+  return A;
+}
+
+// assemble_local_flux_terms (source/LDG.cpp:429-622); minus = left/bottom cell.
+void ldg_flux_blocks(const CarrierTables& ct, int fminus, int fplus, double flen, double pen_h,
+                     std::vector<double> blk[4]) {
+  const int n1 = ct.n1, nd = 3 * n1, nq = ct.nq1;
+  const double nx_ = kFaceNormal[fminus][0], ny_ = kFaceNormal[fminus][1];
+  const double beta = 1.0 / std::sqrt(2.0);  // beta = (1,1)/|(1,1)|
+  // per side, per dof: p.n, v, beta.p at face qp
+  auto vals = [&](int f, int i, int q, double& pn, double& v, double& bp) {
+    int c, a;
+    carrier_comp(i, n1, c, a);
+    double ph = ct.fphi[(f * n1 + a) * nq + q];
+    double px = c == 0 ? ph : 0.0, py = c == 1 ? ph : 0.0;
+    pn = px * nx_ + py * ny_;
+    v = c == 2 ? ph : 0.0;
+    bp = beta * px + beta * py;
+  };
+  const int sides[4][2] = {{fminus, fminus}, {fminus, fplus}, {fplus, fminus}, {fplus, fplus}};
+  const double sh[4] = {+1, +1, -1, -1}, sb[4] = {+1, -1, -1, +1}, sp[4] = {+1, -1, -1, +1};
+  for (int t = 0; t < 4; ++t) {
+    blk[t].assign(nd * nd, 0.0);
+    int ft = sides[t][0], fr = sides[t][1];
+    for (int i = 0; i < nd; ++i)
+      for (int j = 0; j < nd; ++j) {
+        double s = 0.0;
+        for (int q = 0; q < nq; ++q) {
+          double tpn, tv, tbp, rpn, rv, rbp;
+          vals(ft, i, q, tpn, tv, tbp);
+          vals(fr, j, q, rpn, rv, rbp);
+          double Jf = ct.fw[q] * flen;
+          double e = 0.5 * sh[t] * (tpn * rv + tv * rpn) + sb[t] * (tbp * rv - tv * rbp) +
+                     sp[t] * pen_h * tv * rv;
+          s += e * Jf;
+        }
+        blk[t][i * nd + j] = s;
+      }
+  }
+}
+
+// MixedFEM::assemble_local_Poisson_matrix (source/MixedFEM.cpp:29-164).
+std::vector<double> poisson_cell_matrix(const PoissonTables& pt, const CarrierTables& ct, double hx,
+                                        double hy, double eps, double lambda2) {
+  const int nr = pt.n_rt, np = pt.n_phi, nd = nr + np, Q = ct.Q;
+  std::vector<double> A(nd * nd, 0.0);
+  for (int i = 0; i < nd; ++i)
+    for (int j = 0; j < nd; ++j) {
+      double s = 0.0;
+      for (int q = 0; q < Q; ++q) {
+        double JxW = ct.qw[q] * hx * hy;
+        double t = 0.0;
+        if (i < nr && j < nr)
+          t = (1.0 / eps) * (pt.psi_x[i * Q + q] * pt.psi_x[j * Q + q] +
+                             pt.psi_y[i * Q + q] * pt.psi_y[j * Q + q]);
+        else if (i < nr && j >= nr)
+          t = -(pt.div_x[i * Q + q] / hx + pt.div_y[i * Q + q] / hy) * pt.phi[(j - nr) * Q + q];
+        else if (i >= nr && j < nr)
+          t = -lambda2 * pt.phi[(i - nr) * Q + q] *
+              (pt.div_x[j * Q + q] / hx + pt.div_y[j * Q + q] / hy);
+        s += t * JxW;
+      }
+      A[i * nd + j] = s;
+    }
+  return A;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+std::string validate_params(const pecs_params* p, int n_inst) {
+  std::ostringstream e;
+  if (!p) return "params is NULL";
+  if (n_inst < 1) return "n_inst must be >= 1";
+  const pecs_params& a = p[0];
+  if (a.degree < 1 || a.degree > 2) e << "degree must be 1 or 2; ";
+  if (a.nx_semi < 2 || a.ny < 2 || (a.full_system && a.nx_elec < 2)) e << "mesh too small; ";
+  if (a.nx_semi > 4096 || a.ny > 4096 || a.nx_elec > 4096) e << "mesh too large; ";
+  if (!(a.dt > 0) || !(a.lambda2 > 0) || !(a.eps_semi > 0) || (a.full_system && !(a.eps_elec > 0)))
+    e << "dt, lambda2 and permittivities must be > 0; ";
+  for (int c = 0; c < 4; ++c)
+    if (!(a.mu[c] > 0)) e << "mobilities must be > 0; ";
+  if (!(a.x_semi1 > a.x_semi0) || !(a.height > 0) || (a.full_system && !(a.x_elec1 > a.x_semi1)))
+    e << "bad geometry; ";
+  for (int f = 0; f < 4; ++f) {
+    if (a.bc_semi[f] < 0 || a.bc_semi[f] > 3 || a.bc_elec[f] < 0 || a.bc_elec[f] > 3 ||
+        a.bc_poisson[f] < 0 || a.bc_poisson[f] > 3)
+      e << "bad boundary id; ";
+  }
+  for (int i = 1; i < n_inst; ++i) {
+    const pecs_params& b = p[i];
+    bool same = a.degree == b.degree && a.full_system == b.full_system && a.nx_semi == b.nx_semi &&
+                a.nx_elec == b.nx_elec && a.ny == b.ny && a.x_semi0 == b.x_semi0 &&
+                a.x_semi1 == b.x_semi1 && a.x_elec1 == b.x_elec1 && a.height == b.height &&
+                a.lambda2 == b.lambda2 && a.eps_semi == b.eps_semi && a.eps_elec == b.eps_elec &&
+                a.dt == b.dt && a.penalty == b.penalty &&
+                std::memcmp(a.mu, b.mu, sizeof(a.mu)) == 0 &&
+                std::memcmp(a.bc_semi, b.bc_semi, sizeof(a.bc_semi)) == 0 &&
+                std::memcmp(a.bc_elec, b.bc_elec, sizeof(a.bc_elec)) == 0 &&
+                std::memcmp(a.bc_poisson, b.bc_poisson, sizeof(a.bc_poisson)) == 0;
+    if (!same) {
+      e << "instance " << i << " differs from instance 0 in a matrix-defining field; ";
+      break;
+    }
+  }
+  return e.str();
+}
+
+static void assemble_carrier(CarrierSystem& S, const CarrierTables& ct, const pecs_params& P,
+                             double mu1, double mu2) {
+  const Grid& g = S.grid;
+  const int n1 = ct.n1, nd = 3 * n1, nc = g.nc();
+  S.ndofs = 3 * nc * n1;
+  auto dof = [&](int K, int i) { return (i / n1) * nc * n1 + K * n1 + (i % n1); };
+  std::vector<int> r[2], c[2], mr, mc;
+  std::vector<double> v[2], mv;
+  std::map<std::tuple<double, double, int, int, int, int>, std::vector<double>> cache[2];
+  for (int K = 0; K < nc; ++K) {
+    double x0, y0, hx, hy;
+    g.geom(K, x0, y0, hx, hy);
+    int bids[4];
+    for (int f = 0; f < 4; ++f) bids[f] = g.face_bid(K, f);
+    double diam = std::sqrt(hx * hx + hy * hy);
+    auto key = std::make_tuple(hx, hy, bids[0], bids[1], bids[2], bids[3]);
+    for (int s = 0; s < 2; ++s) {
+      auto it = cache[s].find(key);
+      if (it == cache[s].end())
+        it = cache[s].emplace(key, ldg_cell_matrix(ct, hx, hy, s == 0 ? mu1 : mu2, P.dt, 1.0,
+                                                   P.penalty / diam, bids))
+                 .first;
+      const std::vector<double>& A = it->second;
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j) {
+          r[s].push_back(dof(K, i));
+          c[s].push_back(dof(K, j));
+          v[s].push_back(A[i * nd + j]);
+        }
+    }
+    // (1/dt) mass, source/LDG.cpp:40-83
+    for (int a = 0; a < n1; ++a)
+      for (int b = 0; b < n1; ++b) {
+        double s = 0.0;
+        for (int q = 0; q < ct.Q; ++q)
+          s += (1.0 / P.dt) * ct.phi[a * ct.Q + q] * ct.phi[b * ct.Q + q] * ct.qw[q] * hx * hy;
+        mr.push_back(dof(K, 2 * n1 + a));
+        mc.push_back(dof(K, 2 * n1 + b));
+        mv.push_back(s);
+      }
+  }
+  // interior faces (assemble_flux_terms, source/LDG.cpp:283-426)
+  std::map<std::tuple<int, double, double>, std::vector<std::vector<double>>> fcache;
+  for (int K = 0; K < nc; ++K) {
+    int i = K % g.nx, j = K / g.nx;
+    for (int dir = 0; dir < 2; ++dir) {
+      int nb;
+      int fm, fp;
+      if (dir == 0) {
+        if (i >= g.nx - 1) continue;
+        nb = K + 1;
+        fm = kRight;
+        fp = kLeft;
+      } else {
+        if (j >= g.ny - 1) continue;
+        nb = K + g.nx;
+        fm = kTop;
+        fp = kBottom;
+      }
+      double x0, y0, hx, hy, x1, y1, hx1, hy1;
+      g.geom(K, x0, y0, hx, hy);
+      g.geom(nb, x1, y1, hx1, hy1);
+      double flen = dir == 0 ? hy : hx;
+      double h = std::min(std::sqrt(hx * hx + hy * hy), std::sqrt(hx1 * hx1 + hy1 * hy1));
+      auto key = std::make_tuple(fm, flen, h);
+      auto it = fcache.find(key);
+      if (it == fcache.end()) {
+        std::vector<double> blk[4];
+        ldg_flux_blocks(ct, fm, fp, flen, P.penalty / h, blk);
+        it = fcache.emplace(key, std::vector<std::vector<double>>(blk, blk + 4)).first;
+      }
+      const int cells[4][2] = {{K, K}, {K, nb}, {nb, K}, {nb, nb}};
+      for (int t = 0; t < 4; ++t) {
+        const std::vector<double>& B = it->second[t];
+        for (int a = 0; a < nd; ++a)
+          for (int b = 0; b < nd; ++b)
+            for (int s = 0; s < 2; ++s) {
+              r[s].push_back(dof(cells[t][0], a));
+              c[s].push_back(dof(cells[t][1], b));
+              v[s].push_back(B[a * nd + b]);
+            }
+      }
+    }
+  }
+  for (int s = 0; s < 2; ++s) S.A[s] = coo_to_csr(S.ndofs, r[s], c[s], v[s]);
+  S.M = coo_to_csr(S.ndofs, mr, mc, mv);
+  S.dof_cell.resize(S.ndofs);
+  S.dof_class.resize(S.ndofs);
+  for (int K = 0; K < nc; ++K)
+    for (int i = 0; i < nd; ++i) {
+      S.dof_cell[dof(K, i)] = K;
+      S.dof_class[dof(K, i)] = (i < 2 * n1) ? 0 : 1;
+    }
+  S.cell_xy.resize(2 * nc);
+  for (int K = 0; K < nc; ++K) {
+    double x0, y0, hx, hy;
+    g.geom(K, x0, y0, hx, hy);
+    S.cell_xy[2 * K] = x0 + 0.5 * hx;
+    S.cell_xy[2 * K + 1] = y0 + 0.5 * hy;
+  }
+}
+
+static void setup_poisson(PoissonSystem& S, const PoissonTables& pt, const CarrierTables& ct,
+                          const pecs_params& P) {
+  const Grid& g = S.grid;
+  const int k = pt.k, nx = g.nx, ny = g.ny, nc = g.nc();
+  const int nloc = pt.n_rt + pt.n_phi;
+  const int nvert = (nx + 1) * ny, nhor = nx * (ny + 1), nint = 2 * k * (k - 1);
+  const int off_h = nvert * k, off_i = off_h + nhor * k, off_phi = off_i + nc * nint;
+  S.n_rt_total = off_phi;
+  S.ndofs = off_phi + nc * pt.n_phi;
+  S.l2g.assign(nc * nloc, 0);
+  const int nxd = k * (k + 1);
+  for (int K = 0; K < nc; ++K) {
+    int i = K % nx, j = K / nx, cnt = 0;
+    for (int b = 0; b < k; ++b)
+      for (int a = 0; a <= k; ++a) {
+        int loc = a + (k + 1) * b;
+        int gdof;
+        if (a == 0)
+          gdof = (i + (nx + 1) * j) * k + b;
+        else if (a == k)
+          gdof = (i + 1 + (nx + 1) * j) * k + b;
+        else
+          gdof = off_i + K * nint + cnt++;
+        S.l2g[K * nloc + loc] = gdof;
+      }
+    for (int b = 0; b <= k; ++b)
+      for (int a = 0; a < k; ++a) {
+        int loc = nxd + a + k * b;
+        int gdof;
+        if (b == 0)
+          gdof = off_h + (i + nx * j) * k + a;
+        else if (b == k)
+          gdof = off_h + (i + nx * (j + 1)) * k + a;
+        else
+          gdof = off_i + K * nint + cnt++;
+        S.l2g[K * nloc + loc] = gdof;
+      }
+    for (int a = 0; a < pt.n_phi; ++a) S.l2g[K * nloc + pt.n_rt + a] = off_phi + K * pt.n_phi + a;
+  }
+  // zero D.n on Neumann faces (source/Poisson.cpp:32-49)
+  S.constrained.assign(S.ndofs, 0);
+  for (int K = 0; K < nc; ++K)
+    for (int f = 0; f < 4; ++f)
+      if (g.face_bid(K, f) == kNeumann)
+        for (int loc : pt.face_dofs[f]) S.constrained[S.l2g[K * nloc + loc]] = 1;
+  // matrix
+  std::vector<int> r, c;
+  std::vector<double> v;
+  std::map<std::tuple<double, double, double>, std::vector<double>> cache;
+  for (int K = 0; K < nc; ++K) {
+    double x0, y0, hx, hy;
+    g.geom(K, x0, y0, hx, hy);
+    double eps = (g.material[K] == 0 || g.material[K] == 1) ? P.eps_semi : P.eps_elec;
+    auto key = std::make_tuple(hx, hy, eps);
+    auto it = cache.find(key);
+    if (it == cache.end())
+      it = cache.emplace(key, poisson_cell_matrix(pt, ct, hx, hy, eps, P.lambda2)).first;
+    const std::vector<double>& A = it->second;
+    for (int a = 0; a < nloc; ++a) {
+      int ga = S.l2g[K * nloc + a];
+      if (S.constrained[ga]) continue;
+      for (int b = 0; b < nloc; ++b) {
+        int gb = S.l2g[K * nloc + b];
+        if (S.constrained[gb]) continue;
+        r.push_back(ga);
+        c.push_back(gb);
+        v.push_back(A[a * nloc + b]);
+      }
+    }
+  }
+  for (int d = 0; d < S.ndofs; ++d)
+    if (S.constrained[d]) {
+      r.push_back(d);
+      c.push_back(d);
+      v.push_back(1.0);
+    }
+  S.A = coo_to_csr(S.ndofs, r, c, v);
+  // dof -> owning cell: faces to the left/bottom neighbour, cell dofs to the cell
+  S.dof_cell.assign(S.ndofs, -1);
+  for (int K = 0; K < nc; ++K) {
+    int i = K % nx, j = K / nx;
+    for (int loc = 0; loc < nloc; ++loc) {
+      int gd = S.l2g[K * nloc + loc];
+      int owner = K;
+      bool is_left = false, is_bottom = false;
+      for (int t : pt.face_dofs[kLeft]) is_left |= (t == loc);
+      for (int t : pt.face_dofs[kBottom]) is_bottom |= (t == loc);
+      if (is_left && i > 0) owner = K - 1;
+      if (is_bottom && j > 0) owner = K - nx;
+      if (S.dof_cell[gd] < 0) S.dof_cell[gd] = owner;
+    }
+  }
+  S.cell_xy.resize(2 * nc);
+  for (int K = 0; K < nc; ++K) {
+    double x0, y0, hx, hy;
+    g.geom(K, x0, y0, hx, hy);
+    S.cell_xy[2 * K] = x0 + 0.5 * hx;
+    S.cell_xy[2 * K + 1] = y0 + 0.5 * hy;
+  }
+}
+
+Setup::Setup(const std::vector<pecs_params>& p)
+    : inst(p), ct(p[0].degree), pt(p[0].degree, ct) {
+  const pecs_params& P = p[0];
+  k = P.degree;
+  n1 = ct.n1;
+  n_rt = pt.n_rt;
+  n_phi = pt.n_phi;
+  Q = ct.Q;
+  nq1 = ct.nq1;
+  full = P.full_system != 0;
+  semi.grid = uniform(P.x_semi0, P.x_semi1, 0.0, P.height, P.nx_semi, P.ny, P.bc_semi, 0);
+  if (full) elec.grid = uniform(P.x_semi1, P.x_elec1, 0.0, P.height, P.nx_elec, P.ny, P.bc_elec, 2);
+  // Poisson mesh: merged triangulation (Grid.cpp:320-336)
+  Grid& pg = pois.grid;
+  pg.nx = P.nx_semi + (full ? P.nx_elec : 0);
+  pg.ny = P.ny;
+  pg.xs = semi.grid.xs;
+  if (full) pg.xs.insert(pg.xs.end(), elec.grid.xs.begin() + 1, elec.grid.xs.end());
+  pg.ys = semi.grid.ys;
+  for (int f = 0; f < 4; ++f) pg.bc[f] = P.bc_poisson[f];
+  pg.material.resize(pg.nc());
+  for (int K = 0; K < pg.nc(); ++K) pg.material[K] = (K % pg.nx) < P.nx_semi ? 0 : 2;
+
+  assemble_carrier(semi, ct, P, P.mu[0], P.mu[1]);
+  if (full) assemble_carrier(elec, ct, P, P.mu[2], P.mu[3]);
+  setup_poisson(pois, pt, ct, P);
+
+  // setup_mappings (SolarCell.cpp:156-372): identical cell centres
+  s2p.resize(semi.grid.nc());
+  for (int K = 0; K < semi.grid.nc(); ++K) s2p[K] = (K % semi.grid.nx) + pg.nx * (K / semi.grid.nx);
+  if (full) {
+    e2p.resize(elec.grid.nc());
+    for (int K = 0; K < elec.grid.nc(); ++K)
+      e2p[K] = (K % elec.grid.nx) + P.nx_semi + pg.nx * (K / elec.grid.nx);
+    for (int j = 0; j < P.ny; ++j) {
+      int Ks = (semi.grid.nx - 1) + semi.grid.nx * j;
+      int Ke = 0 + elec.grid.nx * j;
+      if (semi.grid.face_bid(Ks, kRight) == kInterface && elec.grid.face_bid(Ke, kLeft) == kInterface) {
+        iface_semi.push_back(Ks);
+        iface_elec.push_back(Ke);
+      }
+    }
+  }
+  for (int K = 0; K < semi.grid.nc(); ++K)
+    for (int f = 0; f < 4; ++f)
+      if (semi.grid.face_bid(K, f) == kSchottky) has_schottky = true;
+
+  // time-independent RHS parts per instance
+  const int ninst = (int)p.size();
+  const int nloc = n_rt + n_phi;
+  for (int fld = 0; fld < 5; ++fld) bconst[fld].assign(ninst, {});
+  iface_ne.assign(ninst, {});
+  iface_pe.assign(ninst, {});
+  schottky_ne.assign(ninst, {});
+  schottky_pe.assign(ninst, {});
+  for (int fld = 0; fld < 4; ++fld) init[fld].assign(ninst, {});
+  std::vector<double> g1, w1;
+  gauss01(k + 1, g1, w1);
+  for (int s = 0; s < ninst; ++s) {
+    const pecs_params& Pi = p[s];
+    for (int reg = 0; reg < (full ? 2 : 1); ++reg) {
+      const CarrierSystem& CS = reg == 0 ? semi : elec;
+      const Grid& g = CS.grid;
+      const int nc = g.nc();
+      for (int cc = 0; cc < 2; ++cc) {
+        int fld = 2 * reg + cc;
+        std::vector<double> b(CS.ndofs, 0.0);
+        for (int K = 0; K < nc; ++K) {
+          double x0, y0, hx, hy;
+          g.geom(K, x0, y0, hx, hy);
+          double diam = std::sqrt(hx * hx + hy * hy);
+          if (reg == 0 && Pi.gen_kind != 0) {
+            for (int a = 0; a < n1; ++a) {
+              double sacc = 0.0;
+              for (int q = 0; q < Q; ++q) {
+                double X = x0 + hx * ct.qx[q], Y = y0 + hy * ct.qy[q];
+                sacc += ct.phi[a * Q + q] * generation(Pi, X, Y) * ct.qw[q] * hx * hy;
+              }
+              b[2 * nc * n1 + K * n1 + a] += sacc;
+            }
+          }
+          for (int f = 0; f < 4; ++f) {
+            if (g.face_bid(K, f) != kDirichlet) continue;
+            double flen = (f == kLeft || f == kRight) ? hy : hx;
+            for (int i = 0; i < 3 * n1; ++i) {
+              int ci = i / n1, a = i % n1;
+              double sacc = 0.0;
+              for (int q = 0; q < nq1; ++q) {
+                double X, Y;
+                if (f == kLeft) { X = x0; Y = y0 + hy * ct.fq[q]; }
+                else if (f == kRight) { X = x0 + hx; Y = y0 + hy * ct.fq[q]; }
+                else if (f == kBottom) { X = x0 + hx * ct.fq[q]; Y = y0; }
+                else { X = x0 + hx * ct.fq[q]; Y = y0 + hy; }
+                double ph = ct.fphi[(f * n1 + a) * nq1 + q];
+                double pn = (ci == 0 ? kFaceNormal[f][0] * ph : 0.0) + (ci == 1 ? kFaceNormal[f][1] * ph : 0.0);
+                double vv = ci == 2 ? ph : 0.0;
+                sacc += (-pn + (Pi.penalty / diam) * vv) * carrier_bc(Pi, fld, X, Y) * ct.fw[q] * flen;
+              }
+              b[ci * nc * n1 + K * n1 + a] += sacc;
+            }
+          }
+        }
+        bconst[fld][s] = std::move(b);
+        // initial conditions: L2 projection with QGauss(k+1) (SolarCell.cpp:1996-2021)
+        std::vector<double> u(CS.ndofs, 0.0);
+        {
+          const int m = k + 1, nq = (int)g1.size();
+          auto nodes = dgq_nodes(k);
+          std::vector<std::vector<double>> L(nq), dL(nq);
+          for (int q = 0; q < nq; ++q) lagrange1d(nodes, g1[q], L[q], dL[q]);
+          std::vector<double> Mref(n1 * n1, 0.0);
+          for (int a = 0; a < n1; ++a)
+            for (int bb = 0; bb < n1; ++bb)
+              for (int qy_ = 0; qy_ < nq; ++qy_)
+                for (int qx_ = 0; qx_ < nq; ++qx_)
+                  Mref[a * n1 + bb] += L[qx_][a % m] * L[qy_][a / m] * L[qx_][bb % m] * L[qy_][bb / m] *
+                                       w1[qx_] * w1[qy_];
+          for (int K = 0; K < nc; ++K) {
+            double x0, y0, hx, hy;
+            g.geom(K, x0, y0, hx, hy);
+            std::vector<double> rhs(n1, 0.0);
+            for (int a = 0; a < n1; ++a)
+              for (int qy_ = 0; qy_ < nq; ++qy_)
+                for (int qx_ = 0; qx_ < nq; ++qx_)
+                  rhs[a] += L[qx_][a % m] * L[qy_][a / m] *
+                            initial_profile(Pi, fld, x0 + hx * g1[qx_], y0 + hy * g1[qy_]) * w1[qx_] *
+                            w1[qy_];
+            // solve Mref c = rhs (Gaussian elimination with partial pivoting)
+            std::vector<double> M = Mref;
+            std::vector<double> c = rhs;
+            for (int col = 0; col < n1; ++col) {
+              int piv = col;
+              for (int rr = col + 1; rr < n1; ++rr)
+                if (std::fabs(M[rr * n1 + col]) > std::fabs(M[piv * n1 + col])) piv = rr;
+              if (piv != col) {
+                for (int cc2 = 0; cc2 < n1; ++cc2) std::swap(M[col * n1 + cc2], M[piv * n1 + cc2]);
+                std::swap(c[col], c[piv]);
+              }
+              for (int rr = col + 1; rr < n1; ++rr) {
+                double f = M[rr * n1 + col] / M[col * n1 + col];
+                for (int cc2 = col; cc2 < n1; ++cc2) M[rr * n1 + cc2] -= f * M[col * n1 + cc2];
+                c[rr] -= f * c[col];
+              }
+            }
+            for (int rr = n1 - 1; rr >= 0; --rr) {
+              double sacc = c[rr];
+              for (int cc2 = rr + 1; cc2 < n1; ++cc2) sacc -= M[rr * n1 + cc2] * c[cc2];
+              c[rr] = sacc / M[rr * n1 + rr];
+            }
+            for (int a = 0; a < n1; ++a) u[2 * nc * n1 + K * n1 + a] = c[a];
+          }
+        }
+        init[fld][s] = std::move(u);
+      }
+    }
+    // Poisson constant part: doping on semiconductor cells + Dirichlet potential
+    std::vector<double> bP(pois.ndofs, 0.0);
+    const Grid& g = pois.grid;
+    for (int K = 0; K < g.nc(); ++K) {
+      double x0, y0, hx, hy;
+      g.geom(K, x0, y0, hx, hy);
+      if (g.material[K] == 0) {
+        for (int a = 0; a < n_phi; ++a) {
+          double sacc = 0.0;
+          for (int q = 0; q < Q; ++q) {
+            double X = x0 + hx * ct.qx[q];
+            double dop = pw(X, Pi.nd, Pi.junction_x) - pw(X, Pi.na, Pi.junction_x);
+            sacc += pt.phi[a * Q + q] * dop * ct.qw[q] * hx * hy;
+          }
+          bP[pois.l2g[K * nloc + n_rt + a]] += -sacc;
+        }
+      }
+      for (int f = 0; f < 4; ++f) {
+        if (g.face_bid(K, f) != kDirichlet) continue;
+        double flen = (f == kLeft || f == kRight) ? hy : hx;
+        for (int i = 0; i < n_rt; ++i) {
+          double sacc = 0.0;
+          for (int q = 0; q < nq1; ++q) {
+            double X, Y;
+            if (f == kLeft) { X = x0; Y = y0 + hy * ct.fq[q]; }
+            else if (f == kRight) { X = x0 + hx; Y = y0 + hy * ct.fq[q]; }
+            else if (f == kBottom) { X = x0 + hx * ct.fq[q]; Y = y0; }
+            else { X = x0 + hx * ct.fq[q]; Y = y0 + hy; }
+            sacc += pt.fpsi_n[(f * n_rt + i) * nq1 + q] * potential_dirichlet(Pi, X, Y) * ct.fw[q] * flen;
+          }
+          bP[pois.l2g[K * nloc + i]] += -sacc;
+        }
+      }
+    }
+    for (int d = 0; d < pois.ndofs; ++d)
+      if (pois.constrained[d]) bP[d] = 0.0;
+    bconst[4][s] = std::move(bP);
+    // interface equilibria at the semiconductor face qp
+    if (full) {
+      std::vector<double> ne(iface_semi.size() * nq1), pe(iface_semi.size() * nq1);
+      for (size_t t = 0; t < iface_semi.size(); ++t) {
+        double x0, y0, hx, hy;
+        semi.grid.geom(iface_semi[t], x0, y0, hx, hy);
+        for (int q = 0; q < nq1; ++q) {
+          double X = x0 + hx, Y = y0 + hy * ct.fq[q];
+          ne[t * nq1 + q] = carrier_bc(Pi, 0, X, Y);
+          pe[t * nq1 + q] = carrier_bc(Pi, 1, X, Y);
+        }
+      }
+      iface_ne[s] = std::move(ne);
+      iface_pe[s] = std::move(pe);
+    }
+    if (has_schottky) {
+      const Grid& gs = semi.grid;
+      std::vector<double> ne(gs.nc() * 4 * nq1, 0.0), pe(gs.nc() * 4 * nq1, 0.0);
+      for (int K = 0; K < gs.nc(); ++K) {
+        double x0, y0, hx, hy;
+        gs.geom(K, x0, y0, hx, hy);
+        for (int f = 0; f < 4; ++f) {
+          if (gs.face_bid(K, f) != kSchottky) continue;
+          for (int q = 0; q < nq1; ++q) {
+            double X, Y;
+            if (f == kLeft) { X = x0; Y = y0 + hy * ct.fq[q]; }
+            else if (f == kRight) { X = x0 + hx; Y = y0 + hy * ct.fq[q]; }
+            else if (f == kBottom) { X = x0 + hx * ct.fq[q]; Y = y0; }
+            else { X = x0 + hx * ct.fq[q]; Y = y0 + hy; }
+            ne[(K * 4 + f) * nq1 + q] = carrier_bc(Pi, 0, X, Y);
+            pe[(K * 4 + f) * nq1 + q] = carrier_bc(Pi, 1, X, Y);
+          }
+        }
+      }
+      schottky_ne[s] = std::move(ne);
+      schottky_pe[s] = std::move(pe);
+    }
+  }
+}
+
+}  // namespace pecs

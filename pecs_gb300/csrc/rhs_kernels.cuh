@@ -1,0 +1,267 @@
+// Per-step right-hand-side kernels of the IMEX loop.
+//
+// k_carrier_rhs restates assemble_local_semiconductor_rhs /
+// assemble_local_electrolyte_rhs plus the M u^{n-1} mat-vec of
+// assemble_semiconductor_rhs / assemble_electrolyte_rhs (reference
+// source/SolarCell.cpp:1037-1726): drift q/eps (p . D) u^{n-1} with D the RT
+// field of the Poisson solution evaluated at the carrier quadrature points,
+// SRH, the semiconductor--electrolyte interface Robin transfer and Schottky
+// terms; generation and Dirichlet data are time independent and arrive
+// pre-assembled in `bconst`.  One thread per (cell, carrier): a k=1 cell owns
+// 4 density dofs and 4 field dofs (96 bytes), so a warp per cell would leave
+// most lanes idle; neighbouring threads read neighbouring dof blocks, so the
+// loads of a warp are contiguous.
+//
+// k_poisson_rhs restates assemble_local_Poisson_rhs_for_semiconductor /
+// _for_electrolyte (SolarCell.cpp:487-815): -(v, sum q_i u_i) on the Phi rows
+// of the matching Poisson cell plus the constant doping/Dirichlet part.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace pecs {
+
+struct Tables {
+  const double* phi;   // n1*Q   carrier basis at cell qp
+  const double* qw;    // Q
+  const double* fphi;  // 4*n1*nq face values
+  const double* fw;    // nq
+  const double* psix;  // nrt*Q  RT basis x-component at cell qp
+  const double* psiy;  // nrt*Q
+  const double* phiP;  // nphi*Q Poisson DGQ_{k-1} basis at cell qp
+  const double* mref;  // n1*n1  unit-square mass matrix
+};
+
+struct RegionDev {
+  int nc;              // cells
+  int nd;              // dofs per carrier vector
+  int field1;          // PECS_FIELD_N (semi) or PECS_FIELD_R (elec)
+  int is_semi;
+  int iface_face;      // face of this region's cells on the interface
+  int partner_face;    // face of the partner cell
+  double inv_eps;      // 1/permittivity of the region
+  double inv_dt;
+  const double2* h;    // (hx, hy) per cell
+  const int4* bid;     // boundary id per face (-1 interior)
+  const int* rt;       // nc*nrt Poisson RT dofs of the matching Poisson cell
+  const int* phid;     // nc*nphi Poisson Phi dofs
+  const int* partner;  // partner cell in the other region or -1
+  const int* iface;    // interface index or -1
+  const double2* ph;   // partner (hx, hy)
+};
+
+struct InstDev {
+  double k_et, k_ht, tau_n, tau_p, n_i, s_n, s_p;
+  int srh;
+  int pad;
+};
+
+struct FieldPtrs {
+  const double* u[5];   // state read (instance stride nd[f])
+  double* out[5];       // written vectors (rhs)
+  const double* bc[5];  // constant rhs parts
+  int nd[5];
+};
+
+template <int K>
+struct Dims {
+  static constexpr int n1 = (K + 1) * (K + 1);
+  static constexpr int nq = K + 2;
+  static constexpr int Q = nq * nq;
+  static constexpr int nrt = 2 * K * (K + 1);
+  static constexpr int nphi = K * K;
+};
+
+// grid: x over (cells of both regions) * 2 carriers, y over instances
+template <int K>
+__global__ void __launch_bounds__(128)
+    k_carrier_rhs(Tables T, RegionDev semi, RegionDev elec, int n_regions, FieldPtrs F,
+                  const InstDev* __restrict__ inst, const double* __restrict__ iface_ne,
+                  const double* __restrict__ iface_pe, int n_iface, const double* __restrict__ sch_ne,
+                  const double* __restrict__ sch_pe, const int* __restrict__ active) {
+  using D = Dims<K>;
+  constexpr int n1 = D::n1, nq = D::nq, Q = D::Q, nrt = D::nrt;
+  const int i = blockIdx.y;
+  if (active && !active[i]) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nsemi2 = 2 * semi.nc;
+  const int ntot = nsemi2 + (n_regions > 1 ? 2 * elec.nc : 0);
+  if (t >= ntot) return;
+  const bool in_semi = t < nsemi2;
+  const RegionDev& R = in_semi ? semi : elec;
+  const RegionDev& O = in_semi ? elec : semi;
+  if (!in_semi) t -= nsemi2;
+  const int c = t >> 1, which = t & 1;  // which: 0 carrier_1, 1 carrier_2
+  const int f1 = R.field1, f = f1 + which;
+  const int nc = R.nc, nd = R.nd;
+  const InstDev P = inst[i];
+  const double* u1p = F.u[f1] + (size_t)i * F.nd[f1] + 2 * nc * n1 + c * n1;
+  const double* u2p = F.u[f1 + 1] + (size_t)i * F.nd[f1 + 1] + 2 * nc * n1 + c * n1;
+  double u1[n1], u2[n1];
+#pragma unroll
+  for (int a = 0; a < n1; ++a) {
+    u1[a] = u1p[a];
+    u2[a] = u2p[a];
+  }
+  const double* Pv = F.u[4] + (size_t)i * F.nd[4];
+  double Dd[nrt];
+#pragma unroll
+  for (int b = 0; b < nrt; ++b) Dd[b] = Pv[R.rt[c * nrt + b]];
+  const double2 h = R.h[c];
+  const double hxhy = h.x * h.y;
+  const double* uo = which ? u2 : u1;
+  const double charge = which ? 1.0 : -1.0;
+  // accumulators: [Jx (n1) | Jy (n1) | u (n1)]
+  double r[3 * n1];
+  const double* bcp = F.bc[f] + (size_t)i * nd;
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp)
+#pragma unroll
+    for (int a = 0; a < n1; ++a) r[comp * n1 + a] = bcp[comp * nc * n1 + c * n1 + a];
+  // (1/dt) M u^{n-1}
+#pragma unroll
+  for (int a = 0; a < n1; ++a) {
+    double s = 0.0;
+#pragma unroll
+    for (int b = 0; b < n1; ++b) s += T.mref[a * n1 + b] * uo[b];
+    r[2 * n1 + a] += s * hxhy * R.inv_dt;
+  }
+  const bool srh = in_semi && P.srh;
+#pragma unroll 1
+  for (int q = 0; q < Q; ++q) {
+    const double JxW = T.qw[q] * hxhy;
+    double uq = 0.0, n = 0.0, p = 0.0;
+#pragma unroll
+    for (int a = 0; a < n1; ++a) {
+      const double ph = T.phi[a * Q + q];
+      n += ph * u1[a];
+      p += ph * u2[a];
+    }
+    uq = which ? p : n;
+    double Ex = 0.0, Ey = 0.0;
+#pragma unroll
+    for (int b = 0; b < nrt; ++b) {
+      Ex += T.psix[b * Q + q] * Dd[b];
+      Ey += T.psiy[b * Q + q] * Dd[b];
+    }
+    const double w = charge * R.inv_eps * uq * JxW;
+    double Rq = 0.0;
+    if (srh) {
+      const double ni = P.n_i;
+      Rq = (ni * ni - n * p) / (P.tau_n * (n + ni) + P.tau_p * (p + ni)) * JxW;
+    }
+#pragma unroll
+    for (int a = 0; a < n1; ++a) {
+      const double ph = T.phi[a * Q + q];
+      r[a] += ph * Ex * w;
+      r[n1 + a] += ph * Ey * w;
+      r[2 * n1 + a] += ph * Rq;
+    }
+  }
+  // interface Robin transfer (SolarCell.cpp:1265-1347, 1630-1716)
+  const int4 bid = R.bid[c];
+  const int bids[4] = {bid.x, bid.y, bid.z, bid.w};
+  if (n_regions > 1 && R.iface[c] >= 0 && bids[R.iface_face] == 0) {
+    const int pc = R.partner[c], ii = R.iface[c];
+    const double* o1p = F.u[O.field1] + (size_t)i * F.nd[O.field1] + 2 * O.nc * n1 + pc * n1;
+    const double* o2p = F.u[O.field1 + 1] + (size_t)i * F.nd[O.field1 + 1] + 2 * O.nc * n1 + pc * n1;
+    const int ff = R.iface_face, pf = R.partner_face;
+    const double flen = (ff == 0 || ff == 1) ? h.y : h.x;
+#pragma unroll 1
+    for (int q = 0; q < nq; ++q) {
+      double a1 = 0.0, a2 = 0.0, b1 = 0.0, b2 = 0.0;
+#pragma unroll
+      for (int a = 0; a < n1; ++a) {
+        const double fo = T.fphi[(ff * n1 + a) * nq + q];
+        const double fp = T.fphi[(pf * n1 + a) * nq + q];
+        a1 += fo * u1[a];
+        a2 += fo * u2[a];
+        b1 += fp * o1p[a];
+        b2 += fp * o2p[a];
+      }
+      // semiconductor-side values n, p and electrolyte-side r, o
+      const double n = in_semi ? a1 : b1, p = in_semi ? a2 : b2;
+      const double rr = in_semi ? b1 : a1, oo = in_semi ? b2 : a2;
+      const double ne = iface_ne[(size_t)i * n_iface * nq + ii * nq + q];
+      const double pe = iface_pe[(size_t)i * n_iface * nq + ii * nq + q];
+      const double Jf = T.fw[q] * flen;
+      const double tn = -P.k_et * (n - ne) * oo * Jf;
+      const double tp = P.k_ht * (p - pe) * rr * Jf;
+      double coef;
+      if (in_semi)
+        coef = which ? tp : tn;
+      else
+        coef = which ? -(tn + tp) : (tn + tp);
+#pragma unroll
+      for (int a = 0; a < n1; ++a) r[2 * n1 + a] += T.fphi[(ff * n1 + a) * nq + q] * coef;
+    }
+  }
+  // Schottky faces (SolarCell.cpp:1348-1404)
+  if (in_semi && sch_ne) {
+#pragma unroll 1
+    for (int fc = 0; fc < 4; ++fc) {
+      if (bids[fc] != 3) continue;
+      const double flen = (fc == 0 || fc == 1) ? h.y : h.x;
+      for (int q = 0; q < nq; ++q) {
+        double val = 0.0;
+#pragma unroll
+        for (int a = 0; a < n1; ++a) val += T.fphi[(fc * n1 + a) * nq + q] * uo[a];
+        const size_t o = (size_t)i * nc * 4 * nq + (size_t)(c * 4 + fc) * nq + q;
+        const double Jf = T.fw[q] * flen;
+        const double coef = which ? P.s_p * (val - sch_pe[o]) * Jf : -P.s_n * (val - sch_ne[o]) * Jf;
+#pragma unroll
+        for (int a = 0; a < n1; ++a) r[2 * n1 + a] += T.fphi[(fc * n1 + a) * nq + q] * coef;
+      }
+    }
+  }
+  double* outp = F.out[f] + (size_t)i * nd;
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp)
+#pragma unroll
+    for (int a = 0; a < n1; ++a) outp[comp * nc * n1 + c * n1 + a] = r[comp * n1 + a];
+}
+
+// grid: x over max(n_rt_total, cells of both regions), y over instances
+template <int K>
+__global__ void __launch_bounds__(128)
+    k_poisson_rhs(Tables T, RegionDev semi, RegionDev elec, int n_regions, FieldPtrs F,
+                  int n_rt_total, const int* __restrict__ active) {
+  using D = Dims<K>;
+  constexpr int n1 = D::n1, Q = D::Q, nphi = D::nphi;
+  const int i = blockIdx.y;
+  if (active && !active[i]) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const double* bc = F.bc[4] + (size_t)i * F.nd[4];
+  double* out = F.out[4] + (size_t)i * F.nd[4];
+  if (t < n_rt_total) out[t] = bc[t];
+  const int ntot = semi.nc + (n_regions > 1 ? elec.nc : 0);
+  if (t >= ntot) return;
+  const bool in_semi = t < semi.nc;
+  const RegionDev& R = in_semi ? semi : elec;
+  const int c = in_semi ? t : t - semi.nc;
+  const int f1 = R.field1;
+  const double* u1 = F.u[f1] + (size_t)i * F.nd[f1] + 2 * R.nc * n1 + c * n1;
+  const double* u2 = F.u[f1 + 1] + (size_t)i * F.nd[f1 + 1] + 2 * R.nc * n1 + c * n1;
+  const double2 h = R.h[c];
+  double acc[nphi];
+#pragma unroll
+  for (int a = 0; a < nphi; ++a) acc[a] = 0.0;
+#pragma unroll 1
+  for (int q = 0; q < Q; ++q) {
+    double a1 = 0.0, a2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < n1; ++a) {
+      a1 += T.phi[a * Q + q] * u1[a];
+      a2 += T.phi[a * Q + q] * u2[a];
+    }
+    const double rho = (-a1 + a2) * T.qw[q] * h.x * h.y;  // charge numbers -1, +1
+#pragma unroll
+    for (int a = 0; a < nphi; ++a) acc[a] += T.phiP[a * Q + q] * rho;
+  }
+#pragma unroll
+  for (int a = 0; a < nphi; ++a) {
+    const int d = R.phid[c * nphi + a];
+    out[d] = bc[d] - acc[a];
+  }
+}
+
+}  // namespace pecs

@@ -1,0 +1,495 @@
+// Level-scheduled multifrontal solve kernels and their host-side plan (solve.cuh).
+#include <algorithm>
+#include <cstring>
+
+#include "solve.cuh"
+
+namespace pecs {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T group_sum(T v, int g) {
+  // xor-butterfly inside aligned groups of g lanes (g a power of two <= 32)
+  for (int o = g >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of the children's update entries that land on front position p.
+__device__ __forceinline__ double gather_updates(const BankView& B, const double* __restrict__ w,
+                                                 int c0, int c1) {
+  double v = 0.0;
+  for (int c = c0; c < c1; ++c) v += w[B.cmap_idx[c]];
+  return v;
+}
+
+// Forward sweep, large node: CTA computes rows [r0, r1) of Gf * d.
+template <typename T, int RB>
+__device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) {
+  const int j = it.x, r0 = it.y, r1 = it.z;
+  const int s = B.s[j];
+  const SetView& st = S.set[B.node_set[j]];
+  const int* own = B.own_idx + B.own_off[j];
+  const int* cptr = B.cmap_ptr + B.cm_off[j];
+  const T* G = static_cast<const T*>(B.G) + B.goff[j];
+  const int wo = B.w_off[j];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int rb = 0; rb < st.nrhs; rb += RB) {
+    const int nr = min(RB, st.nrhs - rb);
+    for (int p = threadIdx.x; p < s; p += blockDim.x) {
+      const int gd = own[p];
+      const int c0 = cptr[p], c1 = cptr[p + 1];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        double v = 0.0;
+        if (r < nr) v = st.b[rb + r][gd] - gather_updates(B, st.w[rb + r], c0, c1);
+        sm[p * RB + r] = (T)v;
+      }
+    }
+    __syncthreads();
+    for (int row = r0 + warp; row < r1; row += nw) {
+      T acc[RB];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = T(0);
+      const T* g = G + (long long)row * s;
+      for (int c = lane; c < s; c += 32) {
+        const T gv = __ldg(g + c);
+#pragma unroll
+        for (int r = 0; r < RB; ++r) acc[r] += gv * sm[c * RB + r];
+      }
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = group_sum(acc[r], 32);
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        if (lane == r && r < nr) {
+          if (row < s) {
+            st.y[rb + r][own[row]] = (double)acc[r];
+          } else {
+            const int t = row - s;
+            double* w = st.w[rb + r];
+            const double cu = gather_updates(B, w, cptr[row], cptr[row + 1]);
+            w[wo + t] = cu + (double)acc[r];
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Forward sweep, small node (s <= kSmallCols): one warp, lane groups per row.
+template <typename T, int RB>
+__device__ void fwd_small(const BankView& B, const SetsView& S, int j, T* sm) {
+  const int s = B.s[j], m = B.m[j];
+  const SetView& st = S.set[B.node_set[j]];
+  const int* own = B.own_idx + B.own_off[j];
+  const int* cptr = B.cmap_ptr + B.cm_off[j];
+  const T* G = static_cast<const T*>(B.G) + B.goff[j];
+  const int wo = B.w_off[j];
+  const int lane = threadIdx.x & 31;
+  const int g = s <= 4 ? 4 : (s <= 8 ? 8 : (s <= 16 ? 16 : 32));
+  const int per = 32 / g, grp = lane / g, gl = lane % g;
+  for (int rb = 0; rb < st.nrhs; rb += RB) {
+    const int nr = min(RB, st.nrhs - rb);
+    for (int p = lane; p < s; p += 32) {
+      const int gd = own[p];
+      const int c0 = cptr[p], c1 = cptr[p + 1];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        double v = 0.0;
+        if (r < nr) v = st.b[rb + r][gd] - gather_updates(B, st.w[rb + r], c0, c1);
+        sm[p * RB + r] = (T)v;
+      }
+    }
+    __syncwarp();
+    for (int row0 = 0; row0 < s + m; row0 += per) {
+      const int row = row0 + grp;
+      T acc[RB];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = T(0);
+      if (row < s + m) {
+        const T* gr = G + (long long)row * s;
+        for (int c = gl; c < s; c += g) {
+          const T gv = __ldg(gr + c);
+#pragma unroll
+          for (int r = 0; r < RB; ++r) acc[r] += gv * sm[c * RB + r];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = group_sum(acc[r], g);
+      if (row < s + m) {
+#pragma unroll
+        for (int r = 0; r < RB; ++r) {
+          if ((r % g) == gl && r < nr) {
+            if (row < s) {
+              st.y[rb + r][own[row]] = (double)acc[r];
+            } else {
+              double* w = st.w[rb + r];
+              const double cu = gather_updates(B, w, cptr[row], cptr[row + 1]);
+              w[wo + row - s] = cu + (double)acc[r];
+            }
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Backward sweep, large node: rows [r0, r1) of Hb * [y_own ; x_upd].
+template <typename T, int RB>
+__device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) {
+  const int j = it.x, r0 = it.y, r1 = it.z;
+  const int s = B.s[j], m = B.m[j], f = s + m;
+  const SetView& st = S.set[B.node_set[j]];
+  const int* own = B.own_idx + B.own_off[j];
+  const int* upd = B.upd_idx + B.upd_off[j];
+  const T* H = static_cast<const T*>(B.H) + B.hoff[j];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int rb = 0; rb < st.nrhs; rb += RB) {
+    const int nr = min(RB, st.nrhs - rb);
+    for (int p = threadIdx.x; p < f; p += blockDim.x) {
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        double v = 0.0;
+        if (r < nr) v = (p < s) ? st.y[rb + r][own[p]] : st.x[rb + r][upd[p - s]];
+        sm[p * RB + r] = (T)v;
+      }
+    }
+    __syncthreads();
+    for (int row = r0 + warp; row < r1; row += nw) {
+      T acc[RB];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = T(0);
+      const T* h = H + (long long)row * f;
+      for (int c = lane; c < f; c += 32) {
+        const T hv = __ldg(h + c);
+#pragma unroll
+        for (int r = 0; r < RB; ++r) acc[r] += hv * sm[c * RB + r];
+      }
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = group_sum(acc[r], 32);
+#pragma unroll
+      for (int r = 0; r < RB; ++r)
+        if (lane == r && r < nr) st.x[rb + r][own[row]] = (double)acc[r];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int RB>
+__device__ void bwd_small(const BankView& B, const SetsView& S, int j, T* sm) {
+  const int s = B.s[j], m = B.m[j], f = s + m;
+  const SetView& st = S.set[B.node_set[j]];
+  const int* own = B.own_idx + B.own_off[j];
+  const int* upd = B.upd_idx + B.upd_off[j];
+  const T* H = static_cast<const T*>(B.H) + B.hoff[j];
+  const int lane = threadIdx.x & 31;
+  const int g = f <= 4 ? 4 : (f <= 8 ? 8 : (f <= 16 ? 16 : 32));
+  const int per = 32 / g, grp = lane / g, gl = lane % g;
+  for (int rb = 0; rb < st.nrhs; rb += RB) {
+    const int nr = min(RB, st.nrhs - rb);
+    for (int p = lane; p < f; p += 32) {
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        double v = 0.0;
+        if (r < nr) v = (p < s) ? st.y[rb + r][own[p]] : st.x[rb + r][upd[p - s]];
+        sm[p * RB + r] = (T)v;
+      }
+    }
+    __syncwarp();
+    for (int row0 = 0; row0 < s; row0 += per) {
+      const int row = row0 + grp;
+      T acc[RB];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = T(0);
+      if (row < s) {
+        const T* hr = H + (long long)row * f;
+        for (int c = gl; c < f; c += g) {
+          const T hv = __ldg(hr + c);
+#pragma unroll
+          for (int r = 0; r < RB; ++r) acc[r] += hv * sm[c * RB + r];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = group_sum(acc[r], g);
+      if (row < s) {
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+          if ((r % g) == gl && r < nr) st.x[rb + r][own[row]] = (double)acc[r];
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <typename T, int RB>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_forward(BankView B, SetsView S, const int4* __restrict__ items, int n_large,
+              const int* __restrict__ small, int n_small) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  if ((int)blockIdx.x < n_large) {
+    fwd_large<T, RB>(B, S, items[blockIdx.x], sm);
+  } else {
+    const int wib = threadIdx.x >> 5;
+    const int idx = ((int)blockIdx.x - n_large) * (kSolveThreads / 32) + wib;
+    if (idx < n_small) fwd_small<T, RB>(B, S, small[idx], sm + wib * kSmallCols * RB);
+  }
+}
+
+template <typename T, int RB>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_backward(BankView B, SetsView S, const int4* __restrict__ items, int n_large,
+               const int* __restrict__ small, int n_small) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  if ((int)blockIdx.x < n_large) {
+    bwd_large<T, RB>(B, S, items[blockIdx.x], sm);
+  } else {
+    const int wib = threadIdx.x >> 5;
+    const int idx = ((int)blockIdx.x - n_large) * (kSolveThreads / 32) + wib;
+    if (idx < n_small) bwd_small<T, RB>(B, S, small[idx], sm + wib * kSmallCols * RB);
+  }
+}
+
+template <typename T, int RB>
+void launch_level(bool forward, const BankView& B, const SetsView& S, const LevelPlan& L,
+                  cudaStream_t st) {
+  const int warps = kSolveThreads / 32;
+  const int nblk = L.n_large + (L.n_small + warps - 1) / warps;
+  if (nblk == 0) return;
+  size_t sm_large = (size_t)L.max_cols * RB * sizeof(T);
+  size_t sm_small = L.n_small ? (size_t)warps * kSmallCols * RB * sizeof(T) : 0;
+  size_t smem = std::max(sm_large, sm_small);
+  if (forward)
+    k_forward<T, RB><<<nblk, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.small.p,
+                                                         L.n_small);
+  else
+    k_backward<T, RB><<<nblk, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.small.p,
+                                                          L.n_small);
+  PECS_CUDA(cudaGetLastError());
+}
+
+template <typename T, int RB>
+void set_smem_limit(size_t bytes) {
+  PECS_CUDA(cudaFuncSetAttribute(k_forward<T, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bytes));
+  PECS_CUDA(cudaFuncSetAttribute(k_backward<T, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bytes));
+}
+
+template <typename T>
+void launch_rb(int rb, bool forward, const BankView& B, const SetsView& S, const LevelPlan& L,
+               cudaStream_t st) {
+  switch (rb) {
+    case 1: launch_level<T, 1>(forward, B, S, L, st); break;
+    case 2: launch_level<T, 2>(forward, B, S, L, st); break;
+    case 4: launch_level<T, 4>(forward, B, S, L, st); break;
+    default: launch_level<T, 8>(forward, B, S, L, st); break;
+  }
+}
+
+}  // namespace
+
+BankView FactorBank::view() const {
+  BankView v;
+  v.s = s_.p;
+  v.m = m_.p;
+  v.goff = goff_.p;
+  v.hoff = hoff_.p;
+  v.own_off = own_off_.p;
+  v.upd_off = upd_off_.p;
+  v.w_off = w_off_.p;
+  v.cm_off = cm_off_.p;
+  v.own_idx = own_idx_.p;
+  v.upd_idx = upd_idx_.p;
+  v.cmap_ptr = cmap_ptr_.p;
+  v.cmap_idx = cmap_idx_.p;
+  v.node_set = node_set_.p;
+  v.G = prec_ == PECS_PREC_FP64 ? (const void*)G64_.p : (const void*)G32_.p;
+  v.H = prec_ == PECS_PREC_FP64 ? (const void*)H64_.p : (const void*)H32_.p;
+  return v;
+}
+
+int FactorBank::kernel_launches_per_solve() const {
+  int n = 0;
+  for (auto& l : fwd_) n += (l.n_large + l.n_small) > 0;
+  for (auto& l : bwd_) n += (l.n_large + l.n_small) > 0;
+  return n;
+}
+
+void FactorBank::build(const std::vector<const MfFactor*>& factors, int precision) {
+  if (factors.empty() || (int)factors.size() > kMaxSets)
+    throw PecsError(PECS_E_ARG, "factor bank needs 1..4 factors");
+  prec_ = precision;
+  n_sets_ = (int)factors.size();
+  std::vector<int> hs, hm, own_off, upd_off, w_off, cm_off, own_idx, upd_idx, cmap_ptr, cmap_idx,
+      node_set;
+  std::vector<long long> goff, hoff;
+  std::vector<double> G, H;
+  long long go = 0, ho = 0;
+  int wtot = 0;
+  struct LevelNodes {
+    std::vector<int> nodes;
+  };
+  std::vector<LevelNodes> fl, bl;
+  int base = 0;
+  for (int fi = 0; fi < n_sets_; ++fi) {
+    const MfFactor& F = *factors[fi];
+    const int N = (int)F.nodes.size();
+    if ((int)F.Gf.size() != N) throw PecsError(PECS_E_STATE, "factor not factorised");
+    // update-vector offsets are local to the factor: each RHS owns a buffer of
+    // set_wtotal(set) doubles
+    std::vector<int> wbase(N);
+    wtot = 0;
+    for (int j = 0; j < N; ++j) {
+      wbase[j] = wtot;
+      wtot += F.nodes[j].m;
+    }
+    set_wtotal_[fi] = std::max(1, wtot);
+    std::vector<int> fpos(F.n, -1);
+    for (int j = 0; j < N; ++j) {
+      const MfNode& nd = F.nodes[j];
+      hs.push_back(nd.s);
+      hm.push_back(nd.m);
+      own_off.push_back((int)own_idx.size());
+      upd_off.push_back((int)upd_idx.size());
+      own_idx.insert(own_idx.end(), nd.own.begin(), nd.own.end());
+      upd_idx.insert(upd_idx.end(), nd.upd.begin(), nd.upd.end());
+      w_off.push_back(wbase[j]);
+      node_set.push_back(fi);
+      goff.push_back(go);
+      hoff.push_back(ho);
+      G.insert(G.end(), F.Gf[j].begin(), F.Gf[j].end());
+      H.insert(H.end(), F.Hb[j].begin(), F.Hb[j].end());
+      go += (long long)F.Gf[j].size();
+      ho += (long long)F.Hb[j].size();
+      // extend-add gather lists per front position
+      const int f = nd.s + nd.m;
+      for (int t = 0; t < nd.s; ++t) fpos[nd.own[t]] = t;
+      for (int t = 0; t < nd.m; ++t) fpos[nd.upd[t]] = nd.s + t;
+      std::vector<std::vector<int>> lists(f);
+      for (int c : nd.children) {
+        const MfNode& ch = F.nodes[c];
+        for (int a = 0; a < ch.m; ++a) {
+          int p = fpos[ch.upd[a]];
+          if (p < 0) throw PecsError(PECS_E_STATE, "extend-add map mismatch");
+          lists[p].push_back(wbase[c] + a);
+        }
+      }
+      for (int t = 0; t < nd.s; ++t) fpos[nd.own[t]] = -1;
+      for (int t = 0; t < nd.m; ++t) fpos[nd.upd[t]] = -1;
+      cm_off.push_back((int)cmap_ptr.size());
+      for (int p = 0; p < f; ++p) {
+        cmap_ptr.push_back((int)cmap_idx.size());
+        cmap_idx.insert(cmap_idx.end(), lists[p].begin(), lists[p].end());
+      }
+      cmap_ptr.push_back((int)cmap_idx.size());
+      if ((int)fl.size() <= nd.height) fl.resize(nd.height + 1);
+      if ((int)bl.size() <= nd.depth) bl.resize(nd.depth + 1);
+      fl[nd.height].nodes.push_back(base + j);
+      bl[nd.depth].nodes.push_back(base + j);
+    }
+    base += N;
+  }
+  entries_ = go + ho;
+  s_.upload(hs);
+  m_.upload(hm);
+  own_off_.upload(own_off);
+  upd_off_.upload(upd_off);
+  w_off_.upload(w_off);
+  cm_off_.upload(cm_off);
+  own_idx_.upload(own_idx);
+  upd_idx_.upload(upd_idx);
+  cmap_ptr_.upload(cmap_ptr);
+  cmap_idx_.upload(cmap_idx);
+  node_set_.upload(node_set);
+  goff_.upload(goff);
+  hoff_.upload(hoff);
+  if (prec_ == PECS_PREC_FP64) {
+    G64_.upload(G);
+    H64_.upload(H);
+    bytes_ = (long long)(G.size() + H.size()) * 8;
+  } else {
+    std::vector<float> g32(G.begin(), G.end()), h32(H.begin(), H.end());
+    G32_.upload(g32);
+    H32_.upload(h32);
+    bytes_ = (long long)(G.size() + H.size()) * 4;
+  }
+  // level plans
+  auto make = [&](const std::vector<LevelNodes>& lv, bool forward, std::vector<LevelPlan>& out) {
+    out.clear();
+    out.resize(lv.size());
+    for (size_t l = 0; l < lv.size(); ++l) {
+      std::vector<int4> items;
+      std::vector<int> small;
+      int max_cols = 0;
+      long long tot = 0;
+      for (int g : lv[l].nodes) tot += (long long)hs[g] * (hs[g] + hm[g]);
+      // aim for enough work items to occupy the GPU, but not tiny ones
+      const long long target = std::max<long long>(4096, tot / 600);
+      for (int g : lv[l].nodes) {
+        const int s = hs[g], m = hm[g], f = s + m;
+        const int cols = forward ? s : f;
+        const int rows = forward ? f : s;
+        const bool is_small = cols <= kSmallCols && (long long)rows * cols <= 16384;
+        if (is_small) {
+          small.push_back(g);
+        } else {
+          int per = (int)std::max<long long>(1, std::min<long long>(rows, target / std::max(1, cols)));
+          for (int r0 = 0; r0 < rows; r0 += per) items.push_back(make_int4(g, r0, std::min(rows, r0 + per), 0));
+          max_cols = std::max(max_cols, cols);
+        }
+      }
+      out[l].n_large = (int)items.size();
+      out[l].n_small = (int)small.size();
+      out[l].max_cols = max_cols;
+      out[l].items.upload(items);
+      out[l].small.upload(small);
+    }
+  };
+  make(fl, true, fwd_);
+  make(bl, false, bwd_);
+  max_cols_ = 0;
+  for (auto& l : fwd_) max_cols_ = std::max(max_cols_, l.max_cols);
+  for (auto& l : bwd_) max_cols_ = std::max(max_cols_, l.max_cols);
+  const size_t esz = prec_ == PECS_PREC_FP64 ? 8 : 4;
+  const size_t small_need = (size_t)(kSolveThreads / 32) * kSmallCols * esz;
+  max_rb_ = 8;
+  while (max_rb_ > 1 && std::max((size_t)max_cols_, small_need / esz) * max_rb_ * esz > kSmemCap)
+    max_rb_ /= 2;
+  if ((size_t)max_cols_ * esz > kSmemCap) throw PecsError(PECS_E_ARG, "front too large for shared memory");
+  const size_t lim = kSmemCap;
+  if (prec_ == PECS_PREC_FP64) {
+    set_smem_limit<double, 1>(lim);
+    set_smem_limit<double, 2>(lim);
+    set_smem_limit<double, 4>(lim);
+    set_smem_limit<double, 8>(lim);
+  } else {
+    set_smem_limit<float, 1>(lim);
+    set_smem_limit<float, 2>(lim);
+    set_smem_limit<float, 4>(lim);
+    set_smem_limit<float, 8>(lim);
+  }
+}
+
+void FactorBank::solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const {
+  const BankView B = view();
+  int rb = max_nrhs <= 1 ? 1 : (max_nrhs <= 2 ? 2 : (max_nrhs <= 4 ? 4 : 8));
+  rb = std::min(rb, max_rb_);
+  for (const LevelPlan& L : fwd_) {
+    if (prec_ == PECS_PREC_FP64)
+      launch_rb<double>(rb, true, B, sets, L, st);
+    else
+      launch_rb<float>(rb, true, B, sets, L, st);
+  }
+  for (const LevelPlan& L : bwd_) {
+    if (prec_ == PECS_PREC_FP64)
+      launch_rb<double>(rb, false, B, sets, L, st);
+    else
+      launch_rb<float>(rb, false, B, sets, L, st);
+  }
+}
+
+}  // namespace pecs

@@ -1,0 +1,92 @@
+// Level-scheduled application of multifrontal LU factors on the GPU.
+//
+// A FactorBank holds one or more factors (mf.hpp) concatenated node-wise.  Each
+// factor is bound to a "RHS set": a list of right-hand sides that share the
+// factor (e.g. electrons and holes of every instance when their mobilities
+// are equal), so that every stored factor entry read from HBM is applied to
+// all of them.  One kernel launch processes one tree level of every factor in
+// the bank: large nodes are split into row chunks handled by a CTA each
+// (warp per row, coalesced row-major reads, warp-shuffle reduction); small
+// nodes are handled by one warp each (lane groups per row).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "common.hpp"
+#include "mf.hpp"
+
+namespace pecs {
+
+constexpr int kMaxSets = 4;
+constexpr int kSmallCols = 128;   // small-node path: columns staged per warp
+constexpr int kSolveThreads = 256;
+constexpr size_t kSmemCap = 200 * 1024;  // dynamic shared memory budget per CTA
+
+struct BankView {  // device pointers, passed by value to kernels
+  const int* s;
+  const int* m;
+  const long long* goff;
+  const long long* hoff;
+  const int* own_off;
+  const int* upd_off;
+  const int* w_off;
+  const int* cm_off;
+  const int* own_idx;
+  const int* upd_idx;
+  const int* cmap_ptr;
+  const int* cmap_idx;
+  const int* node_set;
+  const void* G;
+  const void* H;
+};
+
+struct SetView {
+  int nrhs;
+  double* const* b;  // right-hand sides (read)
+  double* const* y;  // forward result slots
+  double* const* w;  // update-vector workspace (set_wtotal(set) doubles each)
+  double* const* x;  // solutions (written)
+};
+
+struct SetsView {
+  SetView set[kMaxSets];
+};
+
+struct LevelPlan {
+  int n_large = 0, n_small = 0;
+  DBuf<int4> items;   // large: (node, row0, row1, 0)
+  DBuf<int> small;    // small nodes (warp each)
+  int max_cols = 0;   // staged columns per large item
+};
+
+class FactorBank {
+ public:
+  // factors[i] is bound to RHS set i.  precision: PECS_PREC_FP64 or FP32_IR.
+  void build(const std::vector<const MfFactor*>& factors, int precision);
+  // y = forward(b), x = backward(y); w is workspace.  All sets must be bound.
+  void solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const;
+  int set_wtotal(int set) const { return set_wtotal_[set]; }
+  int precision() const { return prec_; }
+  long long entries() const { return entries_; }
+  long long bytes() const { return bytes_; }
+  int n_fwd_levels() const { return (int)fwd_.size(); }
+  int n_bwd_levels() const { return (int)bwd_.size(); }
+  int kernel_launches_per_solve() const;
+
+ private:
+  int prec_ = PECS_PREC_FP64;
+  int n_sets_ = 0;
+  int set_wtotal_[kMaxSets] = {0, 0, 0, 0};
+  long long entries_ = 0, bytes_ = 0;
+  DBuf<int> s_, m_, own_off_, upd_off_, w_off_, cm_off_, own_idx_, upd_idx_, cmap_ptr_, cmap_idx_,
+      node_set_;
+  DBuf<long long> goff_, hoff_;
+  DBuf<double> G64_, H64_;
+  DBuf<float> G32_, H32_;
+  std::vector<LevelPlan> fwd_, bwd_;
+  int max_cols_ = 0, max_rb_ = 8;
+  BankView view() const;
+};
+
+}  // namespace pecs

@@ -1,0 +1,140 @@
+"""Host-side mirror of the reference's class surface on the hot path.
+
+Names, methods and their meaning follow the reference (paths relative to the
+reference project):
+
+* ``Carrier``      -- ChargeCarrierSpace::Carrier (include/Carrier.hpp:38-101):
+  ``set_solver()`` factorises ``system_matrix``; ``solve()`` maps
+  ``system_rhs`` to ``solution`` (source/Carrier.cpp:26-40).
+* ``CarrierPair``  -- ChargeCarrierSpace::CarrierPair (include/CarrierPair.hpp:30-110):
+  ``carrier_1``, ``carrier_2``, ``mass_matrix``, ``penalty``,
+  ``material_permittivity``; ``print_dofs``/``read_dofs`` (CarrierPair.cpp:89-121).
+* ``PoissonData``  -- Poisson::PoissonData (include/Poisson.hpp:26-84):
+  ``set_solver()``, ``solve()`` (LU apply + zero constrained dofs,
+  source/Poisson.cpp:90-105).
+* ``SolarCellProblem`` -- the IMEX loop driver of
+  SOLARCELL::SolarCellProblem::run_full_system (source/SolarCell.cpp:1898-2095)
+  with the stage methods it calls each step.
+
+Errors surface as ``PecsError`` (a RuntimeError), as the reference's
+exceptions reach ``main``'s ``catch (std::exception&)``.
+"""
+from __future__ import annotations
+
+from typing import Optional
+
+import numpy as np
+
+from . import _ffi as F
+from .api import LU, Context, Params
+
+
+class Carrier:
+    def __init__(self, name: str = "", charge_number: float = 0.0, scaled_mobility: float = 1.0):
+        self.name = name
+        self.charge_number = charge_number
+        self.scaled_mobility = scaled_mobility
+        self.system_matrix = None
+        self.system_rhs: Optional[np.ndarray] = None
+        self.solution: Optional[np.ndarray] = None
+        self._lu: Optional[LU] = None
+        # the caller's mesh information needed by nested dissection
+        self.dof_cell = None
+        self.dof_class = None
+        self.cell_xy = None
+
+    def set_name(self, name: str):
+        self.name = name
+
+    def set_solver(self, precision: int = F.PREC_FP64):
+        if self.system_matrix is None or self.dof_cell is None or self.cell_xy is None:
+            raise F.PecsError(F.PECS_E_STATE, "system_matrix and mesh maps must be set first")
+        self._lu = LU(self.system_matrix, self.dof_cell, self.cell_xy, self.dof_class, precision)
+
+    def solve(self):
+        if self._lu is None:
+            raise F.PecsError(F.PECS_E_STATE, "set_solver() must be called first")
+        self.solution = self._lu.solve(self.system_rhs)
+
+
+class CarrierPair:
+    def __init__(self):
+        self.carrier_1 = Carrier()
+        self.carrier_2 = Carrier()
+        self.mass_matrix = None
+        self.penalty = 1.0
+        self.delta_t = 0.0
+        self.material_permittivity = 1.0
+        self.material_name = ""
+
+    def set_name(self, name: str):
+        self.material_name = name
+
+    def print_dofs(self, directory: str = "."):
+        """deal.II Vector::block_write layout: size_t n, then n raw doubles."""
+        import os
+        for c in (self.carrier_1, self.carrier_2):
+            with open(os.path.join(directory, c.name + ".dofs"), "wb") as fh:
+                fh.write(np.uint64(c.solution.size).tobytes())
+                fh.write(np.ascontiguousarray(c.solution, dtype=np.float64).tobytes())
+
+    def read_dofs(self, directory: str = "."):
+        import os
+        for c in (self.carrier_1, self.carrier_2):
+            with open(os.path.join(directory, c.name + ".dofs"), "rb") as fh:
+                n = int(np.frombuffer(fh.read(8), dtype=np.uint64)[0])
+                c.solution = np.frombuffer(fh.read(8 * n), dtype=np.float64).copy()
+
+
+class PoissonData(Carrier):
+    def __init__(self):
+        super().__init__("Poisson")
+        self.constrained: Optional[np.ndarray] = None
+
+    def solve(self):
+        super().solve()
+        if self.constrained is not None:
+            self.solution[self.constrained] = 0.0
+
+
+class SolarCellProblem:
+    """The per-step stages of run_full_system on one GPU-resident context."""
+
+    def __init__(self, params: Params, precision: int = F.PREC_FP64):
+        self.sim_params = params
+        self.ctx = Context(params, precision=precision)
+        self.time = 0.0
+        self.counter = 0
+
+    # stage names of SolarCell.cpp:2057-2075
+    def assemble_semiconductor_rhs(self):
+        """Assembles both regions' carrier right-hand sides in one launch; the
+        electrolyte call below is then a no-op."""
+        self.ctx.assemble_carrier_rhs()
+        self._electrolyte_done = True
+
+    def assemble_electrolyte_rhs(self):
+        if not getattr(self, "_electrolyte_done", False):
+            self.ctx.assemble_carrier_rhs()
+        self._electrolyte_done = False
+
+    def solve_full_system(self):
+        self.ctx.solve_carriers()
+
+    def assemble_Poisson_rhs(self):  # noqa: N802 (reference name)
+        self.ctx.assemble_poisson_rhs()
+
+    def solve_Poisson(self):  # noqa: N802 (reference name)
+        self.ctx.solve_poisson()
+
+    def run_full_system(self, n_steps: int):
+        self.ctx.initialize()
+        for _ in range(n_steps):
+            self.assemble_semiconductor_rhs()
+            self.assemble_electrolyte_rhs()
+            self.solve_full_system()
+            self.assemble_Poisson_rhs()
+            self.solve_Poisson()
+            self.time += self.sim_params.dt
+            self.counter += 1
+        return self.ctx.state()

@@ -1,0 +1,40 @@
+"""The C-ABI library loads and exports every function include/*.h declares."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"\b([a-z_0-9]+)\s*\(", text):
+            name = m.group(1)
+            if name.startswith("pecs_") and not name.endswith("_t"):
+                names.add(name)
+    return sorted(names)
+
+
+def test_headers_declare_functions():
+    names = declared_functions()
+    assert "pecs_create" in names and "pecs_lu_factor" in names and "pecs_lu_host_apply" in names
+    assert len(names) >= 25
+
+
+def test_library_exports_every_declared_symbol(pecs_lib):
+    missing = [n for n in declared_functions() if not hasattr(pecs_lib, n)]
+    assert not missing, missing
+
+
+def test_no_device_is_a_clean_error(pecs_lib):
+    import pecs_gb300 as pg
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(pg.PecsError) as ei:
+        pg.Context(pg.config2(n_refine=2))
+    assert ei.value.code == pg._ffi.PECS_E_NODEVICE

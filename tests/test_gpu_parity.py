@@ -1,0 +1,136 @@
+"""GPU path (through the C ABI) against the CPU oracle on the same seeded
+inputs: right-hand-side assembly, the multifrontal solves, single steps,
+trajectories, batched instances and the FP32 + refinement variant."""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+import oracle
+import pecs_gb300 as pg
+from helpers import FIELD_OF, max_rel, rel_err, to_lib
+from test_lu_host import _maps_carrier, _maps_poisson
+
+pytestmark = pytest.mark.gpu
+
+STEP_TOL = 1e-10     # FP64 path vs FP64 oracle, relative L2 per field
+RHS_TOL = 1e-13
+
+
+def _ctx(P, **kw):
+    return pg.Context(to_lib(P), **kw)
+
+
+def _compare_state(ctx, st, tol, inst=0):
+    for name, v in st.items():
+        got = ctx.get_state(FIELD_OF[name], inst)
+        e = rel_err(got, v)
+        assert e < tol, (name, e)
+
+
+def test_lu_device_solve_matches_scipy(pecs_lib):
+    pb = oracle.Problem(oracle.config2_params(n_refine=3))
+    rng = np.random.default_rng(1)
+    dc, cl, xy = _maps_carrier(pb, pb.semi)
+    lu = pg.LU(pb.A_n, dc, xy, cl)
+    B = rng.standard_normal((3, pb.A_n.shape[0]))
+    X = lu.solve(B)
+    solver = spla.splu(pb.A_n.tocsc())
+    for r in range(3):
+        assert rel_err(X[r], solver.solve(B[r])) < 1e-11
+    dcp, xyp = _maps_poisson(pb)
+    lu = pg.LU(pb.A_P, dcp, xyp)
+    b = pb.poisson_rhs(pb.initial_state())
+    assert rel_err(lu.solve(b), spla.spsolve(pb.A_P.tocsc(), b)) < 1e-12
+    lu32 = pg.LU(pb.A_P, dcp, xyp, precision=pg.PREC_FP32_IR)
+    assert rel_err(lu32.solve(b), spla.spsolve(pb.A_P.tocsc(), b)) < 1e-4
+
+
+@pytest.mark.parametrize("P", [oracle.config2_params(n_refine=3), oracle.config1_params(),
+                               oracle.reference_params(3, 1, dt=1e-4),
+                               oracle.config2_params(n_refine=2, degree=2)],
+                         ids=["config2_r3", "config1", "reference_r3", "config2_r2_k2"])
+def test_initial_state_and_rhs(pecs_lib, P):
+    pb = oracle.Problem(P)
+    st = pb.initial_state()
+    ctx = _ctx(P)
+    ctx.initialize()
+    _compare_state(ctx, st, 1e-12)
+    ctx.assemble_carrier_rhs()
+    rhs = pb.carrier_rhs(st)
+    for name, v in rhs.items():
+        assert max_rel(ctx.get_rhs(FIELD_OF[name]), v) < RHS_TOL, name
+
+
+@pytest.mark.parametrize("P,steps", [(oracle.config2_params(n_refine=3), 20),
+                                     (oracle.config1_params(), 100),
+                                     (oracle.reference_params(3, 1, dt=1e-4), 10),
+                                     (oracle.config2_params(n_refine=2, degree=2), 10),
+                                     (oracle.config2_params(n_refine=3, mu=(1.0, 0.5, 2.0, 1.0)), 10)],
+                         ids=["config2_r3", "config1_100", "reference_r3", "config2_r2_k2", "mu_distinct"])
+def test_trajectory_matches_oracle(pecs_lib, P, steps):
+    pb = oracle.Problem(P)
+    st, _, _ = pb.run(steps)
+    ctx = _ctx(P)
+    ctx.initialize()
+    ctx.step(steps)
+    _compare_state(ctx, st, STEP_TOL)
+    if P.full_system:
+        assert abs(ctx.interface_current()[0] - pb.interface_current(st)) <= \
+            1e-10 * max(1e-30, abs(pb.interface_current(st)))
+
+
+def test_stage_api_equals_step(pecs_lib):
+    P = oracle.config2_params(n_refine=3)
+    a = _ctx(P)
+    a.initialize()
+    for _ in range(3):
+        a.assemble_carrier_rhs()
+        a.solve_carriers()
+        a.assemble_poisson_rhs()
+        a.solve_poisson()
+    b = _ctx(P)
+    b.initialize()
+    b.step(3)
+    for f in a.fields():
+        assert np.array_equal(a.get_state(f), b.get_state(f))
+
+
+def test_batched_instances_match_single(pecs_lib):
+    base = oracle.config2_params(n_refine=3)
+    Ps = [base.copy(phi_app=v, G0=g, tau_n=t, tau_p=t)
+          for v, g, t in ((0.0, 1.0, 1.0), (-0.3, 0.5, 0.3), (0.4, 2.0, 3.0))]
+    ctx = pg.Context([to_lib(P) for P in Ps])
+    ctx.initialize()
+    ctx.step(10)
+    for i, P in enumerate(Ps):
+        st, _, _ = oracle.Problem(P).run(10)
+        _compare_state(ctx, st, STEP_TOL, inst=i)
+
+
+def test_steady_state_graph_and_eager_agree(pecs_lib):
+    P = oracle.config2_params(n_refine=2)
+    res = []
+    for graphs in (True, False):
+        ctx = _ctx(P, use_graphs=graphs)
+        ctx.initialize()
+        steps, rel = ctx.run_to_steady_state(600, 1e-6, check_every=64)
+        res.append((steps[0], ctx.state()))
+    assert res[0][0] == res[1][0]
+    for k in res[0][1]:
+        assert np.array_equal(res[0][1][k], res[1][1][k])
+    pb = oracle.Problem(P)
+    st, n, last = pb.run(600, tol=1e-6)
+    assert abs(n - res[0][0]) <= 1
+    if n == res[0][0]:
+        for k, v in st.items():
+            assert rel_err(res[0][1][k], v) < STEP_TOL
+
+
+def test_fp32_refined_matches_fp64_oracle(pecs_lib):
+    P = oracle.config2_params(n_refine=3)
+    pb = oracle.Problem(P)
+    st, _, _ = pb.run(20)
+    ctx = _ctx(P, precision=pg.PREC_FP32_IR, ir_max_iters=3)
+    ctx.initialize()
+    ctx.step(20)
+    _compare_state(ctx, st, 1e-9)

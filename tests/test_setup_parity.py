@@ -1,0 +1,59 @@
+"""The library's host setup (meshes, DoF maps, LDG and mixed matrices) against
+the oracle's restatement of SolarCellProblem's setup (SolarCell.cpp:377-932,
+LDG.cpp:40-678, MixedFEM.cpp:29-164).  Runs on the CPU via host_setup_only."""
+import numpy as np
+import pytest
+
+import oracle
+import pecs_gb300 as pg
+from helpers import to_lib
+
+CASES = [
+    ("config1", oracle.config1_params()),
+    ("config2_r3", oracle.config2_params(n_refine=3)),
+    ("reference_r3_k1", oracle.reference_params(3, 1)),
+    ("reference_r2_k2", oracle.reference_params(2, 2)),
+    ("config2_r2_k2_mu", oracle.config2_params(n_refine=2, degree=2, mu=(1.0, 0.5, 2.0, 1.0))),
+]
+
+
+def _cmp(A, B):
+    D = (A - B).tocsr()
+    D.eliminate_zeros()
+    scale = max(abs(B).max(), 1e-300)
+    return (abs(D).max() if D.nnz else 0.0) / scale
+
+
+@pytest.mark.parametrize("name,P", CASES, ids=[c[0] for c in CASES])
+def test_matrices_match_oracle(pecs_lib, name, P):
+    ctx = pg.Context(to_lib(P), host_setup_only=True)
+    pb = oracle.Problem(P)
+    assert _cmp(ctx.matrix(pg.MAT_N), pb.A_n) < 1e-14
+    assert _cmp(ctx.matrix(pg.MAT_P), pb.A_p) < 1e-14
+    assert _cmp(ctx.matrix(pg.MAT_POISSON), pb.A_P) < 1e-14
+    assert _cmp(ctx.matrix(pg.MAT_MASS_SEMI), pb.M_semi) < 1e-14
+    if P.full_system:
+        assert _cmp(ctx.matrix(pg.MAT_R), pb.A_r) < 1e-14
+        assert _cmp(ctx.matrix(pg.MAT_O), pb.A_o) < 1e-14
+        assert _cmp(ctx.matrix(pg.MAT_MASS_ELEC), pb.M_elec) < 1e-14
+    info = ctx.info()
+    assert list(info.ndofs)[:2] == [pb.semi.ndofs, pb.semi.ndofs]
+    assert info.ndofs[4] == pb.pois.ndofs
+
+
+def test_equal_mobilities_share_one_factor(pecs_lib):
+    ctx = pg.Context(pg.config2(n_refine=2), host_setup_only=True)
+    assert ctx.info().n_distinct_carrier_factors == 2
+    ctx = pg.Context(pg.config2(n_refine=2, mu=(1.0, 0.5, 1.0, 1.0)), host_setup_only=True)
+    assert ctx.info().n_distinct_carrier_factors == 3
+
+
+def test_invalid_params_are_rejected(pecs_lib):
+    with pytest.raises(pg.PecsError):
+        pg.Context(pg.config2(n_refine=2, degree=3), host_setup_only=True)
+    with pytest.raises(pg.PecsError):
+        pg.Context(pg.config2(n_refine=2, dt=0.0), host_setup_only=True)
+    a = pg.config2(n_refine=2)
+    b = pg.config2(n_refine=3)
+    with pytest.raises(pg.PecsError):
+        pg.Context([a, b], host_setup_only=True)
