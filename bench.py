@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark: steady-state I-V points per second of the PECS half cell on GB300.
+
+Workload (N=1): the coupled semiconductor--electrolyte half cell of the
+benchmark's second configuration -- semiconductor [0,1]^2 and electrolyte
+[1,2]x[0,1], 64x64 cells each (refinement 6), LDG degree 1, mixed RT_0 x DGQ_0
+Poisson (the reference's RT_{k-1} x DGQ_{k-1} pairing), dt = 1e-3, marched from
+the equilibrium initial state until the relative change of every field is
+<= 1e-8 or 5000 steps.  One bench step = one I-V point (one instance) computed
+to steady state.  Inputs are synthetic (no dataset exists for this model).
+
+  value   device-resident throughput: initial state already in HBM; the timed
+          region is initial Poisson solve + time marching with the steady-state
+          test, bracketed by CUDA events on the library's stream.
+  e2e     the same through the public C ABI call pecs_iv_sweep with host
+          buffers: initial state host->device, run, currents and final fields
+          device->host, every step.
+
+--impl reference times the CPU oracle (the restatement of the reference's
+numerics; the deal.II reference itself cannot be built here) on the host cores
+for a bounded sample of the same workload.
+
+Multi-GPU: I-V points are independent, so each rank marches its own instances
+(weak scaling, no data-path collective); the barrier and max-over-ranks time
+use torch.distributed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+MAX_STEPS = 5000
+TOL = 1e-8
+CHECK_EVERY = 50
+L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--refine", type=int, default=6)
+    ap.add_argument("--precision", choices=["fp64", "fp32ir"], default="fp64")
+    ap.add_argument("--n-inst", type=int, default=1, help="instances per GPU per bench step")
+    ap.add_argument("--cpu-sample-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons)}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def load_traffic(key: str):
+    """Per-launch DRAM bytes from the committed ncu summary (profiles/), or None."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+def workload_params(args, rank):
+    import pecs_gb300 as pg
+    n = args.n_inst
+    ps = []
+    for i in range(n):
+        # each rank/instance one point of an I-V sweep (bias in thermal-voltage units)
+        g = rank * n + i
+        bias = 0.0 if n == 1 else -0.5 + (g % 64) / 63.0
+        ps.append(pg.config2(n_refine=args.refine, phi_app=bias))
+    return ps
+
+
+def cpu_baseline(args, steps_to_ss, sample_steps):
+    """The oracle on the host cores: a bounded sample of time steps of the
+    same workload, extrapolated to I-V points/sec with the steps to steady
+    state measured on the GPU."""
+    import oracle
+    P = oracle.config2_params(n_refine=args.refine)
+    pb = oracle.Problem(P)
+    st = pb.initial_state()
+    st = pb.step(st)  # first step builds the LU factors (setup, untimed)
+    t0 = time.perf_counter()
+    for _ in range(sample_steps):
+        st = pb.step(st)
+    dt = (time.perf_counter() - t0) / sample_steps
+    return {"value": 1.0 / (steps_to_ss * dt), "unit": "I-V points/s", "cores": 1, "kind": "port",
+            "sample": f"{sample_steps} IMEX steps of the 64x64+64x64 half cell on the numpy/SuperLU "
+                      f"oracle ({dt * 1e3:.1f} ms/step) x {steps_to_ss} steps to steady state"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import oracle
+    P = oracle.config2_params(n_refine=args.refine)
+    pb = oracle.Problem(P)
+    st = pb.initial_state()
+    st = pb.step(st)
+    steps_to_ss = MAX_STEPS  # the oracle cannot march 5000 steps in a bounded sample
+    per = []
+    for _ in range(args.warmup):
+        st = pb.step(st)
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for _ in range(args.cpu_sample_steps):
+            st = pb.step(st)
+        per.append((time.perf_counter() - t0) / args.cpu_sample_steps)
+    dt = statistics.mean(per)
+    value = 1.0 / (steps_to_ss * dt)
+    line = {
+        "impl": "reference", "metric": "I-V points/sec to steady state", "value": value,
+        "unit": "I-V points/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * steps_to_ss * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"half cell 2x{2**args.refine}x{2**args.refine}, k=1, dt=1e-3, "
+                               f"to steady state (<= {MAX_STEPS} steps)"},
+        "cpu_baseline": {"value": value, "unit": "I-V points/s", "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} x {args.cpu_sample_steps} IMEX steps on the oracle "
+                                   f"({dt * 1e3:.1f} ms/step), extrapolated to {steps_to_ss} steps"},
+        "e2e": {"value": value, "unit": "I-V points/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+
+    import pecs_gb300 as pg
+
+    world, rank, local = dist_init(args)
+    pg.build()
+    prec = pg.PREC_FP64 if args.precision == "fp64" else pg.PREC_FP32_IR
+    params = workload_params(args, rank)
+    ctx = pg.Context(params, precision=prec, device=local)
+    info = ctx.info()
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def one_point():
+        ctx.initialize()
+        steps, rel = ctx.run_to_steady_state(MAX_STEPS, TOL, CHECK_EVERY)
+        return steps, ctx.last_run_steps()
+
+    for _ in range(args.warmup):
+        one_point()
+    # ---- timed region (device-resident inputs) ------------------------------------
+    steps_seen, executed = [], 0
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        ms = 0.0
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0.record(stream)
+            s, ex = one_point()
+            e1.record(stream)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+            steps_seen.append(int(np.max(s)))
+            executed += ex
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = max_over_ranks(ms, world)
+    points = args.n_inst * world * args.steps
+    value = points / (ms * 1e-3)
+    clocks = clk.summary()
+    # ---- end-to-end through the public API (host buffers, pinned) --------------------
+    ctx.initialize()
+    init = {}
+    keep = []
+    h2d = 0
+    for f in range(5):
+        if info.ndofs[f]:
+            t = torch.empty(args.n_inst * info.ndofs[f], dtype=torch.float64, pin_memory=True)
+            a = t.numpy()
+            for i in range(args.n_inst):
+                a[i * info.ndofs[f]:(i + 1) * info.ndofs[f]] = ctx.get_state(f, i)
+            keep.append(t)
+            init[f] = a
+            h2d += a.nbytes
+    d2h = args.n_inst * 8 + sum(args.n_inst * info.ndofs[f] * 8 for f in range(5))
+    ctx.iv_sweep(MAX_STEPS, TOL, CHECK_EVERY, init=init, want_fields=True)  # warm
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cur, st_e2e, fin = ctx.iv_sweep(MAX_STEPS, TOL, CHECK_EVERY, init=init, want_fields=True)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = points / e2e_s
+    # ---- roofline of the dominant kernel: the carrier solve sweep ---------------------
+    ctx.initialize()
+    solve_ms = ctx.time_solve(0, reps=30)
+    nlaunch = info.solve_launches[0]
+    bytes_per_launch = info.solve_bytes[0] / nlaunch
+    achieved = bytes_per_launch / (solve_ms * 1e-3 / nlaunch) / 1e9
+    peak, peak_kind = load_peaks()
+    pois_ms = ctx.time_solve(1, reps=30)
+    launches = executed * info.launches_per_step + args.steps * (1 + info.solve_launches[1])
+    steps_to_ss = int(statistics.median(steps_seen))
+    line = {
+        "metric": "I-V points/sec to steady state", "value": value, "unit": "I-V points/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if prec == pg.PREC_FP64 else "f32 factors + f64 refinement",
+        "data": "synthetic",
+        "config": {"workload": f"half cell 2x{2**args.refine}x{2**args.refine}, LDG k=1, "
+                               f"RT0xDGQ0 Poisson, dt=1e-3, to rel. change <= {TOL} "
+                               f"(<= {MAX_STEPS} steps)",
+                   "instances_per_gpu": args.n_inst, "precision": args.precision,
+                   "steps_to_steady_state": steps_to_ss,
+                   "l2": "flushed (512 MB write) before each timed I-V point; factors "
+                         f"{info.factor_bytes / 1e6:.0f} MB > 129 MB L2"},
+        "e2e": {"value": e2e, "unit": "I-V points/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": load_traffic(f"carrier_solve_r{args.refine}_{args.precision}"),
+                     "kernel": "k_forward/k_backward (carrier multifrontal solve sweep)",
+                     "solve_ms": solve_ms, "poisson_solve_ms": pois_ms,
+                     "bytes_per_sweep": info.solve_bytes[0], "launches_per_sweep": nlaunch},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, steps_to_ss, args.cpu_sample_steps)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -113,6 +113,9 @@ typedef struct pecs_info {
   long long factor_bytes;  /* device bytes of all factors */
   double setup_seconds;    /* host assembly + factorisation */
   int n_distinct_carrier_factors;
+  int launches_per_step;   /* kernel launches of one step incl. steady-state test */
+  double solve_bytes[2];   /* algorithmic bytes of one carrier / Poisson solve sweep */
+  int solve_launches[2];   /* kernel launches of one carrier / Poisson solve sweep */
 } pecs_info;
 
 typedef struct pecs_ctx pecs_ctx;
@@ -160,6 +163,14 @@ int pecs_interface_current(pecs_ctx* ctx, double* out);
 int pecs_iv_sweep(pecs_ctx* ctx, const double* const* init_fields, int max_steps, double tol,
                   int check_every, double* currents, int* steps, double* const* final_fields);
 int pecs_synchronize(pecs_ctx* ctx);
+/* Time steps executed by the last pecs_run_to_steady_state / pecs_iv_sweep
+ * (including steps of a polling interval after the last instance converged). */
+int pecs_last_run_steps(pecs_ctx* ctx);
+/* CUDA stream the context launches on (cudaStream_t as void*). */
+void* pecs_get_stream(pecs_ctx* ctx);
+/* Mean device time (CUDA events on the context's stream) of `reps` back-to-back
+ * applications of the carrier (which = 0) or Poisson (1) factors to all RHS. */
+int pecs_time_solve(pecs_ctx* ctx, int which, int reps, double* ms_per_solve);
 
 /* ---- drop-in direct solver for an externally assembled matrix ------------
  * Carrier::set_solver / PoissonData::set_solver (Carrier.cpp:26-32,

@@ -56,7 +56,8 @@ class pecs_info(C.Structure):
         ("n_inst", C.c_int), ("ndofs", C.c_int * 5), ("factor_entries", C.c_longlong * 3),
         ("factor_levels", C.c_int * 3), ("factor_nodes", C.c_int * 3),
         ("factor_bytes", C.c_longlong), ("setup_seconds", C.c_double),
-        ("n_distinct_carrier_factors", C.c_int),
+        ("n_distinct_carrier_factors", C.c_int), ("launches_per_step", C.c_int),
+        ("solve_bytes", C.c_double * 2), ("solve_launches", C.c_int * 2),
     ]
 
 
@@ -92,6 +93,9 @@ SIGNATURES = [
     ("pecs_iv_sweep", C.c_int, [_vp, C.POINTER(_dp), C.c_int, C.c_double, C.c_int, _dp, _ip,
                                 C.POINTER(_dp)]),
     ("pecs_synchronize", C.c_int, [_vp]),
+    ("pecs_get_stream", _vp, [_vp]),
+    ("pecs_last_run_steps", C.c_int, [_vp]),
+    ("pecs_time_solve", C.c_int, [_vp, C.c_int, C.c_int, _dp]),
     ("pecs_lu_factor", C.c_int, [C.c_int, _ip, _ip, _dp, _ip, _ip, C.c_int, _dp, C.c_int, C.c_int,
                                  C.POINTER(_vp)]),
     ("pecs_lu_solve", C.c_int, [_vp, C.c_int, _dp, _dp]),

@@ -238,6 +238,21 @@ class Context:
                                              steps.ctypes.data_as(C.POINTER(C.c_int)), _dptr(rel)))
         return steps, rel
 
+    def last_run_steps(self) -> int:
+        return lib().pecs_last_run_steps(self._h)
+
+    def stream(self) -> int:
+        return lib().pecs_get_stream(self._h) or 0
+
+    def time_solve(self, which: int, reps: int = 20) -> float:
+        """Mean device milliseconds of one carrier (0) / Poisson (1) solve sweep."""
+        ms = C.c_double()
+        check(lib().pecs_time_solve(self._h, which, reps, C.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        check(lib().pecs_synchronize(self._h))
+
     def interface_current(self) -> np.ndarray:
         out = np.zeros(self.n_inst)
         check(lib().pecs_interface_current(self._h, _dptr(out)))

@@ -42,11 +42,12 @@ void set_error(const std::string& m) { g_last_error = m; }
 // small kernels: residual, axpy, steady-state test, interface current
 // ---------------------------------------------------------------------------
 
-struct VecList {  // up to 256 vectors of equal length per launch
+struct VecList {  // vectors of one refinement sweep
   const double* const* b;
   const double* const* x;
   double* const* out;
   const int* mat;  // matrix index per vector
+  const int* len;  // length per vector
 };
 
 struct CsrDev {
@@ -65,7 +66,7 @@ __global__ void k_residual(CsrSet M, VecList L, int n, const int* __restrict__ a
   const int v = blockIdx.y;
   if (active && !active[vec_inst[v]]) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || i >= L.len[v]) return;
   const CsrDev A = M.m[L.mat[v]];
   const double* x = L.x[v];
   double s = 0.0;
@@ -74,12 +75,12 @@ __global__ void k_residual(CsrSet M, VecList L, int n, const int* __restrict__ a
 }
 
 // x += d
-__global__ void k_axpy(double* const* x, const double* const* d, int n,
+__global__ void k_axpy(double* const* x, const double* const* d, const int* __restrict__ len,
                        const int* __restrict__ active, const int* __restrict__ vec_inst) {
   const int v = blockIdx.y;
   if (active && !active[vec_inst[v]]) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[v][i] += d[v][i];
+  if (i < len[v]) x[v][i] += d[v][i];
 }
 
 constexpr int kRedThreads = 256;
@@ -256,7 +257,7 @@ struct Engine {
   DBuf<double> iface_ne, iface_pe, sch_ne, sch_pe;
   DBuf<int> isemi, ielec;
   // vectors
-  DBuf<double> state[2][5], rhs[5], bconst[5], yv[5], res[5], delta[5], snap[5];
+  DBuf<double> state[2][5], rhs[5], bconst[5], yv[5], res[5], delta[5], snap[5], init_dev[4];
   std::vector<DBuf<double>> wbuf_c, wbuf_p;
   int cur = 0;
   bool carriers_advanced = false;
@@ -271,7 +272,43 @@ struct Engine {
   // graphs
   cudaGraphExec_t graph2[2] = {nullptr, nullptr};  // two steps starting from cur = 0 / 1
   bool graph_valid = false;
-  int kernel_launches_per_step = 0;
+  int launches_per_step() const {
+    const int it = opt.precision == PECS_PREC_FP32_IR ? (opt.ir_max_iters > 0 ? opt.ir_max_iters : 2) : 0;
+    const int lc = bank_c.kernel_launches_per_solve(), lp = bank_p.kernel_launches_per_solve();
+    return 1 + lc * (1 + it) + 2 * it + 1 + lp * (1 + it) + 2 * it + 3;
+  }
+  // algorithmic bytes of one application of a bank to all of its right-hand
+  // sides: every stored factor entry once, plus the vectors (b read, y write +
+  // read, x write, update vectors write + read)
+  double solve_bytes(int which) const {
+    const FactorBank& B = which == 0 ? bank_c : bank_p;
+    const SetTable& t = which == 0 ? tab_c[0][0] : tab_p[0][0];
+    double vec = 0.0;
+    for (int si = 0; si < kMaxSets; ++si) {
+      const int nr = t.view.set[si].nrhs;
+      if (nr == 0) continue;
+      const int fld = which == 0 ? carrier_set_fields()[si][0] : 4;
+      vec += (double)nr * (4.0 * nd[fld] * 8.0 + 2.0 * B.set_wtotal(si) * 8.0);
+    }
+    return (double)B.bytes() + vec;
+  }
+  double time_solves(int which, int reps) {
+    cudaEvent_t e0, e1;
+    PECS_CUDA(cudaEventCreate(&e0));
+    PECS_CUDA(cudaEventCreate(&e1));
+    const FactorBank& B = which == 0 ? bank_c : bank_p;
+    SetTable& t = which == 0 ? tab_c[nxt()][0] : tab_p[nxt()][0];
+    B.solve(t.view, t.max_nrhs, st);  // warm
+    PECS_CUDA(cudaEventRecord(e0, st));
+    for (int r = 0; r < reps; ++r) B.solve(t.view, t.max_nrhs, st);
+    PECS_CUDA(cudaEventRecord(e1, st));
+    PECS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    PECS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return (double)ms / reps;
+  }
 
   ~Engine() {
     for (auto& g : graph2)
@@ -438,6 +475,12 @@ struct Engine {
       bc.reserve(n);
       for (int i = 0; i < n_inst; ++i) bc.insert(bc.end(), S->bconst[f][i].begin(), S->bconst[f][i].end());
       bconst[f].upload(bc);
+      if (f < 4) {
+        std::vector<double> v;
+        v.reserve(n);
+        for (int i = 0; i < n_inst; ++i) v.insert(v.end(), S->init[f][i].begin(), S->init[f][i].end());
+        init_dev[f].upload(v);
+      }
     }
     // solve pointer tables
     int wc = 0, wp = 0;
@@ -591,7 +634,7 @@ struct Engine {
   struct IrLists {
     DBuf<const double*> b, x, d;
     DBuf<double*> out, xw;
-    DBuf<int> mat, vin;
+    DBuf<int> mat, vin, len;
     int nv = 0, n = 0;
   };
   IrLists ir[2][2];  // [target][0 carriers, 1 Poisson]
@@ -602,10 +645,11 @@ struct Engine {
         std::vector<int> flds = which ? std::vector<int>{4} : carrier_fields();
         std::vector<const double*> hb, hx, hd;
         std::vector<double*> hout, hxw;
-        std::vector<int> hm, hi;
+        std::vector<int> hm, hi, hl;
         int n = 0;
         for (int i = 0; i < n_inst; ++i)
           for (int f : flds) {
+            hl.push_back(nd[f]);
             hb.push_back(rhs[f].p + (size_t)i * nd[f]);
             hx.push_back(state[target][f].p + (size_t)i * nd[f]);
             hout.push_back(res[f].p + (size_t)i * nd[f]);
@@ -623,6 +667,7 @@ struct Engine {
         L.xw.upload(hxw);
         L.mat.upload(hm);
         L.vin.upload(hi);
+        L.len.upload(hl);
         L.nv = (int)hb.size();
         L.n = n;
       }
@@ -635,12 +680,12 @@ struct Engine {
     if (opt.precision != PECS_PREC_FP32_IR) return;
     const int iters = opt.ir_max_iters > 0 ? opt.ir_max_iters : 2;
     IrLists& L = ir[target][which];
-    VecList V{L.b.p, L.x.p, L.out.p, L.mat.p};
+    VecList V{L.b.p, L.x.p, L.out.p, L.mat.p, L.len.p};
     for (int it = 0; it < iters; ++it) {
       k_residual<<<dim3((L.n + 127) / 128, L.nv), 128, 0, s>>>(csr, V, L.n, act, L.vin.p);
       PECS_CUDA(cudaGetLastError());
       bank.solve(tab[target][1].view, tab[target][1].max_nrhs, s);
-      k_axpy<<<dim3((L.n + 255) / 256, L.nv), 256, 0, s>>>(L.xw.p, L.d.p, L.n, act, L.vin.p);
+      k_axpy<<<dim3((L.n + 255) / 256, L.nv), 256, 0, s>>>(L.xw.p, L.d.p, L.len.p, act, L.vin.p);
       PECS_CUDA(cudaGetLastError());
     }
   }
@@ -687,13 +732,13 @@ struct Engine {
     PECS_CUDA(cudaGetLastError());
   }
 
+  // Initial conditions from the device-resident projections, then the initial
+  // Poisson solve.  No host traffic.
   void initialize() {
     for (int f = 0; f < 4; ++f) {
       if (nd[f] == 0) continue;
-      std::vector<double> v;
-      for (int i = 0; i < n_inst; ++i) v.insert(v.end(), S->init[f][i].begin(), S->init[f][i].end());
-      PECS_CUDA(cudaMemcpyAsync(state[cur][f].p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, st));
-      PECS_CUDA(cudaStreamSynchronize(st));
+      PECS_CUDA(cudaMemcpyAsync(state[cur][f].p, init_dev[f].p, (size_t)n_inst * nd[f] * 8,
+                                cudaMemcpyDeviceToDevice, st));
     }
     carriers_advanced = false;
     stage_poisson_rhs(st, nullptr);
@@ -737,6 +782,7 @@ struct Engine {
     graph_valid = true;
   }
   double graph_tol = -1.0;
+  int last_run_steps = 0;
 
   void run_to_steady(int max_steps, double tol, int check_every, int* steps, double* relc) {
     if (!initialized) throw PecsError(PECS_E_STATE, "pecs_initialize must be called first");
@@ -744,6 +790,7 @@ struct Engine {
     if (check_every <= 0) check_every = 50;
     check_every += check_every & 1;
     reset_convergence();
+    last_run_steps = 0;
     const bool use_graph = opt.use_graphs != 0;
     if (use_graph && (!graph_valid || graph_tol != tol)) capture_graph(tol);
     int done = 0;
@@ -764,6 +811,7 @@ struct Engine {
         ++k;
       }
       done += k;
+      last_run_steps = done;
       PECS_CUDA(cudaMemcpyAsync(&h_active, n_active.p, 4, cudaMemcpyDeviceToHost, st));
       PECS_CUDA(cudaStreamSynchronize(st));
     }
@@ -925,6 +973,13 @@ int pecs_get_info(pecs_ctx* ctx, pecs_info* info) {
     info->factor_bytes = e.bank_c.bytes() + e.bank_p.bytes();
     info->setup_seconds = e.setup_seconds;
     info->n_distinct_carrier_factors = e.n_fs + e.n_fe;
+    if (!e.host_only) {
+      info->launches_per_step = e.launches_per_step();
+      info->solve_bytes[0] = e.solve_bytes(0);
+      info->solve_bytes[1] = e.solve_bytes(1);
+      info->solve_launches[0] = e.bank_c.kernel_launches_per_solve();
+      info->solve_launches[1] = e.bank_p.kernel_launches_per_solve();
+    }
   })
 }
 
@@ -1103,6 +1158,20 @@ int pecs_iv_sweep(pecs_ctx* ctx, const double* const* init_fields, int max_steps
     }
   })
 }
+
+int pecs_time_solve(pecs_ctx* ctx, int which, int reps, double* ms_per_solve) {
+  PECS_TRY({
+    if (!ctx || !ms_per_solve || reps <= 0 || which < 0 || which > 1)
+      throw PecsError(PECS_E_ARG, "invalid arguments");
+    need_device(ctx->e);
+    if (ctx->e.carriers_advanced) throw PecsError(PECS_E_STATE, "step in progress");
+    *ms_per_solve = ctx->e.time_solves(which, reps);
+  })
+}
+
+int pecs_last_run_steps(pecs_ctx* ctx) { return ctx ? ctx->e.last_run_steps : -1; }
+
+void* pecs_get_stream(pecs_ctx* ctx) { return ctx ? (void*)ctx->e.st : nullptr; }
 
 int pecs_synchronize(pecs_ctx* ctx) {
   PECS_TRY({

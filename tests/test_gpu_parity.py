@@ -12,7 +12,8 @@ from test_lu_host import _maps_carrier, _maps_poisson
 
 pytestmark = pytest.mark.gpu
 
-STEP_TOL = 1e-10     # FP64 path vs FP64 oracle, relative L2 per field
+STEP_TOL = 1e-10     # FP64 path vs FP64 oracle, relative L2 per field (spec bound)
+SOLVE_TOL = 1e-11    # one direct solve: multifrontal LU vs SuperLU, both O(cond * eps)
 RHS_TOL = 1e-13
 
 
@@ -54,7 +55,7 @@ def test_initial_state_and_rhs(pecs_lib, P):
     st = pb.initial_state()
     ctx = _ctx(P)
     ctx.initialize()
-    _compare_state(ctx, st, 1e-12)
+    _compare_state(ctx, st, SOLVE_TOL)
     ctx.assemble_carrier_rhs()
     rhs = pb.carrier_rhs(st)
     for name, v in rhs.items():
