@@ -41,6 +41,9 @@ if ROOT not in sys.path:
 
 MAX_STEPS = 5000
 TOL = 1e-8
+# steps to steady state of the half cell at refinement r (measured by the GPU
+# arm; the oracle marches the same discrete scheme, so the count carries over)
+STEPS_TO_SS = {6: 3886}
 CHECK_EVERY = 50
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
 
@@ -56,6 +59,9 @@ def parse():
     ap.add_argument("--n-inst", type=int, default=1, help="instances per GPU per bench step")
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiler mode: initialise the workload, run this many time steps "
+                         "with direct (non-graph) launches, print one line and exit")
     return ap.parse_args()
 
 
@@ -202,7 +208,8 @@ def run_reference(args):
     pb = oracle.Problem(P)
     st = pb.initial_state()
     st = pb.step(st)
-    steps_to_ss = MAX_STEPS  # the oracle cannot march 5000 steps in a bounded sample
+    # the oracle cannot march thousands of steps in a bounded sample
+    steps_to_ss = STEPS_TO_SS.get(args.refine, MAX_STEPS)
     per = []
     for _ in range(args.warmup):
         st = pb.step(st)
@@ -243,8 +250,16 @@ def main():
     pg.build()
     prec = pg.PREC_FP64 if args.precision == "fp64" else pg.PREC_FP32_IR
     params = workload_params(args, rank)
-    ctx = pg.Context(params, precision=prec, device=local)
+    ctx = pg.Context(params, precision=prec, device=local, use_graphs=args.profile_steps == 0)
     info = ctx.info()
+    if args.profile_steps:
+        ctx.initialize()
+        ctx.step(args.profile_steps)
+        ctx.synchronize()
+        print(json.dumps({"profile_steps": args.profile_steps,
+                          "launches_per_step": info.launches_per_step,
+                          "launches_initialize": 1 + info.solve_launches[1]}))
+        return 0
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
 

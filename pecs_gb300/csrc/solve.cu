@@ -77,18 +77,20 @@ __device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
   }
 }
 
-// Forward sweep, small node (s <= kSmallCols): one warp, lane groups per row.
+// Forward sweep, thin node (s <= kThinCols): the node's Gf is stored
+// column-major, so lane `row` reads Gf[c][row] for c = 0..s-1: consecutive
+// lanes read consecutive addresses and every lane has s independent loads in
+// flight; no cross-lane reduction.  A warp item covers rows [r0, r1).
 template <typename T, int RB>
-__device__ void fwd_small(const BankView& B, const SetsView& S, int j, T* sm) {
-  const int s = B.s[j], m = B.m[j];
+__device__ void fwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
+  const int j = it.x, r0 = it.y, r1 = it.z;
+  const int s = B.s[j], m = B.m[j], f = s + m;
   const SetView& st = S.set[B.node_set[j]];
   const int* own = B.own_idx + B.own_off[j];
   const int* cptr = B.cmap_ptr + B.cm_off[j];
   const T* G = static_cast<const T*>(B.G) + B.goff[j];
   const int wo = B.w_off[j];
   const int lane = threadIdx.x & 31;
-  const int g = s <= 4 ? 4 : (s <= 8 ? 8 : (s <= 16 ? 16 : 32));
-  const int per = 32 / g, grp = lane / g, gl = lane % g;
   for (int rb = 0; rb < st.nrhs; rb += RB) {
     const int nr = min(RB, st.nrhs - rb);
     for (int p = lane; p < s; p += 32) {
@@ -102,34 +104,29 @@ __device__ void fwd_small(const BankView& B, const SetsView& S, int j, T* sm) {
       }
     }
     __syncwarp();
-    for (int row0 = 0; row0 < s + m; row0 += per) {
-      const int row = row0 + grp;
+    for (int row = r0 + lane; row < r1; row += 32) {
       T acc[RB];
 #pragma unroll
       for (int r = 0; r < RB; ++r) acc[r] = T(0);
-      if (row < s + m) {
-        const T* gr = G + (long long)row * s;
-        for (int c = gl; c < s; c += g) {
-          const T gv = __ldg(gr + c);
+      const T* g = G + row;
+#pragma unroll 4
+      for (int c = 0; c < s; ++c) {
+        const T gv = __ldg(g + (long long)c * f);
 #pragma unroll
-          for (int r = 0; r < RB; ++r) acc[r] += gv * sm[c * RB + r];
-        }
+        for (int r = 0; r < RB; ++r) acc[r] += gv * sm[c * RB + r];
       }
+      if (row < s) {
 #pragma unroll
-      for (int r = 0; r < RB; ++r) acc[r] = group_sum(acc[r], g);
-      if (row < s + m) {
+        for (int r = 0; r < RB; ++r)
+          if (r < nr) st.y[rb + r][own[row]] = (double)acc[r];
+      } else {
+        const int c0 = cptr[row], c1 = cptr[row + 1];
 #pragma unroll
-        for (int r = 0; r < RB; ++r) {
-          if ((r % g) == gl && r < nr) {
-            if (row < s) {
-              st.y[rb + r][own[row]] = (double)acc[r];
-            } else {
-              double* w = st.w[rb + r];
-              const double cu = gather_updates(B, w, cptr[row], cptr[row + 1]);
-              w[wo + row - s] = cu + (double)acc[r];
-            }
+        for (int r = 0; r < RB; ++r)
+          if (r < nr) {
+            double* w = st.w[rb + r];
+            w[wo + row - s] = gather_updates(B, w, c0, c1) + (double)acc[r];
           }
-        }
       }
     }
     __syncwarp();
@@ -177,16 +174,16 @@ __device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
   }
 }
 
+// Backward sweep, thin node (s + m <= kThinCols): Hb stored column-major.
 template <typename T, int RB>
-__device__ void bwd_small(const BankView& B, const SetsView& S, int j, T* sm) {
+__device__ void bwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
+  const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j], m = B.m[j], f = s + m;
   const SetView& st = S.set[B.node_set[j]];
   const int* own = B.own_idx + B.own_off[j];
   const int* upd = B.upd_idx + B.upd_off[j];
   const T* H = static_cast<const T*>(B.H) + B.hoff[j];
   const int lane = threadIdx.x & 31;
-  const int g = f <= 4 ? 4 : (f <= 8 ? 8 : (f <= 16 ? 16 : 32));
-  const int per = 32 / g, grp = lane / g, gl = lane % g;
   for (int rb = 0; rb < st.nrhs; rb += RB) {
     const int nr = min(RB, st.nrhs - rb);
     for (int p = lane; p < f; p += 32) {
@@ -198,26 +195,20 @@ __device__ void bwd_small(const BankView& B, const SetsView& S, int j, T* sm) {
       }
     }
     __syncwarp();
-    for (int row0 = 0; row0 < s; row0 += per) {
-      const int row = row0 + grp;
+    for (int row = r0 + lane; row < r1; row += 32) {
       T acc[RB];
 #pragma unroll
       for (int r = 0; r < RB; ++r) acc[r] = T(0);
-      if (row < s) {
-        const T* hr = H + (long long)row * f;
-        for (int c = gl; c < f; c += g) {
-          const T hv = __ldg(hr + c);
+      const T* h = H + row;
+#pragma unroll 4
+      for (int c = 0; c < f; ++c) {
+        const T hv = __ldg(h + (long long)c * s);
 #pragma unroll
-          for (int r = 0; r < RB; ++r) acc[r] += hv * sm[c * RB + r];
-        }
+        for (int r = 0; r < RB; ++r) acc[r] += hv * sm[c * RB + r];
       }
 #pragma unroll
-      for (int r = 0; r < RB; ++r) acc[r] = group_sum(acc[r], g);
-      if (row < s) {
-#pragma unroll
-        for (int r = 0; r < RB; ++r)
-          if ((r % g) == gl && r < nr) st.x[rb + r][own[row]] = (double)acc[r];
-      }
+      for (int r = 0; r < RB; ++r)
+        if (r < nr) st.x[rb + r][own[row]] = (double)acc[r];
     }
     __syncwarp();
   }
@@ -226,7 +217,7 @@ __device__ void bwd_small(const BankView& B, const SetsView& S, int j, T* sm) {
 template <typename T, int RB>
 __global__ void __launch_bounds__(kSolveThreads)
     k_forward(BankView B, SetsView S, const int4* __restrict__ items, int n_large,
-              const int* __restrict__ small, int n_small) {
+              const int4* __restrict__ thin, int n_thin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   if ((int)blockIdx.x < n_large) {
@@ -234,14 +225,14 @@ __global__ void __launch_bounds__(kSolveThreads)
   } else {
     const int wib = threadIdx.x >> 5;
     const int idx = ((int)blockIdx.x - n_large) * (kSolveThreads / 32) + wib;
-    if (idx < n_small) fwd_small<T, RB>(B, S, small[idx], sm + wib * kSmallCols * RB);
+    if (idx < n_thin) fwd_thin<T, RB>(B, S, thin[idx], sm + wib * kThinCols * RB);
   }
 }
 
 template <typename T, int RB>
 __global__ void __launch_bounds__(kSolveThreads)
     k_backward(BankView B, SetsView S, const int4* __restrict__ items, int n_large,
-               const int* __restrict__ small, int n_small) {
+               const int4* __restrict__ thin, int n_thin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   if ((int)blockIdx.x < n_large) {
@@ -249,7 +240,7 @@ __global__ void __launch_bounds__(kSolveThreads)
   } else {
     const int wib = threadIdx.x >> 5;
     const int idx = ((int)blockIdx.x - n_large) * (kSolveThreads / 32) + wib;
-    if (idx < n_small) bwd_small<T, RB>(B, S, small[idx], sm + wib * kSmallCols * RB);
+    if (idx < n_thin) bwd_thin<T, RB>(B, S, thin[idx], sm + wib * kThinCols * RB);
   }
 }
 
@@ -257,17 +248,17 @@ template <typename T, int RB>
 void launch_level(bool forward, const BankView& B, const SetsView& S, const LevelPlan& L,
                   cudaStream_t st) {
   const int warps = kSolveThreads / 32;
-  const int nblk = L.n_large + (L.n_small + warps - 1) / warps;
+  const int nblk = L.n_large + (L.n_thin + warps - 1) / warps;
   if (nblk == 0) return;
   size_t sm_large = (size_t)L.max_cols * RB * sizeof(T);
-  size_t sm_small = L.n_small ? (size_t)warps * kSmallCols * RB * sizeof(T) : 0;
-  size_t smem = std::max(sm_large, sm_small);
+  size_t sm_thin = L.n_thin ? (size_t)warps * kThinCols * RB * sizeof(T) : 0;
+  size_t smem = std::max(sm_large, sm_thin);
   if (forward)
-    k_forward<T, RB><<<nblk, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.small.p,
-                                                         L.n_small);
+    k_forward<T, RB><<<nblk, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
+                                                         L.n_thin);
   else
-    k_backward<T, RB><<<nblk, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.small.p,
-                                                          L.n_small);
+    k_backward<T, RB><<<nblk, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
+                                                          L.n_thin);
   PECS_CUDA(cudaGetLastError());
 }
 
@@ -314,8 +305,8 @@ BankView FactorBank::view() const {
 
 int FactorBank::kernel_launches_per_solve() const {
   int n = 0;
-  for (auto& l : fwd_) n += (l.n_large + l.n_small) > 0;
-  for (auto& l : bwd_) n += (l.n_large + l.n_small) > 0;
+  for (auto& l : fwd_) n += (l.n_large + l.n_thin) > 0;
+  for (auto& l : bwd_) n += (l.n_large + l.n_thin) > 0;
   return n;
 }
 
@@ -361,8 +352,25 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
       node_set.push_back(fi);
       goff.push_back(go);
       hoff.push_back(ho);
-      G.insert(G.end(), F.Gf[j].begin(), F.Gf[j].end());
-      H.insert(H.end(), F.Hb[j].begin(), F.Hb[j].end());
+      {
+        // thin blocks (few columns) are stored column-major for thread-per-row
+        // application; wide blocks row-major for warp-per-row application
+        const int s_ = nd.s, f_ = nd.s + nd.m;
+        const std::vector<double>& g = F.Gf[j];  // f_ x s_ row-major
+        if (s_ <= kThinCols) {
+          for (int c = 0; c < s_; ++c)
+            for (int r = 0; r < f_; ++r) G.push_back(g[(size_t)r * s_ + c]);
+        } else {
+          G.insert(G.end(), g.begin(), g.end());
+        }
+        const std::vector<double>& h = F.Hb[j];  // s_ x f_ row-major
+        if (f_ <= kThinCols) {
+          for (int c = 0; c < f_; ++c)
+            for (int r = 0; r < s_; ++r) H.push_back(h[(size_t)r * f_ + c]);
+        } else {
+          H.insert(H.end(), h.begin(), h.end());
+        }
+      }
       go += (long long)F.Gf[j].size();
       ho += (long long)F.Hb[j].size();
       // extend-add gather lists per front position
@@ -417,36 +425,33 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
     H32_.upload(h32);
     bytes_ = (long long)(G.size() + H.size()) * 4;
   }
-  // level plans
+  // level plans: uniform work units so a level's time is not set by one long
+  // item.  Thin nodes (cols <= kThinCols): warp items of <= kThinRows rows.
+  // Wide nodes: CTA items of <= kWideRows rows (kWideRows/8 rows per warp).
   auto make = [&](const std::vector<LevelNodes>& lv, bool forward, std::vector<LevelPlan>& out) {
     out.clear();
     out.resize(lv.size());
     for (size_t l = 0; l < lv.size(); ++l) {
-      std::vector<int4> items;
-      std::vector<int> small;
+      std::vector<int4> items, thin;
       int max_cols = 0;
-      long long tot = 0;
-      for (int g : lv[l].nodes) tot += (long long)hs[g] * (hs[g] + hm[g]);
-      // aim for enough work items to occupy the GPU, but not tiny ones
-      const long long target = std::max<long long>(4096, tot / 600);
       for (int g : lv[l].nodes) {
         const int s = hs[g], m = hm[g], f = s + m;
         const int cols = forward ? s : f;
         const int rows = forward ? f : s;
-        const bool is_small = cols <= kSmallCols && (long long)rows * cols <= 16384;
-        if (is_small) {
-          small.push_back(g);
+        if (cols <= kThinCols) {
+          for (int r0 = 0; r0 < rows; r0 += kThinRows)
+            thin.push_back(make_int4(g, r0, std::min(rows, r0 + kThinRows), 0));
         } else {
-          int per = (int)std::max<long long>(1, std::min<long long>(rows, target / std::max(1, cols)));
-          for (int r0 = 0; r0 < rows; r0 += per) items.push_back(make_int4(g, r0, std::min(rows, r0 + per), 0));
+          for (int r0 = 0; r0 < rows; r0 += kWideRows)
+            items.push_back(make_int4(g, r0, std::min(rows, r0 + kWideRows), 0));
           max_cols = std::max(max_cols, cols);
         }
       }
       out[l].n_large = (int)items.size();
-      out[l].n_small = (int)small.size();
+      out[l].n_thin = (int)thin.size();
       out[l].max_cols = max_cols;
       out[l].items.upload(items);
-      out[l].small.upload(small);
+      out[l].thin.upload(thin);
     }
   };
   make(fl, true, fwd_);
@@ -455,7 +460,7 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
   for (auto& l : fwd_) max_cols_ = std::max(max_cols_, l.max_cols);
   for (auto& l : bwd_) max_cols_ = std::max(max_cols_, l.max_cols);
   const size_t esz = prec_ == PECS_PREC_FP64 ? 8 : 4;
-  const size_t small_need = (size_t)(kSolveThreads / 32) * kSmallCols * esz;
+  const size_t small_need = (size_t)(kSolveThreads / 32) * kThinCols * esz;
   max_rb_ = 8;
   while (max_rb_ > 1 && std::max((size_t)max_cols_, small_need / esz) * max_rb_ * esz > kSmemCap)
     max_rb_ /= 2;

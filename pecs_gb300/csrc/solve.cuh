@@ -5,9 +5,10 @@
 // factor (e.g. electrons and holes of every instance when their mobilities
 // are equal), so that every stored factor entry read from HBM is applied to
 // all of them.  One kernel launch processes one tree level of every factor in
-// the bank: large nodes are split into row chunks handled by a CTA each
-// (warp per row, coalesced row-major reads, warp-shuffle reduction); small
-// nodes are handled by one warp each (lane groups per row).
+// the bank: wide nodes are split into row chunks handled by a CTA each
+// (warp per row, coalesced row-major reads, warp-shuffle reduction); thin
+// nodes (few columns) are stored column-major and applied thread-per-row,
+// in warp-sized row chunks.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -19,7 +20,9 @@
 namespace pecs {
 
 constexpr int kMaxSets = 4;
-constexpr int kSmallCols = 128;   // small-node path: columns staged per warp
+constexpr int kThinCols = 128;   // nodes with at most this many columns: thread per row
+constexpr int kThinRows = 64;    // rows per warp item of a thin node
+constexpr int kWideRows = 32;    // rows per CTA item of a wide node
 constexpr int kSolveThreads = 256;
 constexpr size_t kSmemCap = 200 * 1024;  // dynamic shared memory budget per CTA
 
@@ -54,9 +57,9 @@ struct SetsView {
 };
 
 struct LevelPlan {
-  int n_large = 0, n_small = 0;
-  DBuf<int4> items;   // large: (node, row0, row1, 0)
-  DBuf<int> small;    // small nodes (warp each)
+  int n_large = 0, n_thin = 0;
+  DBuf<int4> items;   // wide nodes: (node, row0, row1, 0), one CTA each
+  DBuf<int4> thin;    // thin nodes: (node, row0, row1, 0), one warp each
   int max_cols = 0;   // staged columns per large item
 };
 
