@@ -21,8 +21,8 @@ namespace pecs {
 
 constexpr int kMaxSets = 4;
 constexpr int kThinCols = 128;   // nodes with at most this many columns: thread per row
-constexpr int kThinRows = 64;    // rows per warp item of a thin node
-constexpr int kWideRows = 32;    // rows per CTA item of a wide node
+constexpr int kThinRows = 32;    // rows per warp item of a thin node (one per lane)
+constexpr int kWideRows = 8;     // rows per CTA item of a wide node (one per warp)
 constexpr int kSolveThreads = 256;
 constexpr size_t kSmemCap = 200 * 1024;  // dynamic shared memory budget per CTA
 
