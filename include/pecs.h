@@ -189,6 +189,22 @@ int pecs_lu_solve_device(pecs_lu* lu, int nrhs, const double* b_dev, double* x_d
 int pecs_lu_stats(pecs_lu* lu, long long* entries, int* levels, int* nodes, int* max_front);
 void pecs_lu_destroy(pecs_lu* lu);
 
+/* Same solve as pecs_lu_solve_device for callers that cannot allocate device
+ * memory when they solve (their own pool owns the GPU's memory, or they run
+ * under a fixed memory budget).  It has no counterpart in the reference.  The
+ * sweeps' scratch lives in one file-scope device array of 2^20 doubles (8 MiB)
+ * that every GPU loading the library holds until exit; a solve needs
+ * nrhs*(n + update-vector length) doubles of it and nrhs <= 8, larger requests
+ * return PECS_E_ARG.  Nothing is allocated: the factors must already be on the
+ * current device (any earlier pecs_lu_solve or pecs_lu_solve_device call on the
+ * handle uploads them), else PECS_E_STATE.  The first call on a device looks
+ * up the array's device address; make that first call before any stream
+ * capture.  All calls share the array and leave their contents in it (every
+ * value a sweep reads is written earlier in the same sweep, so nothing needs
+ * clearing); calls that overlap on the GPU race on it. */
+int pecs_lu_solve_device_noalloc(pecs_lu* lu, int nrhs, const double* b_dev, double* x_dev,
+                                 void* stream);
+
 #ifdef __cplusplus
 }
 #endif

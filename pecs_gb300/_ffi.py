@@ -102,6 +102,7 @@ SIGNATURES = [
     ("pecs_lu_solve_device", C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     ("pecs_lu_stats", C.c_int, [_vp, C.POINTER(C.c_longlong), _ip, _ip, _ip]),
     ("pecs_lu_destroy", None, [_vp]),
+    ("pecs_lu_solve_device_noalloc", C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     ("pecs_lu_host_apply", C.c_int, [_vp, _dp, _dp]),
 ]
 

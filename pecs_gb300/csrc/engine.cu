@@ -1293,6 +1293,95 @@ int pecs_lu_stats(pecs_lu* lu, long long* entries, int* levels, int* nodes, int*
 
 void pecs_lu_destroy(pecs_lu* lu) { delete lu; }
 
+// ---- solve for callers that cannot allocate device memory ------------------
+// Some callers may not allocate device memory at solve time: an application
+// whose memory is carved up by its own pool allocator, a code that has to stay
+// inside a fixed device-memory budget, or a host library called from a context
+// where cudaMalloc is not allowed.  pecs_lu_solve_device_noalloc runs the same
+// forward/backward sweeps as pecs_lu_solve_device, but keeps the sweeps'
+// scratch -- the forward-sweep slots and the per-node update vectors -- in the
+// fixed file-scope array below instead of memory owned by the handle, and
+// allocates nothing.  Every GPU that loads the library holds the array (8 MiB)
+// until the process exits.
+}  // extern "C"
+
+namespace pecs {
+namespace {
+constexpr size_t kNoAllocScratchDoubles = size_t(1) << 20;  // 8 MiB
+constexpr int kNoAllocMaxRhs = 8;
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+static __device__ __align__(256) double* g_noalloc_ptrs[4 * kNoAllocMaxRhs];
+
+struct NoAllocSlot {
+  double* scratch = nullptr;
+  double** ptrs = nullptr;
+};
+std::mutex g_noalloc_mu;
+NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices];
+
+// Device addresses of the static arrays on the current device (looked up once
+// per device: the host-side names are only stand-ins for them).
+NoAllocSlot noalloc_slot(int dev) {
+  if (dev < 0 || dev >= kNoAllocMaxDevices) throw PecsError(PECS_E_ARG, "device ordinal too large");
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  NoAllocSlot& s = g_noalloc_slot[dev];
+  if (!s.scratch) {
+    void* a = nullptr;
+    void* b = nullptr;
+    PECS_CUDA(cudaGetSymbolAddress(&a, g_noalloc_scratch));
+    PECS_CUDA(cudaGetSymbolAddress(&b, g_noalloc_ptrs));
+    s.scratch = static_cast<double*>(a);
+    s.ptrs = static_cast<double**>(b);
+  }
+  return s;
+}
+}  // namespace
+}  // namespace pecs
+
+extern "C" {
+
+int pecs_lu_solve_device_noalloc(pecs_lu* lu, int nrhs, const double* b_dev, double* x_dev,
+                                 void* stream) {
+  PECS_TRY({
+    if (!lu || !b_dev || !x_dev) throw PecsError(PECS_E_ARG, "invalid arguments");
+    if (nrhs < 1 || nrhs > kNoAllocMaxRhs)
+      throw PecsError(PECS_E_ARG, "nrhs must be 1.." + std::to_string(kNoAllocMaxRhs));
+    LuHandle& h = lu->h;
+    if (!h.uploaded)
+      throw PecsError(PECS_E_STATE,
+                      "the factors are not on the device yet: one pecs_lu_solve or "
+                      "pecs_lu_solve_device call on this handle uploads them");
+    const size_t n = (size_t)h.F.n, nw = (size_t)h.bank.set_wtotal(0);
+    const size_t need = (size_t)nrhs * (n + nw);
+    if (need > kNoAllocScratchDoubles)
+      throw PecsError(PECS_E_ARG, "this solve needs " + std::to_string(need) +
+                                      " doubles of scratch; the static scratch holds " +
+                                      std::to_string(kNoAllocScratchDoubles));
+    int dev = -1;
+    PECS_CUDA(cudaGetDevice(&dev));
+    cudaPointerAttributes pa;
+    PECS_CUDA(cudaPointerGetAttributes(&pa, h.y.p));
+    if (pa.device != dev)
+      throw PecsError(PECS_E_ARG, "the current device is not the device holding the factors");
+    NoAllocSlot slot = noalloc_slot(dev);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h.st;
+    double* table[4 * kNoAllocMaxRhs];
+    for (int r = 0; r < nrhs; ++r) {
+      table[r] = const_cast<double*>(b_dev) + (size_t)r * n;
+      table[nrhs + r] = slot.scratch + (size_t)r * n;
+      table[2 * nrhs + r] = slot.scratch + (size_t)nrhs * n + (size_t)r * nw;
+      table[3 * nrhs + r] = x_dev + (size_t)r * n;
+    }
+    // pageable source: the call returns once the table has been staged
+    PECS_CUDA(cudaMemcpyAsync(slot.ptrs, table, sizeof(double*) * 4 * nrhs, cudaMemcpyHostToDevice, s));
+    SetsView sv{};
+    sv.set[0] = SetView{nrhs, slot.ptrs, slot.ptrs + nrhs, slot.ptrs + 2 * nrhs, slot.ptrs + 3 * nrhs};
+    h.bank.solve(sv, nrhs, s);
+    PECS_CUDA(cudaStreamSynchronize(s));
+  })
+}
+
 // diagnostic: apply the host copy of the factors (no GPU involved)
 int pecs_lu_host_apply(pecs_lu* lu, const double* b, double* x) {
   PECS_TRY({

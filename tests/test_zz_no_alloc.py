@@ -1,0 +1,77 @@
+"""pecs_lu_solve_device_noalloc: the solve for callers that cannot allocate
+device memory at solve time (their own pool owns the GPU's memory, or they
+must stay inside a fixed memory budget).  Its sweeps keep their scratch in a
+fixed file-scope device array instead of handle-owned memory.  Checked
+through the C ABI against the allocating entry point pecs_lu_solve_device, on
+two calls in a row (the array keeps the previous call's contents), and for
+its size limits.  This file is collected last on purpose."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+import pecs_gb300 as pg
+from test_lu_host import _maps_carrier, _maps_poisson
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12   # same kernels on the same factors: agreement to rounding
+
+
+def _noalloc(lu, nrhs, b_ptr, x_ptr):
+    return pg.lib().pecs_lu_solve_device_noalloc(lu._h, nrhs, C.c_void_p(b_ptr), C.c_void_p(x_ptr),
+                                                 C.c_void_p(0))
+
+
+def _rel(a, b):
+    return float((a - b).norm() / b.norm())
+
+
+@pytest.mark.parametrize("system", ["carrier", "poisson"])
+def test_noalloc_matches_allocating_solve_twice(pecs_lib, system):
+    torch = pytest.importorskip("torch")
+    pb = oracle.Problem(oracle.config2_params(n_refine=4))
+    if system == "carrier":
+        dc, cl, xy = _maps_carrier(pb, pb.semi)
+        lu = pg.LU(pb.A_n, dc, xy, cl)
+        n = pb.A_n.shape[0]
+    else:
+        dc, xy = _maps_poisson(pb)
+        lu = pg.LU(pb.A_P, dc, xy)
+        n = pb.A_P.shape[0]
+    nrhs = 2
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    for call in range(2):   # two calls in a row share the static scratch
+        b = torch.randn(nrhs, n, dtype=torch.float64, device="cuda", generator=gen)
+        x_ref = torch.zeros_like(b)
+        lu.solve_device(b.data_ptr(), x_ref.data_ptr(), nrhs=nrhs)   # allocating entry point
+        x = torch.full_like(b, float("nan"))
+        pg._ffi.check(_noalloc(lu, nrhs, b.data_ptr(), x.data_ptr()))
+        torch.cuda.synchronize()
+        assert torch.isfinite(x).all()
+        assert _rel(x, x_ref) < TOL, (call, _rel(x, x_ref))
+
+
+def test_noalloc_limits_and_preconditions(pecs_lib):
+    torch = pytest.importorskip("torch")
+    pb = oracle.Problem(oracle.config2_params(n_refine=6))
+    dc, cl, xy = _maps_carrier(pb, pb.semi)
+    lu = pg.LU(pb.A_n, dc, xy, cl)
+    n = pb.A_n.shape[0]
+    b = torch.ones(8, n, dtype=torch.float64, device="cuda")
+    x = torch.zeros_like(b)
+    # factors not yet on the device: refused, nothing allocated
+    assert _noalloc(lu, 1, b.data_ptr(), x.data_ptr()) == pg._ffi.PECS_E_STATE
+    lu.solve_device(b.data_ptr(), x.data_ptr(), nrhs=1)
+    # more right-hand sides than the scratch holds: a clear error
+    code = _noalloc(lu, 8, b.data_ptr(), x.data_ptr())
+    assert code == pg._ffi.PECS_E_ARG
+    assert b"scratch" in pg.lib().pecs_last_error()
+    assert _noalloc(lu, 9, b.data_ptr(), x.data_ptr()) == pg._ffi.PECS_E_ARG
+    # one right-hand side of this size fits
+    x1 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    x2 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    lu.solve_device(b[0].data_ptr(), x1.data_ptr(), nrhs=1)
+    pg._ffi.check(_noalloc(lu, 1, b[0].data_ptr(), x2.data_ptr()))
+    assert _rel(x2, x1) < TOL
