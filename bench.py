@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--refine", type=int, default=6)
-    ap.add_argument("--precision", choices=["fp64", "fp32ir"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "fp32ir", "mixed"], default="fp64")
     ap.add_argument("--n-inst", type=int, default=1, help="instances per GPU per bench step")
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -248,7 +248,7 @@ def main():
 
     world, rank, local = dist_init(args)
     pg.build()
-    prec = pg.PREC_FP64 if args.precision == "fp64" else pg.PREC_FP32_IR
+    prec = {"fp64": pg.PREC_FP64, "fp32ir": pg.PREC_FP32_IR, "mixed": pg.PREC_FP32_MIXED}[args.precision]
     params = workload_params(args, rank)
     ctx = pg.Context(params, precision=prec, device=local, use_graphs=args.profile_steps == 0)
     info = ctx.info()
@@ -332,7 +332,9 @@ def main():
         "metric": "I-V points/sec to steady state", "value": value, "unit": "I-V points/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if prec == pg.PREC_FP64 else "f32 factors + f64 refinement",
+        "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp32ir": "f32 factors + f64 refinement",
+                  "mixed": "f32 factors/quadrature + double-float refinement"}[args.precision],
         "data": "synthetic",
         "config": {"workload": f"half cell 2x{2**args.refine}x{2**args.refine}, LDG k=1, "
                                f"RT0xDGQ0 Poisson, dt=1e-3, to rel. change <= {TOL} "

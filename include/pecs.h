@@ -64,6 +64,10 @@ extern "C" {
 /* solver precision */
 #define PECS_PREC_FP64 0    /* FP64 factors, FP64 arithmetic */
 #define PECS_PREC_FP32_IR 1 /* FP32 factors + FP64-residual iterative refinement */
+/* FP32 factors + refinement with FP32-pair ("double-float") residuals, RHS
+ * quadrature terms in FP32 (constant and mass terms FP64), FP32 convergence
+ * sums: the batched throughput mode (GB300 runs FP32 ~60x faster than FP64) */
+#define PECS_PREC_FP32_MIXED 2
 
 /*
  * Already-scaled parameters of one instance (the role of
@@ -97,7 +101,8 @@ typedef struct pecs_options {
   int precision;     /* PECS_PREC_* */
   int leaf_cells;    /* nested-dissection leaf size in cells (0 = default) */
   int use_graphs;    /* capture a time step in a CUDA graph (1 = yes) */
-  int ir_max_iters;  /* FP32_IR: refinement sweeps per solve (0 = default) */
+  int ir_max_iters;  /* FP32 modes: refinement sweeps per solve (0 = default: 2 for
+                        FP32_IR, 1 for FP32_MIXED; < 0 = none) */
   double ir_tol;     /* FP32_IR: target relative residual (0 = default 1e-12) */
   int device;        /* CUDA device ordinal */
   int host_setup_only; /* 1: build meshes, matrices and factors on the host only

@@ -22,7 +22,7 @@ PECS_E_NODEVICE = -6
 INTERFACE, DIRICHLET, NEUMANN, SCHOTTKY = 0, 1, 2, 3
 FIELD_N, FIELD_P, FIELD_R, FIELD_O, FIELD_POISSON = 0, 1, 2, 3, 4
 MAT_N, MAT_P, MAT_R, MAT_O, MAT_POISSON, MAT_MASS_SEMI, MAT_MASS_ELEC = range(7)
-PREC_FP64, PREC_FP32_IR = 0, 1
+PREC_FP64, PREC_FP32_IR, PREC_FP32_MIXED = 0, 1, 2
 
 
 class pecs_params(C.Structure):

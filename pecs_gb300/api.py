@@ -18,7 +18,7 @@ import numpy as np
 
 from . import _ffi as F
 from ._ffi import (DIRICHLET, INTERFACE, NEUMANN, SCHOTTKY, FIELD_N, FIELD_O, FIELD_P,
-                   FIELD_POISSON, FIELD_R, PREC_FP32_IR, PREC_FP64, check, lib)
+                   FIELD_POISSON, FIELD_R, PREC_FP32_IR, PREC_FP32_MIXED, PREC_FP64, check, lib)
 
 
 @dataclass
@@ -119,7 +119,7 @@ def reference_params(n_refine: int = 4, degree: int = 1, **kw) -> Params:
 
 
 def default_options(precision: int = PREC_FP64, use_graphs: bool = True, leaf_cells: int = 8,
-                    ir_max_iters: int = 2, device: int = 0,
+                    ir_max_iters: int = 0, device: int = 0,
                     host_setup_only: bool = False) -> F.pecs_options:
     o = F.pecs_options()
     lib().pecs_default_options(C.byref(o))
@@ -140,7 +140,7 @@ class Context:
     """A group of instances resident on one GPU (pecs_create)."""
 
     def __init__(self, params: Sequence[Params] | Params, precision: int = PREC_FP64,
-                 use_graphs: bool = True, leaf_cells: int = 8, ir_max_iters: int = 2,
+                 use_graphs: bool = True, leaf_cells: int = 8, ir_max_iters: int = 0,
                  device: int = 0, host_setup_only: bool = False):
         if isinstance(params, Params):
             params = [params]

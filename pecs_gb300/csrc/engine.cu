@@ -83,15 +83,67 @@ __global__ void k_axpy(double* const* x, const double* const* d, const int* __re
   if (i < len[v]) x[v][i] += d[v][i];
 }
 
+// x -> (hi, lo) float pair with x = hi + lo to ~2^-48 relative
+__global__ void k_split(const double* const* x, float2* const* xs, const int* __restrict__ len,
+                        const int* __restrict__ active, const int* __restrict__ vec_inst) {
+  const int v = blockIdx.y;
+  if (active && !active[vec_inst[v]]) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len[v]) return;
+  const double a = x[v][i];
+  const float hi = __double2float_rn(a);
+  xs[v][i] = make_float2(hi, __double2float_rn(a - (double)hi));
+}
+
+struct CsrDf {  // matrix values split into FP32 (hi, lo) pairs
+  const int* rp;
+  const int* ci;
+  const float2* v;
+};
+
+struct CsrDfSet {
+  CsrDf m[5];
+};
+
+// out = b - A x with the sum in FP32-pair ("double-float") arithmetic:
+// products are exact through fmaf, partial sums through TwoSum, so the
+// residual keeps ~46-bit accuracy while running on the FP32 pipe.
+__global__ void k_residual_df(CsrDfSet M, const double* const* b, const float2* const* xs,
+                              double* const* out, const int* __restrict__ mat,
+                              const int* __restrict__ len, const int* __restrict__ active,
+                              const int* __restrict__ vec_inst) {
+  const int v = blockIdx.y;
+  if (active && !active[vec_inst[v]]) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len[v]) return;
+  const CsrDf A = M.m[mat[v]];
+  const float2* x = xs[v];
+  float sh = 0.f, sl = 0.f;
+  for (int p = A.rp[i]; p < A.rp[i + 1]; ++p) {
+    const float2 a = A.v[p], xv = x[A.ci[p]];
+    const float ph = a.x * xv.x;
+    const float pe = fmaf(a.x, xv.x, -ph) + fmaf(a.x, xv.y, a.y * xv.x);
+    const float t = sh + ph;                      // TwoSum(sh, ph)
+    const float z = t - sh;
+    const float e = (sh - (t - z)) + (ph - z);
+    sh = t;
+    sl += e + pe;
+  }
+  out[v][i] = b[v][i] - ((double)sh + (double)sl);
+}
+
 constexpr int kRedThreads = 256;
 constexpr int kRedChunks = 16;
 
-// partial sums of |new-old|^2 and |new|^2: grid (kRedChunks, 5 fields, n_inst)
+// partial sums of |new-old|^2 and |new|^2: grid (kRedChunks, 5 fields, n_inst).
+// The difference is always formed in FP64 (a 1e-8 relative change is below
+// FP32 resolution); Acc is the type the squares are summed in.
+template <typename Acc>
 __global__ void k_relchange_partial(FieldPtrs NEW, FieldPtrs OLD, int n_fields,
                                     double2* __restrict__ partial) {
   const int chunk = blockIdx.x, fld = blockIdx.y, i = blockIdx.z;
   __shared__ double sd[kRedThreads], sn[kRedThreads];
-  double d2 = 0.0, n2 = 0.0;
+  Acc d2 = 0, n2 = 0;
   if (fld < n_fields) {
     const int f = fld == n_fields - 1 ? 4 : fld;
     const int nd = NEW.nd[f];
@@ -101,12 +153,13 @@ __global__ void k_relchange_partial(FieldPtrs NEW, FieldPtrs OLD, int n_fields,
     const int lo = chunk * per, hi = min(nd, lo + per);
     for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
       const double x = a[t], y = b[t];
-      d2 += (x - y) * (x - y);
-      n2 += x * x;
+      const Acc d = (Acc)(x - y), xa = (Acc)x;
+      d2 += d * d;
+      n2 += xa * xa;
     }
   }
-  sd[threadIdx.x] = d2;
-  sn[threadIdx.x] = n2;
+  sd[threadIdx.x] = (double)d2;
+  sn[threadIdx.x] = (double)n2;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) {
@@ -248,6 +301,7 @@ struct Engine {
   CsrSet csr{};
   // tables and regions
   DBuf<double> t_phi, t_qw, t_fphi, t_fw, t_psix, t_psiy, t_phiP, t_mref;
+  DBuf<float> tf_phi, tf_qw, tf_fphi, tf_fw, tf_psix, tf_psiy;
   Tables T{};
   DBuf<double2> h_[2], ph_[2];
   DBuf<int4> bid_[2];
@@ -272,10 +326,19 @@ struct Engine {
   // graphs
   cudaGraphExec_t graph2[2] = {nullptr, nullptr};  // two steps starting from cur = 0 / 1
   bool graph_valid = false;
+  // refinement sweeps per solve: none for FP64 factors; ir_max_iters > 0 sets
+  // the count, < 0 disables refinement, 0 selects the default
+  int ir_iters() const {
+    if (opt.precision == PECS_PREC_FP64) return 0;
+    if (opt.ir_max_iters < 0) return 0;
+    if (opt.ir_max_iters > 0) return opt.ir_max_iters;
+    return opt.precision == PECS_PREC_FP32_MIXED ? 1 : 2;
+  }
   int launches_per_step() const {
-    const int it = opt.precision == PECS_PREC_FP32_IR ? (opt.ir_max_iters > 0 ? opt.ir_max_iters : 2) : 0;
+    const int it = ir_iters();
+    const int per_it = opt.precision == PECS_PREC_FP32_MIXED ? 3 : 2;
     const int lc = bank_c.kernel_launches_per_solve(), lp = bank_p.kernel_launches_per_solve();
-    return 1 + lc * (1 + it) + 2 * it + 1 + lp * (1 + it) + 2 * it + 3;
+    return 1 + lc * (1 + it) + per_it * it + 1 + lp * (1 + it) + per_it * it + 3;
   }
   // algorithmic bytes of one application of a bank to all of its right-hand
   // sides: every stored factor entry once, plus the vectors (b read, y write +
@@ -438,8 +501,9 @@ struct Engine {
     std::vector<const MfFactor*> cf;
     for (int t = 0; t < n_fs; ++t) cf.push_back(&fs[t]);
     for (int t = 0; t < n_fe; ++t) cf.push_back(&fe[t]);
-    bank_c.build(cf, opt.precision);
-    bank_p.build({&fp}, opt.precision);
+    const int fprec = opt.precision == PECS_PREC_FP64 ? PECS_PREC_FP64 : PECS_PREC_FP32_IR;
+    bank_c.build(cf, fprec);
+    bank_p.build({&fp}, fprec);
     // free host copies of the factor values (structure is kept for stats)
     for (auto* F : {&fs[0], &fs[1], &fe[0], &fe[1], &fp}) {
       std::vector<std::vector<double>>().swap(F->Gf);
@@ -454,6 +518,16 @@ struct Engine {
       A_ci[f].upload(mats[f]->col);
       A_v[f].upload(mats[f]->val);
       csr.m[f] = CsrDev{A_rp[f].p, A_ci[f].p, A_v[f].p};
+      if (opt.precision == PECS_PREC_FP32_MIXED) {
+        std::vector<float2> sv(mats[f]->val.size());
+        for (size_t t = 0; t < sv.size(); ++t) {
+          const double a = mats[f]->val[t];
+          const float hi = (float)a;
+          sv[t] = make_float2(hi, (float)(a - (double)hi));
+        }
+        Adf[f].upload(sv);
+        csr_df.m[f] = CsrDf{A_rp[f].p, A_ci[f].p, Adf[f].p};
+      }
     }
     upload_tables();
     upload_regions();
@@ -524,7 +598,15 @@ struct Engine {
       for (int b = 0; b < ct.n1; ++b)
         for (int q = 0; q < ct.Q; ++q) mref[a * ct.n1 + b] += ct.phi[a * ct.Q + q] * ct.phi[b * ct.Q + q] * ct.qw[q];
     t_mref.upload(mref);
-    T = Tables{t_phi.p, t_qw.p, t_fphi.p, t_fw.p, t_psix.p, t_psiy.p, t_phiP.p, t_mref.p};
+    auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+    tf_phi.upload(f32(ct.phi));
+    tf_qw.upload(f32(ct.qw));
+    tf_fphi.upload(f32(ct.fphi));
+    tf_fw.upload(f32(ct.fw));
+    tf_psix.upload(f32(pt.psi_x));
+    tf_psiy.upload(f32(pt.psi_y));
+    T = Tables{t_phi.p,  t_qw.p,  t_fphi.p,  t_fw.p,   t_psix.p,  t_psiy.p, t_phiP.p,
+               t_mref.p, tf_phi.p, tf_qw.p, tf_fphi.p, tf_fw.p, tf_psix.p, tf_psiy.p};
   }
 
   void upload_regions() {
@@ -609,12 +691,20 @@ struct Engine {
     const int nif = (int)S->iface_semi.size();
     const double* sne = S->has_schottky ? sch_ne.p : nullptr;
     const double* spe = S->has_schottky ? sch_pe.p : nullptr;
-    if (S->k == 1)
-      k_carrier_rhs<1><<<grid, 128, 0, s>>>(T, R[0], R[1], full ? 2 : 1, F, inst.p, iface_ne.p,
-                                            iface_pe.p, nif, sne, spe, act);
+    const bool mixed = opt.precision == PECS_PREC_FP32_MIXED;
+    const int nreg = full ? 2 : 1;
+    if (S->k == 1 && !mixed)
+      k_carrier_rhs<1, double><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
+                                                    iface_pe.p, nif, sne, spe, act);
+    else if (S->k == 1)
+      k_carrier_rhs<1, float><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
+                                                   iface_pe.p, nif, sne, spe, act);
+    else if (!mixed)
+      k_carrier_rhs<2, double><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
+                                                    iface_pe.p, nif, sne, spe, act);
     else
-      k_carrier_rhs<2><<<grid, 128, 0, s>>>(T, R[0], R[1], full ? 2 : 1, F, inst.p, iface_ne.p,
-                                            iface_pe.p, nif, sne, spe, act);
+      k_carrier_rhs<2, float><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
+                                                   iface_pe.p, nif, sne, spe, act);
     PECS_CUDA(cudaGetLastError());
   }
 
@@ -635,8 +725,12 @@ struct Engine {
     DBuf<const double*> b, x, d;
     DBuf<double*> out, xw;
     DBuf<int> mat, vin, len;
+    DBuf<float2*> xs;  // split copies of x (mixed mode)
+    std::vector<DBuf<float2>> xs_store;
     int nv = 0, n = 0;
   };
+  DBuf<float2> Adf[5];
+  CsrDfSet csr_df{};
   IrLists ir[2][2];  // [target][0 carriers, 1 Poisson]
 
   void prepare_ir() {
@@ -669,6 +763,15 @@ struct Engine {
         L.vin.upload(hi);
         L.len.upload(hl);
         L.nv = (int)hb.size();
+        if (opt.precision == PECS_PREC_FP32_MIXED) {
+          std::vector<float2*> hs;
+          for (size_t v = 0; v < hb.size(); ++v) {
+            L.xs_store.emplace_back();
+            L.xs_store.back().alloc(hl[v]);
+            hs.push_back(L.xs_store.back().p);
+          }
+          L.xs.upload(hs);
+        }
         L.n = n;
       }
   }
@@ -677,12 +780,20 @@ struct Engine {
   void solve_bank(const FactorBank& bank, SetTable (&tab)[2][2], int target, int which,
                   cudaStream_t s, const int* act) {
     bank.solve(tab[target][0].view, tab[target][0].max_nrhs, s);
-    if (opt.precision != PECS_PREC_FP32_IR) return;
-    const int iters = opt.ir_max_iters > 0 ? opt.ir_max_iters : 2;
+    const int iters = ir_iters();
+    if (iters == 0) return;
     IrLists& L = ir[target][which];
     VecList V{L.b.p, L.x.p, L.out.p, L.mat.p, L.len.p};
+    const bool mixed = opt.precision == PECS_PREC_FP32_MIXED;
     for (int it = 0; it < iters; ++it) {
-      k_residual<<<dim3((L.n + 127) / 128, L.nv), 128, 0, s>>>(csr, V, L.n, act, L.vin.p);
+      if (mixed) {
+        k_split<<<dim3((L.n + 255) / 256, L.nv), 256, 0, s>>>(L.x.p, L.xs.p, L.len.p, act, L.vin.p);
+        PECS_CUDA(cudaGetLastError());
+        k_residual_df<<<dim3((L.n + 127) / 128, L.nv), 128, 0, s>>>(
+            csr_df, L.b.p, (const float2* const*)L.xs.p, L.out.p, L.mat.p, L.len.p, act, L.vin.p);
+      } else {
+        k_residual<<<dim3((L.n + 127) / 128, L.nv), 128, 0, s>>>(csr, V, L.n, act, L.vin.p);
+      }
       PECS_CUDA(cudaGetLastError());
       bank.solve(tab[target][1].view, tab[target][1].max_nrhs, s);
       k_axpy<<<dim3((L.n + 255) / 256, L.nv), 256, 0, s>>>(L.xw.p, L.d.p, L.len.p, act, L.vin.p);
@@ -723,7 +834,12 @@ struct Engine {
     const int old = cur;
     full_step(s, active.p);
     FieldPtrs NEW = fields(state[cur], nullptr), OLD = fields(state[old], nullptr);
-    k_relchange_partial<<<dim3(kRedChunks, 5, n_inst), kRedThreads, 0, s>>>(NEW, OLD, n_fields, partial.p);
+    if (opt.precision == PECS_PREC_FP32_MIXED)
+      k_relchange_partial<float><<<dim3(kRedChunks, 5, n_inst), kRedThreads, 0, s>>>(NEW, OLD, n_fields,
+                                                                                    partial.p);
+    else
+      k_relchange_partial<double><<<dim3(kRedChunks, 5, n_inst), kRedThreads, 0, s>>>(NEW, OLD, n_fields,
+                                                                                     partial.p);
     PECS_CUDA(cudaGetLastError());
     k_converge<<<1, 256, 0, s>>>(partial.p, n_inst, n_fields, tol, conv_step.p, rel.p, step_ctr.p,
                                  active.p, n_active.p);
@@ -932,7 +1048,8 @@ int pecs_create(const pecs_params* params, int n_inst, const pecs_options* opt, 
     pecs_options o;
     pecs_default_options(&o);
     if (opt) o = *opt;
-    if (o.precision != PECS_PREC_FP64 && o.precision != PECS_PREC_FP32_IR)
+    if (o.precision != PECS_PREC_FP64 && o.precision != PECS_PREC_FP32_IR &&
+        o.precision != PECS_PREC_FP32_MIXED)
       throw PecsError(PECS_E_ARG, "unknown precision");
     std::unique_ptr<pecs_ctx> c(new pecs_ctx());
     c->e.create(std::vector<pecs_params>(params, params + n_inst), o);

@@ -29,6 +29,8 @@ struct Tables {
   const double* psiy;  // nrt*Q
   const double* phiP;  // nphi*Q Poisson DGQ_{k-1} basis at cell qp
   const double* mref;  // n1*n1  unit-square mass matrix
+  // FP32 copies for the mixed-precision path
+  const float *phi_f, *qw_f, *fphi_f, *fw_f, *psix_f, *psiy_f;
 };
 
 struct RegionDev {
@@ -71,8 +73,20 @@ struct Dims {
   static constexpr int nphi = K * K;
 };
 
-// grid: x over (cells of both regions) * 2 carriers, y over instances
-template <int K>
+template <typename Tq>
+__device__ __forceinline__ const Tq* tab(const double* d, const float* f);
+template <>
+__device__ __forceinline__ const double* tab<double>(const double* d, const float*) { return d; }
+template <>
+__device__ __forceinline__ const float* tab<float>(const double*, const float* f) { return f; }
+
+// grid: x over (cells of both regions) * 2 carriers, y over instances.
+// Tq is the arithmetic type of the quadrature terms (drift, SRH, interface,
+// Schottky).  Tq = double is the FP64 path.  Tq = float is the mixed path: the
+// dominant, time-integrating part of the RHS -- the constant part and
+// (1/dt) M u^{n-1} -- stays FP64, and only the O(|D| dt)-relative corrections
+// run on the FP32 pipe (GB300 issues FP32 FMAs ~60x faster than FP64).
+template <int K, typename Tq>
 __global__ void __launch_bounds__(128)
     k_carrier_rhs(Tables T, RegionDev semi, RegionDev elec, int n_regions, FieldPtrs F,
                   const InstDev* __restrict__ inst, const double* __restrict__ iface_ne,
@@ -94,64 +108,61 @@ __global__ void __launch_bounds__(128)
   const int f1 = R.field1, f = f1 + which;
   const int nc = R.nc, nd = R.nd;
   const InstDev P = inst[i];
+  const Tq* phi = tab<Tq>(T.phi, T.phi_f);
+  const Tq* qw = tab<Tq>(T.qw, T.qw_f);
+  const Tq* fphi = tab<Tq>(T.fphi, T.fphi_f);
+  const Tq* fw = tab<Tq>(T.fw, T.fw_f);
+  const Tq* psix = tab<Tq>(T.psix, T.psix_f);
+  const Tq* psiy = tab<Tq>(T.psiy, T.psiy_f);
   const double* u1p = F.u[f1] + (size_t)i * F.nd[f1] + 2 * nc * n1 + c * n1;
   const double* u2p = F.u[f1 + 1] + (size_t)i * F.nd[f1 + 1] + 2 * nc * n1 + c * n1;
-  double u1[n1], u2[n1];
+  double uown[n1];
+  Tq u1[n1], u2[n1];
 #pragma unroll
   for (int a = 0; a < n1; ++a) {
-    u1[a] = u1p[a];
-    u2[a] = u2p[a];
+    const double x1 = u1p[a], x2 = u2p[a];
+    uown[a] = which ? x2 : x1;
+    u1[a] = (Tq)x1;
+    u2[a] = (Tq)x2;
   }
   const double* Pv = F.u[4] + (size_t)i * F.nd[4];
-  double Dd[nrt];
+  Tq Dd[nrt];
 #pragma unroll
-  for (int b = 0; b < nrt; ++b) Dd[b] = Pv[R.rt[c * nrt + b]];
+  for (int b = 0; b < nrt; ++b) Dd[b] = (Tq)Pv[R.rt[c * nrt + b]];
   const double2 h = R.h[c];
   const double hxhy = h.x * h.y;
-  const double* uo = which ? u2 : u1;
-  const double charge = which ? 1.0 : -1.0;
-  // accumulators: [Jx (n1) | Jy (n1) | u (n1)]
-  double r[3 * n1];
-  const double* bcp = F.bc[f] + (size_t)i * nd;
+  const Tq hxhy_q = (Tq)hxhy;
+  const Tq charge = which ? Tq(1) : Tq(-1);
+  const Tq inv_eps = (Tq)R.inv_eps;
+  // quadrature-term accumulators: [Jx (n1) | Jy (n1) | u (n1)]
+  Tq r[3 * n1];
 #pragma unroll
-  for (int comp = 0; comp < 3; ++comp)
-#pragma unroll
-    for (int a = 0; a < n1; ++a) r[comp * n1 + a] = bcp[comp * nc * n1 + c * n1 + a];
-  // (1/dt) M u^{n-1}
-#pragma unroll
-  for (int a = 0; a < n1; ++a) {
-    double s = 0.0;
-#pragma unroll
-    for (int b = 0; b < n1; ++b) s += T.mref[a * n1 + b] * uo[b];
-    r[2 * n1 + a] += s * hxhy * R.inv_dt;
-  }
+  for (int a = 0; a < 3 * n1; ++a) r[a] = Tq(0);
   const bool srh = in_semi && P.srh;
+  const Tq ni = (Tq)P.n_i, taun = (Tq)P.tau_n, taup = (Tq)P.tau_p;
 #pragma unroll 1
   for (int q = 0; q < Q; ++q) {
-    const double JxW = T.qw[q] * hxhy;
-    double uq = 0.0, n = 0.0, p = 0.0;
+    const Tq JxW = qw[q] * hxhy_q;
+    Tq n = 0, p = 0;
 #pragma unroll
     for (int a = 0; a < n1; ++a) {
-      const double ph = T.phi[a * Q + q];
+      const Tq ph = phi[a * Q + q];
       n += ph * u1[a];
       p += ph * u2[a];
     }
-    uq = which ? p : n;
-    double Ex = 0.0, Ey = 0.0;
+    const Tq uq = which ? p : n;
+    Tq Ex = 0, Ey = 0;
 #pragma unroll
     for (int b = 0; b < nrt; ++b) {
-      Ex += T.psix[b * Q + q] * Dd[b];
-      Ey += T.psiy[b * Q + q] * Dd[b];
+      Ex += psix[b * Q + q] * Dd[b];
+      Ey += psiy[b * Q + q] * Dd[b];
     }
-    const double w = charge * R.inv_eps * uq * JxW;
-    double Rq = 0.0;
-    if (srh) {
-      const double ni = P.n_i;
-      Rq = (ni * ni - n * p) / (P.tau_n * (n + ni) + P.tau_p * (p + ni)) * JxW;
-    }
+    const Tq w = charge * inv_eps * uq * JxW;
+    Tq Rq = 0;
+    if (srh) Rq = (ni * ni - n * p) / (taun * (n + ni) + taup * (p + ni)) * JxW;
 #pragma unroll
     for (int a = 0; a < n1; ++a) {
-      const double ph = T.phi[a * Q + q];
+      const Tq ph = phi[a * Q + q];
       r[a] += ph * Ex * w;
       r[n1 + a] += ph * Ey * w;
       r[2 * n1 + a] += ph * Rq;
@@ -165,34 +176,35 @@ __global__ void __launch_bounds__(128)
     const double* o1p = F.u[O.field1] + (size_t)i * F.nd[O.field1] + 2 * O.nc * n1 + pc * n1;
     const double* o2p = F.u[O.field1 + 1] + (size_t)i * F.nd[O.field1 + 1] + 2 * O.nc * n1 + pc * n1;
     const int ff = R.iface_face, pf = R.partner_face;
-    const double flen = (ff == 0 || ff == 1) ? h.y : h.x;
+    const Tq flen = (Tq)((ff == 0 || ff == 1) ? h.y : h.x);
+    const Tq ket = (Tq)P.k_et, kht = (Tq)P.k_ht;
 #pragma unroll 1
     for (int q = 0; q < nq; ++q) {
-      double a1 = 0.0, a2 = 0.0, b1 = 0.0, b2 = 0.0;
+      Tq a1 = 0, a2 = 0, b1 = 0, b2 = 0;
 #pragma unroll
       for (int a = 0; a < n1; ++a) {
-        const double fo = T.fphi[(ff * n1 + a) * nq + q];
-        const double fp = T.fphi[(pf * n1 + a) * nq + q];
+        const Tq fo = fphi[(ff * n1 + a) * nq + q];
+        const Tq fp = fphi[(pf * n1 + a) * nq + q];
         a1 += fo * u1[a];
         a2 += fo * u2[a];
-        b1 += fp * o1p[a];
-        b2 += fp * o2p[a];
+        b1 += fp * (Tq)o1p[a];
+        b2 += fp * (Tq)o2p[a];
       }
       // semiconductor-side values n, p and electrolyte-side r, o
-      const double n = in_semi ? a1 : b1, p = in_semi ? a2 : b2;
-      const double rr = in_semi ? b1 : a1, oo = in_semi ? b2 : a2;
-      const double ne = iface_ne[(size_t)i * n_iface * nq + ii * nq + q];
-      const double pe = iface_pe[(size_t)i * n_iface * nq + ii * nq + q];
-      const double Jf = T.fw[q] * flen;
-      const double tn = -P.k_et * (n - ne) * oo * Jf;
-      const double tp = P.k_ht * (p - pe) * rr * Jf;
-      double coef;
+      const Tq n = in_semi ? a1 : b1, p = in_semi ? a2 : b2;
+      const Tq rr = in_semi ? b1 : a1, oo = in_semi ? b2 : a2;
+      const Tq ne = (Tq)iface_ne[(size_t)i * n_iface * nq + ii * nq + q];
+      const Tq pe = (Tq)iface_pe[(size_t)i * n_iface * nq + ii * nq + q];
+      const Tq Jf = fw[q] * flen;
+      const Tq tn = -ket * (n - ne) * oo * Jf;
+      const Tq tp = kht * (p - pe) * rr * Jf;
+      Tq coef;
       if (in_semi)
         coef = which ? tp : tn;
       else
         coef = which ? -(tn + tp) : (tn + tp);
 #pragma unroll
-      for (int a = 0; a < n1; ++a) r[2 * n1 + a] += T.fphi[(ff * n1 + a) * nq + q] * coef;
+      for (int a = 0; a < n1; ++a) r[2 * n1 + a] += fphi[(ff * n1 + a) * nq + q] * coef;
     }
   }
   // Schottky faces (SolarCell.cpp:1348-1404)
@@ -200,24 +212,38 @@ __global__ void __launch_bounds__(128)
 #pragma unroll 1
     for (int fc = 0; fc < 4; ++fc) {
       if (bids[fc] != 3) continue;
-      const double flen = (fc == 0 || fc == 1) ? h.y : h.x;
+      const Tq flen = (Tq)((fc == 0 || fc == 1) ? h.y : h.x);
       for (int q = 0; q < nq; ++q) {
-        double val = 0.0;
+        Tq val = 0;
 #pragma unroll
-        for (int a = 0; a < n1; ++a) val += T.fphi[(fc * n1 + a) * nq + q] * uo[a];
+        for (int a = 0; a < n1; ++a) val += fphi[(fc * n1 + a) * nq + q] * (which ? u2[a] : u1[a]);
         const size_t o = (size_t)i * nc * 4 * nq + (size_t)(c * 4 + fc) * nq + q;
-        const double Jf = T.fw[q] * flen;
-        const double coef = which ? P.s_p * (val - sch_pe[o]) * Jf : -P.s_n * (val - sch_ne[o]) * Jf;
+        const Tq Jf = fw[q] * flen;
+        const Tq coef = which ? (Tq)P.s_p * (val - (Tq)sch_pe[o]) * Jf
+                              : -(Tq)P.s_n * (val - (Tq)sch_ne[o]) * Jf;
 #pragma unroll
-        for (int a = 0; a < n1; ++a) r[2 * n1 + a] += T.fphi[(fc * n1 + a) * nq + q] * coef;
+        for (int a = 0; a < n1; ++a) r[2 * n1 + a] += fphi[(fc * n1 + a) * nq + q] * coef;
       }
     }
   }
+  // constant part + (1/dt) M u^{n-1} in FP64, then the quadrature terms
+  const double* bcp = F.bc[f] + (size_t)i * nd;
   double* outp = F.out[f] + (size_t)i * nd;
 #pragma unroll
-  for (int comp = 0; comp < 3; ++comp)
+  for (int comp = 0; comp < 2; ++comp)
 #pragma unroll
-    for (int a = 0; a < n1; ++a) outp[comp * nc * n1 + c * n1 + a] = r[comp * n1 + a];
+    for (int a = 0; a < n1; ++a) {
+      const size_t o = (size_t)comp * nc * n1 + c * n1 + a;
+      outp[o] = bcp[o] + (double)r[comp * n1 + a];
+    }
+#pragma unroll
+  for (int a = 0; a < n1; ++a) {
+    double s = 0.0;
+#pragma unroll
+    for (int b = 0; b < n1; ++b) s += T.mref[a * n1 + b] * uown[b];
+    const size_t o = (size_t)2 * nc * n1 + c * n1 + a;
+    outp[o] = bcp[o] + s * hxhy * R.inv_dt + (double)r[2 * n1 + a];
+  }
 }
 
 // grid: x over max(n_rt_total, cells of both regions), y over instances

@@ -135,3 +135,34 @@ def test_fp32_refined_matches_fp64_oracle(pecs_lib):
     ctx.initialize()
     ctx.step(20)
     _compare_state(ctx, st, 1e-9)
+
+
+@pytest.mark.parametrize("iters", [1, 2])
+def test_mixed_precision_within_1e6_of_fp64_oracle(pecs_lib, iters):
+    """FP32 factors + double-float refinement + FP32 quadrature terms: the
+    batched throughput mode must stay within 1e-6 of the FP64 oracle."""
+    P = oracle.config2_params(n_refine=3)
+    pb = oracle.Problem(P)
+    st, _, _ = pb.run(20)
+    ctx = _ctx(P, precision=pg.PREC_FP32_MIXED, ir_max_iters=iters)
+    ctx.initialize()
+    ctx.step(20)
+    _compare_state(ctx, st, 1e-6)
+
+
+def test_mixed_precision_steady_state_and_current(pecs_lib):
+    base = oracle.config2_params(n_refine=3)
+    Ps = [base.copy(phi_app=v) for v in (-0.4, 0.0, 0.4)]
+    ctx = pg.Context([to_lib(P) for P in Ps], precision=pg.PREC_FP32_MIXED)
+    ctx.initialize()
+    steps, rel = ctx.run_to_steady_state(5000, 1e-8, check_every=50)
+    cur = ctx.interface_current()
+    ref = pg.Context([to_lib(P) for P in Ps])
+    ref.initialize()
+    steps64, _ = ref.run_to_steady_state(5000, 1e-8, check_every=50)
+    cur64 = ref.interface_current()
+    for i in range(len(Ps)):
+        assert abs(int(steps[i]) - int(steps64[i])) <= 0.05 * steps64[i] + 2
+        for f in ctx.fields():
+            assert rel_err(ctx.get_state(f, i), ref.get_state(f, i)) < 1e-6
+        assert abs(cur[i] - cur64[i]) <= 1e-6 * abs(cur64[i])
