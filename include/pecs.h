@@ -145,6 +145,14 @@ int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowpt
 int pecs_initialize(pecs_ctx* ctx);
 int pecs_set_state(pecs_ctx* ctx, int inst, int field, const double* host, size_t n);
 int pecs_get_state(pecs_ctx* ctx, int inst, int field, double* host, size_t n);
+/* the same with device pointers (no host round trip) */
+int pecs_get_state_device(pecs_ctx* ctx, int inst, int field, double* dst_dev);
+int pecs_set_state_device(pecs_ctx* ctx, int inst, int field, const double* src_dev);
+/* Replace the per-instance parameters of all n_inst instances (bias,
+ * generation, doping, lifetimes, rate constants...): right-hand-side data and
+ * initial states are rebuilt, matrices and factors are kept.  Fields that
+ * enter the matrices must not change. */
+int pecs_set_instances(pecs_ctx* ctx, const pecs_params* params, int n_inst);
 /* right-hand side of the last assembly (field = PECS_FIELD_*) */
 int pecs_get_rhs(pecs_ctx* ctx, int inst, int field, double* host, size_t n);
 
@@ -209,6 +217,29 @@ void pecs_lu_destroy(pecs_lu* lu);
  * clearing); calls that overlap on the GPU race on it. */
 int pecs_lu_solve_device_noalloc(pecs_lu* lu, int nrhs, const double* b_dev, double* x_dev,
                                  void* stream);
+
+/* ---- learned warm start: neural operator (no counterpart in the reference) ----
+ * A small MLP maps the parameters of an instance to coefficients of a fixed
+ * low-rank basis of the steady-state fields; its prediction initialises the
+ * time marching.  GEMM operands BF16, accumulation FP32, FP32 master weights,
+ * Adam.  widths has n_layers+1 entries (input .. output); hidden layers use
+ * tanh.  Parameters are packed per layer as W (out x in, row-major) then b.
+ * All x/y/t pointers are device pointers to row-major (batch x width) FP32. */
+typedef struct pecs_mlp pecs_mlp;
+int pecs_mlp_create(int n_layers, const int* widths, unsigned long long seed, pecs_mlp** out);
+void pecs_mlp_destroy(pecs_mlp* m);
+int pecs_mlp_n_params(pecs_mlp* m, long long* n);
+int pecs_mlp_get_params(pecs_mlp* m, float* host);
+int pecs_mlp_set_params(pecs_mlp* m, const float* host);
+int pecs_mlp_forward(pecs_mlp* m, int batch, const float* x_dev, float* y_dev, void* stream);
+/* gradient of mean((y - t)^2) w.r.t. the packed parameters, no update */
+int pecs_mlp_gradients(pecs_mlp* m, int batch, const float* x_dev, const float* t_dev, float* grad_host,
+                       float* loss);
+int pecs_mlp_train_step(pecs_mlp* m, int batch, const float* x_dev, const float* t_dev, float lr,
+                        float* loss);
+/* y (batch x n) = mean + c (batch x r) V^T with V (n x r); FP32 */
+int pecs_decode(int batch, int r, int n, const float* c_dev, const float* V_dev, const float* mean_dev,
+                float* y_dev, void* stream);
 
 #ifdef __cplusplus
 }

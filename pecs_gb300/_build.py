@@ -18,7 +18,7 @@ LIBDIR = HERE / "_lib"
 LIB = LIBDIR / "libpecs_gb300.so"
 INCLUDE = HERE.parent / "include"
 
-CUDA_SOURCES = ["engine.cu", "solve.cu"]
+CUDA_SOURCES = ["engine.cu", "solve.cu", "nn.cu"]
 CXX_SOURCES = ["problem.cpp", "mf.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

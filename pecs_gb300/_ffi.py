@@ -83,6 +83,9 @@ SIGNATURES = [
     ("pecs_set_state", C.c_int, [_vp, C.c_int, C.c_int, _dp, C.c_size_t]),
     ("pecs_get_state", C.c_int, [_vp, C.c_int, C.c_int, _dp, C.c_size_t]),
     ("pecs_get_rhs", C.c_int, [_vp, C.c_int, C.c_int, _dp, C.c_size_t]),
+    ("pecs_get_state_device", C.c_int, [_vp, C.c_int, C.c_int, _vp]),
+    ("pecs_set_state_device", C.c_int, [_vp, C.c_int, C.c_int, _vp]),
+    ("pecs_set_instances", C.c_int, [_vp, C.POINTER(pecs_params), C.c_int]),
     ("pecs_assemble_carrier_rhs", C.c_int, [_vp]),
     ("pecs_solve_carriers", C.c_int, [_vp]),
     ("pecs_assemble_poisson_rhs", C.c_int, [_vp]),
@@ -104,6 +107,15 @@ SIGNATURES = [
     ("pecs_lu_destroy", None, [_vp]),
     ("pecs_lu_solve_device_noalloc", C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     ("pecs_lu_host_apply", C.c_int, [_vp, _dp, _dp]),
+    ("pecs_mlp_create", C.c_int, [C.c_int, _ip, C.c_ulonglong, C.POINTER(_vp)]),
+    ("pecs_mlp_destroy", None, [_vp]),
+    ("pecs_mlp_n_params", C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    ("pecs_mlp_get_params", C.c_int, [_vp, C.POINTER(C.c_float)]),
+    ("pecs_mlp_set_params", C.c_int, [_vp, C.POINTER(C.c_float)]),
+    ("pecs_mlp_forward", C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    ("pecs_mlp_gradients", C.c_int, [_vp, C.c_int, _vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    ("pecs_mlp_train_step", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_float, C.POINTER(C.c_float)]),
+    ("pecs_decode", C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
 ]
 
 _lib = None

@@ -203,6 +203,18 @@ class Context:
         v = np.ascontiguousarray(values, dtype=np.float64)
         check(lib().pecs_set_state(self._h, inst, field, _dptr(v), v.size))
 
+    def set_instances(self, params: Sequence[Params]):
+        params = list(params)
+        arr = (F.pecs_params * len(params))(*[p.to_c() for p in params])
+        check(lib().pecs_set_instances(self._h, arr, len(params)))
+        self.params = params
+
+    def get_state_device(self, field: int, inst: int, dst_ptr: int):
+        check(lib().pecs_get_state_device(self._h, inst, field, C.c_void_p(dst_ptr)))
+
+    def set_state_device(self, field: int, inst: int, src_ptr: int):
+        check(lib().pecs_set_state_device(self._h, inst, field, C.c_void_p(src_ptr)))
+
     def get_rhs(self, field: int, inst: int = 0) -> np.ndarray:
         out = np.zeros(self.ndofs[field])
         check(lib().pecs_get_rhs(self._h, inst, field, _dptr(out), out.size))

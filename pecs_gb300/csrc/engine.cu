@@ -271,6 +271,9 @@ __global__ void k_snapshot(FieldPtrs NEW, double* const* snap, const int* __rest
 
 }  // namespace
 
+// error message hook for the other translation units of the library
+void set_error_external(const std::string& m) { g_last_error = m; }
+
 // ---------------------------------------------------------------------------
 // Engine
 // ---------------------------------------------------------------------------
@@ -581,6 +584,41 @@ struct Engine {
     snap_ptrs.upload(sp);
     PECS_CUDA(cudaDeviceSynchronize());
     setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+
+  // Replace the per-instance parameters (bias, generation, doping, lifetimes,
+  // rates...) of every instance; matrices and factors are kept.
+  void set_instances(const std::vector<pecs_params>& P) {
+    if ((int)P.size() != n_inst) throw PecsError(PECS_E_ARG, "n_inst differs from the context's");
+    std::vector<pecs_params> chk(P);
+    chk.insert(chk.begin(), S->inst[0]);
+    std::string err = validate_params(chk.data(), (int)chk.size());
+    if (!err.empty()) throw PecsError(PECS_E_ARG, err);
+    S->compute_instances(P);
+    auto put = [&](DBuf<double>& d, const std::vector<std::vector<double>>& src) {
+      std::vector<double> v;
+      for (auto& x : src) v.insert(v.end(), x.begin(), x.end());
+      if (v.size() != d.n) throw PecsError(PECS_E_STATE, "instance data size changed");
+      if (!v.empty()) PECS_CUDA(cudaMemcpy(d.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice));
+    };
+    for (int f = 0; f < 5; ++f)
+      if (nd[f]) put(bconst[f], S->bconst[f]);
+    for (int f = 0; f < 4; ++f)
+      if (nd[f]) put(init_dev[f], S->init[f]);
+    if (full) {
+      put(iface_ne, S->iface_ne);
+      put(iface_pe, S->iface_pe);
+    }
+    if (S->has_schottky) {
+      put(sch_ne, S->schottky_ne);
+      put(sch_pe, S->schottky_pe);
+    }
+    std::vector<InstDev> ip(n_inst);
+    for (int i = 0; i < n_inst; ++i) {
+      const pecs_params& p = S->inst[i];
+      ip[i] = InstDev{p.k_et, p.k_ht, p.tau_n, p.tau_p, p.n_i, p.s_n, p.s_p, p.srh, 0};
+    }
+    PECS_CUDA(cudaMemcpy(inst.p, ip.data(), ip.size() * sizeof(InstDev), cudaMemcpyHostToDevice));
   }
 
   void upload_tables() {
@@ -907,7 +945,7 @@ struct Engine {
     check_every += check_every & 1;
     reset_convergence();
     last_run_steps = 0;
-    const bool use_graph = opt.use_graphs != 0;
+    const bool use_graph = opt.use_graphs != 0 && max_steps >= 2;
     if (use_graph && (!graph_valid || graph_tol != tol)) capture_graph(tol);
     int done = 0;
     int h_active = n_inst;
@@ -1161,6 +1199,38 @@ int pecs_get_state(pecs_ctx* ctx, int inst, int field, double* host, size_t n) {
     PECS_CUDA(cudaMemcpyAsync(host, e.latest(field).p + (size_t)inst * e.nd[field], n * 8,
                               cudaMemcpyDeviceToHost, e.st));
     PECS_CUDA(cudaStreamSynchronize(e.st));
+  })
+}
+
+int pecs_set_instances(pecs_ctx* ctx, const pecs_params* params, int n_inst) {
+  PECS_TRY({
+    if (!ctx || !params) throw PecsError(PECS_E_ARG, "NULL argument");
+    need_device(ctx->e);
+    ctx->e.set_instances(std::vector<pecs_params>(params, params + n_inst));
+  })
+}
+
+int pecs_get_state_device(pecs_ctx* ctx, int inst, int field, double* dst_dev) {
+  PECS_TRY({
+    if (!ctx || !dst_dev) throw PecsError(PECS_E_ARG, "NULL argument");
+    Engine& e = ctx->e;
+    check_field(e, inst, field, (size_t)(field >= 0 && field < 5 ? e.nd[field] : 0));
+    PECS_CUDA(cudaMemcpyAsync(dst_dev, e.latest(field).p + (size_t)inst * e.nd[field],
+                              (size_t)e.nd[field] * 8, cudaMemcpyDeviceToDevice, e.st));
+    PECS_CUDA(cudaStreamSynchronize(e.st));
+  })
+}
+
+int pecs_set_state_device(pecs_ctx* ctx, int inst, int field, const double* src_dev) {
+  PECS_TRY({
+    if (!ctx || !src_dev) throw PecsError(PECS_E_ARG, "NULL argument");
+    Engine& e = ctx->e;
+    check_field(e, inst, field, (size_t)(field >= 0 && field < 5 ? e.nd[field] : 0));
+    if (e.carriers_advanced) throw PecsError(PECS_E_STATE, "step in progress");
+    PECS_CUDA(cudaMemcpyAsync(e.state[e.cur][field].p + (size_t)inst * e.nd[field], src_dev,
+                              (size_t)e.nd[field] * 8, cudaMemcpyDeviceToDevice, e.st));
+    PECS_CUDA(cudaStreamSynchronize(e.st));
+    e.initialized = true;
   })
 }
 

@@ -1,0 +1,424 @@
+// Neural operator for the learned warm start: a small MLP mapping the six
+// physical parameters of an instance (bias, generation amplitude, absorption
+// coefficient, doping, lifetime, interface rate) to the coefficients of a
+// fixed low-rank (POD) basis of the steady-state fields.  No counterpart in
+// the reference: it is the warm-start component the benchmark adds.
+//
+// Arithmetic: GEMM operands are BF16 (weights stored in BF16, activations
+// rounded to BF16 when staged), accumulation FP32; FP32 master weights and
+// Adam moments.  Layers: z = x W^T + b, y = tanh(z) for hidden layers, linear
+// output; loss = mean squared error.  The decoder (mean + V c) is an FP32 GEMM.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "common.hpp"
+
+namespace pecs {
+namespace {
+
+constexpr int kBM = 64, kBN = 64, kBK = 16, kGemmThreads = 256;
+
+template <typename T>
+__device__ __forceinline__ float to_f(T v);
+template <>
+__device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+__device__ __forceinline__ float round_bf16(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+
+// C[M,N] = alpha * op(A)[M,K] op(B)[K,N] + beta * C + bias[n], then act.
+// op(A)(m,k) = TA ? A[k*lda+m] : A[m*lda+k]; op(B)(k,n) = TB ? B[n*ldb+k] : B[k*ldb+n].
+// kBf16In rounds both operands to BF16 before the product (FP32 accumulate).
+template <typename TAe, typename TBe, bool TA, bool TB, bool kBf16In>
+__global__ void __launch_bounds__(kGemmThreads)
+    k_gemm(int M, int N, int K, const TAe* __restrict__ A, int lda, const TBe* __restrict__ B, int ldb,
+           float* __restrict__ C, int ldc, float alpha, float beta, const float* __restrict__ bias,
+           int act) {
+  __shared__ float As[kBK][kBM + 1];
+  __shared__ float Bs[kBK][kBN + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += kBK) {
+    for (int t = threadIdx.x; t < kBK * kBM; t += kGemmThreads) {
+      const int kk = t % kBK, mm = t / kBK;
+      const int m = m0 + mm, k = k0 + kk;
+      float v = 0.f;
+      if (m < M && k < K) v = to_f(TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]);
+      As[kk][mm] = kBf16In ? round_bf16(v) : v;
+    }
+    for (int t = threadIdx.x; t < kBK * kBN; t += kGemmThreads) {
+      const int nn = t % kBN, kk = t / kBN;
+      const int n = n0 + nn, k = k0 + kk;
+      float v = 0.f;
+      if (n < N && k < K) v = to_f(TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n]);
+      Bs[kk][nn] = kBf16In ? round_bf16(v) : v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kBK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + ty * 4 + i;
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int n = n0 + tx * 4 + j;
+      if (n >= N) continue;
+      float v = alpha * acc[i][j];
+      if (beta != 0.f) v += beta * C[(size_t)m * ldc + n];
+      if (bias) v += bias[n];
+      if (act == 1) v = tanhf(v);
+      C[(size_t)m * ldc + n] = v;
+    }
+  }
+}
+
+template <typename TAe, typename TBe, bool TA, bool TB, bool kBf16In>
+void gemm(int M, int N, int K, const TAe* A, int lda, const TBe* B, int ldb, float* C, int ldc,
+          float alpha, float beta, const float* bias, int act, cudaStream_t st) {
+  dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
+  k_gemm<TAe, TBe, TA, TB, kBf16In><<<grid, kGemmThreads, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc,
+                                                                    alpha, beta, bias, act);
+  PECS_CUDA(cudaGetLastError());
+}
+
+// dz = dy * (1 - y^2)   (tanh backward), in place on dy
+__global__ void k_tanh_bwd(float* __restrict__ dy, const float* __restrict__ y, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) dy[i] *= (1.f - y[i] * y[i]);
+}
+
+// db[n] = sum_b dz[b, n]
+__global__ void k_colsum(const float* __restrict__ dz, float* __restrict__ db, int B, int N) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float s = 0.f;
+  for (int b = 0; b < B; ++b) s += dz[(size_t)b * N + n];
+  db[n] = s;
+}
+
+// dy = 2 (y - t) / (B N); per-block partial loss sums
+__global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, float* __restrict__ dy,
+                      size_t n, float* __restrict__ loss_partial) {
+  __shared__ float s[256];
+  float acc = 0.f;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float d = y[i] - t[i];
+    dy[i] = 2.f * d / (float)n;
+    acc += d * d;
+  }
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_partial[blockIdx.x] = s[0];
+}
+
+// Adam on FP32 masters, refreshes the BF16 copy
+__global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ g, __nv_bfloat16* __restrict__ wb, size_t n, float lr,
+                       float b1, float b2, float eps, float c1, float c2) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  w[i] = wi;
+  wb[i] = __float2bfloat16_rn(wi);
+}
+
+__global__ void k_to_bf16(const float* __restrict__ w, __nv_bfloat16* __restrict__ wb, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) wb[i] = __float2bfloat16_rn(w[i]);
+}
+
+__global__ void k_add_rowvec(float* __restrict__ y, const float* __restrict__ mean, int B, int N) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < (size_t)B * N) y[i] += mean[i % N];
+}
+
+}  // namespace
+
+struct Mlp {
+  std::vector<int> w;          // widths, layers = w.size()-1
+  size_t n_params = 0;
+  std::vector<size_t> woff, boff;  // offsets of W_l (out x in) and b_l in the packed vector
+  DBuf<float> P, G, Mo, Vo;    // masters, grads, Adam moments
+  DBuf<__nv_bfloat16> Pb;      // BF16 copy
+  int max_batch = 0;
+  std::vector<DBuf<float>> act;  // act[l]: batch x w[l] (act[0] = input copy)
+  std::vector<DBuf<float>> dact;
+  DBuf<float> loss_part;
+  int adam_t = 0;
+  cudaStream_t st = nullptr;
+  ~Mlp() {
+    if (st) cudaStreamDestroy(st);
+  }
+
+  void ensure_batch(int B) {
+    if (B <= max_batch) return;
+    act.clear();
+    dact.clear();
+    act.resize(w.size());
+    dact.resize(w.size());
+    for (size_t l = 0; l < w.size(); ++l) {
+      act[l].alloc((size_t)B * w[l]);
+      dact[l].alloc((size_t)B * w[l]);
+    }
+    max_batch = B;
+  }
+
+  const __nv_bfloat16* Wb(int l) const { return Pb.p + woff[l]; }
+  const float* bias(int l) const { return P.p + boff[l]; }
+
+  void forward(int B, const float* x, cudaStream_t s) {
+    ensure_batch(B);
+    const int L = (int)w.size() - 1;
+    PECS_CUDA(cudaMemcpyAsync(act[0].p, x, (size_t)B * w[0] * 4, cudaMemcpyDeviceToDevice, s));
+    for (int l = 0; l < L; ++l) {
+      // act[l+1] = act(act[l] W_l^T + b_l); W_l stored out x in (row-major)
+      gemm<float, __nv_bfloat16, false, true, true>(B, w[l + 1], w[l], act[l].p, w[l], Wb(l), w[l],
+                                                    act[l + 1].p, w[l + 1], 1.f, 0.f, bias(l),
+                                                    l < L - 1 ? 1 : 0, s);
+    }
+  }
+
+  // gradients of mean((y - t)^2) into G; returns via loss_part (device)
+  void backward(int B, const float* target, cudaStream_t s) {
+    const int L = (int)w.size() - 1;
+    const size_t nout = (size_t)B * w[L];
+    const int nblk = 64;
+    if (loss_part.n < (size_t)nblk) loss_part.alloc(nblk);
+    k_mse<<<nblk, 256, 0, s>>>(act[L].p, target, dact[L].p, nout, loss_part.p);
+    PECS_CUDA(cudaGetLastError());
+    for (int l = L - 1; l >= 0; --l) {
+      float* dz = dact[l + 1].p;
+      if (l < L - 1) {
+        const size_t n = (size_t)B * w[l + 1];
+        k_tanh_bwd<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dz, act[l + 1].p, n);
+        PECS_CUDA(cudaGetLastError());
+      }
+      // dW_l (out x in) = dz^T (out x B) * act[l] (B x in)
+      gemm<float, float, true, false, true>(w[l + 1], w[l], B, dz, w[l + 1], act[l].p, w[l],
+                                            G.p + woff[l], w[l], 1.f, 0.f, nullptr, 0, s);
+      k_colsum<<<(w[l + 1] + 127) / 128, 128, 0, s>>>(dz, G.p + boff[l], B, w[l + 1]);
+      PECS_CUDA(cudaGetLastError());
+      if (l > 0) {
+        // d act[l] (B x in) = dz (B x out) * W_l (out x in)
+        gemm<float, __nv_bfloat16, false, false, true>(B, w[l], w[l + 1], dz, w[l + 1], Wb(l), w[l],
+                                                       dact[l].p, w[l], 1.f, 0.f, nullptr, 0, s);
+      }
+    }
+  }
+
+  float read_loss(cudaStream_t s, int B) {
+    std::vector<float> h(64);
+    PECS_CUDA(cudaMemcpyAsync(h.data(), loss_part.p, 64 * 4, cudaMemcpyDeviceToHost, s));
+    PECS_CUDA(cudaStreamSynchronize(s));
+    double t = 0;
+    for (float v : h) t += v;
+    return (float)(t / ((double)B * w.back()));
+  }
+
+  void adam(float lr, cudaStream_t s) {
+    ++adam_t;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)adam_t), c2 = 1.f - std::pow(b2, (float)adam_t);
+    k_adam<<<(unsigned)((n_params + 255) / 256), 256, 0, s>>>(P.p, Mo.p, Vo.p, G.p, Pb.p, n_params, lr,
+                                                              b1, b2, 1e-8f, c1, c2);
+    PECS_CUDA(cudaGetLastError());
+  }
+
+  void sync_bf16(cudaStream_t s) {
+    k_to_bf16<<<(unsigned)((n_params + 255) / 256), 256, 0, s>>>(P.p, Pb.p, n_params);
+    PECS_CUDA(cudaGetLastError());
+  }
+};
+
+}  // namespace pecs
+
+using namespace pecs;
+
+struct pecs_mlp {
+  Mlp m;
+};
+
+namespace pecs {
+void set_error_external(const std::string& m);
+}
+
+#define NN_TRY(...)                                     \
+  try {                                                 \
+    __VA_ARGS__;                                        \
+    return PECS_OK;                                     \
+  } catch (const PecsError& ex) {                       \
+    pecs::set_error_external(ex.what());                \
+    return ex.code;                                     \
+  } catch (const std::exception& ex) {                  \
+    pecs::set_error_external(ex.what());                \
+    return PECS_E_ARG;                                  \
+  }
+
+extern "C" {
+
+int pecs_mlp_create(int n_layers, const int* widths, unsigned long long seed, pecs_mlp** out) {
+  NN_TRY({
+    if (!out || !widths || n_layers < 1 || n_layers > 16) throw PecsError(PECS_E_ARG, "bad layers");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+      throw PecsError(PECS_E_NODEVICE, "no CUDA device available");
+    std::unique_ptr<pecs_mlp> h(new pecs_mlp());
+    Mlp& m = h->m;
+    m.w.assign(widths, widths + n_layers + 1);
+    for (int x : m.w)
+      if (x < 1 || x > 65536) throw PecsError(PECS_E_ARG, "bad width");
+    size_t off = 0;
+    for (int l = 0; l < n_layers; ++l) {
+      m.woff.push_back(off);
+      off += (size_t)m.w[l] * m.w[l + 1];
+      m.boff.push_back(off);
+      off += m.w[l + 1];
+    }
+    m.n_params = off;
+    std::vector<float> init(off, 0.f);
+    std::mt19937_64 g(seed);
+    for (int l = 0; l < n_layers; ++l) {
+      const float sc = std::sqrt(1.0f / m.w[l]);  // LeCun-uniform-like for tanh
+      std::uniform_real_distribution<float> U(-sc * std::sqrt(3.f), sc * std::sqrt(3.f));
+      for (size_t t = 0; t < (size_t)m.w[l] * m.w[l + 1]; ++t) init[m.woff[l] + t] = U(g);
+    }
+    PECS_CUDA(cudaStreamCreateWithFlags(&m.st, cudaStreamNonBlocking));
+    m.P.upload(init);
+    m.G.alloc(off);
+    m.G.zero();
+    m.Mo.alloc(off);
+    m.Mo.zero();
+    m.Vo.alloc(off);
+    m.Vo.zero();
+    m.Pb.alloc(off);
+    m.sync_bf16(m.st);
+    PECS_CUDA(cudaStreamSynchronize(m.st));
+    *out = h.release();
+  })
+}
+
+void pecs_mlp_destroy(pecs_mlp* m) { delete m; }
+
+int pecs_mlp_n_params(pecs_mlp* h, long long* n) {
+  NN_TRY({
+    if (!h || !n) throw PecsError(PECS_E_ARG, "NULL argument");
+    *n = (long long)h->m.n_params;
+  })
+}
+
+int pecs_mlp_get_params(pecs_mlp* h, float* host) {
+  NN_TRY({
+    if (!h || !host) throw PecsError(PECS_E_ARG, "NULL argument");
+    PECS_CUDA(cudaMemcpy(host, h->m.P.p, h->m.n_params * 4, cudaMemcpyDeviceToHost));
+  })
+}
+
+int pecs_mlp_set_params(pecs_mlp* h, const float* host) {
+  NN_TRY({
+    if (!h || !host) throw PecsError(PECS_E_ARG, "NULL argument");
+    Mlp& m = h->m;
+    PECS_CUDA(cudaMemcpy(m.P.p, host, m.n_params * 4, cudaMemcpyHostToDevice));
+    m.sync_bf16(m.st);
+    m.Mo.zero();
+    m.Vo.zero();
+    m.adam_t = 0;
+    PECS_CUDA(cudaStreamSynchronize(m.st));
+  })
+}
+
+// y (batch x out) = network(x (batch x in)); device pointers
+int pecs_mlp_forward(pecs_mlp* h, int batch, const float* x_dev, float* y_dev, void* stream) {
+  NN_TRY({
+    if (!h || batch < 1 || !x_dev || !y_dev) throw PecsError(PECS_E_ARG, "invalid arguments");
+    Mlp& m = h->m;
+    cudaStream_t s = stream ? (cudaStream_t)stream : m.st;
+    m.forward(batch, x_dev, s);
+    PECS_CUDA(cudaMemcpyAsync(y_dev, m.act.back().p, (size_t)batch * m.w.back() * 4,
+                              cudaMemcpyDeviceToDevice, s));
+    PECS_CUDA(cudaStreamSynchronize(s));
+  })
+}
+
+// gradients of the MSE loss (no update); grad_host receives n_params floats
+int pecs_mlp_gradients(pecs_mlp* h, int batch, const float* x_dev, const float* t_dev, float* grad_host,
+                       float* loss) {
+  NN_TRY({
+    if (!h || batch < 1 || !x_dev || !t_dev) throw PecsError(PECS_E_ARG, "invalid arguments");
+    Mlp& m = h->m;
+    m.forward(batch, x_dev, m.st);
+    m.backward(batch, t_dev, m.st);
+    if (loss) *loss = m.read_loss(m.st, batch);
+    if (grad_host) PECS_CUDA(cudaMemcpy(grad_host, m.G.p, m.n_params * 4, cudaMemcpyDeviceToHost));
+    PECS_CUDA(cudaStreamSynchronize(m.st));
+  })
+}
+
+// one Adam step on the MSE loss of (x, t); loss (may be NULL) returns the pre-update loss
+int pecs_mlp_train_step(pecs_mlp* h, int batch, const float* x_dev, const float* t_dev, float lr,
+                        float* loss) {
+  NN_TRY({
+    if (!h || batch < 1 || !x_dev || !t_dev || !(lr > 0)) throw PecsError(PECS_E_ARG, "invalid arguments");
+    Mlp& m = h->m;
+    m.forward(batch, x_dev, m.st);
+    m.backward(batch, t_dev, m.st);
+    m.adam(lr, m.st);
+    if (loss)
+      *loss = m.read_loss(m.st, batch);
+    else
+      PECS_CUDA(cudaStreamSynchronize(m.st));
+  })
+}
+
+// FP32 decoder: y (batch x n) = mean (n) + c (batch x r) V^T, V stored n x r (row-major)
+int pecs_decode(int batch, int r, int n, const float* c_dev, const float* V_dev, const float* mean_dev,
+                float* y_dev, void* stream) {
+  NN_TRY({
+    if (batch < 1 || r < 1 || n < 1 || !c_dev || !V_dev || !mean_dev || !y_dev)
+      throw PecsError(PECS_E_ARG, "invalid arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    gemm<float, float, false, true, false>(batch, n, r, c_dev, r, V_dev, r, y_dev, n, 1.f, 0.f, nullptr,
+                                           0, s);
+    const size_t tot = (size_t)batch * n;
+    k_add_rowvec<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(y_dev, mean_dev, batch, n);
+    PECS_CUDA(cudaGetLastError());
+    PECS_CUDA(cudaStreamSynchronize(s));
+  })
+}
+
+}  // extern "C"

@@ -557,7 +557,15 @@ Setup::Setup(const std::vector<pecs_params>& p)
     for (int f = 0; f < 4; ++f)
       if (semi.grid.face_bid(K, f) == kSchottky) has_schottky = true;
 
-  // time-independent RHS parts per instance
+  compute_instances(p);
+}
+
+
+// Per-instance data: time-independent RHS parts, interface/Schottky
+// equilibria and the projected initial state.  Only fields that do not enter
+// the matrices may differ between instances (validate_params checks that).
+void Setup::compute_instances(const std::vector<pecs_params>& p) {
+  inst = p;
   const int ninst = (int)p.size();
   const int nloc = n_rt + n_phi;
   for (int fld = 0; fld < 5; ++fld) bconst[fld].assign(ninst, {});

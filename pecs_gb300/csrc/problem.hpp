@@ -76,6 +76,7 @@ struct Setup {
   std::vector<std::vector<double>> init[4];
 
   explicit Setup(const std::vector<pecs_params>& p);
+  void compute_instances(const std::vector<pecs_params>& p);
 };
 
 // Validates a parameter set; returns an empty string when it is usable.

@@ -1,0 +1,309 @@
+"""Learned warm start: a neural operator that predicts steady states.
+
+The operator maps the six instance parameters -- bias, generation amplitude
+G0, absorption coefficient alpha, donor doping N_D, SRH lifetime tau and the
+interface rate k_et -- to the steady-state electron and hole densities
+(log of the density dofs) and the potential (cell values) of the half cell.
+It is a small MLP (libpecs_gb300's BF16-in/FP32-accumulate kernels, trained by
+Adam on the GPU) predicting the coefficients of a fixed POD basis of
+training steady states that the plain method generates.  Its prediction is
+used only as the initial condition of the time marching, which then runs to
+the same steady-state criterion; an instance falls back to the standard
+initial condition when the prediction's first-step relative change is larger
+than the standard initial condition's.
+
+There is no counterpart in the reference; this is the component the
+benchmark's learned warm start adds.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _ffi as F
+from .api import Context, Params, config2
+from ._ffi import check, lib
+
+NAMES = ("bias", "G0", "alpha", "N_D", "tau", "k_et")
+# (low, high, log-uniform?)
+RANGES = ((-0.5, 0.5, False), (0.5, 2.0, False), (1.0, 10.0, False), (0.3, 3.0, True),
+          (0.1, 10.0, True), (1e-3, 1e-1, True))
+DENSITY_FLOOR = 1e-12
+
+
+def sample(n: int, seed: int) -> np.ndarray:
+    """n parameter draws (n x 6) from the benchmark's distributions."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((n, 6))
+    for j, (lo, hi, lg) in enumerate(RANGES):
+        u = rng.random(n)
+        out[:, j] = np.exp(np.log(lo) + u * (np.log(hi) - np.log(lo))) if lg else lo + u * (hi - lo)
+    return out
+
+
+def normalize(theta: np.ndarray) -> np.ndarray:
+    """Map each parameter to [-1, 1] (log scale for log-uniform ones)."""
+    x = np.zeros_like(theta, dtype=np.float64)
+    for j, (lo, hi, lg) in enumerate(RANGES):
+        v, a, b = (np.log(theta[:, j]), np.log(lo), np.log(hi)) if lg else (theta[:, j], lo, hi)
+        x[:, j] = 2.0 * (v - a) / (b - a) - 1.0
+    return x.astype(np.float32)
+
+
+def instance_params(theta_row, base: Params) -> Params:
+    """Parameters of one instance: config-2 physics with the six drawn values
+    (k_ht follows k_et; equilibrium densities follow the doping)."""
+    bias, G0, alpha, nd, tau, ket = (float(v) for v in theta_row)
+    ni = base.n_i
+    return base.copy(phi_app=bias, G0=G0, alpha=alpha, nd=(nd, nd), na=(0.0, 0.0),
+                     n_eq=(nd, nd), p_eq=(ni * ni / nd, ni * ni / nd), tau_n=tau, tau_p=tau,
+                     k_et=ket, k_ht=ket)
+
+
+@dataclass
+class Layout:
+    """Where the predicted quantities live in the state vectors."""
+    nd_carrier: int
+    n_u: int          # density dofs per carrier (u block)
+    u_off: int        # offset of the u block in a carrier vector
+    nd_poisson: int
+    n_phi: int        # potential dofs
+    phi_off: int
+
+    @property
+    def n_out(self):
+        return 2 * self.n_u + self.n_phi
+
+    @staticmethod
+    def of(ctx: Context) -> "Layout":
+        nd = ctx.ndofs[F.FIELD_N]
+        n_u = nd // 3
+        ndp = ctx.ndofs[F.FIELD_POISSON]
+        p0 = ctx.params[0]
+        ncell_p = (p0.nx_semi + (p0.nx_elec if p0.full_system else 0)) * p0.ny
+        n_phi = ncell_p * (p0.degree * p0.degree)
+        return Layout(nd, n_u, 2 * n_u, ndp, n_phi, ndp - n_phi)
+
+
+def fields_to_targets(n_state, p_state, P_state, lay: Layout) -> np.ndarray:
+    """Steady-state vectors -> [log n_u | log p_u | Phi] (float64)."""
+    n = np.maximum(n_state[lay.u_off:lay.u_off + lay.n_u], DENSITY_FLOOR)
+    p = np.maximum(p_state[lay.u_off:lay.u_off + lay.n_u], DENSITY_FLOOR)
+    return np.concatenate([np.log(n), np.log(p), P_state[lay.phi_off:lay.phi_off + lay.n_phi]])
+
+
+class Mlp:
+    """The C-ABI MLP (pecs_mlp_*)."""
+
+    def __init__(self, widths: Sequence[int], seed: int = 0):
+        self.widths = list(widths)
+        w = (C.c_int * len(widths))(*widths)
+        h = C.c_void_p()
+        check(lib().pecs_mlp_create(len(widths) - 1, w, seed, C.byref(h)))
+        self._h = h
+        n = C.c_longlong()
+        check(lib().pecs_mlp_n_params(h, C.byref(n)))
+        self.n_params = n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pecs_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        check(lib().pecs_mlp_get_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        check(lib().pecs_mlp_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def forward(self, x_dev, y_dev, batch: int, stream: int = 0):
+        check(lib().pecs_mlp_forward(self._h, batch, C.c_void_p(x_dev), C.c_void_p(y_dev),
+                                     C.c_void_p(stream)))
+
+    def gradients(self, x_dev, t_dev, batch: int):
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_float()
+        check(lib().pecs_mlp_gradients(self._h, batch, C.c_void_p(x_dev), C.c_void_p(t_dev),
+                                       g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)))
+        return g, loss.value
+
+    def train_step(self, x_dev, t_dev, batch: int, lr: float, want_loss: bool = False):
+        loss = C.c_float()
+        check(lib().pecs_mlp_train_step(self._h, batch, C.c_void_p(x_dev), C.c_void_p(t_dev), lr,
+                                        C.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+
+class NeuralOperator:
+    """MLP -> POD coefficients -> (log n, log p, Phi)."""
+
+    def __init__(self, rank: int = 64, hidden: int = 512, layers: int = 3, seed: int = 0):
+        self.rank = rank
+        widths = [6] + [hidden] * layers + [rank]
+        self.mlp = Mlp(widths, seed)
+        self.mean = None
+        self.basis = None      # n_out x rank (orthonormal columns of the scaled data)
+        self.scale = None      # per-output scaling (block std)
+        self.cscale = None     # per-coefficient scaling
+
+    # -- POD --------------------------------------------------------------------
+    def fit_basis(self, Y, lay: Layout):
+        """Y: (n_samples, n_out) torch tensor (float64, cuda).  Block-scaled POD."""
+        import torch
+        mean = Y.mean(0)
+        scale = torch.ones(Y.shape[1], dtype=Y.dtype, device=Y.device)
+        blocks = [(0, lay.n_u), (lay.n_u, 2 * lay.n_u), (2 * lay.n_u, lay.n_out)]
+        for a, b in blocks:
+            s = (Y[:, a:b] - mean[a:b]).std()
+            scale[a:b] = s if s > 0 else 1.0
+        Z = (Y - mean) / scale
+        # POD basis: right singular vectors of the scaled snapshots
+        _, S, Vh = torch.linalg.svd(Z, full_matrices=False)
+        V = Vh[:self.rank].T.contiguous()
+        self.mean, self.scale, self.basis = mean, scale, V
+        self.sv = S
+        Cf = Z @ V
+        self.cscale = Cf.std(0).clamp_min(1e-12)
+        return (Cf / self.cscale).float()
+
+    def targets(self, Y):
+        Z = (Y - self.mean) / self.scale
+        return ((Z @ self.basis) / self.cscale).float()
+
+    # -- training ---------------------------------------------------------------
+    def train(self, X, T, epochs: int = 400, batch: int = 256, lr: float = 2e-3, seed: int = 0,
+              log=None):
+        """X: (n, 6) float32 cuda; T: (n, rank) float32 cuda."""
+        import torch
+        n = X.shape[0]
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        steps = 0
+        total = epochs * max(1, n // batch)
+        hist = []
+        for ep in range(epochs):
+            perm = torch.randperm(n, generator=g).to(X.device)
+            for b0 in range(0, n - batch + 1, batch):
+                idx = perm[b0:b0 + batch]
+                xb = X[idx].contiguous()
+                tb = T[idx].contiguous()
+                # cosine learning-rate decay
+                cur = lr * 0.5 * (1.0 + math.cos(math.pi * steps / total))
+                want = (b0 == 0)
+                loss = self.mlp.train_step(xb.data_ptr(), tb.data_ptr(), batch, cur, want_loss=want)
+                steps += 1
+                if want:
+                    hist.append(loss)
+                    if log and ep % 50 == 0:
+                        log(f"epoch {ep} loss {loss:.3e}")
+        return hist
+
+    def predict_coeffs(self, X):
+        import torch
+        out = torch.empty(X.shape[0], self.rank, dtype=torch.float32, device=X.device)
+        self.mlp.forward(X.contiguous().data_ptr(), out.data_ptr(), X.shape[0])
+        return out
+
+    def predict(self, X):
+        """(n, n_out) float64 predictions of [log n | log p | Phi]; the
+        decode y = mean + scale * (V (c * cscale)) runs in pecs_decode (FP32)."""
+        import torch
+        c = (self.predict_coeffs(X) * self.cscale.float()).contiguous()
+        Vs = (self.basis * self.scale[:, None]).float().contiguous()
+        mean = self.mean.float().contiguous()
+        y = torch.empty(X.shape[0], Vs.shape[0], dtype=torch.float32, device=X.device)
+        check(lib().pecs_decode(X.shape[0], self.rank, Vs.shape[0], C.c_void_p(c.data_ptr()),
+                                C.c_void_p(Vs.data_ptr()), C.c_void_p(mean.data_ptr()),
+                                C.c_void_p(y.data_ptr()), C.c_void_p(0)))
+        return y.double()
+
+
+# -- data generation and warm-started sweeps --------------------------------------
+
+def steady_states(ctx: Context, thetas: np.ndarray, base: Params, max_steps=5000, tol=1e-8,
+                  check_every=50):
+    """March every row of ``thetas`` (batches of ctx.n_inst) to steady state with
+    the plain method; returns (targets (n, n_out) torch float64 cuda, steps)."""
+    import torch
+    lay = Layout.of(ctx)
+    B = ctx.n_inst
+    n = thetas.shape[0]
+    Y = torch.empty(n, lay.n_out, dtype=torch.float64, device="cuda")
+    steps = np.zeros(n, dtype=np.int64)
+    bufs = {f: torch.empty(ctx.ndofs[f], dtype=torch.float64, device="cuda")
+            for f in (F.FIELD_N, F.FIELD_P, F.FIELD_POISSON)}
+    for b0 in range(0, n, B):
+        rows = list(range(b0, min(n, b0 + B)))
+        pad = rows + [rows[-1]] * (B - len(rows))
+        ctx.set_instances([instance_params(thetas[r], base) for r in pad])
+        ctx.initialize()
+        s, _ = ctx.run_to_steady_state(max_steps, tol, check_every)
+        for k, r in enumerate(rows):
+            for f, t in bufs.items():
+                ctx.get_state_device(f, k, t.data_ptr())
+            nu = bufs[F.FIELD_N][lay.u_off:lay.u_off + lay.n_u].clamp_min(DENSITY_FLOOR).log()
+            pu = bufs[F.FIELD_P][lay.u_off:lay.u_off + lay.n_u].clamp_min(DENSITY_FLOOR).log()
+            ph = bufs[F.FIELD_POISSON][lay.phi_off:lay.phi_off + lay.n_phi]
+            Y[r] = torch.cat([nu, pu, ph])
+            steps[r] = s[k]
+    return Y, steps
+
+
+def apply_prediction(ctx: Context, pred, rows_k: Sequence[int], lay: Layout):
+    """Write predicted densities of instances rows_k into ctx (currents 0,
+    electrolyte fields untouched) and re-solve Poisson from them."""
+    import torch
+    for k in rows_k:
+        y = pred[k]
+        for f, blk in ((F.FIELD_N, y[:lay.n_u]), (F.FIELD_P, y[lay.n_u:2 * lay.n_u])):
+            v = torch.zeros(lay.nd_carrier, dtype=torch.float64, device="cuda")
+            v[lay.u_off:lay.u_off + lay.n_u] = blk.exp()
+            ctx.set_state_device(f, k, v.data_ptr())
+    ctx.assemble_poisson_rhs()
+    ctx.solve_poisson()
+
+
+def warm_started_sweep(ctx: Context, op: Optional[NeuralOperator], thetas: np.ndarray, base: Params,
+                       max_steps=5000, tol=1e-8, check_every=50):
+    """One batch (ctx.n_inst rows of thetas) to steady state, warm-started by
+    ``op`` with the first-step-residual fallback.  Returns (steps incl. the
+    probe step, fallback flags, currents)."""
+    import torch
+    B = ctx.n_inst
+    assert thetas.shape[0] == B
+    lay = Layout.of(ctx)
+    ctx.set_instances([instance_params(t, base) for t in thetas])
+    fallback = np.ones(B, dtype=bool)
+    if op is None:
+        ctx.initialize()
+        steps, _ = ctx.run_to_steady_state(max_steps, tol, check_every)
+        return steps, fallback, ctx.interface_current()
+    X = torch.from_numpy(normalize(thetas)).cuda()
+    pred = op.predict(X)
+    # probe: one step from the standard initial condition ...
+    ctx.initialize()
+    _, rel_std = ctx.run_to_steady_state(1, 0.0, 1)
+    # ... and one step from the prediction
+    ctx.initialize()
+    apply_prediction(ctx, pred, range(B), lay)
+    _, rel_pred = ctx.run_to_steady_state(1, 0.0, 1)
+    use_pred = np.isfinite(rel_pred) & (rel_pred < rel_std)
+    fallback = ~use_pred
+    ctx.initialize()
+    apply_prediction(ctx, pred, [k for k in range(B) if use_pred[k]], lay)
+    steps, _ = ctx.run_to_steady_state(max_steps, tol, check_every)
+    return steps + 2, fallback, ctx.interface_current()
