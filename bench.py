@@ -59,6 +59,13 @@ def parse():
     ap.add_argument("--n-inst", type=int, default=1, help="instances per GPU per bench step")
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", choices=["full", "plain"], default="full",
+                    help="full: learned warm start + 64-instance batches (FP32-mixed) with the "
+                         "plain FP64 path measured beside it; plain: one configuration only")
+    ap.add_argument("--batch-inst", type=int, default=64)
+    ap.add_argument("--model", default=os.path.join(ROOT, "pecs_gb300", "models", "warmstart_r6.npz"))
+    ap.add_argument("--train-samples", type=int, default=256,
+                    help="training draws when no trained model file is present")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiler mode: initialise the workload, run this many time steps "
                          "with direct (non-graph) launches, print one line and exit")
@@ -241,6 +248,12 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "full" and not args.profile_steps:
+        return run_full(args)
+    return run_plain(args)
+
+
+def run_plain(args):
     import numpy as np
     import torch
 
@@ -356,6 +369,164 @@ def main():
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, steps_to_ss, args.cpu_sample_steps)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def plain_point(pg, refine, local):
+    """The plain FP64 single-instance path (config 2): one I-V point."""
+    ctx = pg.Context([pg.config2(n_refine=refine)], precision=pg.PREC_FP64, device=local)
+    ctx.initialize()
+    ctx.run_to_steady_state(MAX_STEPS, TOL, CHECK_EVERY)   # warm
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.initialize()
+    steps, _ = ctx.run_to_steady_state(MAX_STEPS, TOL, CHECK_EVERY)
+    e1.record(stream)
+    e1.synchronize()
+    return 1.0 / (e0.elapsed_time(e1) * 1e-3), int(steps[0]), ctx
+
+
+def run_full(args):
+    """Learned + batched: held-out I-V points in batches of args.batch_inst
+    instances (FP32-mixed), each warm-started by the neural operator with the
+    first-step fallback; the plain FP64 single-instance path measured beside."""
+    import numpy as np
+    import torch
+
+    import pecs_gb300 as pg
+    from pecs_gb300 import learned as L
+
+    world, rank, local = dist_init(args)
+    pg.build()
+    B = args.batch_inst
+    base = pg.config2(n_refine=args.refine)
+    # held-out draws (seed differs from the training seed), sharded by rank
+    n_batches = args.warmup + args.steps + 2
+    thetas = L.sample(B * n_batches * world, seed=777)[rank * B * n_batches:(rank + 1) * B * n_batches]
+    ctx = pg.Context([L.instance_params(t, base) for t in thetas[:B]], precision=pg.PREC_FP32_MIXED,
+                     device=local)
+    info = ctx.info()
+    trained_here = None
+    if os.path.exists(args.model):
+        op = L.NeuralOperator.load(args.model)
+    else:   # no committed model: train a small one now (untimed setup)
+        tr = L.sample(args.train_samples, seed=2026)
+        Y, _ = L.steady_states(ctx, tr, base)
+        op = L.NeuralOperator(rank=32, hidden=256, seed=0)
+        T = op.fit_basis(Y, L.Layout.of(ctx))
+        op.train(torch.from_numpy(L.normalize(tr)).cuda(), T, epochs=400, batch=64, lr=2e-3)
+        trained_here = args.train_samples
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    batches = [thetas[b * B:(b + 1) * B] for b in range(n_batches)]
+
+    def params_of(rows):
+        return [L.instance_params(t, base) for t in rows]
+
+    for b in range(args.warmup):
+        L.warm_started_sweep(ctx, op, batches[b], base)
+    # ---- timed: device-resident inputs (parameters uploaded before each batch) -----
+    ms, steps_all, fb_all, executed = 0.0, [], [], 0
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for b in range(args.warmup, args.warmup + args.steps):
+            ctx.set_instances(params_of(batches[b]))
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s_b, fb, cur = L.warm_started_sweep(ctx, op, batches[b], base, set_params=False)
+            e1.record(stream)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+            steps_all.extend(s_b.tolist())
+            fb_all.extend(fb.tolist())
+            executed += ctx.last_run_steps() + 2
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = max_over_ranks(ms, world)
+    points = B * args.steps * world
+    value = points / (ms * 1e-3)
+    clocks = clk.summary()
+    # ---- e2e: host parameters in, currents and fields out, through the public API ---
+    e2e_b = batches[args.warmup + args.steps]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s_e, fb_e, cur_e = L.warm_started_sweep(ctx, op, e2e_b, base)   # parameters host -> device
+    finals = {f: np.zeros(B * info.ndofs[f]) for f in range(5) if info.ndofs[f]}
+    for f, a in finals.items():
+        for i in range(B):
+            a[i * info.ndofs[f]:(i + 1) * info.ndofs[f]] = ctx.get_state(f, i)
+    e2e = B * world / max_over_ranks(time.perf_counter() - t0, world)
+    h2d = B * (sum(info.ndofs[f] for f in range(5)) * 8 + info.ndofs[4] * 8)   # constant RHS parts
+    d2h = B * 8 + sum(a.nbytes for a in finals.values())
+    # ---- accuracy: FP64 plain runs of a few instances of the e2e batch ------------
+    nchk = 4
+    ref = pg.Context(params_of(e2e_b[:nchk]), precision=pg.PREC_FP64, device=local)
+    ref.initialize()
+    ref.run_to_steady_state(MAX_STEPS, TOL, CHECK_EVERY)
+    cur_ref = ref.interface_current()
+    err_fields, err_cur = 0.0, 0.0
+    for i in range(nchk):
+        for f in ref.fields():
+            a = finals[f][i * info.ndofs[f]:(i + 1) * info.ndofs[f]]
+            r = ref.get_state(f, i)
+            err_fields = max(err_fields, float(np.linalg.norm(a - r) / np.linalg.norm(r)))
+        err_cur = max(err_cur, float(abs(cur_e[i] - cur_ref[i]) / abs(cur_ref[i])))
+    del ref
+    # ---- plain path (config 2, FP64, single instance) ---------------------------------
+    plain_value, plain_steps, pctx = plain_point(pg, args.refine, local)
+    pinfo = pctx.info()
+    solve_ms = pctx.time_solve(0, reps=30)
+    nlaunch = pinfo.solve_launches[0]
+    achieved = pinfo.solve_bytes[0] / (solve_ms * 1e-3) / 1e9
+    fast_ms = ctx.time_solve(0, reps=10)
+    fast_gbs = info.solve_bytes[0] / (fast_ms * 1e-3) / 1e9
+    peak, peak_kind = load_peaks()
+    del pctx
+    line = {
+        "metric": "I-V points/sec to steady state", "value": value, "unit": "I-V points/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 factors/quadrature + double-float refinement (learned+batched); "
+                                      "f64 plain",
+        "data": "synthetic",
+        "config": {"workload": f"learned+batched: {B} held-out I-V points per batch on the half cell "
+                               f"2x{2**args.refine}x{2**args.refine}, LDG k=1, RT0xDGQ0 Poisson, dt=1e-3, "
+                               f"warm-started, to rel. change <= {TOL} (<= {MAX_STEPS} steps)",
+                   "bench_step": f"one batch of {B} I-V points", "instances_per_gpu": B,
+                   "model": os.path.basename(args.model) if trained_here is None
+                   else f"trained in-run on {trained_here} draws",
+                   "l2": "flushed (512 MB write) before each timed batch"},
+        "plain": {"value": plain_value, "unit": "I-V points/s", "steps_to_steady_state": plain_steps,
+                  "workload": "config 2: one instance, FP64, standard initial condition"},
+        "speedup_vs_plain": value / plain_value,
+        "warm_start": {"median_steps": float(np.median(steps_all)), "fallback_rate": float(np.mean(fb_all)),
+                       "plain_steps": plain_steps},
+        "accuracy_vs_fp64": {"fields_rel_l2_max": err_fields, "current_rel_max": err_cur,
+                             "instances_checked": nchk},
+        "e2e": {"value": e2e, "unit": "I-V points/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": load_traffic(f"carrier_solve_r{args.refine}_fp64"),
+                     "kernel": "k_forward/k_backward carrier solve sweep, plain FP64 single instance",
+                     "solve_ms": solve_ms, "launches_per_sweep": nlaunch,
+                     "batched_fp32": {"solve_ms": fast_ms, "achieved_gbs": fast_gbs,
+                                      "frac": fast_gbs / peak, "rhs_per_sweep": 2 * B}},
+        "gpu_launches": executed * info.launches_per_step,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, plain_steps, args.cpu_sample_steps)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

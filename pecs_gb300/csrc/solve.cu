@@ -34,7 +34,10 @@ __device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
   const T* G = static_cast<const T*>(B.G) + B.goff[j];
   const int wo = B.w_off[j];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int rb = 0; rb < st.nrhs; rb += RB) {
+  {
+    // one chunk of RB right-hand sides per blockIdx.y
+    const int rb = blockIdx.y * RB;
+    if (rb >= st.nrhs) return;
     const int nr = min(RB, st.nrhs - rb);
     for (int p = threadIdx.x; p < s; p += blockDim.x) {
       const int gd = own[p];
@@ -47,31 +50,54 @@ __device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
       }
     }
     __syncthreads();
-    for (int row = r0 + warp; row < r1; row += nw) {
+    // warps per row: 1 (8 rows per item) .. 8 (1 row per item, columns split)
+    const int nrows = r1 - r0;
+    const int wpr = nrows <= 1 ? 8 : (nrows <= 2 ? 4 : (nrows <= 4 ? 2 : 1));
+    T* red = sm + (size_t)s * RB;  // nw x RB partial sums
+    for (int rbase = r0; rbase < r1; rbase += nw / wpr) {
+      const int row = rbase + warp / wpr, part = warp % wpr;
       T acc[RB];
 #pragma unroll
       for (int r = 0; r < RB; ++r) acc[r] = T(0);
-      const T* g = G + (long long)row * s;
-      for (int c = lane; c < s; c += 32) {
-        const T gv = __ldg(g + c);
+      if (row < r1) {
+        const T* g = G + (long long)row * s;
+        for (int c = part * 32 + lane; c < s; c += 32 * wpr) {
+          const T gv = __ldg(g + c);
 #pragma unroll
-        for (int r = 0; r < RB; ++r) acc[r] += gv * sm[c * RB + r];
+          for (int r = 0; r < RB; ++r) acc[r] += gv * sm[c * RB + r];
+        }
       }
 #pragma unroll
       for (int r = 0; r < RB; ++r) acc[r] = group_sum(acc[r], 32);
+      if (wpr > 1) {
+        if (lane == 0)
 #pragma unroll
-      for (int r = 0; r < RB; ++r) {
-        if (lane == r && r < nr) {
-          if (row < s) {
-            st.y[rb + r][own[row]] = (double)acc[r];
-          } else {
-            const int t = row - s;
-            double* w = st.w[rb + r];
-            const double cu = gather_updates(B, w, cptr[row], cptr[row + 1]);
-            w[wo + t] = cu + (double)acc[r];
+          for (int r = 0; r < RB; ++r) red[warp * RB + r] = acc[r];
+        __syncthreads();
+        if (part == 0)
+#pragma unroll
+          for (int r = 0; r < RB; ++r) {
+            T t = T(0);
+            for (int q = 0; q < wpr; ++q) t += red[(warp + q) * RB + r];
+            acc[r] = t;
+          }
+      }
+      if (part == 0 && row < r1) {
+#pragma unroll
+        for (int r = 0; r < RB; ++r) {
+          if (lane == r && r < nr) {
+            if (row < s) {
+              st.y[rb + r][own[row]] = (double)acc[r];
+            } else {
+              const int t = row - s;
+              double* w = st.w[rb + r];
+              const double cu = gather_updates(B, w, cptr[row], cptr[row + 1]);
+              w[wo + t] = cu + (double)acc[r];
+            }
           }
         }
       }
+      if (wpr > 1) __syncthreads();
     }
     __syncthreads();
   }
@@ -91,7 +117,10 @@ __device__ void fwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
   const T* G = static_cast<const T*>(B.G) + B.goff[j];
   const int wo = B.w_off[j];
   const int lane = threadIdx.x & 31;
-  for (int rb = 0; rb < st.nrhs; rb += RB) {
+  {
+    // one chunk of RB right-hand sides per blockIdx.y
+    const int rb = blockIdx.y * RB;
+    if (rb >= st.nrhs) return;
     const int nr = min(RB, st.nrhs - rb);
     for (int p = lane; p < s; p += 32) {
       const int gd = own[p];
@@ -143,7 +172,10 @@ __device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
   const int* upd = B.upd_idx + B.upd_off[j];
   const T* H = static_cast<const T*>(B.H) + B.hoff[j];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int rb = 0; rb < st.nrhs; rb += RB) {
+  {
+    // one chunk of RB right-hand sides per blockIdx.y
+    const int rb = blockIdx.y * RB;
+    if (rb >= st.nrhs) return;
     const int nr = min(RB, st.nrhs - rb);
     for (int p = threadIdx.x; p < f; p += blockDim.x) {
 #pragma unroll
@@ -154,21 +186,43 @@ __device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
       }
     }
     __syncthreads();
-    for (int row = r0 + warp; row < r1; row += nw) {
+    const int nrows = r1 - r0;
+    const int wpr = nrows <= 1 ? 8 : (nrows <= 2 ? 4 : (nrows <= 4 ? 2 : 1));
+    T* red = sm + (size_t)f * RB;
+    for (int rbase = r0; rbase < r1; rbase += nw / wpr) {
+      const int row = rbase + warp / wpr, part = warp % wpr;
       T acc[RB];
 #pragma unroll
       for (int r = 0; r < RB; ++r) acc[r] = T(0);
-      const T* h = H + (long long)row * f;
-      for (int c = lane; c < f; c += 32) {
-        const T hv = __ldg(h + c);
+      if (row < r1) {
+        const T* h = H + (long long)row * f;
+        for (int c = part * 32 + lane; c < f; c += 32 * wpr) {
+          const T hv = __ldg(h + c);
 #pragma unroll
-        for (int r = 0; r < RB; ++r) acc[r] += hv * sm[c * RB + r];
+          for (int r = 0; r < RB; ++r) acc[r] += hv * sm[c * RB + r];
+        }
       }
 #pragma unroll
       for (int r = 0; r < RB; ++r) acc[r] = group_sum(acc[r], 32);
+      if (wpr > 1) {
+        if (lane == 0)
 #pragma unroll
-      for (int r = 0; r < RB; ++r)
-        if (lane == r && r < nr) st.x[rb + r][own[row]] = (double)acc[r];
+          for (int r = 0; r < RB; ++r) red[warp * RB + r] = acc[r];
+        __syncthreads();
+        if (part == 0)
+#pragma unroll
+          for (int r = 0; r < RB; ++r) {
+            T t = T(0);
+            for (int q = 0; q < wpr; ++q) t += red[(warp + q) * RB + r];
+            acc[r] = t;
+          }
+      }
+      if (part == 0 && row < r1) {
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+          if (lane == r && r < nr) st.x[rb + r][own[row]] = (double)acc[r];
+      }
+      if (wpr > 1) __syncthreads();
     }
     __syncthreads();
   }
@@ -184,7 +238,10 @@ __device__ void bwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
   const int* upd = B.upd_idx + B.upd_off[j];
   const T* H = static_cast<const T*>(B.H) + B.hoff[j];
   const int lane = threadIdx.x & 31;
-  for (int rb = 0; rb < st.nrhs; rb += RB) {
+  {
+    // one chunk of RB right-hand sides per blockIdx.y
+    const int rb = blockIdx.y * RB;
+    if (rb >= st.nrhs) return;
     const int nr = min(RB, st.nrhs - rb);
     for (int p = lane; p < f; p += 32) {
 #pragma unroll
@@ -246,18 +303,19 @@ __global__ void __launch_bounds__(kSolveThreads)
 
 template <typename T, int RB>
 void launch_level(bool forward, const BankView& B, const SetsView& S, const LevelPlan& L,
-                  cudaStream_t st) {
+                  int max_nrhs, cudaStream_t st) {
   const int warps = kSolveThreads / 32;
   const int nblk = L.n_large + (L.n_thin + warps - 1) / warps;
   if (nblk == 0) return;
-  size_t sm_large = (size_t)L.max_cols * RB * sizeof(T);
+  size_t sm_large = ((size_t)L.max_cols + kSolveThreads / 32) * RB * sizeof(T);
   size_t sm_thin = L.n_thin ? (size_t)warps * kThinCols * RB * sizeof(T) : 0;
   size_t smem = std::max(sm_large, sm_thin);
+  const dim3 grid(nblk, (max_nrhs + RB - 1) / RB);
   if (forward)
-    k_forward<T, RB><<<nblk, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
+    k_forward<T, RB><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
                                                          L.n_thin);
   else
-    k_backward<T, RB><<<nblk, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
+    k_backward<T, RB><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
                                                           L.n_thin);
   PECS_CUDA(cudaGetLastError());
 }
@@ -272,12 +330,12 @@ void set_smem_limit(size_t bytes) {
 
 template <typename T>
 void launch_rb(int rb, bool forward, const BankView& B, const SetsView& S, const LevelPlan& L,
-               cudaStream_t st) {
+               int max_nrhs, cudaStream_t st) {
   switch (rb) {
-    case 1: launch_level<T, 1>(forward, B, S, L, st); break;
-    case 2: launch_level<T, 2>(forward, B, S, L, st); break;
-    case 4: launch_level<T, 4>(forward, B, S, L, st); break;
-    default: launch_level<T, 8>(forward, B, S, L, st); break;
+    case 1: launch_level<T, 1>(forward, B, S, L, max_nrhs, st); break;
+    case 2: launch_level<T, 2>(forward, B, S, L, max_nrhs, st); break;
+    case 4: launch_level<T, 4>(forward, B, S, L, max_nrhs, st); break;
+    default: launch_level<T, 8>(forward, B, S, L, max_nrhs, st); break;
   }
 }
 
@@ -442,10 +500,27 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
           for (int r0 = 0; r0 < rows; r0 += kThinRows)
             thin.push_back(make_int4(g, r0, std::min(rows, r0 + kThinRows), 0));
         } else {
-          for (int r0 = 0; r0 < rows; r0 += kWideRows)
-            items.push_back(make_int4(g, r0, std::min(rows, r0 + kWideRows), 0));
           max_cols = std::max(max_cols, cols);
         }
+      }
+      // wide nodes: 8 rows per CTA item (one per warp), fewer when the level
+      // would not give the GPU enough CTAs -- down to one row whose columns are
+      // split over the CTA's eight warps
+      long long wide_rows = 0;
+      for (int g : lv[l].nodes) {
+        const int s = hs[g], m = hm[g];
+        const int cols = forward ? s : s + m;
+        if (cols > kThinCols) wide_rows += forward ? s + m : s;
+      }
+      int per = kWideRows;
+      while (per > 1 && wide_rows / per < 2 * kTargetCtas) per /= 2;
+      for (int g : lv[l].nodes) {
+        const int s = hs[g], m = hm[g], f = s + m;
+        const int cols = forward ? s : f;
+        const int rows = forward ? f : s;
+        if (cols <= kThinCols) continue;
+        for (int r0 = 0; r0 < rows; r0 += per)
+          items.push_back(make_int4(g, r0, std::min(rows, r0 + per), 0));
       }
       out[l].n_large = (int)items.size();
       out[l].n_thin = (int)thin.size();
@@ -462,7 +537,8 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
   const size_t esz = prec_ == PECS_PREC_FP64 ? 8 : 4;
   const size_t small_need = (size_t)(kSolveThreads / 32) * kThinCols * esz;
   max_rb_ = 8;
-  while (max_rb_ > 1 && std::max((size_t)max_cols_, small_need / esz) * max_rb_ * esz > kSmemCap)
+  while (max_rb_ > 1 &&
+         std::max((size_t)max_cols_ + kSolveThreads / 32, small_need / esz) * max_rb_ * esz > kSmemCap)
     max_rb_ /= 2;
   if ((size_t)max_cols_ * esz > kSmemCap) throw PecsError(PECS_E_ARG, "front too large for shared memory");
   const size_t lim = kSmemCap;
@@ -485,15 +561,15 @@ void FactorBank::solve(const SetsView& sets, int max_nrhs, cudaStream_t st) cons
   rb = std::min(rb, max_rb_);
   for (const LevelPlan& L : fwd_) {
     if (prec_ == PECS_PREC_FP64)
-      launch_rb<double>(rb, true, B, sets, L, st);
+      launch_rb<double>(rb, true, B, sets, L, max_nrhs, st);
     else
-      launch_rb<float>(rb, true, B, sets, L, st);
+      launch_rb<float>(rb, true, B, sets, L, max_nrhs, st);
   }
   for (const LevelPlan& L : bwd_) {
     if (prec_ == PECS_PREC_FP64)
-      launch_rb<double>(rb, false, B, sets, L, st);
+      launch_rb<double>(rb, false, B, sets, L, max_nrhs, st);
     else
-      launch_rb<float>(rb, false, B, sets, L, st);
+      launch_rb<float>(rb, false, B, sets, L, max_nrhs, st);
   }
 }
 

@@ -23,6 +23,7 @@ constexpr int kMaxSets = 4;
 constexpr int kThinCols = 128;   // nodes with at most this many columns: thread per row
 constexpr int kThinRows = 32;    // rows per warp item of a thin node (one per lane)
 constexpr int kWideRows = 8;     // rows per CTA item of a wide node (one per warp)
+constexpr int kTargetCtas = 152; // SMs of a GB300: levels with fewer wide items split rows
 constexpr int kSolveThreads = 256;
 constexpr size_t kSmemCap = 200 * 1024;  // dynamic shared memory budget per CTA
 

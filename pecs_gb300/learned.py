@@ -152,6 +152,21 @@ class Mlp:
 class NeuralOperator:
     """MLP -> POD coefficients -> (log n, log p, Phi)."""
 
+    @staticmethod
+    def load(path: str) -> "NeuralOperator":
+        import torch
+        d = np.load(path)
+        widths = [int(w) for w in d["widths"]]
+        op = NeuralOperator(rank=int(d["rank"]), hidden=widths[1], layers=len(widths) - 2)
+        op.mlp.set_params(d["params"])
+        dev = "cuda"
+        op.mean = torch.from_numpy(d["mean"]).to(dev)
+        op.scale = torch.from_numpy(d["scale"]).to(dev)
+        op.basis = torch.from_numpy(d["basis"]).double().to(dev)
+        op.cscale = torch.from_numpy(d["cscale"]).to(dev)
+        op.refine = int(d["refine"])
+        return op
+
     def __init__(self, rank: int = 64, hidden: int = 512, layers: int = 3, seed: int = 0):
         self.rank = rank
         widths = [6] + [hidden] * layers + [rank]
@@ -278,15 +293,17 @@ def apply_prediction(ctx: Context, pred, rows_k: Sequence[int], lay: Layout):
 
 
 def warm_started_sweep(ctx: Context, op: Optional[NeuralOperator], thetas: np.ndarray, base: Params,
-                       max_steps=5000, tol=1e-8, check_every=50):
+                       max_steps=5000, tol=1e-8, check_every=50, set_params: bool = True):
     """One batch (ctx.n_inst rows of thetas) to steady state, warm-started by
     ``op`` with the first-step-residual fallback.  Returns (steps incl. the
-    probe step, fallback flags, currents)."""
+    probe steps, fallback flags, currents).  set_params=False assumes the
+    instances already carry these parameters."""
     import torch
     B = ctx.n_inst
     assert thetas.shape[0] == B
     lay = Layout.of(ctx)
-    ctx.set_instances([instance_params(t, base) for t in thetas])
+    if set_params:
+        ctx.set_instances([instance_params(t, base) for t in thetas])
     fallback = np.ones(B, dtype=bool)
     if op is None:
         ctx.initialize()
