@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--model", default=os.path.join(ROOT, "pecs_gb300", "models", "warmstart_r6.npz"))
     ap.add_argument("--train-samples", type=int, default=256,
                     help="training draws when no trained model file is present")
+    ap.add_argument("--steady", action="store_true",
+                    help="profiler mode: also run once to steady state and list the steps")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiler mode: initialise the workload, run this many time steps "
                          "with direct (non-graph) launches, print one line and exit")
@@ -267,11 +269,23 @@ def run_plain(args):
     info = ctx.info()
     if args.profile_steps:
         ctx.initialize()
+        ctx.step(3)
+        ctx.synchronize()
+        t0 = time.perf_counter()
         ctx.step(args.profile_steps)
         ctx.synchronize()
-        print(json.dumps({"profile_steps": args.profile_steps,
-                          "launches_per_step": info.launches_per_step,
-                          "launches_initialize": 1 + info.solve_launches[1]}))
+        ms_step = (time.perf_counter() - t0) * 1e3 / args.profile_steps
+        out = {"profile_steps": args.profile_steps, "n_inst": args.n_inst,
+               "precision": args.precision, "ms_per_time_step": ms_step,
+               "launches_per_step": info.launches_per_step,
+               "launches_initialize": 1 + info.solve_launches[1],
+               "carrier_sweep_ms": ctx.time_solve(0, reps=5),
+               "poisson_sweep_ms": ctx.time_solve(1, reps=5)}
+        if args.steady:
+            ctx.initialize()
+            steps, rel = ctx.run_to_steady_state(MAX_STEPS, TOL, CHECK_EVERY)
+            out["steady_steps"] = sorted(int(v) for v in steps)
+        print(json.dumps(out))
         return 0
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
