@@ -8,6 +8,31 @@ namespace pecs {
 
 namespace {
 
+// Loads RB consecutive staged values (16-byte aligned) with vector loads.
+template <typename T, int RB>
+__device__ __forceinline__ void load_rhs(const T* p, T (&v)[RB]) {
+  if constexpr (sizeof(T) == 4 && RB % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < RB / 4; ++q) {
+      const float4 t = reinterpret_cast<const float4*>(p)[q];
+      v[4 * q] = t.x;
+      v[4 * q + 1] = t.y;
+      v[4 * q + 2] = t.z;
+      v[4 * q + 3] = t.w;
+    }
+  } else if constexpr (sizeof(T) == 8 && RB % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < RB / 2; ++q) {
+      const double2 t = reinterpret_cast<const double2*>(p)[q];
+      v[2 * q] = t.x;
+      v[2 * q + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < RB; ++r) v[r] = p[r];
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ T group_sum(T v, int g) {
   // xor-butterfly inside aligned groups of g lanes (g a power of two <= 32)
@@ -46,7 +71,7 @@ __device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
         if (r < nr) v = st.b[rb + r][gd] - gather_updates(B, st.w[rb + r], c0, c1);
-        sm[p * RB + r] = (T)v;
+        sm[r * s + p] = (T)v;  // RHS-major: lanes of a warp read consecutive columns
       }
     }
     __syncthreads();
@@ -64,7 +89,7 @@ __device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
         for (int c = part * 32 + lane; c < s; c += 32 * wpr) {
           const T gv = __ldg(g + c);
 #pragma unroll
-          for (int r = 0; r < RB; ++r) acc[r] += gv * sm[c * RB + r];
+          for (int r = 0; r < RB; ++r) acc[r] += gv * sm[r * s + c];
         }
       }
 #pragma unroll
@@ -141,8 +166,10 @@ __device__ void fwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
 #pragma unroll 4
       for (int c = 0; c < s; ++c) {
         const T gv = __ldg(g + (long long)c * f);
+        T dv[RB];
+        load_rhs<T, RB>(sm + c * RB, dv);
 #pragma unroll
-        for (int r = 0; r < RB; ++r) acc[r] += gv * sm[c * RB + r];
+        for (int r = 0; r < RB; ++r) acc[r] += gv * dv[r];
       }
       if (row < s) {
 #pragma unroll
@@ -182,7 +209,7 @@ __device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
         if (r < nr) v = (p < s) ? st.y[rb + r][own[p]] : st.x[rb + r][upd[p - s]];
-        sm[p * RB + r] = (T)v;
+        sm[r * f + p] = (T)v;
       }
     }
     __syncthreads();
@@ -199,7 +226,7 @@ __device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
         for (int c = part * 32 + lane; c < f; c += 32 * wpr) {
           const T hv = __ldg(h + c);
 #pragma unroll
-          for (int r = 0; r < RB; ++r) acc[r] += hv * sm[c * RB + r];
+          for (int r = 0; r < RB; ++r) acc[r] += hv * sm[r * f + c];
         }
       }
 #pragma unroll
@@ -260,8 +287,10 @@ __device__ void bwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
 #pragma unroll 4
       for (int c = 0; c < f; ++c) {
         const T hv = __ldg(h + (long long)c * s);
+        T dv[RB];
+        load_rhs<T, RB>(sm + c * RB, dv);
 #pragma unroll
-        for (int r = 0; r < RB; ++r) acc[r] += hv * sm[c * RB + r];
+        for (int r = 0; r < RB; ++r) acc[r] += hv * dv[r];
       }
 #pragma unroll
       for (int r = 0; r < RB; ++r)
@@ -335,7 +364,8 @@ void launch_rb(int rb, bool forward, const BankView& B, const SetsView& S, const
     case 1: launch_level<T, 1>(forward, B, S, L, max_nrhs, st); break;
     case 2: launch_level<T, 2>(forward, B, S, L, max_nrhs, st); break;
     case 4: launch_level<T, 4>(forward, B, S, L, max_nrhs, st); break;
-    default: launch_level<T, 8>(forward, B, S, L, max_nrhs, st); break;
+    case 8: launch_level<T, 8>(forward, B, S, L, max_nrhs, st); break;
+    default: launch_level<T, 16>(forward, B, S, L, max_nrhs, st); break;
   }
 }
 
@@ -536,7 +566,7 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
   for (auto& l : bwd_) max_cols_ = std::max(max_cols_, l.max_cols);
   const size_t esz = prec_ == PECS_PREC_FP64 ? 8 : 4;
   const size_t small_need = (size_t)(kSolveThreads / 32) * kThinCols * esz;
-  max_rb_ = 8;
+  max_rb_ = 16;
   while (max_rb_ > 1 &&
          std::max((size_t)max_cols_ + kSolveThreads / 32, small_need / esz) * max_rb_ * esz > kSmemCap)
     max_rb_ /= 2;
@@ -547,17 +577,20 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
     set_smem_limit<double, 2>(lim);
     set_smem_limit<double, 4>(lim);
     set_smem_limit<double, 8>(lim);
+    set_smem_limit<double, 16>(lim);
   } else {
     set_smem_limit<float, 1>(lim);
     set_smem_limit<float, 2>(lim);
     set_smem_limit<float, 4>(lim);
     set_smem_limit<float, 8>(lim);
+    set_smem_limit<float, 16>(lim);
   }
 }
 
 void FactorBank::solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const {
   const BankView B = view();
-  int rb = max_nrhs <= 1 ? 1 : (max_nrhs <= 2 ? 2 : (max_nrhs <= 4 ? 4 : 8));
+  int rb = max_nrhs <= 1 ? 1 : (max_nrhs <= 2 ? 2 : (max_nrhs <= 4 ? 4 : (max_nrhs <= 8 ? 8 : 16)));
+  if (prec_ == PECS_PREC_FP64) rb = std::min(rb, 8);  // FP64: register budget
   rb = std::min(rb, max_rb_);
   for (const LevelPlan& L : fwd_) {
     if (prec_ == PECS_PREC_FP64)

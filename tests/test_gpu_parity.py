@@ -151,21 +151,35 @@ def test_mixed_precision_within_1e6_of_fp64_oracle(pecs_lib, iters):
 
 
 def test_mixed_precision_steady_state_and_current(pecs_lib):
-    """Steady states of the mixed mode vs FP64.  Both runs stop at a 1e-10
-    per-step change: at 1e-8 a run stops ~rel_change/(decay rate * dt) ~ 3e-6
-    short of the fixed point, which would swamp the precision error."""
+    """Fixed points of the mixed mode vs FP64.  Both march 6000 steps, past
+    the point where FP64 changes by < 1e-10 per step (a run stopped at a
+    1e-8 change sits ~rel_change/(decay rate * dt) ~ 3e-6 short of the fixed
+    point, and the mixed mode's FP32 terms leave a per-step noise floor
+    between 1e-10 and 1e-8, so stopping criteria cannot be compared)."""
     base = oracle.config2_params(n_refine=3)
     Ps = [base.copy(phi_app=v) for v in (-0.4, 0.0, 0.4)]
-    ctx = pg.Context([to_lib(P) for P in Ps], precision=pg.PREC_FP32_MIXED)
-    ctx.initialize()
-    steps, rel = ctx.run_to_steady_state(8000, 1e-10, check_every=50)
-    cur = ctx.interface_current()
-    ref = pg.Context([to_lib(P) for P in Ps])
-    ref.initialize()
-    steps64, _ = ref.run_to_steady_state(8000, 1e-10, check_every=50)
-    cur64 = ref.interface_current()
+    res = {}
+    for prec in (pg.PREC_FP32_MIXED, pg.PREC_FP64):
+        ctx = pg.Context([to_lib(P) for P in Ps], precision=prec)
+        ctx.initialize()
+        ctx.step(6000)
+        res[prec] = (ctx, ctx.interface_current())
+    (mx, cur), (ref, cur64) = res[pg.PREC_FP32_MIXED], res[pg.PREC_FP64]
     for i in range(len(Ps)):
-        assert abs(int(steps[i]) - int(steps64[i])) <= 0.05 * steps64[i] + 2
-        for f in ctx.fields():
-            assert rel_err(ctx.get_state(f, i), ref.get_state(f, i)) < 1e-6
+        for f in mx.fields():
+            assert rel_err(mx.get_state(f, i), ref.get_state(f, i)) < 1e-6
         assert abs(cur[i] - cur64[i]) <= 1e-6 * abs(cur64[i])
+
+
+def test_mixed_precision_converges_at_the_benchmark_criterion(pecs_lib):
+    """At the benchmark's 1e-8 criterion the mixed mode stops within a few
+    percent of the FP64 step count."""
+    base = oracle.config2_params(n_refine=3)
+    Ps = [base.copy(phi_app=v) for v in (-0.4, 0.0, 0.4)]
+    steps = {}
+    for prec in (pg.PREC_FP32_MIXED, pg.PREC_FP64):
+        ctx = pg.Context([to_lib(P) for P in Ps], precision=prec)
+        ctx.initialize()
+        steps[prec], _ = ctx.run_to_steady_state(5000, 1e-8, check_every=50)
+    for a, b in zip(steps[pg.PREC_FP32_MIXED], steps[pg.PREC_FP64]):
+        assert abs(int(a) - int(b)) <= 0.05 * int(b) + 2
