@@ -132,6 +132,87 @@ __global__ void k_residual_df(CsrDfSet M, const double* const* b, const float2* 
   out[v][i] = b[v][i] - ((double)sh + (double)sl);
 }
 
+// ---- interleaved [dof][rhs] buffers of the batched solves --------------------
+// dst[d * R + k] = src_k[d]   (32 x 32 tiles through shared memory)
+__global__ void k_gather_il(const double* const* __restrict__ src, double* __restrict__ dst, int n,
+                            int R) {
+  __shared__ double t[32][33];
+  const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k = k0 + kk, d = d0 + threadIdx.x;
+    t[kk][threadIdx.x] = (k < R && d < n) ? src[k][d] : 0.0;
+  }
+  __syncthreads();
+  for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
+    const int d = d0 + dd, k = k0 + threadIdx.x;
+    if (d < n && k < R) dst[(size_t)d * R + k] = t[threadIdx.x][dd];
+  }
+}
+
+// dst_k[d] = src[d * R + k]
+__global__ void k_scatter_il(const double* __restrict__ src, double* const* __restrict__ dst, int n,
+                             int R) {
+  __shared__ double t[32][33];
+  const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
+    const int d = d0 + dd, k = k0 + threadIdx.x;
+    t[dd][threadIdx.x] = (d < n && k < R) ? src[(size_t)d * R + k] : 0.0;
+  }
+  __syncthreads();
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k = k0 + kk, d = d0 + threadIdx.x;
+    if (k < R && d < n) dst[k][d] = t[threadIdx.x][kk];
+  }
+}
+
+__global__ void k_split_il(const double* __restrict__ x, float2* __restrict__ xs, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = x[i];
+  const float hi = __double2float_rn(a);
+  xs[i] = make_float2(hi, __double2float_rn(a - (double)hi));
+}
+
+__global__ void k_axpy_il(double* __restrict__ x, const double* __restrict__ d, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) x[i] += d[i];
+}
+
+// r = b - A x for R right-hand sides sharing A: one warp per row, lanes over
+// right-hand sides (matrix entries broadcast, vectors read contiguously);
+// FP32-pair products and sums as in k_residual_df.
+__global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const float2* __restrict__ xs,
+                                 double* __restrict__ r, int n, int R) {
+  const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int k = blockIdx.y * 32 + (threadIdx.x & 31);
+  if (row >= n || k >= R) return;
+  float sh = 0.f, sl = 0.f;
+  for (int p = A.rp[row]; p < A.rp[row + 1]; ++p) {
+    const float2 a = A.v[p], xv = xs[(size_t)A.ci[p] * R + k];
+    const float ph = a.x * xv.x;
+    const float pe = fmaf(a.x, xv.x, -ph) + fmaf(a.x, xv.y, a.y * xv.x);
+    const float t = sh + ph;
+    const float z = t - sh;
+    const float e = (sh - (t - z)) + (ph - z);
+    sh = t;
+    sl += e + pe;
+  }
+  const size_t o = (size_t)row * R + k;
+  r[o] = b[o] - ((double)sh + (double)sl);
+}
+
+// FP64 variant (FP32_IR mode)
+__global__ void k_residual_il(CsrDev A, const double* __restrict__ b, const double* __restrict__ x,
+                              double* __restrict__ r, int n, int R) {
+  const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int k = blockIdx.y * 32 + (threadIdx.x & 31);
+  if (row >= n || k >= R) return;
+  double acc = 0.0;
+  for (int p = A.rp[row]; p < A.rp[row + 1]; ++p) acc += A.v[p] * x[(size_t)A.ci[p] * R + k];
+  const size_t o = (size_t)row * R + k;
+  r[o] = b[o] - acc;
+}
+
 constexpr int kRedThreads = 256;
 constexpr int kRedChunks = 16;
 
@@ -319,8 +400,22 @@ struct Engine {
   int cur = 0;
   bool carriers_advanced = false;
   bool initialized = false;
-  // solve pointer tables: [nxt][0=main, 1=correction]
+  // solve pointer tables: [nxt][0=main, 1=correction] (kept for the timing entry)
   SetTable tab_c[2][2], tab_p[2][2];
+  // interleaved buffers of the batched solves, per bank (0 carriers, 1 Poisson) and set
+  struct IlSet {
+    int n = 0, R = 0, mat = 0;
+    DBuf<double> B, Y, W, X, Rr, D;
+    DBuf<float2> Xs;
+    DBuf<const double*> src;       // rhs vector of each column
+    DBuf<double*> dst[2];          // state vector of each column, per ping-pong target
+  };
+  struct IlBank {
+    int n_sets = 0;
+    IlSet set[kMaxSets];
+    int max_R = 0;
+  };
+  IlBank il[2];
   DBuf<double*> snap_ptrs;
   // steady state
   DBuf<double2> partial;
@@ -339,9 +434,10 @@ struct Engine {
   }
   int launches_per_step() const {
     const int it = ir_iters();
-    const int per_it = opt.precision == PECS_PREC_FP32_MIXED ? 3 : 2;
+    const int per_it = opt.precision == PECS_PREC_FP32_MIXED ? 3 : 2;  // (split,) residual, axpy
     const int lc = bank_c.kernel_launches_per_solve(), lp = bank_p.kernel_launches_per_solve();
-    return 1 + lc * (1 + it) + per_it * it + 1 + lp * (1 + it) + per_it * it + 3;
+    const int sc = il[0].n_sets, sp = il[1].n_sets;
+    return 1 + lc * (1 + it) + sc * (2 + per_it * it) + 1 + lp * (1 + it) + sp * (2 + per_it * it) + 3;
   }
   // algorithmic bytes of one application of a bank to all of its right-hand
   // sides: every stored factor entry once, plus the vectors (b read, y write +
@@ -363,10 +459,10 @@ struct Engine {
     PECS_CUDA(cudaEventCreate(&e0));
     PECS_CUDA(cudaEventCreate(&e1));
     const FactorBank& B = which == 0 ? bank_c : bank_p;
-    SetTable& t = which == 0 ? tab_c[nxt()][0] : tab_p[nxt()][0];
-    B.solve(t.view, t.max_nrhs, st);  // warm
+    const IlSetsView v = il_view(which, false);
+    B.solve(v, il[which].max_R, st);  // warm
     PECS_CUDA(cudaEventRecord(e0, st));
-    for (int r = 0; r < reps; ++r) B.solve(t.view, t.max_nrhs, st);
+    for (int r = 0; r < reps; ++r) B.solve(v, il[which].max_R, st);
     PECS_CUDA(cudaEventRecord(e1, st));
     PECS_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -434,6 +530,94 @@ struct Engine {
       tab.max_nrhs = std::max(tab.max_nrhs, (int)hb.size());
     }
     wcount = std::max(wcount, widx);
+  }
+
+  void build_il(int which, const std::vector<std::vector<int>>& set_fields, const FactorBank& bank) {
+    IlBank& I = il[which];
+    I.n_sets = (int)set_fields.size();
+    I.max_R = 0;
+    for (int si = 0; si < I.n_sets; ++si) {
+      IlSet& S_ = I.set[si];
+      const int f0 = set_fields[si][0];
+      S_.n = nd[f0];
+      S_.R = n_inst * (int)set_fields[si].size();
+      S_.mat = f0;
+      const size_t nR = (size_t)S_.n * S_.R;
+      S_.B.alloc(nR);
+      S_.Y.alloc(nR);
+      S_.X.alloc(nR);
+      S_.W.alloc((size_t)bank.set_wtotal(si) * S_.R);
+      S_.W.zero();
+      if (opt.precision != PECS_PREC_FP64) {
+        S_.Rr.alloc(nR);
+        S_.D.alloc(nR);
+        if (opt.precision == PECS_PREC_FP32_MIXED) S_.Xs.alloc(nR);
+      }
+      std::vector<const double*> src;
+      std::vector<double*> dst[2];
+      for (int i = 0; i < n_inst; ++i)
+        for (int f : set_fields[si]) {
+          src.push_back(rhs[f].p + (size_t)i * nd[f]);
+          for (int t = 0; t < 2; ++t) dst[t].push_back(state[t][f].p + (size_t)i * nd[f]);
+        }
+      S_.src.upload(src);
+      for (int t = 0; t < 2; ++t) S_.dst[t].upload(dst[t]);
+      I.max_R = std::max(I.max_R, S_.R);
+    }
+  }
+
+  IlSetsView il_view(int which, bool correction) {
+    IlSetsView v{};
+    IlBank& I = il[which];
+    for (int si = 0; si < I.n_sets; ++si) {
+      IlSet& S_ = I.set[si];
+      v.set[si] = correction ? IlSetView{S_.R, S_.Rr.p, S_.Y.p, S_.W.p, S_.D.p}
+                             : IlSetView{S_.R, S_.B.p, S_.Y.p, S_.W.p, S_.X.p};
+    }
+    return v;
+  }
+
+  // x = A^-1 b for every right-hand side of a bank, in the interleaved layout:
+  // gather the instance-major RHS vectors, sweep (+ refinement), scatter the
+  // solutions into state[target].
+  void solve_bank_il(const FactorBank& bank, int which, int target, cudaStream_t s) {
+    IlBank& I = il[which];
+    const dim3 tb(32, 8);
+    for (int si = 0; si < I.n_sets; ++si) {
+      IlSet& S_ = I.set[si];
+      k_gather_il<<<dim3((S_.n + 31) / 32, (S_.R + 31) / 32), tb, 0, s>>>(S_.src.p, S_.B.p, S_.n, S_.R);
+      PECS_CUDA(cudaGetLastError());
+    }
+    bank.solve(il_view(which, false), I.max_R, s);
+    const int iters = ir_iters();
+    for (int it = 0; it < iters; ++it) {
+      for (int si = 0; si < I.n_sets; ++si) {
+        IlSet& S_ = I.set[si];
+        const size_t nR = (size_t)S_.n * S_.R;
+        const dim3 rg((S_.n + 7) / 8, (S_.R + 31) / 32);
+        if (opt.precision == PECS_PREC_FP32_MIXED) {
+          k_split_il<<<(unsigned)((nR + 255) / 256), 256, 0, s>>>(S_.X.p, S_.Xs.p, nR);
+          PECS_CUDA(cudaGetLastError());
+          k_residual_df_il<<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.Xs.p, S_.Rr.p, S_.n, S_.R);
+        } else {
+          k_residual_il<<<rg, 256, 0, s>>>(csr.m[S_.mat], S_.B.p, S_.X.p, S_.Rr.p, S_.n, S_.R);
+        }
+        PECS_CUDA(cudaGetLastError());
+      }
+      bank.solve(il_view(which, true), I.max_R, s);
+      for (int si = 0; si < I.n_sets; ++si) {
+        IlSet& S_ = I.set[si];
+        const size_t nR = (size_t)S_.n * S_.R;
+        k_axpy_il<<<(unsigned)((nR + 255) / 256), 256, 0, s>>>(S_.X.p, S_.D.p, nR);
+        PECS_CUDA(cudaGetLastError());
+      }
+    }
+    for (int si = 0; si < I.n_sets; ++si) {
+      IlSet& S_ = I.set[si];
+      k_scatter_il<<<dim3((S_.n + 31) / 32, (S_.R + 31) / 32), tb, 0, s>>>(S_.X.p, S_.dst[target].p,
+                                                                           S_.n, S_.R);
+      PECS_CUDA(cudaGetLastError());
+    }
   }
 
   std::vector<std::vector<int>> carrier_set_fields() const {
@@ -569,6 +753,8 @@ struct Engine {
       build_sets({{4}}, bank_p, res, delta, wbuf_p, wp, tab_p[nx][1]);
     }
     prepare_ir();
+    build_il(0, csf, bank_c);
+    build_il(1, {{4}}, bank_p);
     // steady-state buffers
     partial.alloc((size_t)n_inst * 5 * kRedChunks);
     partial.zero();
@@ -845,7 +1031,7 @@ struct Engine {
 
   void stage_carrier_rhs(cudaStream_t s, const int* act) { launch_carrier_rhs(s, act); }
   void stage_solve_carriers(cudaStream_t s, const int* act) {
-    solve_bank(bank_c, tab_c, nxt(), 0, s, act);
+    solve_bank_il(bank_c, 0, nxt(), s);
     carriers_advanced = true;
   }
   void stage_poisson_rhs(cudaStream_t s, const int* act) {
@@ -853,7 +1039,7 @@ struct Engine {
   }
   void stage_solve_poisson(cudaStream_t s, const int* act) {
     const int target = carriers_advanced ? nxt() : cur;
-    solve_bank(bank_p, tab_p, target, 1, s, act);
+    solve_bank_il(bank_p, 1, target, s);
     if (carriers_advanced) {
       cur = nxt();
       carriers_advanced = false;

@@ -40,20 +40,52 @@ __device__ __forceinline__ T group_sum(T v, int g) {
   return v;
 }
 
+// Vector access for the two RHS layouts: an array of per-RHS vectors
+// (SetView) or one interleaved [dof][rhs] buffer per set (IlSetView).
+__device__ __forceinline__ double getb(const SetView& s, int r, int d) { return s.b[r][d]; }
+__device__ __forceinline__ double gety(const SetView& s, int r, int d) { return s.y[r][d]; }
+__device__ __forceinline__ double getx(const SetView& s, int r, int d) { return s.x[r][d]; }
+__device__ __forceinline__ double getw(const SetView& s, int r, int d) { return s.w[r][d]; }
+__device__ __forceinline__ void puty(const SetView& s, int r, int d, double v) { s.y[r][d] = v; }
+__device__ __forceinline__ void putx(const SetView& s, int r, int d, double v) { s.x[r][d] = v; }
+__device__ __forceinline__ void putw(const SetView& s, int r, int d, double v) { s.w[r][d] = v; }
+__device__ __forceinline__ double getb(const IlSetView& s, int r, int d) {
+  return s.b[(size_t)d * s.nrhs + r];
+}
+__device__ __forceinline__ double gety(const IlSetView& s, int r, int d) {
+  return s.y[(size_t)d * s.nrhs + r];
+}
+__device__ __forceinline__ double getx(const IlSetView& s, int r, int d) {
+  return s.x[(size_t)d * s.nrhs + r];
+}
+__device__ __forceinline__ double getw(const IlSetView& s, int r, int d) {
+  return s.w[(size_t)d * s.nrhs + r];
+}
+__device__ __forceinline__ void puty(const IlSetView& s, int r, int d, double v) {
+  s.y[(size_t)d * s.nrhs + r] = v;
+}
+__device__ __forceinline__ void putx(const IlSetView& s, int r, int d, double v) {
+  s.x[(size_t)d * s.nrhs + r] = v;
+}
+__device__ __forceinline__ void putw(const IlSetView& s, int r, int d, double v) {
+  s.w[(size_t)d * s.nrhs + r] = v;
+}
+
 // Sum of the children's update entries that land on front position p.
-__device__ __forceinline__ double gather_updates(const BankView& B, const double* __restrict__ w,
-                                                 int c0, int c1) {
+template <typename SVi>
+__device__ __forceinline__ double gather_updates(const BankView& B, const SVi& st, int r, int c0,
+                                                 int c1) {
   double v = 0.0;
-  for (int c = c0; c < c1; ++c) v += w[B.cmap_idx[c]];
+  for (int c = c0; c < c1; ++c) v += getw(st, r, B.cmap_idx[c]);
   return v;
 }
 
 // Forward sweep, large node: CTA computes rows [r0, r1) of Gf * d.
-template <typename T, int RB>
-__device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) {
+template <typename T, int RB, typename SV>
+__device__ void fwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
   const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j];
-  const SetView& st = S.set[B.node_set[j]];
+  const auto& st = S.set[B.node_set[j]];
   const int* own = B.own_idx + B.own_off[j];
   const int* cptr = B.cmap_ptr + B.cm_off[j];
   const T* G = static_cast<const T*>(B.G) + B.goff[j];
@@ -70,7 +102,7 @@ __device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
 #pragma unroll
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
-        if (r < nr) v = st.b[rb + r][gd] - gather_updates(B, st.w[rb + r], c0, c1);
+        if (r < nr) v = getb(st, rb + r, gd) - gather_updates(B, st, rb + r, c0, c1);
         sm[r * s + p] = (T)v;  // RHS-major: lanes of a warp read consecutive columns
       }
     }
@@ -112,12 +144,11 @@ __device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
         for (int r = 0; r < RB; ++r) {
           if (lane == r && r < nr) {
             if (row < s) {
-              st.y[rb + r][own[row]] = (double)acc[r];
+              puty(st, rb + r, own[row], (double)acc[r]);
             } else {
               const int t = row - s;
-              double* w = st.w[rb + r];
-              const double cu = gather_updates(B, w, cptr[row], cptr[row + 1]);
-              w[wo + t] = cu + (double)acc[r];
+              const double cu = gather_updates(B, st, rb + r, cptr[row], cptr[row + 1]);
+              putw(st, rb + r, wo + t, cu + (double)acc[r]);
             }
           }
         }
@@ -132,11 +163,11 @@ __device__ void fwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
 // column-major, so lane `row` reads Gf[c][row] for c = 0..s-1: consecutive
 // lanes read consecutive addresses and every lane has s independent loads in
 // flight; no cross-lane reduction.  A warp item covers rows [r0, r1).
-template <typename T, int RB>
-__device__ void fwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
+template <typename T, int RB, typename SV>
+__device__ void fwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
   const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j], m = B.m[j], f = s + m;
-  const SetView& st = S.set[B.node_set[j]];
+  const auto& st = S.set[B.node_set[j]];
   const int* own = B.own_idx + B.own_off[j];
   const int* cptr = B.cmap_ptr + B.cm_off[j];
   const T* G = static_cast<const T*>(B.G) + B.goff[j];
@@ -153,7 +184,7 @@ __device__ void fwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
 #pragma unroll
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
-        if (r < nr) v = st.b[rb + r][gd] - gather_updates(B, st.w[rb + r], c0, c1);
+        if (r < nr) v = getb(st, rb + r, gd) - gather_updates(B, st, rb + r, c0, c1);
         sm[p * RB + r] = (T)v;
       }
     }
@@ -174,15 +205,12 @@ __device__ void fwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
       if (row < s) {
 #pragma unroll
         for (int r = 0; r < RB; ++r)
-          if (r < nr) st.y[rb + r][own[row]] = (double)acc[r];
+          if (r < nr) puty(st, rb + r, own[row], (double)acc[r]);
       } else {
         const int c0 = cptr[row], c1 = cptr[row + 1];
 #pragma unroll
         for (int r = 0; r < RB; ++r)
-          if (r < nr) {
-            double* w = st.w[rb + r];
-            w[wo + row - s] = gather_updates(B, w, c0, c1) + (double)acc[r];
-          }
+          if (r < nr) putw(st, rb + r, wo + row - s, gather_updates(B, st, rb + r, c0, c1) + (double)acc[r]);
       }
     }
     __syncwarp();
@@ -190,11 +218,11 @@ __device__ void fwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
 }
 
 // Backward sweep, large node: rows [r0, r1) of Hb * [y_own ; x_upd].
-template <typename T, int RB>
-__device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) {
+template <typename T, int RB, typename SV>
+__device__ void bwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
   const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j], m = B.m[j], f = s + m;
-  const SetView& st = S.set[B.node_set[j]];
+  const auto& st = S.set[B.node_set[j]];
   const int* own = B.own_idx + B.own_off[j];
   const int* upd = B.upd_idx + B.upd_off[j];
   const T* H = static_cast<const T*>(B.H) + B.hoff[j];
@@ -208,7 +236,7 @@ __device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
 #pragma unroll
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
-        if (r < nr) v = (p < s) ? st.y[rb + r][own[p]] : st.x[rb + r][upd[p - s]];
+        if (r < nr) v = (p < s) ? gety(st, rb + r, own[p]) : getx(st, rb + r, upd[p - s]);
         sm[r * f + p] = (T)v;
       }
     }
@@ -247,7 +275,7 @@ __device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
       if (part == 0 && row < r1) {
 #pragma unroll
         for (int r = 0; r < RB; ++r)
-          if (lane == r && r < nr) st.x[rb + r][own[row]] = (double)acc[r];
+          if (lane == r && r < nr) putx(st, rb + r, own[row], (double)acc[r]);
       }
       if (wpr > 1) __syncthreads();
     }
@@ -256,11 +284,11 @@ __device__ void bwd_large(const BankView& B, const SetsView& S, int4 it, T* sm) 
 }
 
 // Backward sweep, thin node (s + m <= kThinCols): Hb stored column-major.
-template <typename T, int RB>
-__device__ void bwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
+template <typename T, int RB, typename SV>
+__device__ void bwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
   const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j], m = B.m[j], f = s + m;
-  const SetView& st = S.set[B.node_set[j]];
+  const auto& st = S.set[B.node_set[j]];
   const int* own = B.own_idx + B.own_off[j];
   const int* upd = B.upd_idx + B.upd_off[j];
   const T* H = static_cast<const T*>(B.H) + B.hoff[j];
@@ -274,7 +302,7 @@ __device__ void bwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
 #pragma unroll
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
-        if (r < nr) v = (p < s) ? st.y[rb + r][own[p]] : st.x[rb + r][upd[p - s]];
+        if (r < nr) v = (p < s) ? gety(st, rb + r, own[p]) : getx(st, rb + r, upd[p - s]);
         sm[p * RB + r] = (T)v;
       }
     }
@@ -294,44 +322,44 @@ __device__ void bwd_thin(const BankView& B, const SetsView& S, int4 it, T* sm) {
       }
 #pragma unroll
       for (int r = 0; r < RB; ++r)
-        if (r < nr) st.x[rb + r][own[row]] = (double)acc[r];
+        if (r < nr) putx(st, rb + r, own[row], (double)acc[r]);
     }
     __syncwarp();
   }
 }
 
-template <typename T, int RB>
+template <typename T, int RB, typename SV>
 __global__ void __launch_bounds__(kSolveThreads)
-    k_forward(BankView B, SetsView S, const int4* __restrict__ items, int n_large,
+    k_forward(BankView B, SV S, const int4* __restrict__ items, int n_large,
               const int4* __restrict__ thin, int n_thin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   if ((int)blockIdx.x < n_large) {
-    fwd_large<T, RB>(B, S, items[blockIdx.x], sm);
+    fwd_large<T, RB, SV>(B, S, items[blockIdx.x], sm);
   } else {
     const int wib = threadIdx.x >> 5;
     const int idx = ((int)blockIdx.x - n_large) * (kSolveThreads / 32) + wib;
-    if (idx < n_thin) fwd_thin<T, RB>(B, S, thin[idx], sm + wib * kThinCols * RB);
+    if (idx < n_thin) fwd_thin<T, RB, SV>(B, S, thin[idx], sm + wib * kThinCols * RB);
   }
 }
 
-template <typename T, int RB>
+template <typename T, int RB, typename SV>
 __global__ void __launch_bounds__(kSolveThreads)
-    k_backward(BankView B, SetsView S, const int4* __restrict__ items, int n_large,
+    k_backward(BankView B, SV S, const int4* __restrict__ items, int n_large,
                const int4* __restrict__ thin, int n_thin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   if ((int)blockIdx.x < n_large) {
-    bwd_large<T, RB>(B, S, items[blockIdx.x], sm);
+    bwd_large<T, RB, SV>(B, S, items[blockIdx.x], sm);
   } else {
     const int wib = threadIdx.x >> 5;
     const int idx = ((int)blockIdx.x - n_large) * (kSolveThreads / 32) + wib;
-    if (idx < n_thin) bwd_thin<T, RB>(B, S, thin[idx], sm + wib * kThinCols * RB);
+    if (idx < n_thin) bwd_thin<T, RB, SV>(B, S, thin[idx], sm + wib * kThinCols * RB);
   }
 }
 
-template <typename T, int RB>
-void launch_level(bool forward, const BankView& B, const SetsView& S, const LevelPlan& L,
+template <typename T, int RB, typename SV>
+void launch_level(bool forward, const BankView& B, const SV& S, const LevelPlan& L,
                   int max_nrhs, cudaStream_t st) {
   const int warps = kSolveThreads / 32;
   const int nblk = L.n_large + (L.n_thin + warps - 1) / warps;
@@ -341,31 +369,35 @@ void launch_level(bool forward, const BankView& B, const SetsView& S, const Leve
   size_t smem = std::max(sm_large, sm_thin);
   const dim3 grid(nblk, (max_nrhs + RB - 1) / RB);
   if (forward)
-    k_forward<T, RB><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
-                                                         L.n_thin);
+    k_forward<T, RB, SV><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
+                                                             L.n_thin);
   else
-    k_backward<T, RB><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
-                                                          L.n_thin);
+    k_backward<T, RB, SV><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
+                                                              L.n_thin);
   PECS_CUDA(cudaGetLastError());
 }
 
 template <typename T, int RB>
 void set_smem_limit(size_t bytes) {
-  PECS_CUDA(cudaFuncSetAttribute(k_forward<T, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)bytes));
-  PECS_CUDA(cudaFuncSetAttribute(k_backward<T, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)bytes));
+  PECS_CUDA(cudaFuncSetAttribute(k_forward<T, RB, SetsView>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  PECS_CUDA(cudaFuncSetAttribute(k_backward<T, RB, SetsView>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  PECS_CUDA(cudaFuncSetAttribute(k_forward<T, RB, IlSetsView>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  PECS_CUDA(cudaFuncSetAttribute(k_backward<T, RB, IlSetsView>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
 }
 
-template <typename T>
-void launch_rb(int rb, bool forward, const BankView& B, const SetsView& S, const LevelPlan& L,
+template <typename T, typename SV>
+void launch_rb(int rb, bool forward, const BankView& B, const SV& S, const LevelPlan& L,
                int max_nrhs, cudaStream_t st) {
   switch (rb) {
-    case 1: launch_level<T, 1>(forward, B, S, L, max_nrhs, st); break;
-    case 2: launch_level<T, 2>(forward, B, S, L, max_nrhs, st); break;
-    case 4: launch_level<T, 4>(forward, B, S, L, max_nrhs, st); break;
-    case 8: launch_level<T, 8>(forward, B, S, L, max_nrhs, st); break;
-    default: launch_level<T, 16>(forward, B, S, L, max_nrhs, st); break;
+    case 1: launch_level<T, 1, SV>(forward, B, S, L, max_nrhs, st); break;
+    case 2: launch_level<T, 2, SV>(forward, B, S, L, max_nrhs, st); break;
+    case 4: launch_level<T, 4, SV>(forward, B, S, L, max_nrhs, st); break;
+    case 8: launch_level<T, 8, SV>(forward, B, S, L, max_nrhs, st); break;
+    default: launch_level<T, 16, SV>(forward, B, S, L, max_nrhs, st); break;
   }
 }
 
@@ -587,23 +619,32 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
   }
 }
 
-void FactorBank::solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const {
+template <typename SV>
+void FactorBank::solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const {
   const BankView B = view();
   int rb = max_nrhs <= 1 ? 1 : (max_nrhs <= 2 ? 2 : (max_nrhs <= 4 ? 4 : (max_nrhs <= 8 ? 8 : 16)));
   if (prec_ == PECS_PREC_FP64) rb = std::min(rb, 8);  // FP64: register budget
   rb = std::min(rb, max_rb_);
   for (const LevelPlan& L : fwd_) {
     if (prec_ == PECS_PREC_FP64)
-      launch_rb<double>(rb, true, B, sets, L, max_nrhs, st);
+      launch_rb<double, SV>(rb, true, B, sets, L, max_nrhs, st);
     else
-      launch_rb<float>(rb, true, B, sets, L, max_nrhs, st);
+      launch_rb<float, SV>(rb, true, B, sets, L, max_nrhs, st);
   }
   for (const LevelPlan& L : bwd_) {
     if (prec_ == PECS_PREC_FP64)
-      launch_rb<double>(rb, false, B, sets, L, max_nrhs, st);
+      launch_rb<double, SV>(rb, false, B, sets, L, max_nrhs, st);
     else
-      launch_rb<float>(rb, false, B, sets, L, max_nrhs, st);
+      launch_rb<float, SV>(rb, false, B, sets, L, max_nrhs, st);
   }
+}
+
+void FactorBank::solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const {
+  solve_impl(sets, max_nrhs, st);
+}
+
+void FactorBank::solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const {
+  solve_impl(sets, max_nrhs, st);
 }
 
 }  // namespace pecs

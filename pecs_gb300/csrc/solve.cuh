@@ -57,6 +57,20 @@ struct SetsView {
   SetView set[kMaxSets];
 };
 
+// Interleaved layout: all right-hand sides of a set in one buffer, element
+// (dof d, rhs r) at d * nrhs + r, so a dof's values are contiguous.
+struct IlSetView {
+  int nrhs;
+  const double* b;
+  double* y;
+  double* w;  // update vectors, set_wtotal(set) x nrhs
+  double* x;
+};
+
+struct IlSetsView {
+  IlSetView set[kMaxSets];
+};
+
 struct LevelPlan {
   int n_large = 0, n_thin = 0;
   DBuf<int4> items;   // wide nodes: (node, row0, row1, 0), one CTA each
@@ -70,6 +84,7 @@ class FactorBank {
   void build(const std::vector<const MfFactor*>& factors, int precision);
   // y = forward(b), x = backward(y); w is workspace.  All sets must be bound.
   void solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const;
+  void solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const;
   int set_wtotal(int set) const { return set_wtotal_[set]; }
   int precision() const { return prec_; }
   long long entries() const { return entries_; }
@@ -91,6 +106,8 @@ class FactorBank {
   std::vector<LevelPlan> fwd_, bwd_;
   int max_cols_ = 0, max_rb_ = 8;
   BankView view() const;
+  template <typename SV>
+  void solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const;
 };
 
 }  // namespace pecs
