@@ -689,8 +689,11 @@ struct Engine {
     for (int t = 0; t < n_fs; ++t) cf.push_back(&fs[t]);
     for (int t = 0; t < n_fe; ++t) cf.push_back(&fe[t]);
     const int fprec = opt.precision == PECS_PREC_FP64 ? PECS_PREC_FP64 : PECS_PREC_FP32_IR;
-    bank_c.build(cf, fprec);
-    bank_p.build({&fp}, fprec);
+    // many right-hand sides per set: panel kernels (lanes over right-hand sides)
+    int min_rc = 1 << 30;
+    for (auto& f : carrier_set_fields()) min_rc = std::min(min_rc, n_inst * (int)f.size());
+    bank_c.build(cf, fprec, min_rc >= kPanelMinRhs);
+    bank_p.build({&fp}, fprec, n_inst >= kPanelMinRhs);
     // free host copies of the factor values (structure is kept for stats)
     for (auto* F : {&fs[0], &fs[1], &fe[0], &fe[1], &fp}) {
       std::vector<std::vector<double>>().swap(F->Gf);

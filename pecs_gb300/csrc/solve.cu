@@ -401,6 +401,246 @@ void launch_rb(int rb, bool forward, const BankView& B, const SV& S, const Level
   }
 }
 
+
+// ---- panel path --------------------------------------------------------------
+constexpr int kPanelKcF32 = 128;  // staged columns per chunk, FP32 blocks
+constexpr int kPanelKcF64 = 64;   // staged columns per chunk, FP64 blocks
+constexpr size_t kPanelSmem = 100 * 1024;
+
+// RPL consecutive doubles of one interleaved row (offset a multiple of RPL).
+template <int RPL>
+__device__ __forceinline__ void ld_rhs(const double* p, double (&v)[RPL]) {
+  if constexpr (RPL == 1) {
+    v[0] = p[0];
+  } else {
+#pragma unroll
+    for (int q = 0; q < RPL / 2; ++q) {
+      const double2 t = reinterpret_cast<const double2*>(p)[q];
+      v[2 * q] = t.x;
+      v[2 * q + 1] = t.y;
+    }
+  }
+}
+
+template <int RPL>
+__device__ __forceinline__ void st_rhs(double* p, const double (&v)[RPL]) {
+  if constexpr (RPL == 1) {
+    p[0] = v[0];
+  } else {
+#pragma unroll
+    for (int q = 0; q < RPL / 2; ++q)
+      reinterpret_cast<double2*>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+  }
+}
+
+// n consecutive shared-memory values (16-byte aligned when n * sizeof(T) >= 16).
+template <typename T, int N>
+__device__ __forceinline__ void lds(const T* p, T (&v)[N]) {
+  if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < N / 4; ++q) {
+      const float4 t = reinterpret_cast<const float4*>(p)[q];
+      v[4 * q] = t.x;
+      v[4 * q + 1] = t.y;
+      v[4 * q + 2] = t.z;
+      v[4 * q + 3] = t.w;
+    }
+  } else if constexpr (sizeof(T) == 8 && N % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < N / 2; ++q) {
+      const double2 t = reinterpret_cast<const double2*>(p)[q];
+      v[2 * q] = t.x;
+      v[2 * q + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < N; ++q) v[q] = p[q];
+  }
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void sts(T* p, const double (&v)[N]) {
+  if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < N / 4; ++q)
+      reinterpret_cast<float4*>(p)[q] =
+          make_float4((float)v[4 * q], (float)v[4 * q + 1], (float)v[4 * q + 2], (float)v[4 * q + 3]);
+  } else if constexpr (sizeof(T) == 8 && N % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < N / 2; ++q)
+      reinterpret_cast<double2*>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < N; ++q) p[q] = (T)v[q];
+  }
+}
+
+// One item = rows [r0, r1) of one node's block (Gf for the forward sweep, Hb
+// for the backward sweep; both column-major with leading dimension = row
+// count), applied to the right-hand-side chunk blockIdx.y (32 * RPL RHS).
+// Rows are tiled ri at a time (ri in {4, 8, 16, 32}): warp (g, part) owns rows
+// 4g..4g+3 of the tile and the chunk columns k = part (mod 32 / ri); partial
+// sums of the column parts are added through shared memory.
+template <typename T, int RPL, bool FWD>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_panel(BankView B, IlSetsView S, const int4* __restrict__ items, int kc_cap, int ds_rows) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int RC = 32 * RPL;
+  const int4 it = items[blockIdx.x];
+  const int j = it.x, r0 = it.y, r1 = it.z, ri = it.w;
+  const int s = B.s[j], m = B.m[j], f = s + m;
+  const IlSetView st = S.set[B.node_set[j]];
+  const int R = st.nrhs;
+  const int rc0 = blockIdx.y * RC;
+  if (rc0 >= R) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rl = rc0 + lane * RPL;  // first right-hand side of this lane
+  const bool lane_ok = rl < R;      // R is a multiple of RPL
+  const int K = FWD ? s : f;
+  const int ld = FWD ? f : s;
+  const T* M = FWD ? static_cast<const T*>(B.G) + B.goff[j] : static_cast<const T*>(B.H) + B.hoff[j];
+  const int* own = B.own_idx + B.own_off[j];
+  const int* upd = B.upd_idx + B.upd_off[j];
+  const int* cptr = B.cmap_ptr + B.cm_off[j];
+  const int nrows = r1 - r0;
+  const int wpr = 32 / ri;  // warps sharing a row group (column parts)
+  const int g = warp / wpr, part = warp % wpr;
+  T* Ds = reinterpret_cast<T*>(smem_raw);   // [ds_rows][RC], ds_rows >= 32 when ri < 32
+  T* Gs = Ds + (size_t)ds_rows * RC;         // [kc_cap][ri]
+  T acc[4][RPL];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int q = 0; q < RPL; ++q) acc[i][q] = T(0);
+  for (int k0 = 0; k0 < K; k0 += kc_cap) {
+    const int kc = min(kc_cap, K - k0);
+    for (int k = warp; k < kc; k += kSolveThreads / 32) {
+      const int p = k0 + k;
+      double v[RPL];
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) v[q] = 0.0;
+      if (lane_ok) {
+        if (FWD) {
+          ld_rhs<RPL>(st.b + (size_t)own[p] * R + rl, v);
+          for (int c = cptr[p]; c < cptr[p + 1]; ++c) {
+            double u[RPL];
+            ld_rhs<RPL>(st.w + (size_t)B.cmap_idx[c] * R + rl, u);
+#pragma unroll
+            for (int q = 0; q < RPL; ++q) v[q] -= u[q];
+          }
+        } else {
+          const double* src = p < s ? st.y + (size_t)own[p] * R : st.x + (size_t)upd[p - s] * R;
+          ld_rhs<RPL>(src + rl, v);
+        }
+      }
+      sts<T, RPL>(Ds + (size_t)k * RC + lane * RPL, v);
+    }
+    for (int idx = threadIdx.x; idx < kc * ri; idx += kSolveThreads) {
+      const int k = idx / ri, i = idx - k * ri;
+      Gs[idx] = i < nrows ? __ldg(M + (size_t)(k0 + k) * ld + r0 + i) : T(0);
+    }
+    __syncthreads();
+    for (int k = part; k < kc; k += wpr) {
+      T gv[4], dv[RPL];
+      lds<T, 4>(Gs + k * ri + 4 * g, gv);
+      lds<T, RPL>(Ds + (size_t)k * RC + lane * RPL, dv);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) acc[i][q] += gv[i] * dv[q];
+    }
+    __syncthreads();
+  }
+  // row i of the item -> its destination
+  auto emit = [&](int i, double (&v)[RPL]) {
+    const int row = r0 + i;
+    if (FWD) {
+      if (row < s) {
+        st_rhs<RPL>(st.y + (size_t)own[row] * R + rl, v);
+      } else {
+        for (int c = cptr[row]; c < cptr[row + 1]; ++c) {
+          double u[RPL];
+          ld_rhs<RPL>(st.w + (size_t)B.cmap_idx[c] * R + rl, u);
+#pragma unroll
+          for (int q = 0; q < RPL; ++q) v[q] += u[q];
+        }
+        st_rhs<RPL>(st.w + (size_t)(B.w_off[j] + row - s) * R + rl, v);
+      }
+    } else {
+      st_rhs<RPL>(st.x + (size_t)own[row] * R + rl, v);
+    }
+  };
+  if (wpr == 1) {
+    if (!lane_ok) return;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (4 * g + i < nrows) {
+        double v[RPL];
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) v[q] = (double)acc[i][q];
+        emit(4 * g + i, v);
+      }
+    }
+  } else {
+    T* red = Ds;  // [wpr][ri][RC] = 32 * RC values
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int q = 0; q < RPL; ++q)
+        red[((size_t)part * ri + 4 * g + i) * RC + lane * RPL + q] = acc[i][q];
+    __syncthreads();
+    if (!lane_ok) return;
+    for (int i = warp; i < nrows; i += kSolveThreads / 32) {
+      double v[RPL];
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) {
+        T t = T(0);
+        for (int p = 0; p < wpr; ++p) t += red[((size_t)p * ri + i) * RC + lane * RPL + q];
+        v[q] = (double)t;
+      }
+      emit(i, v);
+    }
+  }
+}
+
+template <typename T, int RPL>
+void launch_panel(bool forward, const BankView& B, const IlSetsView& S, const PanelPlan& L,
+                  int max_nrhs, cudaStream_t st) {
+  if (L.n_items == 0) return;
+  const int kcap = sizeof(T) == 4 ? kPanelKcF32 : kPanelKcF64;
+  const int kc = std::min(kcap, std::max(1, L.max_k));
+  constexpr int RC = 32 * RPL;
+  const int ds_rows = L.min_ri < 32 ? std::max(kc, 32) : kc;
+  const size_t smem = ((size_t)ds_rows * RC + (size_t)kc * L.max_ri) * sizeof(T);
+  const dim3 grid(L.n_items, (max_nrhs + RC - 1) / RC);
+  if (forward)
+    k_panel<T, RPL, true><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, kc, ds_rows);
+  else
+    k_panel<T, RPL, false><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, kc, ds_rows);
+  PECS_CUDA(cudaGetLastError());
+}
+
+template <typename T>
+void set_panel_smem_limit() {
+  const int lim = (int)kPanelSmem;
+  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+}
+
+template <typename T>
+void launch_panel_rpl(int rpl, bool forward, const BankView& B, const IlSetsView& S,
+                      const PanelPlan& L, int max_nrhs, cudaStream_t st) {
+  switch (rpl) {
+    case 1: launch_panel<T, 1>(forward, B, S, L, max_nrhs, st); break;
+    case 2: launch_panel<T, 2>(forward, B, S, L, max_nrhs, st); break;
+    default: launch_panel<T, 4>(forward, B, S, L, max_nrhs, st); break;
+  }
+}
+
 }  // namespace
 
 BankView FactorBank::view() const {
@@ -425,15 +665,18 @@ BankView FactorBank::view() const {
 
 int FactorBank::kernel_launches_per_solve() const {
   int n = 0;
+  for (auto& l : pfwd_) n += l.n_items > 0;
+  for (auto& l : pbwd_) n += l.n_items > 0;
   for (auto& l : fwd_) n += (l.n_large + l.n_thin) > 0;
   for (auto& l : bwd_) n += (l.n_large + l.n_thin) > 0;
   return n;
 }
 
-void FactorBank::build(const std::vector<const MfFactor*>& factors, int precision) {
+void FactorBank::build(const std::vector<const MfFactor*>& factors, int precision, bool panel) {
   if (factors.empty() || (int)factors.size() > kMaxSets)
     throw PecsError(PECS_E_ARG, "factor bank needs 1..4 factors");
   prec_ = precision;
+  panel_ = panel;
   n_sets_ = (int)factors.size();
   std::vector<int> hs, hm, own_off, upd_off, w_off, cm_off, own_idx, upd_idx, cmap_ptr, cmap_idx,
       node_set;
@@ -477,14 +720,14 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
         // application; wide blocks row-major for warp-per-row application
         const int s_ = nd.s, f_ = nd.s + nd.m;
         const std::vector<double>& g = F.Gf[j];  // f_ x s_ row-major
-        if (s_ <= kThinCols) {
+        if (panel || s_ <= kThinCols) {
           for (int c = 0; c < s_; ++c)
             for (int r = 0; r < f_; ++r) G.push_back(g[(size_t)r * s_ + c]);
         } else {
           G.insert(G.end(), g.begin(), g.end());
         }
         const std::vector<double>& h = F.Hb[j];  // s_ x f_ row-major
-        if (f_ <= kThinCols) {
+        if (panel || f_ <= kThinCols) {
           for (int c = 0; c < f_; ++c)
             for (int r = 0; r < s_; ++r) H.push_back(h[(size_t)r * f_ + c]);
         } else {
@@ -591,6 +834,55 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
       out[l].thin.upload(thin);
     }
   };
+  if (panel) {
+    // panel items: a node's rows in tiles of ri <= 32 rows; levels that would
+    // not fill the GPU use shorter tiles (more CTAs, column parts per warp)
+    auto make_panel = [&](const std::vector<LevelNodes>& lv, bool forward, std::vector<PanelPlan>& out) {
+      out.clear();
+      out.resize(lv.size());
+      for (size_t l = 0; l < lv.size(); ++l) {
+        int cap = 32;
+        auto count = [&](int c) {
+          long long n = 0;
+          for (int g : lv[l].nodes) {
+            const int rows = forward ? hs[g] + hm[g] : hs[g];
+            n += (rows + c - 1) / c;
+          }
+          return n;
+        };
+        while (cap > 4 && count(cap) < 2 * kTargetCtas) cap /= 2;
+        std::vector<int4> items;
+        int max_k = 0, max_ri = 4, min_ri = 32;
+        for (int g : lv[l].nodes) {
+          const int s = hs[g], m = hm[g];
+          const int rows = forward ? s + m : s;
+          max_k = std::max(max_k, forward ? s : s + m);
+          const int nit = (rows + cap - 1) / cap;
+          const int per = (rows + nit - 1) / nit;
+          int ri = 4;
+          while (ri < per) ri *= 2;
+          max_ri = std::max(max_ri, ri);
+          min_ri = std::min(min_ri, ri);
+          for (int r0 = 0; r0 < rows; r0 += per)
+            items.push_back(make_int4(g, r0, std::min(rows, r0 + per), ri));
+        }
+        out[l].n_items = (int)items.size();
+        out[l].max_k = max_k;
+        out[l].max_ri = max_ri;
+        out[l].min_ri = min_ri;
+        out[l].items.upload(items);
+      }
+    };
+    make_panel(fl, true, pfwd_);
+    make_panel(bl, false, pbwd_);
+    fwd_.clear();
+    bwd_.clear();
+    if (prec_ == PECS_PREC_FP64)
+      set_panel_smem_limit<double>();
+    else
+      set_panel_smem_limit<float>();
+    return;
+  }
   make(fl, true, fwd_);
   make(bl, false, bwd_);
   max_cols_ = 0;
@@ -640,11 +932,35 @@ void FactorBank::solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const
 }
 
 void FactorBank::solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const {
+  if (panel_) throw PecsError(PECS_E_STATE, "panel factor bank needs the interleaved layout");
   solve_impl(sets, max_nrhs, st);
 }
 
 void FactorBank::solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const {
-  solve_impl(sets, max_nrhs, st);
+  if (panel_)
+    solve_panel(sets, max_nrhs, st);
+  else
+    solve_impl(sets, max_nrhs, st);
+}
+
+void FactorBank::solve_panel(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const {
+  // right-hand sides per lane: as many as fill the lanes, dividing every set's count
+  int rpl = max_nrhs >= 96 ? 4 : (max_nrhs >= 48 ? 2 : 1);
+  for (int si = 0; si < n_sets_; ++si)
+    while (rpl > 1 && sets.set[si].nrhs % rpl != 0) rpl /= 2;
+  const BankView B = view();
+  for (const PanelPlan& L : pfwd_) {
+    if (prec_ == PECS_PREC_FP64)
+      launch_panel_rpl<double>(rpl, true, B, sets, L, max_nrhs, st);
+    else
+      launch_panel_rpl<float>(rpl, true, B, sets, L, max_nrhs, st);
+  }
+  for (const PanelPlan& L : pbwd_) {
+    if (prec_ == PECS_PREC_FP64)
+      launch_panel_rpl<double>(rpl, false, B, sets, L, max_nrhs, st);
+    else
+      launch_panel_rpl<float>(rpl, false, B, sets, L, max_nrhs, st);
+  }
 }
 
 }  // namespace pecs

@@ -8,7 +8,12 @@
 // the bank: wide nodes are split into row chunks handled by a CTA each
 // (warp per row, coalesced row-major reads, warp-shuffle reduction); thin
 // nodes (few columns) are stored column-major and applied thread-per-row,
-// in warp-sized row chunks.
+// in warp-sized row chunks.  A bank built for many right-hand sides per set
+// ("panel" banks) stores every block column-major and applies each node as a
+// small dense GEMM: a CTA stages a chunk of columns of the right-hand sides
+// (interleaved layout: a dof's values are contiguous) and of the block in
+// shared memory, each warp accumulates a 4-row x (32 * RPL)-RHS register tile
+// with lanes over right-hand sides, so every global access is coalesced.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -26,6 +31,7 @@ constexpr int kWideRows = 8;     // rows per CTA item of a wide node (one per wa
 constexpr int kTargetCtas = 152; // SMs of a GB300: levels with fewer wide items split rows
 constexpr int kSolveThreads = 256;
 constexpr size_t kSmemCap = 200 * 1024;  // dynamic shared memory budget per CTA
+constexpr int kPanelMinRhs = 32;  // right-hand sides per set from which banks use the panel kernels
 
 struct BankView {  // device pointers, passed by value to kernels
   const int* s;
@@ -71,6 +77,17 @@ struct IlSetsView {
   IlSetView set[kMaxSets];
 };
 
+// One level of the panel path: items (node, row0, row1, rows per tile), one
+// CTA each; every item applies its rows of the node's block to a chunk of
+// right-hand sides held in shared memory, lanes over right-hand sides.
+struct PanelPlan {
+  int n_items = 0;
+  DBuf<int4> items;
+  int max_k = 0;   // largest column count of the level's nodes
+  int max_ri = 0;  // largest rows-per-tile of the level's items
+  int min_ri = 32; // smallest rows-per-tile (< 32: column parts reduce in shared memory)
+};
+
 struct LevelPlan {
   int n_large = 0, n_thin = 0;
   DBuf<int4> items;   // wide nodes: (node, row0, row1, 0), one CTA each
@@ -81,7 +98,9 @@ struct LevelPlan {
 class FactorBank {
  public:
   // factors[i] is bound to RHS set i.  precision: PECS_PREC_FP64 or FP32_IR.
-  void build(const std::vector<const MfFactor*>& factors, int precision);
+  // panel: store every block column-major and apply it with the panel
+  // kernels (many right-hand sides per set, interleaved layout only).
+  void build(const std::vector<const MfFactor*>& factors, int precision, bool panel = false);
   // y = forward(b), x = backward(y); w is workspace.  All sets must be bound.
   void solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const;
   void solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const;
@@ -92,6 +111,7 @@ class FactorBank {
   int n_fwd_levels() const { return (int)fwd_.size(); }
   int n_bwd_levels() const { return (int)bwd_.size(); }
   int kernel_launches_per_solve() const;
+  bool panel() const { return panel_; }
 
  private:
   int prec_ = PECS_PREC_FP64;
@@ -104,7 +124,10 @@ class FactorBank {
   DBuf<double> G64_, H64_;
   DBuf<float> G32_, H32_;
   std::vector<LevelPlan> fwd_, bwd_;
+  std::vector<PanelPlan> pfwd_, pbwd_;
+  bool panel_ = false;
   int max_cols_ = 0, max_rb_ = 8;
+  void solve_panel(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const;
   BankView view() const;
   template <typename SV>
   void solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const;

@@ -183,3 +183,35 @@ def test_mixed_precision_converges_at_the_benchmark_criterion(pecs_lib):
         steps[prec], _ = ctx.run_to_steady_state(5000, 1e-8, check_every=50)
     for a, b in zip(steps[pg.PREC_FP32_MIXED], steps[pg.PREC_FP64]):
         assert abs(int(a) - int(b)) <= 0.05 * int(b) + 2
+
+
+def _panel_instances(n, base):
+    rng = np.random.default_rng(7)
+    return [base.copy(phi_app=float(rng.uniform(-0.4, 0.4)), G0=float(rng.uniform(0.5, 2.0)),
+                      tau_n=float(rng.uniform(0.3, 3.0)), tau_p=float(rng.uniform(0.3, 3.0)))
+            for _ in range(n)]
+
+
+@pytest.mark.parametrize("n_inst", [40, 64])
+def test_panel_batches_match_oracle(pecs_lib, n_inst):
+    """Many instances per factor switch the banks to the panel kernels
+    (lanes over right-hand sides): 40 instances give 80 carrier and 40 Poisson
+    right-hand sides (partial chunks, one and two per lane), 64 give 128 and
+    64.  FP64 factors: every checked instance within the step tolerance."""
+    Ps = _panel_instances(n_inst, oracle.config2_params(n_refine=3))
+    ctx = pg.Context([to_lib(P) for P in Ps])
+    ctx.initialize()
+    ctx.step(5)
+    for i in (0, n_inst // 2 + 1, n_inst - 1):
+        st, _, _ = oracle.Problem(Ps[i]).run(5)
+        _compare_state(ctx, st, STEP_TOL, inst=i)
+
+
+def test_panel_mixed_batch_within_1e6(pecs_lib):
+    Ps = _panel_instances(64, oracle.config2_params(n_refine=3))
+    ctx = pg.Context([to_lib(P) for P in Ps], precision=pg.PREC_FP32_MIXED)
+    ctx.initialize()
+    ctx.step(20)
+    for i in (3, 63):
+        st, _, _ = oracle.Problem(Ps[i]).run(20)
+        _compare_state(ctx, st, 1e-6, inst=i)
