@@ -481,11 +481,30 @@ __device__ __forceinline__ void sts(T* p, const double (&v)[N]) {
 // Rows are tiled ri at a time (ri in {4, 8, 16, 32}): warp (g, part) owns rows
 // 4g..4g+3 of the tile and the chunk columns k = part (mod 32 / ri); partial
 // sums of the column parts are added through shared memory.
+//
+// Every column chunk runs in three phases so that no warp waits on a chain of
+// dependent loads: (A) the chunk's index metadata -- source rows, child-update
+// ranges and child-update rows -- and its block tile are read by all threads
+// at once into shared memory; (B) warps gather the right-hand-side rows
+// (lanes over right-hand sides, coalesced) and subtract the children's
+// updates; (C) the register tiles accumulate.  The item's destination rows
+// and their child-update lists are staged the same way with the first chunk.
+constexpr int kPanelCm = 1024;  // staged child-update rows per chunk (more: read from global)
+constexpr int kPanelEcm = 512;  // staged child-update rows of the item's update rows
+
+template <typename T>
+__host__ __device__ constexpr size_t panel_smem_bytes(int ds_rows, int rc, int kc, int ri_max) {
+  return ((size_t)ds_rows * rc + (size_t)kc * ri_max) * sizeof(T) +
+         ((size_t)2 * kc + 1 + kPanelCm + 3 * 32 + kPanelEcm) * sizeof(int);
+}
+
 template <typename T, int RPL, bool FWD>
 __global__ void __launch_bounds__(kSolveThreads)
-    k_panel(BankView B, IlSetsView S, const int4* __restrict__ items, int kc_cap, int ds_rows) {
+    k_panel(BankView B, IlSetsView S, const int4* __restrict__ items, int kc_cap, int ds_rows,
+            int ri_max) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int RC = 32 * RPL;
+  constexpr int NW = kSolveThreads / 32;
   const int4 it = items[blockIdx.x];
   const int j = it.x, r0 = it.y, r1 = it.z, ri = it.w;
   const int s = B.s[j], m = B.m[j], f = s + m;
@@ -493,7 +512,7 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int R = st.nrhs;
   const int rc0 = blockIdx.y * RC;
   if (rc0 >= R) return;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int rl = rc0 + lane * RPL;  // first right-hand side of this lane
   const bool lane_ok = rl < R;      // R is a multiple of RPL
   const int K = FWD ? s : f;
@@ -505,8 +524,32 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int nrows = r1 - r0;
   const int wpr = 32 / ri;  // warps sharing a row group (column parts)
   const int g = warp / wpr, part = warp % wpr;
-  T* Ds = reinterpret_cast<T*>(smem_raw);   // [ds_rows][RC], ds_rows >= 32 when ri < 32
-  T* Gs = Ds + (size_t)ds_rows * RC;         // [kc_cap][ri]
+  T* Ds = reinterpret_cast<T*>(smem_raw);  // [ds_rows][RC], ds_rows >= 32 when ri < 32
+  T* Gs = Ds + (size_t)ds_rows * RC;        // [kc_cap][ri]
+  int* src_s = reinterpret_cast<int*>(Gs + (size_t)kc_cap * ri_max);  // [kc_cap]
+  int* cp_s = src_s + kc_cap;                                          // [kc_cap + 1]
+  int* cm_s = cp_s + kc_cap + 1;                                       // [kPanelCm]
+  int* dst_s = cm_s + kPanelCm;                                        // [32]
+  int* e0_s = dst_s + 32;                                              // [32]
+  int* e1_s = e0_s + 32;                                               // [32]
+  int* ecm_s = e1_s + 32;                                              // [kPanelEcm]
+  // destination rows of the item and (forward) their child-update lists
+  const int ebase = FWD ? cptr[r0] : 0;
+  if (tid < nrows) {
+    const int row = r0 + tid;
+    if (FWD) {
+      dst_s[tid] = row < s ? own[row] : B.w_off[j] + row - s;
+      const int a = cptr[row];
+      e0_s[tid] = a - ebase;
+      e1_s[tid] = (row < s ? a : cptr[row + 1]) - ebase;
+    } else {
+      dst_s[tid] = own[row];
+    }
+  }
+  if (FWD) {
+    const int ne = min(cptr[r1] - ebase, kPanelEcm);
+    for (int idx = tid; idx < ne; idx += kSolveThreads) ecm_s[idx] = B.cmap_idx[ebase + idx];
+  }
   T acc[4][RPL];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -514,32 +557,54 @@ __global__ void __launch_bounds__(kSolveThreads)
     for (int q = 0; q < RPL; ++q) acc[i][q] = T(0);
   for (int k0 = 0; k0 < K; k0 += kc_cap) {
     const int kc = min(kc_cap, K - k0);
-    for (int k = warp; k < kc; k += kSolveThreads / 32) {
-      const int p = k0 + k;
+    // (A) metadata and block tile
+    const int cbase = FWD ? cptr[k0] : 0;
+    if (tid < kc) {
+      const int p = k0 + tid;
+      if (FWD) {
+        src_s[tid] = own[p];
+        cp_s[tid] = cptr[p] - cbase;
+      } else {
+        src_s[tid] = p < s ? own[p] : ~upd[p - s];
+      }
+    }
+    if (FWD) {
+      const int nc = cptr[k0 + kc] - cbase;
+      if (tid == 0) cp_s[kc] = nc;
+      const int ncs = min(nc, kPanelCm);
+      for (int idx = tid; idx < ncs; idx += kSolveThreads) cm_s[idx] = B.cmap_idx[cbase + idx];
+    }
+    for (int idx = tid; idx < kc * ri; idx += kSolveThreads) {
+      const int k = idx / ri, i = idx - k * ri;
+      Gs[idx] = i < nrows ? __ldg(M + (size_t)(k0 + k) * ld + r0 + i) : T(0);
+    }
+    __syncthreads();
+    // (B) right-hand-side rows
+#pragma unroll 2
+    for (int k = warp; k < kc; k += NW) {
+      const int sr = src_s[k];
       double v[RPL];
 #pragma unroll
       for (int q = 0; q < RPL; ++q) v[q] = 0.0;
       if (lane_ok) {
         if (FWD) {
-          ld_rhs<RPL>(st.b + (size_t)own[p] * R + rl, v);
-          for (int c = cptr[p]; c < cptr[p + 1]; ++c) {
+          ld_rhs<RPL>(st.b + (size_t)sr * R + rl, v);
+          for (int c = cp_s[k]; c < cp_s[k + 1]; ++c) {
+            const int wi = c < kPanelCm ? cm_s[c] : B.cmap_idx[cbase + c];
             double u[RPL];
-            ld_rhs<RPL>(st.w + (size_t)B.cmap_idx[c] * R + rl, u);
+            ld_rhs<RPL>(st.w + (size_t)wi * R + rl, u);
 #pragma unroll
             for (int q = 0; q < RPL; ++q) v[q] -= u[q];
           }
         } else {
-          const double* src = p < s ? st.y + (size_t)own[p] * R : st.x + (size_t)upd[p - s] * R;
+          const double* src = sr >= 0 ? st.y + (size_t)sr * R : st.x + (size_t)(~sr) * R;
           ld_rhs<RPL>(src + rl, v);
         }
       }
       sts<T, RPL>(Ds + (size_t)k * RC + lane * RPL, v);
     }
-    for (int idx = threadIdx.x; idx < kc * ri; idx += kSolveThreads) {
-      const int k = idx / ri, i = idx - k * ri;
-      Gs[idx] = i < nrows ? __ldg(M + (size_t)(k0 + k) * ld + r0 + i) : T(0);
-    }
     __syncthreads();
+    // (C) register tiles
     for (int k = part; k < kc; k += wpr) {
       T gv[4], dv[RPL];
       lds<T, 4>(Gs + k * ri + 4 * g, gv);
@@ -553,21 +618,22 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
   // row i of the item -> its destination
   auto emit = [&](int i, double (&v)[RPL]) {
-    const int row = r0 + i;
+    const int dst = dst_s[i];
     if (FWD) {
-      if (row < s) {
-        st_rhs<RPL>(st.y + (size_t)own[row] * R + rl, v);
+      if (r0 + i < s) {
+        st_rhs<RPL>(st.y + (size_t)dst * R + rl, v);
       } else {
-        for (int c = cptr[row]; c < cptr[row + 1]; ++c) {
+        for (int c = e0_s[i]; c < e1_s[i]; ++c) {
+          const int wi = c < kPanelEcm ? ecm_s[c] : B.cmap_idx[ebase + c];
           double u[RPL];
-          ld_rhs<RPL>(st.w + (size_t)B.cmap_idx[c] * R + rl, u);
+          ld_rhs<RPL>(st.w + (size_t)wi * R + rl, u);
 #pragma unroll
           for (int q = 0; q < RPL; ++q) v[q] += u[q];
         }
-        st_rhs<RPL>(st.w + (size_t)(B.w_off[j] + row - s) * R + rl, v);
+        st_rhs<RPL>(st.w + (size_t)dst * R + rl, v);
       }
     } else {
-      st_rhs<RPL>(st.x + (size_t)own[row] * R + rl, v);
+      st_rhs<RPL>(st.x + (size_t)dst * R + rl, v);
     }
   };
   if (wpr == 1) {
@@ -590,7 +656,7 @@ __global__ void __launch_bounds__(kSolveThreads)
         red[((size_t)part * ri + 4 * g + i) * RC + lane * RPL + q] = acc[i][q];
     __syncthreads();
     if (!lane_ok) return;
-    for (int i = warp; i < nrows; i += kSolveThreads / 32) {
+    for (int i = warp; i < nrows; i += NW) {
       double v[RPL];
 #pragma unroll
       for (int q = 0; q < RPL; ++q) {
@@ -603,20 +669,44 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
 }
 
+// Tile shape of one level for nrhs right-hand sides: the longest row tiles and
+// the most right-hand sides per lane that still give the GPU two CTAs per SM.
+// Fewer right-hand sides per CTA is tried first (it keeps the staged columns
+// per output value higher than shorter row tiles do).
+struct PanelChoice {
+  int cap_idx, rpl;
+};
+
+PanelChoice choose_panel(const PanelPlan& L, int max_nrhs, int rpl_max) {
+  static const int order[6][2] = {{0, 4}, {0, 2}, {0, 1}, {1, 1}, {2, 1}, {3, 1}};
+  PanelChoice best{0, 1};
+  long long best_ctas = -1;
+  for (auto& o : order) {
+    if (o[1] > rpl_max) continue;
+    const long long ctas = (long long)L.tiles[o[0]].n_items * ((max_nrhs + 32 * o[1] - 1) / (32 * o[1]));
+    if (ctas >= 2 * kTargetCtas) return PanelChoice{o[0], o[1]};
+    if (ctas > best_ctas) {
+      best_ctas = ctas;
+      best = PanelChoice{o[0], o[1]};
+    }
+  }
+  return best;
+}
+
 template <typename T, int RPL>
-void launch_panel(bool forward, const BankView& B, const IlSetsView& S, const PanelPlan& L,
-                  int max_nrhs, cudaStream_t st) {
-  if (L.n_items == 0) return;
+void launch_panel(bool forward, const BankView& B, const IlSetsView& S, const PanelTiles& P,
+                  int max_k, int max_nrhs, cudaStream_t st) {
+  if (P.n_items == 0) return;
   const int kcap = sizeof(T) == 4 ? kPanelKcF32 : kPanelKcF64;
-  const int kc = std::min(kcap, std::max(1, L.max_k));
+  const int kc = std::min(kcap, std::max(1, max_k));
   constexpr int RC = 32 * RPL;
-  const int ds_rows = L.min_ri < 32 ? std::max(kc, 32) : kc;
-  const size_t smem = ((size_t)ds_rows * RC + (size_t)kc * L.max_ri) * sizeof(T);
-  const dim3 grid(L.n_items, (max_nrhs + RC - 1) / RC);
+  const int ds_rows = P.min_ri < 32 ? std::max(kc, 32) : kc;
+  const size_t smem = panel_smem_bytes<T>(ds_rows, RC, kc, P.max_ri);
+  const dim3 grid(P.n_items, (max_nrhs + RC - 1) / RC);
   if (forward)
-    k_panel<T, RPL, true><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, kc, ds_rows);
+    k_panel<T, RPL, true><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows, P.max_ri);
   else
-    k_panel<T, RPL, false><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, kc, ds_rows);
+    k_panel<T, RPL, false><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows, P.max_ri);
   PECS_CUDA(cudaGetLastError());
 }
 
@@ -632,15 +722,16 @@ void set_panel_smem_limit() {
 }
 
 template <typename T>
-void launch_panel_rpl(int rpl, bool forward, const BankView& B, const IlSetsView& S,
-                      const PanelPlan& L, int max_nrhs, cudaStream_t st) {
-  switch (rpl) {
-    case 1: launch_panel<T, 1>(forward, B, S, L, max_nrhs, st); break;
-    case 2: launch_panel<T, 2>(forward, B, S, L, max_nrhs, st); break;
-    default: launch_panel<T, 4>(forward, B, S, L, max_nrhs, st); break;
+void launch_panel_level(bool forward, const BankView& B, const IlSetsView& S, const PanelPlan& L,
+                        int max_nrhs, int rpl_max, cudaStream_t st) {
+  const PanelChoice c = choose_panel(L, max_nrhs, rpl_max);
+  const PanelTiles& P = L.tiles[c.cap_idx];
+  switch (c.rpl) {
+    case 1: launch_panel<T, 1>(forward, B, S, P, L.max_k, max_nrhs, st); break;
+    case 2: launch_panel<T, 2>(forward, B, S, P, L.max_k, max_nrhs, st); break;
+    default: launch_panel<T, 4>(forward, B, S, P, L.max_k, max_nrhs, st); break;
   }
 }
-
 }  // namespace
 
 BankView FactorBank::view() const {
@@ -665,8 +756,8 @@ BankView FactorBank::view() const {
 
 int FactorBank::kernel_launches_per_solve() const {
   int n = 0;
-  for (auto& l : pfwd_) n += l.n_items > 0;
-  for (auto& l : pbwd_) n += l.n_items > 0;
+  for (auto& l : pfwd_) n += l.tiles[0].n_items > 0;
+  for (auto& l : pbwd_) n += l.tiles[0].n_items > 0;
   for (auto& l : fwd_) n += (l.n_large + l.n_thin) > 0;
   for (auto& l : bwd_) n += (l.n_large + l.n_thin) > 0;
   return n;
@@ -835,42 +926,37 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
     }
   };
   if (panel) {
-    // panel items: a node's rows in tiles of ri <= 32 rows; levels that would
-    // not fill the GPU use shorter tiles (more CTAs, column parts per warp)
+    // panel items: a node's rows in tiles of ri <= cap rows, for caps 32, 16,
+    // 8 and 4 (levels that would not fill the GPU use shorter tiles: more
+    // CTAs, column parts per warp)
     auto make_panel = [&](const std::vector<LevelNodes>& lv, bool forward, std::vector<PanelPlan>& out) {
       out.clear();
       out.resize(lv.size());
       for (size_t l = 0; l < lv.size(); ++l) {
-        int cap = 32;
-        auto count = [&](int c) {
-          long long n = 0;
+        int max_k = 0;
+        for (int g : lv[l].nodes) max_k = std::max(max_k, forward ? hs[g] : hs[g] + hm[g]);
+        out[l].max_k = max_k;
+        for (int ci = 0; ci < 4; ++ci) {
+          const int cap = 32 >> ci;
+          std::vector<int4> items;
+          int max_ri = 4, min_ri = 32;
           for (int g : lv[l].nodes) {
             const int rows = forward ? hs[g] + hm[g] : hs[g];
-            n += (rows + c - 1) / c;
+            const int nit = (rows + cap - 1) / cap;
+            const int per = (rows + nit - 1) / nit;
+            int ri = 4;
+            while (ri < per) ri *= 2;
+            max_ri = std::max(max_ri, ri);
+            min_ri = std::min(min_ri, ri);
+            for (int r0 = 0; r0 < rows; r0 += per)
+              items.push_back(make_int4(g, r0, std::min(rows, r0 + per), ri));
           }
-          return n;
-        };
-        while (cap > 4 && count(cap) < 2 * kTargetCtas) cap /= 2;
-        std::vector<int4> items;
-        int max_k = 0, max_ri = 4, min_ri = 32;
-        for (int g : lv[l].nodes) {
-          const int s = hs[g], m = hm[g];
-          const int rows = forward ? s + m : s;
-          max_k = std::max(max_k, forward ? s : s + m);
-          const int nit = (rows + cap - 1) / cap;
-          const int per = (rows + nit - 1) / nit;
-          int ri = 4;
-          while (ri < per) ri *= 2;
-          max_ri = std::max(max_ri, ri);
-          min_ri = std::min(min_ri, ri);
-          for (int r0 = 0; r0 < rows; r0 += per)
-            items.push_back(make_int4(g, r0, std::min(rows, r0 + per), ri));
+          PanelTiles& P = out[l].tiles[ci];
+          P.n_items = (int)items.size();
+          P.max_ri = max_ri;
+          P.min_ri = min_ri;
+          P.items.upload(items);
         }
-        out[l].n_items = (int)items.size();
-        out[l].max_k = max_k;
-        out[l].max_ri = max_ri;
-        out[l].min_ri = min_ri;
-        out[l].items.upload(items);
       }
     };
     make_panel(fl, true, pfwd_);
@@ -944,22 +1030,22 @@ void FactorBank::solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) co
 }
 
 void FactorBank::solve_panel(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const {
-  // right-hand sides per lane: as many as fill the lanes, dividing every set's count
+  // right-hand sides per lane: at most as many as fill the lanes, dividing every set's count
   int rpl = max_nrhs >= 96 ? 4 : (max_nrhs >= 48 ? 2 : 1);
   for (int si = 0; si < n_sets_; ++si)
     while (rpl > 1 && sets.set[si].nrhs % rpl != 0) rpl /= 2;
   const BankView B = view();
   for (const PanelPlan& L : pfwd_) {
     if (prec_ == PECS_PREC_FP64)
-      launch_panel_rpl<double>(rpl, true, B, sets, L, max_nrhs, st);
+      launch_panel_level<double>(true, B, sets, L, max_nrhs, rpl, st);
     else
-      launch_panel_rpl<float>(rpl, true, B, sets, L, max_nrhs, st);
+      launch_panel_level<float>(true, B, sets, L, max_nrhs, rpl, st);
   }
   for (const PanelPlan& L : pbwd_) {
     if (prec_ == PECS_PREC_FP64)
-      launch_panel_rpl<double>(rpl, false, B, sets, L, max_nrhs, st);
+      launch_panel_level<double>(false, B, sets, L, max_nrhs, rpl, st);
     else
-      launch_panel_rpl<float>(rpl, false, B, sets, L, max_nrhs, st);
+      launch_panel_level<float>(false, B, sets, L, max_nrhs, rpl, st);
   }
 }
 

@@ -79,13 +79,18 @@ struct IlSetsView {
 
 // One level of the panel path: items (node, row0, row1, rows per tile), one
 // CTA each; every item applies its rows of the node's block to a chunk of
-// right-hand sides held in shared memory, lanes over right-hand sides.
-struct PanelPlan {
+// right-hand sides held in shared memory, lanes over right-hand sides.  Items
+// are kept for row-tile caps 32, 16, 8 and 4; the launch picks one.
+struct PanelTiles {
   int n_items = 0;
+  int max_ri = 4;   // largest rows-per-tile of the items
+  int min_ri = 32;  // smallest (< 32: column parts reduce in shared memory)
   DBuf<int4> items;
-  int max_k = 0;   // largest column count of the level's nodes
-  int max_ri = 0;  // largest rows-per-tile of the level's items
-  int min_ri = 32; // smallest rows-per-tile (< 32: column parts reduce in shared memory)
+};
+
+struct PanelPlan {
+  int max_k = 0;  // largest column count of the level's nodes
+  PanelTiles tiles[4];
 };
 
 struct LevelPlan {
