@@ -107,6 +107,10 @@ typedef struct pecs_options {
   int device;        /* CUDA device ordinal */
   int host_setup_only; /* 1: build meshes, matrices and factors on the host only
                           (no device work; for inspecting the setup) */
+  int panel_chunk;     /* panel solve kernels (>= 32 right-hand sides per factor): staged
+                          block columns per chunk (0 = default: 128 FP32, 64 FP64) */
+  int panel_min_ctas;  /* panel solve kernels: CTAs a level must reach before shorter row
+                          tiles or fewer right-hand sides per CTA are used (0 = default 304) */
 } pecs_options;
 
 typedef struct pecs_info {

@@ -692,8 +692,9 @@ struct Engine {
     // many right-hand sides per set: panel kernels (lanes over right-hand sides)
     int min_rc = 1 << 30;
     for (auto& f : carrier_set_fields()) min_rc = std::min(min_rc, n_inst * (int)f.size());
-    bank_c.build(cf, fprec, min_rc >= kPanelMinRhs);
-    bank_p.build({&fp}, fprec, n_inst >= kPanelMinRhs);
+    const PanelTuning tu{opt.panel_chunk, opt.panel_min_ctas};
+    bank_c.build(cf, fprec, min_rc >= kPanelMinRhs, tu);
+    bank_p.build({&fp}, fprec, n_inst >= kPanelMinRhs, tu);
     // free host copies of the factor values (structure is kept for stats)
     for (auto* F : {&fs[0], &fs[1], &fe[0], &fe[1], &fp}) {
       std::vector<std::vector<double>>().swap(F->Gf);

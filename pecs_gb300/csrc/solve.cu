@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     }
     __syncthreads();
     // (B) right-hand-side rows
-#pragma unroll 2
+#pragma unroll 4
     for (int k = warp; k < kc; k += NW) {
       const int sr = src_s[k];
       double v[RPL];
@@ -677,14 +677,14 @@ struct PanelChoice {
   int cap_idx, rpl;
 };
 
-PanelChoice choose_panel(const PanelPlan& L, int max_nrhs, int rpl_max) {
+PanelChoice choose_panel(const PanelPlan& L, int max_nrhs, int rpl_max, int min_ctas) {
   static const int order[6][2] = {{0, 4}, {0, 2}, {0, 1}, {1, 1}, {2, 1}, {3, 1}};
   PanelChoice best{0, 1};
   long long best_ctas = -1;
   for (auto& o : order) {
     if (o[1] > rpl_max) continue;
     const long long ctas = (long long)L.tiles[o[0]].n_items * ((max_nrhs + 32 * o[1] - 1) / (32 * o[1]));
-    if (ctas >= 2 * kTargetCtas) return PanelChoice{o[0], o[1]};
+    if (ctas >= min_ctas) return PanelChoice{o[0], o[1]};
     if (ctas > best_ctas) {
       best_ctas = ctas;
       best = PanelChoice{o[0], o[1]};
@@ -695,9 +695,8 @@ PanelChoice choose_panel(const PanelPlan& L, int max_nrhs, int rpl_max) {
 
 template <typename T, int RPL>
 void launch_panel(bool forward, const BankView& B, const IlSetsView& S, const PanelTiles& P,
-                  int max_k, int max_nrhs, cudaStream_t st) {
+                  int max_k, int max_nrhs, int kcap, cudaStream_t st) {
   if (P.n_items == 0) return;
-  const int kcap = sizeof(T) == 4 ? kPanelKcF32 : kPanelKcF64;
   const int kc = std::min(kcap, std::max(1, max_k));
   constexpr int RC = 32 * RPL;
   const int ds_rows = P.min_ri < 32 ? std::max(kc, 32) : kc;
@@ -723,13 +722,13 @@ void set_panel_smem_limit() {
 
 template <typename T>
 void launch_panel_level(bool forward, const BankView& B, const IlSetsView& S, const PanelPlan& L,
-                        int max_nrhs, int rpl_max, cudaStream_t st) {
-  const PanelChoice c = choose_panel(L, max_nrhs, rpl_max);
+                        int max_nrhs, int rpl_max, const PanelTuning& tu, cudaStream_t st) {
+  const PanelChoice c = choose_panel(L, max_nrhs, rpl_max, tu.min_ctas);
   const PanelTiles& P = L.tiles[c.cap_idx];
   switch (c.rpl) {
-    case 1: launch_panel<T, 1>(forward, B, S, P, L.max_k, max_nrhs, st); break;
-    case 2: launch_panel<T, 2>(forward, B, S, P, L.max_k, max_nrhs, st); break;
-    default: launch_panel<T, 4>(forward, B, S, P, L.max_k, max_nrhs, st); break;
+    case 1: launch_panel<T, 1>(forward, B, S, P, L.max_k, max_nrhs, tu.chunk, st); break;
+    case 2: launch_panel<T, 2>(forward, B, S, P, L.max_k, max_nrhs, tu.chunk, st); break;
+    default: launch_panel<T, 4>(forward, B, S, P, L.max_k, max_nrhs, tu.chunk, st); break;
   }
 }
 }  // namespace
@@ -763,11 +762,18 @@ int FactorBank::kernel_launches_per_solve() const {
   return n;
 }
 
-void FactorBank::build(const std::vector<const MfFactor*>& factors, int precision, bool panel) {
+void FactorBank::build(const std::vector<const MfFactor*>& factors, int precision, bool panel,
+                       PanelTuning tuning) {
   if (factors.empty() || (int)factors.size() > kMaxSets)
     throw PecsError(PECS_E_ARG, "factor bank needs 1..4 factors");
   prec_ = precision;
   panel_ = panel;
+  tune_ = tuning;
+  if (tune_.chunk < 0 || tune_.chunk > 128 || tune_.min_ctas < 0)
+    throw PecsError(PECS_E_ARG, "panel tuning out of range");
+  if (tune_.chunk == 0) tune_.chunk = precision == PECS_PREC_FP64 ? kPanelKcF64 : kPanelKcF32;
+  if (prec_ == PECS_PREC_FP64) tune_.chunk = std::min(tune_.chunk, kPanelKcF64);
+  if (tune_.min_ctas == 0) tune_.min_ctas = 2 * kTargetCtas;
   n_sets_ = (int)factors.size();
   std::vector<int> hs, hm, own_off, upd_off, w_off, cm_off, own_idx, upd_idx, cmap_ptr, cmap_idx,
       node_set;
@@ -1037,15 +1043,15 @@ void FactorBank::solve_panel(const IlSetsView& sets, int max_nrhs, cudaStream_t 
   const BankView B = view();
   for (const PanelPlan& L : pfwd_) {
     if (prec_ == PECS_PREC_FP64)
-      launch_panel_level<double>(true, B, sets, L, max_nrhs, rpl, st);
+      launch_panel_level<double>(true, B, sets, L, max_nrhs, rpl, tune_, st);
     else
-      launch_panel_level<float>(true, B, sets, L, max_nrhs, rpl, st);
+      launch_panel_level<float>(true, B, sets, L, max_nrhs, rpl, tune_, st);
   }
   for (const PanelPlan& L : pbwd_) {
     if (prec_ == PECS_PREC_FP64)
-      launch_panel_level<double>(false, B, sets, L, max_nrhs, rpl, st);
+      launch_panel_level<double>(false, B, sets, L, max_nrhs, rpl, tune_, st);
     else
-      launch_panel_level<float>(false, B, sets, L, max_nrhs, rpl, st);
+      launch_panel_level<float>(false, B, sets, L, max_nrhs, rpl, tune_, st);
   }
 }
 

@@ -100,12 +100,18 @@ struct LevelPlan {
   int max_cols = 0;   // staged columns per large item
 };
 
+struct PanelTuning {
+  int chunk = 0;     // staged block columns per chunk (0: 128 FP32, 64 FP64)
+  int min_ctas = 0;  // CTAs a level must reach before shorter tiles are used (0: 2 x SMs)
+};
+
 class FactorBank {
  public:
   // factors[i] is bound to RHS set i.  precision: PECS_PREC_FP64 or FP32_IR.
   // panel: store every block column-major and apply it with the panel
   // kernels (many right-hand sides per set, interleaved layout only).
-  void build(const std::vector<const MfFactor*>& factors, int precision, bool panel = false);
+  void build(const std::vector<const MfFactor*>& factors, int precision, bool panel = false,
+             PanelTuning tuning = PanelTuning());
   // y = forward(b), x = backward(y); w is workspace.  All sets must be bound.
   void solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const;
   void solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const;
@@ -131,6 +137,7 @@ class FactorBank {
   std::vector<LevelPlan> fwd_, bwd_;
   std::vector<PanelPlan> pfwd_, pbwd_;
   bool panel_ = false;
+  PanelTuning tune_;
   int max_cols_ = 0, max_rb_ = 8;
   void solve_panel(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const;
   BankView view() const;
