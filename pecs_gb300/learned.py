@@ -206,6 +206,7 @@ class NeuralOperator:
         """X: (n, 6) float32 cuda; T: (n, rank) float32 cuda."""
         import torch
         n = X.shape[0]
+        batch = min(batch, n)
         g = torch.Generator(device="cpu").manual_seed(seed)
         steps = 0
         total = epochs * max(1, n // batch)
