@@ -405,7 +405,8 @@ void launch_rb(int rb, bool forward, const BankView& B, const SV& S, const Level
 // ---- panel path --------------------------------------------------------------
 constexpr int kPanelKcF32 = 128;  // staged columns per chunk, FP32 blocks
 constexpr int kPanelKcF64 = 64;   // staged columns per chunk, FP64 blocks
-constexpr size_t kPanelSmem = 100 * 1024;
+constexpr size_t kPanelSmem = 160 * 1024;
+constexpr int kPanelCmMax = 4096;  // staged child-update rows per node (more: read from global)
 
 // RPL consecutive doubles of one interleaved row (offset a multiple of RPL).
 template <int RPL>
@@ -482,33 +483,31 @@ __device__ __forceinline__ void sts(T* p, const double (&v)[N]) {
 // 4g..4g+3 of the tile and the chunk columns k = part (mod 32 / ri); partial
 // sums of the column parts are added through shared memory.
 //
-// Every column chunk runs in three phases so that no warp waits on a chain of
-// dependent loads: (A) the chunk's index metadata -- source rows, child-update
-// ranges and child-update rows -- and its block tile are read by all threads
-// at once into shared memory; (B) warps gather the right-hand-side rows
-// (lanes over right-hand sides, coalesced) and subtract the children's
-// updates; (C) the register tiles accumulate.  The item's destination rows
-// and their child-update lists are staged the same way with the first chunk.
-constexpr int kPanelCm = 1024;  // staged child-update rows per chunk (more: read from global)
-constexpr int kPanelEcm = 512;  // staged child-update rows of the item's update rows
-
+// The kernel is bound by the latency of dependent loads, so it is written to
+// keep their chain short: the item record carries everything about its node
+// (sizes, offsets, the node's child-update list range); one round of loads by
+// all threads stages the node's index metadata (source rows, child-update
+// ranges and rows) and the block tile in shared memory; the next round gathers
+// the right-hand-side rows (lanes over right-hand sides, coalesced) and
+// subtracts the children's updates; then the register tiles accumulate and the
+// rows are written.
 template <typename T>
-__host__ __device__ constexpr size_t panel_smem_bytes(int ds_rows, int rc, int kc, int ri_max) {
-  return ((size_t)ds_rows * rc + (size_t)kc * ri_max) * sizeof(T) +
-         ((size_t)2 * kc + 1 + kPanelCm + 3 * 32 + kPanelEcm) * sizeof(int);
+__host__ __device__ constexpr size_t panel_smem_bytes(int ds_rows, int rc, int kc, int ri_max,
+                                                      int meta_ints) {
+  return ((size_t)ds_rows * rc + (size_t)kc * ri_max) * sizeof(T) + (size_t)meta_ints * sizeof(int);
 }
 
 template <typename T, int RPL, bool FWD>
 __global__ void __launch_bounds__(kSolveThreads)
-    k_panel(BankView B, IlSetsView S, const int4* __restrict__ items, int kc_cap, int ds_rows,
-            int ri_max) {
+    k_panel(BankView B, IlSetsView S, const PanelItem* __restrict__ items, int kc_cap, int ds_rows,
+            int ri_max, int max_s, int max_f, int cm_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int RC = 32 * RPL;
   constexpr int NW = kSolveThreads / 32;
-  const int4 it = items[blockIdx.x];
-  const int j = it.x, r0 = it.y, r1 = it.z, ri = it.w;
-  const int s = B.s[j], m = B.m[j], f = s + m;
-  const IlSetView st = S.set[B.node_set[j]];
+  const PanelItem I = items[blockIdx.x];
+  const int r0 = I.a.y, r1 = I.a.z, ri = I.a.w;
+  const int s = I.b.x, m = I.b.y, f = s + m, w_off = I.b.w;
+  const IlSetView st = S.set[I.b.z];
   const int R = st.nrhs;
   const int rc0 = blockIdx.y * RC;
   if (rc0 >= R) return;
@@ -517,38 +516,32 @@ __global__ void __launch_bounds__(kSolveThreads)
   const bool lane_ok = rl < R;      // R is a multiple of RPL
   const int K = FWD ? s : f;
   const int ld = FWD ? f : s;
-  const T* M = FWD ? static_cast<const T*>(B.G) + B.goff[j] : static_cast<const T*>(B.H) + B.hoff[j];
-  const int* own = B.own_idx + B.own_off[j];
-  const int* upd = B.upd_idx + B.upd_off[j];
-  const int* cptr = B.cmap_ptr + B.cm_off[j];
+  const T* M = static_cast<const T*>(FWD ? B.G : B.H) + (((long long)I.c.y << 32) | (unsigned)I.c.x);
   const int nrows = r1 - r0;
   const int wpr = 32 / ri;  // warps sharing a row group (column parts)
   const int g = warp / wpr, part = warp % wpr;
   T* Ds = reinterpret_cast<T*>(smem_raw);  // [ds_rows][RC], ds_rows >= 32 when ri < 32
   T* Gs = Ds + (size_t)ds_rows * RC;        // [kc_cap][ri]
-  int* src_s = reinterpret_cast<int*>(Gs + (size_t)kc_cap * ri_max);  // [kc_cap]
-  int* cp_s = src_s + kc_cap;                                          // [kc_cap + 1]
-  int* cm_s = cp_s + kc_cap + 1;                                       // [kPanelCm]
-  int* dst_s = cm_s + kPanelCm;                                        // [32]
-  int* e0_s = dst_s + 32;                                              // [32]
-  int* e1_s = e0_s + 32;                                               // [32]
-  int* ecm_s = e1_s + 32;                                              // [kPanelEcm]
-  // destination rows of the item and (forward) their child-update lists
-  const int ebase = FWD ? cptr[r0] : 0;
-  if (tid < nrows) {
-    const int row = r0 + tid;
+  // index metadata of the whole node:
+  //   forward:  src_s[s] = own rows; cp_s[f + 1] = child-update ranges per front
+  //             position (relative to the node's first entry); cm_s = child rows
+  //   backward: src_s[f] = own rows (y) / ~update rows (x)
+  int* src_s = reinterpret_cast<int*>(Gs + (size_t)kc_cap * ri_max);
+  int* cp_s = src_s + (FWD ? max_s : max_f);
+  int* cm_s = cp_s + max_f + 1;
+  const int cbase = I.d.y, ncm = I.d.z;
+  {
+    const int* own = B.own_idx + I.c.z;
     if (FWD) {
-      dst_s[tid] = row < s ? own[row] : B.w_off[j] + row - s;
-      const int a = cptr[row];
-      e0_s[tid] = a - ebase;
-      e1_s[tid] = (row < s ? a : cptr[row + 1]) - ebase;
+      const int* cptr = B.cmap_ptr + I.d.x;
+      for (int p = tid; p < s; p += kSolveThreads) src_s[p] = own[p];
+      for (int p = tid; p <= f; p += kSolveThreads) cp_s[p] = cptr[p] - cbase;
+      const int n = min(ncm, cm_cap);
+      for (int c = tid; c < n; c += kSolveThreads) cm_s[c] = B.cmap_idx[cbase + c];
     } else {
-      dst_s[tid] = own[row];
+      const int* upd = B.upd_idx + I.c.w;
+      for (int p = tid; p < f; p += kSolveThreads) src_s[p] = p < s ? own[p] : ~upd[p - s];
     }
-  }
-  if (FWD) {
-    const int ne = min(cptr[r1] - ebase, kPanelEcm);
-    for (int idx = tid; idx < ne; idx += kSolveThreads) ecm_s[idx] = B.cmap_idx[ebase + idx];
   }
   T acc[4][RPL];
 #pragma unroll
@@ -557,40 +550,23 @@ __global__ void __launch_bounds__(kSolveThreads)
     for (int q = 0; q < RPL; ++q) acc[i][q] = T(0);
   for (int k0 = 0; k0 < K; k0 += kc_cap) {
     const int kc = min(kc_cap, K - k0);
-    // (A) metadata and block tile
-    const int cbase = FWD ? cptr[k0] : 0;
-    if (tid < kc) {
-      const int p = k0 + tid;
-      if (FWD) {
-        src_s[tid] = own[p];
-        cp_s[tid] = cptr[p] - cbase;
-      } else {
-        src_s[tid] = p < s ? own[p] : ~upd[p - s];
-      }
-    }
-    if (FWD) {
-      const int nc = cptr[k0 + kc] - cbase;
-      if (tid == 0) cp_s[kc] = nc;
-      const int ncs = min(nc, kPanelCm);
-      for (int idx = tid; idx < ncs; idx += kSolveThreads) cm_s[idx] = B.cmap_idx[cbase + idx];
-    }
     for (int idx = tid; idx < kc * ri; idx += kSolveThreads) {
       const int k = idx / ri, i = idx - k * ri;
       Gs[idx] = i < nrows ? __ldg(M + (size_t)(k0 + k) * ld + r0 + i) : T(0);
     }
-    __syncthreads();
-    // (B) right-hand-side rows
+    __syncthreads();  // metadata (first chunk) and block tile staged
 #pragma unroll 4
     for (int k = warp; k < kc; k += NW) {
-      const int sr = src_s[k];
+      const int p = k0 + k;
+      const int sr = src_s[p];
       double v[RPL];
 #pragma unroll
       for (int q = 0; q < RPL; ++q) v[q] = 0.0;
       if (lane_ok) {
         if (FWD) {
           ld_rhs<RPL>(st.b + (size_t)sr * R + rl, v);
-          for (int c = cp_s[k]; c < cp_s[k + 1]; ++c) {
-            const int wi = c < kPanelCm ? cm_s[c] : B.cmap_idx[cbase + c];
+          for (int c = cp_s[p]; c < cp_s[p + 1]; ++c) {
+            const int wi = c < cm_cap ? cm_s[c] : B.cmap_idx[cbase + c];
             double u[RPL];
             ld_rhs<RPL>(st.w + (size_t)wi * R + rl, u);
 #pragma unroll
@@ -604,7 +580,6 @@ __global__ void __launch_bounds__(kSolveThreads)
       sts<T, RPL>(Ds + (size_t)k * RC + lane * RPL, v);
     }
     __syncthreads();
-    // (C) register tiles
     for (int k = part; k < kc; k += wpr) {
       T gv[4], dv[RPL];
       lds<T, 4>(Gs + k * ri + 4 * g, gv);
@@ -618,22 +593,22 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
   // row i of the item -> its destination
   auto emit = [&](int i, double (&v)[RPL]) {
-    const int dst = dst_s[i];
+    const int row = r0 + i;
     if (FWD) {
-      if (r0 + i < s) {
-        st_rhs<RPL>(st.y + (size_t)dst * R + rl, v);
+      if (row < s) {
+        st_rhs<RPL>(st.y + (size_t)src_s[row] * R + rl, v);
       } else {
-        for (int c = e0_s[i]; c < e1_s[i]; ++c) {
-          const int wi = c < kPanelEcm ? ecm_s[c] : B.cmap_idx[ebase + c];
+        for (int c = cp_s[row]; c < cp_s[row + 1]; ++c) {
+          const int wi = c < cm_cap ? cm_s[c] : B.cmap_idx[cbase + c];
           double u[RPL];
           ld_rhs<RPL>(st.w + (size_t)wi * R + rl, u);
 #pragma unroll
           for (int q = 0; q < RPL; ++q) v[q] += u[q];
         }
-        st_rhs<RPL>(st.w + (size_t)dst * R + rl, v);
+        st_rhs<RPL>(st.w + (size_t)(w_off + row - s) * R + rl, v);
       }
     } else {
-      st_rhs<RPL>(st.x + (size_t)dst * R + rl, v);
+      st_rhs<RPL>(st.x + (size_t)src_s[row] * R + rl, v);
     }
   };
   if (wpr == 1) {
@@ -694,18 +669,21 @@ PanelChoice choose_panel(const PanelPlan& L, int max_nrhs, int rpl_max, int min_
 }
 
 template <typename T, int RPL>
-void launch_panel(bool forward, const BankView& B, const IlSetsView& S, const PanelTiles& P,
-                  int max_k, int max_nrhs, int kcap, cudaStream_t st) {
+void launch_panel(bool forward, const BankView& B, const IlSetsView& S, const PanelPlan& L,
+                  const PanelTiles& P, int max_nrhs, int kcap, cudaStream_t st) {
   if (P.n_items == 0) return;
-  const int kc = std::min(kcap, std::max(1, max_k));
+  const int kc = std::min(kcap, std::max(1, L.max_k));
   constexpr int RC = 32 * RPL;
   const int ds_rows = P.min_ri < 32 ? std::max(kc, 32) : kc;
-  const size_t smem = panel_smem_bytes<T>(ds_rows, RC, kc, P.max_ri);
+  const int meta = forward ? L.max_s + L.max_f + 1 + L.cm_cap : L.max_f;
+  const size_t smem = panel_smem_bytes<T>(ds_rows, RC, kc, P.max_ri, meta);
   const dim3 grid(P.n_items, (max_nrhs + RC - 1) / RC);
   if (forward)
-    k_panel<T, RPL, true><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows, P.max_ri);
+    k_panel<T, RPL, true><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows, P.max_ri,
+                                                             L.max_s, L.max_f, L.cm_cap);
   else
-    k_panel<T, RPL, false><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows, P.max_ri);
+    k_panel<T, RPL, false><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows, P.max_ri,
+                                                              L.max_s, L.max_f, L.cm_cap);
   PECS_CUDA(cudaGetLastError());
 }
 
@@ -726,9 +704,9 @@ void launch_panel_level(bool forward, const BankView& B, const IlSetsView& S, co
   const PanelChoice c = choose_panel(L, max_nrhs, rpl_max, tu.min_ctas);
   const PanelTiles& P = L.tiles[c.cap_idx];
   switch (c.rpl) {
-    case 1: launch_panel<T, 1>(forward, B, S, P, L.max_k, max_nrhs, tu.chunk, st); break;
-    case 2: launch_panel<T, 2>(forward, B, S, P, L.max_k, max_nrhs, tu.chunk, st); break;
-    default: launch_panel<T, 4>(forward, B, S, P, L.max_k, max_nrhs, tu.chunk, st); break;
+    case 1: launch_panel<T, 1>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
+    case 2: launch_panel<T, 2>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
+    default: launch_panel<T, 4>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
   }
 }
 }  // namespace
@@ -939,12 +917,21 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
       out.clear();
       out.resize(lv.size());
       for (size_t l = 0; l < lv.size(); ++l) {
-        int max_k = 0;
-        for (int g : lv[l].nodes) max_k = std::max(max_k, forward ? hs[g] : hs[g] + hm[g]);
+        int max_k = 0, max_s = 1, max_f = 1, max_cm = 0;
+        for (int g : lv[l].nodes) {
+          const int f = hs[g] + hm[g];
+          max_k = std::max(max_k, forward ? hs[g] : f);
+          max_s = std::max(max_s, hs[g]);
+          max_f = std::max(max_f, f);
+          max_cm = std::max(max_cm, cmap_ptr[cm_off[g] + f] - cmap_ptr[cm_off[g]]);
+        }
         out[l].max_k = max_k;
+        out[l].max_s = max_s;
+        out[l].max_f = max_f;
+        out[l].cm_cap = std::min(max_cm, kPanelCmMax);
         for (int ci = 0; ci < 4; ++ci) {
           const int cap = 32 >> ci;
-          std::vector<int4> items;
+          std::vector<PanelItem> items;
           int max_ri = 4, min_ri = 32;
           for (int g : lv[l].nodes) {
             const int rows = forward ? hs[g] + hm[g] : hs[g];
@@ -954,8 +941,17 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
             while (ri < per) ri *= 2;
             max_ri = std::max(max_ri, ri);
             min_ri = std::min(min_ri, ri);
-            for (int r0 = 0; r0 < rows; r0 += per)
-              items.push_back(make_int4(g, r0, std::min(rows, r0 + per), ri));
+            const long long off = forward ? goff[g] : hoff[g];
+            const int cb = cmap_ptr[cm_off[g]];
+            const int ncm = cmap_ptr[cm_off[g] + hs[g] + hm[g]] - cb;
+            for (int r0 = 0; r0 < rows; r0 += per) {
+              PanelItem it;
+              it.a = make_int4(g, r0, std::min(rows, r0 + per), ri);
+              it.b = make_int4(hs[g], hm[g], node_set[g], w_off[g]);
+              it.c = make_int4((int)(off & 0xffffffffll), (int)(off >> 32), own_off[g], upd_off[g]);
+              it.d = make_int4(cm_off[g], cb, ncm, 0);
+              items.push_back(it);
+            }
           }
           PanelTiles& P = out[l].tiles[ci];
           P.n_items = (int)items.size();

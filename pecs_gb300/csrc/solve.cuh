@@ -81,15 +81,26 @@ struct IlSetsView {
 // CTA each; every item applies its rows of the node's block to a chunk of
 // right-hand sides held in shared memory, lanes over right-hand sides.  Items
 // are kept for row-tile caps 32, 16, 8 and 4; the launch picks one.
+// One panel item: a row range of one node and everything about the node the
+// kernel needs, so that a single round of loads starts it.
+struct __align__(16) PanelItem {
+  int4 a;  // node, row0, row1, rows per tile
+  int4 b;  // s, m, RHS set, update-vector offset
+  int4 c;  // block offset (low, high 32 bits), own-index offset, update-index offset
+  int4 d;  // child-map pointer offset, first child-map entry, child-map entries, 0
+};
+
 struct PanelTiles {
   int n_items = 0;
   int max_ri = 4;   // largest rows-per-tile of the items
   int min_ri = 32;  // smallest (< 32: column parts reduce in shared memory)
-  DBuf<int4> items;
+  DBuf<PanelItem> items;
 };
 
 struct PanelPlan {
-  int max_k = 0;  // largest column count of the level's nodes
+  int max_k = 0;   // largest column count of the level's nodes
+  int max_s = 1, max_f = 1;
+  int cm_cap = 0;  // child-map entries staged per node (the level's largest, capped)
   PanelTiles tiles[4];
 };
 
