@@ -42,14 +42,6 @@ void set_error(const std::string& m) { g_last_error = m; }
 // small kernels: residual, axpy, steady-state test, interface current
 // ---------------------------------------------------------------------------
 
-struct VecList {  // vectors of one refinement sweep
-  const double* const* b;
-  const double* const* x;
-  double* const* out;
-  const int* mat;  // matrix index per vector
-  const int* len;  // length per vector
-};
-
 struct CsrDev {
   const int* rp;
   const int* ci;
@@ -60,41 +52,6 @@ struct CsrSet {
   CsrDev m[5];
 };
 
-// out = b - A x   (one thread per row; grid.y = vector)
-__global__ void k_residual(CsrSet M, VecList L, int n, const int* __restrict__ active,
-                           const int* __restrict__ vec_inst) {
-  const int v = blockIdx.y;
-  if (active && !active[vec_inst[v]]) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || i >= L.len[v]) return;
-  const CsrDev A = M.m[L.mat[v]];
-  const double* x = L.x[v];
-  double s = 0.0;
-  for (int p = A.rp[i]; p < A.rp[i + 1]; ++p) s += A.v[p] * x[A.ci[p]];
-  L.out[v][i] = L.b[v][i] - s;
-}
-
-// x += d
-__global__ void k_axpy(double* const* x, const double* const* d, const int* __restrict__ len,
-                       const int* __restrict__ active, const int* __restrict__ vec_inst) {
-  const int v = blockIdx.y;
-  if (active && !active[vec_inst[v]]) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < len[v]) x[v][i] += d[v][i];
-}
-
-// x -> (hi, lo) float pair with x = hi + lo to ~2^-48 relative
-__global__ void k_split(const double* const* x, float2* const* xs, const int* __restrict__ len,
-                        const int* __restrict__ active, const int* __restrict__ vec_inst) {
-  const int v = blockIdx.y;
-  if (active && !active[vec_inst[v]]) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= len[v]) return;
-  const double a = x[v][i];
-  const float hi = __double2float_rn(a);
-  xs[v][i] = make_float2(hi, __double2float_rn(a - (double)hi));
-}
-
 struct CsrDf {  // matrix values split into FP32 (hi, lo) pairs
   const int* rp;
   const int* ci;
@@ -104,33 +61,6 @@ struct CsrDf {  // matrix values split into FP32 (hi, lo) pairs
 struct CsrDfSet {
   CsrDf m[5];
 };
-
-// out = b - A x with the sum in FP32-pair ("double-float") arithmetic:
-// products are exact through fmaf, partial sums through TwoSum, so the
-// residual keeps ~46-bit accuracy while running on the FP32 pipe.
-__global__ void k_residual_df(CsrDfSet M, const double* const* b, const float2* const* xs,
-                              double* const* out, const int* __restrict__ mat,
-                              const int* __restrict__ len, const int* __restrict__ active,
-                              const int* __restrict__ vec_inst) {
-  const int v = blockIdx.y;
-  if (active && !active[vec_inst[v]]) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= len[v]) return;
-  const CsrDf A = M.m[mat[v]];
-  const float2* x = xs[v];
-  float sh = 0.f, sl = 0.f;
-  for (int p = A.rp[i]; p < A.rp[i + 1]; ++p) {
-    const float2 a = A.v[p], xv = x[A.ci[p]];
-    const float ph = a.x * xv.x;
-    const float pe = fmaf(a.x, xv.x, -ph) + fmaf(a.x, xv.y, a.y * xv.x);
-    const float t = sh + ph;                      // TwoSum(sh, ph)
-    const float z = t - sh;
-    const float e = (sh - (t - z)) + (ph - z);
-    sh = t;
-    sl += e + pe;
-  }
-  out[v][i] = b[v][i] - ((double)sh + (double)sl);
-}
 
 // ---- interleaved [dof][rhs] buffers of the batched solves --------------------
 // dst[d * R + k] = src_k[d]   (32 x 32 tiles through shared memory)
@@ -150,13 +80,14 @@ __global__ void k_gather_il(const double* const* __restrict__ src, double* __res
 }
 
 // dst_k[d] = src[d * R + k]
-__global__ void k_scatter_il(const double* __restrict__ src, double* const* __restrict__ dst, int n,
+template <typename V>
+__global__ void k_scatter_il(const V* __restrict__ src, double* const* __restrict__ dst, int n,
                              int R) {
   __shared__ double t[32][33];
   const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
     const int d = d0 + dd, k = k0 + threadIdx.x;
-    t[dd][threadIdx.x] = (d < n && k < R) ? src[(size_t)d * R + k] : 0.0;
+    t[dd][threadIdx.x] = (d < n && k < R) ? (double)src[(size_t)d * R + k] : 0.0;
   }
   __syncthreads();
   for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
@@ -173,14 +104,32 @@ __global__ void k_split_il(const double* __restrict__ x, float2* __restrict__ xs
   xs[i] = make_float2(hi, __double2float_rn(a - (double)hi));
 }
 
-__global__ void k_axpy_il(double* __restrict__ x, const double* __restrict__ d, size_t n) {
+template <typename V>
+__global__ void k_axpy_il(double* __restrict__ x, const V* __restrict__ d, size_t n) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i < n) x[i] += d[i];
+  if (i < n) x[i] += (double)d[i];
+}
+
+// x = (double) x32, and its FP32-pair split (exact: the low part is zero)
+__global__ void k_split_il_f(const float* __restrict__ x32, double* __restrict__ x,
+                             float2* __restrict__ xs, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float v = x32[i];
+  x[i] = (double)v;
+  xs[i] = make_float2(v, 0.f);
+}
+
+__global__ void k_widen_il(const float* __restrict__ x32, double* __restrict__ x, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) x[i] = (double)x32[i];
 }
 
 // r = b - A x for R right-hand sides sharing A: one warp per row, lanes over
-// right-hand sides (matrix entries broadcast, vectors read contiguously);
-// FP32-pair products and sums as in k_residual_df.
+// right-hand sides (matrix entries broadcast, vectors read contiguously).
+// The sum runs in FP32-pair ("double-float") arithmetic: products are exact
+// through fmaf, partial sums through TwoSum, so the residual keeps ~46-bit
+// accuracy while running on the FP32 pipe.
 __global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const float2* __restrict__ xs,
                                  double* __restrict__ r, int n, int R) {
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
@@ -395,17 +344,16 @@ struct Engine {
   DBuf<double> iface_ne, iface_pe, sch_ne, sch_pe;
   DBuf<int> isemi, ielec;
   // vectors
-  DBuf<double> state[2][5], rhs[5], bconst[5], yv[5], res[5], delta[5], snap[5], init_dev[4];
-  std::vector<DBuf<double>> wbuf_c, wbuf_p;
+  DBuf<double> state[2][5], rhs[5], bconst[5], snap[5], init_dev[4];
   int cur = 0;
   bool carriers_advanced = false;
   bool initialized = false;
-  // solve pointer tables: [nxt][0=main, 1=correction] (kept for the timing entry)
-  SetTable tab_c[2][2], tab_p[2][2];
   // interleaved buffers of the batched solves, per bank (0 carriers, 1 Poisson) and set
   struct IlSet {
     int n = 0, R = 0, mat = 0;
+    bool f32 = false;              // panel bank with FP32 factors: float sweep vectors
     DBuf<double> B, Y, W, X, Rr, D;
+    DBuf<float> Y32, W32, X32, D32;
     DBuf<float2> Xs;
     DBuf<const double*> src;       // rhs vector of each column
     DBuf<double*> dst[2];          // state vector of each column, per ping-pong target
@@ -440,17 +388,17 @@ struct Engine {
     return 1 + lc * (1 + it) + sc * (2 + per_it * it) + 1 + lp * (1 + it) + sp * (2 + per_it * it) + 3;
   }
   // algorithmic bytes of one application of a bank to all of its right-hand
-  // sides: every stored factor entry once, plus the vectors (b read, y write +
-  // read, x write, update vectors write + read)
+  // sides: every stored factor entry once, plus the vectors (b read in FP64;
+  // y write + read, x write, update vectors write + read, in the sweep's
+  // vector type: float for FP32 panel banks, else double)
   double solve_bytes(int which) const {
     const FactorBank& B = which == 0 ? bank_c : bank_p;
-    const SetTable& t = which == 0 ? tab_c[0][0] : tab_p[0][0];
+    const IlBank& I = il[which];
     double vec = 0.0;
-    for (int si = 0; si < kMaxSets; ++si) {
-      const int nr = t.view.set[si].nrhs;
-      if (nr == 0) continue;
-      const int fld = which == 0 ? carrier_set_fields()[si][0] : 4;
-      vec += (double)nr * (4.0 * nd[fld] * 8.0 + 2.0 * B.set_wtotal(si) * 8.0);
+    for (int si = 0; si < I.n_sets; ++si) {
+      const IlSet& S_ = I.set[si];
+      const double vb = S_.f32 ? 4.0 : 8.0;
+      vec += (double)S_.R * ((8.0 + 3.0 * vb) * S_.n + 2.0 * vb * B.set_wtotal(si));
     }
     return (double)B.bytes() + vec;
   }
@@ -459,10 +407,9 @@ struct Engine {
     PECS_CUDA(cudaEventCreate(&e0));
     PECS_CUDA(cudaEventCreate(&e1));
     const FactorBank& B = which == 0 ? bank_c : bank_p;
-    const IlSetsView v = il_view(which, false);
-    B.solve(v, il[which].max_R, st);  // warm
+    bank_sweep(B, which, false, st);  // warm
     PECS_CUDA(cudaEventRecord(e0, st));
-    for (int r = 0; r < reps; ++r) B.solve(v, il[which].max_R, st);
+    for (int r = 0; r < reps; ++r) bank_sweep(B, which, false, st);
     PECS_CUDA(cudaEventRecord(e1, st));
     PECS_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -489,49 +436,6 @@ struct Engine {
     return F;
   }
 
-  void build_sets(const std::vector<std::vector<int>>& set_fields, const FactorBank& bank,
-                  DBuf<double>* bsrc, DBuf<double>* xdst, std::vector<DBuf<double>>& wbufs,
-                  int& wcount, SetTable& tab) {
-    const int ns = (int)set_fields.size();
-    tab.b.resize(ns);
-    tab.y.resize(ns);
-    tab.w.resize(ns);
-    tab.x.resize(ns);
-    tab.max_nrhs = 0;
-    int widx = 0;
-    for (int si = 0; si < ns; ++si) {
-      std::vector<double*> hb, hy, hw, hx;
-      for (int i = 0; i < n_inst; ++i)
-        for (int f : set_fields[si]) {
-          hb.push_back(bsrc[f].p + (size_t)i * nd[f]);
-          hy.push_back(yv[f].p + (size_t)i * nd[f]);
-          hx.push_back(xdst[f].p + (size_t)i * nd[f]);
-          if (widx >= (int)wbufs.size()) {
-            wbufs.emplace_back();
-            wbufs.back().alloc(bank.set_wtotal(si));
-            wbufs.back().zero();
-          }
-          if ((int)wbufs[widx].n < bank.set_wtotal(si)) {
-            wbufs[widx].alloc(bank.set_wtotal(si));
-            wbufs[widx].zero();
-          }
-          hw.push_back(wbufs[widx].p);
-          ++widx;
-        }
-      tab.b[si].upload(hb);
-      tab.y[si].upload(hy);
-      tab.w[si].upload(hw);
-      tab.x[si].upload(hx);
-      tab.view.set[si].nrhs = (int)hb.size();
-      tab.view.set[si].b = tab.b[si].p;
-      tab.view.set[si].y = tab.y[si].p;
-      tab.view.set[si].w = tab.w[si].p;
-      tab.view.set[si].x = tab.x[si].p;
-      tab.max_nrhs = std::max(tab.max_nrhs, (int)hb.size());
-    }
-    wcount = std::max(wcount, widx);
-  }
-
   void build_il(int which, const std::vector<std::vector<int>>& set_fields, const FactorBank& bank) {
     IlBank& I = il[which];
     I.n_sets = (int)set_fields.size();
@@ -543,14 +447,25 @@ struct Engine {
       S_.R = n_inst * (int)set_fields[si].size();
       S_.mat = f0;
       const size_t nR = (size_t)S_.n * S_.R;
+      S_.f32 = bank.panel() && opt.precision != PECS_PREC_FP64;
       S_.B.alloc(nR);
-      S_.Y.alloc(nR);
       S_.X.alloc(nR);
-      S_.W.alloc((size_t)bank.set_wtotal(si) * S_.R);
-      S_.W.zero();
+      if (S_.f32) {
+        S_.Y32.alloc(nR);
+        S_.X32.alloc(nR);
+        S_.W32.alloc((size_t)bank.set_wtotal(si) * S_.R);
+        S_.W32.zero();
+      } else {
+        S_.Y.alloc(nR);
+        S_.W.alloc((size_t)bank.set_wtotal(si) * S_.R);
+        S_.W.zero();
+      }
       if (opt.precision != PECS_PREC_FP64) {
         S_.Rr.alloc(nR);
-        S_.D.alloc(nR);
+        if (S_.f32)
+          S_.D32.alloc(nR);
+        else
+          S_.D.alloc(nR);
         if (opt.precision == PECS_PREC_FP32_MIXED) S_.Xs.alloc(nR);
       }
       std::vector<const double*> src;
@@ -564,6 +479,24 @@ struct Engine {
       for (int t = 0; t < 2; ++t) S_.dst[t].upload(dst[t]);
       I.max_R = std::max(I.max_R, S_.R);
     }
+  }
+
+  IlSetsViewF il_view_f(int which, bool correction) {
+    IlSetsViewF v{};
+    IlBank& I = il[which];
+    for (int si = 0; si < I.n_sets; ++si) {
+      IlSet& S_ = I.set[si];
+      v.set[si] = correction ? IlSetViewF{S_.R, S_.Rr.p, S_.Y32.p, S_.W32.p, S_.D32.p}
+                             : IlSetViewF{S_.R, S_.B.p, S_.Y32.p, S_.W32.p, S_.X32.p};
+    }
+    return v;
+  }
+  bool il_f32(int which) const { return il[which].n_sets > 0 && il[which].set[0].f32; }
+  void bank_sweep(const FactorBank& bank, int which, bool correction, cudaStream_t s) {
+    if (il_f32(which))
+      bank.solve(il_view_f(which, correction), il[which].max_R, s);
+    else
+      bank.solve(il_view(which, correction), il[which].max_R, s);
   }
 
   IlSetsView il_view(int which, bool correction) {
@@ -583,39 +516,54 @@ struct Engine {
   void solve_bank_il(const FactorBank& bank, int which, int target, cudaStream_t s) {
     IlBank& I = il[which];
     const dim3 tb(32, 8);
+    const bool f32 = il_f32(which);
     for (int si = 0; si < I.n_sets; ++si) {
       IlSet& S_ = I.set[si];
       k_gather_il<<<dim3((S_.n + 31) / 32, (S_.R + 31) / 32), tb, 0, s>>>(S_.src.p, S_.B.p, S_.n, S_.R);
       PECS_CUDA(cudaGetLastError());
     }
-    bank.solve(il_view(which, false), I.max_R, s);
+    bank_sweep(bank, which, false, s);
     const int iters = ir_iters();
     for (int it = 0; it < iters; ++it) {
       for (int si = 0; si < I.n_sets; ++si) {
         IlSet& S_ = I.set[si];
         const size_t nR = (size_t)S_.n * S_.R;
+        const unsigned eg = (unsigned)((nR + 255) / 256);
         const dim3 rg((S_.n + 7) / 8, (S_.R + 31) / 32);
         if (opt.precision == PECS_PREC_FP32_MIXED) {
-          k_split_il<<<(unsigned)((nR + 255) / 256), 256, 0, s>>>(S_.X.p, S_.Xs.p, nR);
+          if (f32 && it == 0)
+            k_split_il_f<<<eg, 256, 0, s>>>(S_.X32.p, S_.X.p, S_.Xs.p, nR);
+          else
+            k_split_il<<<eg, 256, 0, s>>>(S_.X.p, S_.Xs.p, nR);
           PECS_CUDA(cudaGetLastError());
           k_residual_df_il<<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.Xs.p, S_.Rr.p, S_.n, S_.R);
         } else {
+          if (f32 && it == 0) {
+            k_widen_il<<<eg, 256, 0, s>>>(S_.X32.p, S_.X.p, nR);
+            PECS_CUDA(cudaGetLastError());
+          }
           k_residual_il<<<rg, 256, 0, s>>>(csr.m[S_.mat], S_.B.p, S_.X.p, S_.Rr.p, S_.n, S_.R);
         }
         PECS_CUDA(cudaGetLastError());
       }
-      bank.solve(il_view(which, true), I.max_R, s);
+      bank_sweep(bank, which, true, s);
       for (int si = 0; si < I.n_sets; ++si) {
         IlSet& S_ = I.set[si];
         const size_t nR = (size_t)S_.n * S_.R;
-        k_axpy_il<<<(unsigned)((nR + 255) / 256), 256, 0, s>>>(S_.X.p, S_.D.p, nR);
+        if (f32)
+          k_axpy_il<float><<<(unsigned)((nR + 255) / 256), 256, 0, s>>>(S_.X.p, S_.D32.p, nR);
+        else
+          k_axpy_il<double><<<(unsigned)((nR + 255) / 256), 256, 0, s>>>(S_.X.p, S_.D.p, nR);
         PECS_CUDA(cudaGetLastError());
       }
     }
     for (int si = 0; si < I.n_sets; ++si) {
       IlSet& S_ = I.set[si];
-      k_scatter_il<<<dim3((S_.n + 31) / 32, (S_.R + 31) / 32), tb, 0, s>>>(S_.X.p, S_.dst[target].p,
-                                                                           S_.n, S_.R);
+      const dim3 sg((S_.n + 31) / 32, (S_.R + 31) / 32);
+      if (f32 && iters == 0)
+        k_scatter_il<float><<<sg, tb, 0, s>>>(S_.X32.p, S_.dst[target].p, S_.n, S_.R);
+      else
+        k_scatter_il<double><<<sg, tb, 0, s>>>(S_.X.p, S_.dst[target].p, S_.n, S_.R);
       PECS_CUDA(cudaGetLastError());
     }
   }
@@ -732,9 +680,6 @@ struct Engine {
       }
       rhs[f].alloc(n);
       rhs[f].zero();
-      yv[f].alloc(n);
-      res[f].alloc(n);
-      delta[f].alloc(n);
       snap[f].alloc(n);
       std::vector<double> bc;
       bc.reserve(n);
@@ -747,17 +692,7 @@ struct Engine {
         init_dev[f].upload(v);
       }
     }
-    // solve pointer tables
-    int wc = 0, wp = 0;
-    auto csf = carrier_set_fields();
-    for (int nx = 0; nx < 2; ++nx) {
-      build_sets(csf, bank_c, rhs, state[nx], wbuf_c, wc, tab_c[nx][0]);
-      build_sets(csf, bank_c, res, delta, wbuf_c, wc, tab_c[nx][1]);
-      build_sets({{4}}, bank_p, rhs, state[nx], wbuf_p, wp, tab_p[nx][0]);
-      build_sets({{4}}, bank_p, res, delta, wbuf_p, wp, tab_p[nx][1]);
-    }
-    prepare_ir();
-    build_il(0, csf, bank_c);
+    build_il(0, carrier_set_fields(), bank_c);
     build_il(1, {{4}}, bank_p);
     // steady-state buffers
     partial.alloc((size_t)n_inst * 5 * kRedChunks);
@@ -948,86 +883,8 @@ struct Engine {
     PECS_CUDA(cudaGetLastError());
   }
 
-  // Device vector lists for the refinement sweeps, key = target*8 + first field.
-  struct IrLists {
-    DBuf<const double*> b, x, d;
-    DBuf<double*> out, xw;
-    DBuf<int> mat, vin, len;
-    DBuf<float2*> xs;  // split copies of x (mixed mode)
-    std::vector<DBuf<float2>> xs_store;
-    int nv = 0, n = 0;
-  };
   DBuf<float2> Adf[5];
   CsrDfSet csr_df{};
-  IrLists ir[2][2];  // [target][0 carriers, 1 Poisson]
-
-  void prepare_ir() {
-    for (int target = 0; target < 2; ++target)
-      for (int which = 0; which < 2; ++which) {
-        std::vector<int> flds = which ? std::vector<int>{4} : carrier_fields();
-        std::vector<const double*> hb, hx, hd;
-        std::vector<double*> hout, hxw;
-        std::vector<int> hm, hi, hl;
-        int n = 0;
-        for (int i = 0; i < n_inst; ++i)
-          for (int f : flds) {
-            hl.push_back(nd[f]);
-            hb.push_back(rhs[f].p + (size_t)i * nd[f]);
-            hx.push_back(state[target][f].p + (size_t)i * nd[f]);
-            hout.push_back(res[f].p + (size_t)i * nd[f]);
-            hxw.push_back(state[target][f].p + (size_t)i * nd[f]);
-            hd.push_back(delta[f].p + (size_t)i * nd[f]);
-            hm.push_back(f);
-            hi.push_back(i);
-            n = std::max(n, nd[f]);
-          }
-        IrLists& L = ir[target][which];
-        L.b.upload(hb);
-        L.x.upload(hx);
-        L.d.upload(hd);
-        L.out.upload(hout);
-        L.xw.upload(hxw);
-        L.mat.upload(hm);
-        L.vin.upload(hi);
-        L.len.upload(hl);
-        L.nv = (int)hb.size();
-        if (opt.precision == PECS_PREC_FP32_MIXED) {
-          std::vector<float2*> hs;
-          for (size_t v = 0; v < hb.size(); ++v) {
-            L.xs_store.emplace_back();
-            L.xs_store.back().alloc(hl[v]);
-            hs.push_back(L.xs_store.back().p);
-          }
-          L.xs.upload(hs);
-        }
-        L.n = n;
-      }
-  }
-
-  // x = A^-1 b into state[target]; FP32 factors add FP64-residual refinement sweeps.
-  void solve_bank(const FactorBank& bank, SetTable (&tab)[2][2], int target, int which,
-                  cudaStream_t s, const int* act) {
-    bank.solve(tab[target][0].view, tab[target][0].max_nrhs, s);
-    const int iters = ir_iters();
-    if (iters == 0) return;
-    IrLists& L = ir[target][which];
-    VecList V{L.b.p, L.x.p, L.out.p, L.mat.p, L.len.p};
-    const bool mixed = opt.precision == PECS_PREC_FP32_MIXED;
-    for (int it = 0; it < iters; ++it) {
-      if (mixed) {
-        k_split<<<dim3((L.n + 255) / 256, L.nv), 256, 0, s>>>(L.x.p, L.xs.p, L.len.p, act, L.vin.p);
-        PECS_CUDA(cudaGetLastError());
-        k_residual_df<<<dim3((L.n + 127) / 128, L.nv), 128, 0, s>>>(
-            csr_df, L.b.p, (const float2* const*)L.xs.p, L.out.p, L.mat.p, L.len.p, act, L.vin.p);
-      } else {
-        k_residual<<<dim3((L.n + 127) / 128, L.nv), 128, 0, s>>>(csr, V, L.n, act, L.vin.p);
-      }
-      PECS_CUDA(cudaGetLastError());
-      bank.solve(tab[target][1].view, tab[target][1].max_nrhs, s);
-      k_axpy<<<dim3((L.n + 255) / 256, L.nv), 256, 0, s>>>(L.xw.p, L.d.p, L.len.p, act, L.vin.p);
-      PECS_CUDA(cudaGetLastError());
-    }
-  }
 
   std::vector<int> carrier_fields() const {
     return full ? std::vector<int>{0, 1, 2, 3} : std::vector<int>{0, 1};

@@ -1,6 +1,7 @@
 // Level-scheduled multifrontal solve kernels and their host-side plan (solve.cuh).
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "solve.cuh"
 
@@ -408,7 +409,8 @@ constexpr int kPanelKcF64 = 64;   // staged columns per chunk, FP64 blocks
 constexpr size_t kPanelSmem = 160 * 1024;
 constexpr int kPanelCmMax = 4096;  // staged child-update rows per node (more: read from global)
 
-// RPL consecutive doubles of one interleaved row (offset a multiple of RPL).
+// RPL consecutive values of one interleaved row (offset a multiple of RPL),
+// double or float storage, double registers.
 template <int RPL>
 __device__ __forceinline__ void ld_rhs(const double* p, double (&v)[RPL]) {
   if constexpr (RPL == 1) {
@@ -424,6 +426,19 @@ __device__ __forceinline__ void ld_rhs(const double* p, double (&v)[RPL]) {
 }
 
 template <int RPL>
+__device__ __forceinline__ void ld_rhs(const float* p, double (&v)[RPL]) {
+  if constexpr (RPL == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+  } else if constexpr (RPL == 2) {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    v[0] = t.x, v[1] = t.y;
+  } else {
+    v[0] = p[0];
+  }
+}
+
+template <int RPL>
 __device__ __forceinline__ void st_rhs(double* p, const double (&v)[RPL]) {
   if constexpr (RPL == 1) {
     p[0] = v[0];
@@ -431,6 +446,17 @@ __device__ __forceinline__ void st_rhs(double* p, const double (&v)[RPL]) {
 #pragma unroll
     for (int q = 0; q < RPL / 2; ++q)
       reinterpret_cast<double2*>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+  }
+}
+
+template <int RPL>
+__device__ __forceinline__ void st_rhs(float* p, const double (&v)[RPL]) {
+  if constexpr (RPL == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+  } else if constexpr (RPL == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2((float)v[0], (float)v[1]);
+  } else {
+    p[0] = (float)v[0];
   }
 }
 
@@ -497,9 +523,9 @@ __host__ __device__ constexpr size_t panel_smem_bytes(int ds_rows, int rc, int k
   return ((size_t)ds_rows * rc + (size_t)kc * ri_max) * sizeof(T) + (size_t)meta_ints * sizeof(int);
 }
 
-template <typename T, int RPL, bool FWD>
+template <typename T, int RPL, bool FWD, typename SVT>
 __global__ void __launch_bounds__(kSolveThreads)
-    k_panel(BankView B, IlSetsView S, const PanelItem* __restrict__ items, int kc_cap, int ds_rows,
+    k_panel(BankView B, SVT S, const PanelItem* __restrict__ items, int kc_cap, int ds_rows,
             int ri_max, int max_s, int max_f, int cm_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int RC = 32 * RPL;
@@ -507,7 +533,7 @@ __global__ void __launch_bounds__(kSolveThreads)
   const PanelItem I = items[blockIdx.x];
   const int r0 = I.a.y, r1 = I.a.z, ri = I.a.w;
   const int s = I.b.x, m = I.b.y, f = s + m, w_off = I.b.w;
-  const IlSetView st = S.set[I.b.z];
+  const auto st = S.set[I.b.z];
   const int R = st.nrhs;
   const int rc0 = blockIdx.y * RC;
   if (rc0 >= R) return;
@@ -573,7 +599,7 @@ __global__ void __launch_bounds__(kSolveThreads)
             for (int q = 0; q < RPL; ++q) v[q] -= u[q];
           }
         } else {
-          const double* src = sr >= 0 ? st.y + (size_t)sr * R : st.x + (size_t)(~sr) * R;
+          const auto* src = sr >= 0 ? st.y + (size_t)sr * R : st.x + (size_t)(~sr) * R;
           ld_rhs<RPL>(src + rl, v);
         }
       }
@@ -668,8 +694,8 @@ PanelChoice choose_panel(const PanelPlan& L, int max_nrhs, int rpl_max, int min_
   return best;
 }
 
-template <typename T, int RPL>
-void launch_panel(bool forward, const BankView& B, const IlSetsView& S, const PanelPlan& L,
+template <typename T, int RPL, typename SVT>
+void launch_panel(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
                   const PanelTiles& P, int max_nrhs, int kcap, cudaStream_t st) {
   if (P.n_items == 0) return;
   const int kc = std::min(kcap, std::max(1, L.max_k));
@@ -679,34 +705,37 @@ void launch_panel(bool forward, const BankView& B, const IlSetsView& S, const Pa
   const size_t smem = panel_smem_bytes<T>(ds_rows, RC, kc, P.max_ri, meta);
   const dim3 grid(P.n_items, (max_nrhs + RC - 1) / RC);
   if (forward)
-    k_panel<T, RPL, true><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows, P.max_ri,
-                                                             L.max_s, L.max_f, L.cm_cap);
+    k_panel<T, RPL, true, SVT><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows,
+                                                                  P.max_ri, L.max_s, L.max_f, L.cm_cap);
   else
-    k_panel<T, RPL, false><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows, P.max_ri,
-                                                              L.max_s, L.max_f, L.cm_cap);
+    k_panel<T, RPL, false, SVT><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows,
+                                                                   P.max_ri, L.max_s, L.max_f, L.cm_cap);
   PECS_CUDA(cudaGetLastError());
 }
 
-template <typename T>
+template <typename T, typename SVT>
 void set_panel_smem_limit() {
   const int lim = (int)kPanelSmem;
-  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  PECS_CUDA(cudaFuncSetAttribute(k_panel<T, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  auto set = [&](const void* fn) {
+    PECS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  };
+  set((const void*)k_panel<T, 1, true, SVT>);
+  set((const void*)k_panel<T, 2, true, SVT>);
+  set((const void*)k_panel<T, 4, true, SVT>);
+  set((const void*)k_panel<T, 1, false, SVT>);
+  set((const void*)k_panel<T, 2, false, SVT>);
+  set((const void*)k_panel<T, 4, false, SVT>);
 }
 
-template <typename T>
-void launch_panel_level(bool forward, const BankView& B, const IlSetsView& S, const PanelPlan& L,
+template <typename T, typename SVT>
+void launch_panel_level(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
                         int max_nrhs, int rpl_max, const PanelTuning& tu, cudaStream_t st) {
   const PanelChoice c = choose_panel(L, max_nrhs, rpl_max, tu.min_ctas);
   const PanelTiles& P = L.tiles[c.cap_idx];
   switch (c.rpl) {
-    case 1: launch_panel<T, 1>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
-    case 2: launch_panel<T, 2>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
-    default: launch_panel<T, 4>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
+    case 1: launch_panel<T, 1, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
+    case 2: launch_panel<T, 2, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
+    default: launch_panel<T, 4, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
   }
 }
 }  // namespace
@@ -965,10 +994,12 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
     make_panel(bl, false, pbwd_);
     fwd_.clear();
     bwd_.clear();
-    if (prec_ == PECS_PREC_FP64)
-      set_panel_smem_limit<double>();
-    else
-      set_panel_smem_limit<float>();
+    if (prec_ == PECS_PREC_FP64) {
+      set_panel_smem_limit<double, IlSetsView>();
+    } else {
+      set_panel_smem_limit<float, IlSetsView>();
+      set_panel_smem_limit<float, IlSetsViewF>();
+    }
     return;
   }
   make(fl, true, fwd_);
@@ -1031,24 +1062,32 @@ void FactorBank::solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) co
     solve_impl(sets, max_nrhs, st);
 }
 
-void FactorBank::solve_panel(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const {
+template <typename SVT>
+void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) const {
   // right-hand sides per lane: at most as many as fill the lanes, dividing every set's count
   int rpl = max_nrhs >= 96 ? 4 : (max_nrhs >= 48 ? 2 : 1);
   for (int si = 0; si < n_sets_; ++si)
     while (rpl > 1 && sets.set[si].nrhs % rpl != 0) rpl /= 2;
   const BankView B = view();
-  for (const PanelPlan& L : pfwd_) {
-    if (prec_ == PECS_PREC_FP64)
-      launch_panel_level<double>(true, B, sets, L, max_nrhs, rpl, tune_, st);
-    else
-      launch_panel_level<float>(true, B, sets, L, max_nrhs, rpl, tune_, st);
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool fwd = pass == 0;
+    for (const PanelPlan& L : fwd ? pfwd_ : pbwd_) {
+      if constexpr (std::is_same<SVT, IlSetsViewF>::value) {
+        launch_panel_level<float, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
+      } else {
+        if (prec_ == PECS_PREC_FP64)
+          launch_panel_level<double, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
+        else
+          launch_panel_level<float, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
+      }
+    }
   }
-  for (const PanelPlan& L : pbwd_) {
-    if (prec_ == PECS_PREC_FP64)
-      launch_panel_level<double>(false, B, sets, L, max_nrhs, rpl, tune_, st);
-    else
-      launch_panel_level<float>(false, B, sets, L, max_nrhs, rpl, tune_, st);
-  }
+}
+
+void FactorBank::solve(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st) const {
+  if (!panel_ || prec_ == PECS_PREC_FP64)
+    throw PecsError(PECS_E_STATE, "float solve vectors need a panel bank with FP32 factors");
+  solve_panel(sets, max_nrhs, st);
 }
 
 }  // namespace pecs

@@ -77,6 +77,22 @@ struct IlSetsView {
   IlSetView set[kMaxSets];
 };
 
+// Interleaved layout with single-precision sweep vectors (FP32 factors on the
+// panel path): the right-hand sides stay double, y / update vectors / x are
+// float -- they carry the FP32 factors' results, and refinement adds the
+// correction to a double solution outside the sweep.
+struct IlSetViewF {
+  int nrhs;
+  const double* b;
+  float* y;
+  float* w;
+  float* x;
+};
+
+struct IlSetsViewF {
+  IlSetViewF set[kMaxSets];
+};
+
 // One level of the panel path: items (node, row0, row1, rows per tile), one
 // CTA each; every item applies its rows of the node's block to a chunk of
 // right-hand sides held in shared memory, lanes over right-hand sides.  Items
@@ -126,6 +142,7 @@ class FactorBank {
   // y = forward(b), x = backward(y); w is workspace.  All sets must be bound.
   void solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const;
   void solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const;
+  void solve(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st) const;
   int set_wtotal(int set) const { return set_wtotal_[set]; }
   int precision() const { return prec_; }
   long long entries() const { return entries_; }
@@ -150,7 +167,8 @@ class FactorBank {
   bool panel_ = false;
   PanelTuning tune_;
   int max_cols_ = 0, max_rb_ = 8;
-  void solve_panel(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const;
+  template <typename SVT>
+  void solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) const;
   BankView view() const;
   template <typename SV>
   void solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const;
