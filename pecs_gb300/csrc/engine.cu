@@ -63,9 +63,11 @@ struct CsrDfSet {
 };
 
 // ---- interleaved [dof][rhs] buffers of the batched solves --------------------
-// dst[d * R + k] = src_k[d]   (32 x 32 tiles through shared memory)
-__global__ void k_gather_il(const double* const* __restrict__ src, double* __restrict__ dst, int n,
-                            int R) {
+// dst[d * R + k] = src_k[d]   (32 x 32 tiles through shared memory); dst32,
+// when given, receives the same values rounded to float (the right-hand sides
+// of the FP32 sweeps)
+__global__ void k_gather_il(const double* const* __restrict__ src, double* __restrict__ dst,
+                            float* __restrict__ dst32, int n, int R) {
   __shared__ double t[32][33];
   const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
@@ -75,7 +77,11 @@ __global__ void k_gather_il(const double* const* __restrict__ src, double* __res
   __syncthreads();
   for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
     const int d = d0 + dd, k = k0 + threadIdx.x;
-    if (d < n && k < R) dst[(size_t)d * R + k] = t[threadIdx.x][dd];
+    if (d < n && k < R) {
+      const double v = t[threadIdx.x][dd];
+      dst[(size_t)d * R + k] = v;
+      if (dst32) dst32[(size_t)d * R + k] = (float)v;
+    }
   }
 }
 
@@ -110,14 +116,11 @@ __global__ void k_axpy_il(double* __restrict__ x, const V* __restrict__ d, size_
   if (i < n) x[i] += (double)d[i];
 }
 
-// x = (double) x32, and its FP32-pair split (exact: the low part is zero)
-__global__ void k_split_il_f(const float* __restrict__ x32, double* __restrict__ x,
-                             float2* __restrict__ xs, size_t n) {
+// x = (double) x32 + (double) d32
+__global__ void k_sum_il(const float* __restrict__ x32, const float* __restrict__ d32,
+                         double* __restrict__ x, size_t n) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float v = x32[i];
-  x[i] = (double)v;
-  xs[i] = make_float2(v, 0.f);
+  if (i < n) x[i] = (double)x32[i] + (double)d32[i];
 }
 
 __global__ void k_widen_il(const float* __restrict__ x32, double* __restrict__ x, size_t n) {
@@ -130,14 +133,20 @@ __global__ void k_widen_il(const float* __restrict__ x32, double* __restrict__ x
 // The sum runs in FP32-pair ("double-float") arithmetic: products are exact
 // through fmaf, partial sums through TwoSum, so the residual keeps ~46-bit
 // accuracy while running on the FP32 pipe.
-__global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const float2* __restrict__ xs,
-                                 double* __restrict__ r, int n, int R) {
+// X is float2 (an FP32 pair) or float (a pair with zero low part: the first
+// refinement of an FP32 sweep's solution); RT the residual's storage type.
+__device__ __forceinline__ float2 as_pair(float2 v) { return v; }
+__device__ __forceinline__ float2 as_pair(float v) { return make_float2(v, 0.f); }
+
+template <typename X, typename RT>
+__global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const X* __restrict__ xs,
+                                 RT* __restrict__ r, int n, int R) {
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int k = blockIdx.y * 32 + (threadIdx.x & 31);
   if (row >= n || k >= R) return;
   float sh = 0.f, sl = 0.f;
   for (int p = A.rp[row]; p < A.rp[row + 1]; ++p) {
-    const float2 a = A.v[p], xv = xs[(size_t)A.ci[p] * R + k];
+    const float2 a = A.v[p], xv = as_pair(xs[(size_t)A.ci[p] * R + k]);
     const float ph = a.x * xv.x;
     const float pe = fmaf(a.x, xv.x, -ph) + fmaf(a.x, xv.y, a.y * xv.x);
     const float t = sh + ph;
@@ -147,19 +156,20 @@ __global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const fl
     sl += e + pe;
   }
   const size_t o = (size_t)row * R + k;
-  r[o] = b[o] - ((double)sh + (double)sl);
+  r[o] = (RT)(b[o] - ((double)sh + (double)sl));
 }
 
 // FP64 variant (FP32_IR mode)
+template <typename RT>
 __global__ void k_residual_il(CsrDev A, const double* __restrict__ b, const double* __restrict__ x,
-                              double* __restrict__ r, int n, int R) {
+                              RT* __restrict__ r, int n, int R) {
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int k = blockIdx.y * 32 + (threadIdx.x & 31);
   if (row >= n || k >= R) return;
   double acc = 0.0;
   for (int p = A.rp[row]; p < A.rp[row + 1]; ++p) acc += A.v[p] * x[(size_t)A.ci[p] * R + k];
   const size_t o = (size_t)row * R + k;
-  r[o] = b[o] - acc;
+  r[o] = (RT)(b[o] - acc);
 }
 
 constexpr int kRedThreads = 256;
@@ -353,7 +363,7 @@ struct Engine {
     int n = 0, R = 0, mat = 0;
     bool f32 = false;              // panel bank with FP32 factors: float sweep vectors
     DBuf<double> B, Y, W, X, Rr, D;
-    DBuf<float> Y32, W32, X32, D32;
+    DBuf<float> B32, Y32, W32, X32, D32, Rr32;
     DBuf<float2> Xs;
     DBuf<const double*> src;       // rhs vector of each column
     DBuf<double*> dst[2];          // state vector of each column, per ping-pong target
@@ -380,17 +390,31 @@ struct Engine {
     if (opt.ir_max_iters > 0) return opt.ir_max_iters;
     return opt.precision == PECS_PREC_FP32_MIXED ? 1 : 2;
   }
+  // element-wise launches per set of one solve: gather, scatter and, per
+  // refinement sweep, the residual and its helpers (split / widen, axpy / sum)
+  int set_launches_per_solve(int which) const {
+    const int iters = ir_iters();
+    const bool mixed = opt.precision == PECS_PREC_FP32_MIXED;
+    int n = 2;
+    for (int it = 0; it < iters; ++it) {
+      if (il_f32(which))
+        n += mixed ? (it == 0 ? 2 : 3) : (it == 0 ? 3 : 2);
+      else
+        n += mixed ? 3 : 2;
+    }
+    return n;
+  }
   int launches_per_step() const {
     const int it = ir_iters();
-    const int per_it = opt.precision == PECS_PREC_FP32_MIXED ? 3 : 2;  // (split,) residual, axpy
     const int lc = bank_c.kernel_launches_per_solve(), lp = bank_p.kernel_launches_per_solve();
     const int sc = il[0].n_sets, sp = il[1].n_sets;
-    return 1 + lc * (1 + it) + sc * (2 + per_it * it) + 1 + lp * (1 + it) + sp * (2 + per_it * it) + 3;
+    return 1 + lc * (1 + it) + sc * set_launches_per_solve(0) + 1 + lp * (1 + it) +
+           sp * set_launches_per_solve(1) + 3;
   }
   // algorithmic bytes of one application of a bank to all of its right-hand
-  // sides: every stored factor entry once, plus the vectors (b read in FP64;
-  // y write + read, x write, update vectors write + read, in the sweep's
-  // vector type: float for FP32 panel banks, else double)
+  // sides: every stored factor entry once, plus the vectors (b read, y write +
+  // read, x write, update vectors write + read, in the sweep's vector type:
+  // float for FP32 panel banks, else double)
   double solve_bytes(int which) const {
     const FactorBank& B = which == 0 ? bank_c : bank_p;
     const IlBank& I = il[which];
@@ -398,7 +422,7 @@ struct Engine {
     for (int si = 0; si < I.n_sets; ++si) {
       const IlSet& S_ = I.set[si];
       const double vb = S_.f32 ? 4.0 : 8.0;
-      vec += (double)S_.R * ((8.0 + 3.0 * vb) * S_.n + 2.0 * vb * B.set_wtotal(si));
+      vec += (double)S_.R * (4.0 * vb * S_.n + 2.0 * vb * B.set_wtotal(si));
     }
     return (double)B.bytes() + vec;
   }
@@ -451,6 +475,7 @@ struct Engine {
       S_.B.alloc(nR);
       S_.X.alloc(nR);
       if (S_.f32) {
+        S_.B32.alloc(nR);
         S_.Y32.alloc(nR);
         S_.X32.alloc(nR);
         S_.W32.alloc((size_t)bank.set_wtotal(si) * S_.R);
@@ -461,11 +486,13 @@ struct Engine {
         S_.W.zero();
       }
       if (opt.precision != PECS_PREC_FP64) {
-        S_.Rr.alloc(nR);
-        if (S_.f32)
+        if (S_.f32) {
+          S_.Rr32.alloc(nR);
           S_.D32.alloc(nR);
-        else
+        } else {
+          S_.Rr.alloc(nR);
           S_.D.alloc(nR);
+        }
         if (opt.precision == PECS_PREC_FP32_MIXED) S_.Xs.alloc(nR);
       }
       std::vector<const double*> src;
@@ -486,8 +513,8 @@ struct Engine {
     IlBank& I = il[which];
     for (int si = 0; si < I.n_sets; ++si) {
       IlSet& S_ = I.set[si];
-      v.set[si] = correction ? IlSetViewF{S_.R, S_.Rr.p, S_.Y32.p, S_.W32.p, S_.D32.p}
-                             : IlSetViewF{S_.R, S_.B.p, S_.Y32.p, S_.W32.p, S_.X32.p};
+      v.set[si] = correction ? IlSetViewF{S_.R, S_.Rr32.p, S_.Y32.p, S_.W32.p, S_.D32.p}
+                             : IlSetViewF{S_.R, S_.B32.p, S_.Y32.p, S_.W32.p, S_.X32.p};
     }
     return v;
   }
@@ -517,32 +544,45 @@ struct Engine {
     IlBank& I = il[which];
     const dim3 tb(32, 8);
     const bool f32 = il_f32(which);
+    const bool mixed = opt.precision == PECS_PREC_FP32_MIXED;
     for (int si = 0; si < I.n_sets; ++si) {
       IlSet& S_ = I.set[si];
-      k_gather_il<<<dim3((S_.n + 31) / 32, (S_.R + 31) / 32), tb, 0, s>>>(S_.src.p, S_.B.p, S_.n, S_.R);
+      k_gather_il<<<dim3((S_.n + 31) / 32, (S_.R + 31) / 32), tb, 0, s>>>(
+          S_.src.p, S_.B.p, f32 ? S_.B32.p : nullptr, S_.n, S_.R);
       PECS_CUDA(cudaGetLastError());
     }
     bank_sweep(bank, which, false, s);
     const int iters = ir_iters();
+    auto egrid = [](size_t nR) { return (unsigned)((nR + 255) / 256); };
     for (int it = 0; it < iters; ++it) {
       for (int si = 0; si < I.n_sets; ++si) {
         IlSet& S_ = I.set[si];
         const size_t nR = (size_t)S_.n * S_.R;
-        const unsigned eg = (unsigned)((nR + 255) / 256);
         const dim3 rg((S_.n + 7) / 8, (S_.R + 31) / 32);
-        if (opt.precision == PECS_PREC_FP32_MIXED) {
-          if (f32 && it == 0)
-            k_split_il_f<<<eg, 256, 0, s>>>(S_.X32.p, S_.X.p, S_.Xs.p, nR);
-          else
-            k_split_il<<<eg, 256, 0, s>>>(S_.X.p, S_.Xs.p, nR);
-          PECS_CUDA(cudaGetLastError());
-          k_residual_df_il<<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.Xs.p, S_.Rr.p, S_.n, S_.R);
-        } else {
-          if (f32 && it == 0) {
-            k_widen_il<<<eg, 256, 0, s>>>(S_.X32.p, S_.X.p, nR);
+        if (f32) {
+          // FP32 sweep vectors: the residual is stored in float for the next sweep
+          if (mixed && it == 0) {
+            k_residual_df_il<float, float><<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.X32.p,
+                                                              S_.Rr32.p, S_.n, S_.R);
+          } else if (mixed) {
+            k_split_il<<<egrid(nR), 256, 0, s>>>(S_.X.p, S_.Xs.p, nR);
             PECS_CUDA(cudaGetLastError());
+            k_residual_df_il<float2, float><<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.Xs.p,
+                                                               S_.Rr32.p, S_.n, S_.R);
+          } else {
+            if (it == 0) {
+              k_widen_il<<<egrid(nR), 256, 0, s>>>(S_.X32.p, S_.X.p, nR);
+              PECS_CUDA(cudaGetLastError());
+            }
+            k_residual_il<float><<<rg, 256, 0, s>>>(csr.m[S_.mat], S_.B.p, S_.X.p, S_.Rr32.p, S_.n, S_.R);
           }
-          k_residual_il<<<rg, 256, 0, s>>>(csr.m[S_.mat], S_.B.p, S_.X.p, S_.Rr.p, S_.n, S_.R);
+        } else if (mixed) {
+          k_split_il<<<egrid(nR), 256, 0, s>>>(S_.X.p, S_.Xs.p, nR);
+          PECS_CUDA(cudaGetLastError());
+          k_residual_df_il<float2, double><<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.Xs.p,
+                                                              S_.Rr.p, S_.n, S_.R);
+        } else {
+          k_residual_il<double><<<rg, 256, 0, s>>>(csr.m[S_.mat], S_.B.p, S_.X.p, S_.Rr.p, S_.n, S_.R);
         }
         PECS_CUDA(cudaGetLastError());
       }
@@ -550,10 +590,12 @@ struct Engine {
       for (int si = 0; si < I.n_sets; ++si) {
         IlSet& S_ = I.set[si];
         const size_t nR = (size_t)S_.n * S_.R;
-        if (f32)
-          k_axpy_il<float><<<(unsigned)((nR + 255) / 256), 256, 0, s>>>(S_.X.p, S_.D32.p, nR);
+        if (f32 && mixed && it == 0)
+          k_sum_il<<<egrid(nR), 256, 0, s>>>(S_.X32.p, S_.D32.p, S_.X.p, nR);
+        else if (f32)
+          k_axpy_il<float><<<egrid(nR), 256, 0, s>>>(S_.X.p, S_.D32.p, nR);
         else
-          k_axpy_il<double><<<(unsigned)((nR + 255) / 256), 256, 0, s>>>(S_.X.p, S_.D.p, nR);
+          k_axpy_il<double><<<egrid(nR), 256, 0, s>>>(S_.X.p, S_.D.p, nR);
         PECS_CUDA(cudaGetLastError());
       }
     }

@@ -410,47 +410,49 @@ constexpr size_t kPanelSmem = 160 * 1024;
 constexpr int kPanelCmMax = 4096;  // staged child-update rows per node (more: read from global)
 
 // RPL consecutive values of one interleaved row (offset a multiple of RPL),
-// double or float storage, double registers.
-template <int RPL>
-__device__ __forceinline__ void ld_rhs(const double* p, double (&v)[RPL]) {
+// double or float storage, registers of type VR (the storage type converts
+// only where the two differ -- on GB300 every FP64 operation, conversions
+// included, runs on the narrow FP64 unit, so the FP32 path keeps none).
+template <int RPL, typename VR>
+__device__ __forceinline__ void ld_rhs(const double* p, VR (&v)[RPL]) {
   if constexpr (RPL == 1) {
-    v[0] = p[0];
+    v[0] = (VR)p[0];
   } else {
 #pragma unroll
     for (int q = 0; q < RPL / 2; ++q) {
       const double2 t = reinterpret_cast<const double2*>(p)[q];
-      v[2 * q] = t.x;
-      v[2 * q + 1] = t.y;
+      v[2 * q] = (VR)t.x;
+      v[2 * q + 1] = (VR)t.y;
     }
   }
 }
 
-template <int RPL>
-__device__ __forceinline__ void ld_rhs(const float* p, double (&v)[RPL]) {
+template <int RPL, typename VR>
+__device__ __forceinline__ void ld_rhs(const float* p, VR (&v)[RPL]) {
   if constexpr (RPL == 4) {
     const float4 t = *reinterpret_cast<const float4*>(p);
-    v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+    v[0] = (VR)t.x, v[1] = (VR)t.y, v[2] = (VR)t.z, v[3] = (VR)t.w;
   } else if constexpr (RPL == 2) {
     const float2 t = *reinterpret_cast<const float2*>(p);
-    v[0] = t.x, v[1] = t.y;
+    v[0] = (VR)t.x, v[1] = (VR)t.y;
   } else {
-    v[0] = p[0];
+    v[0] = (VR)p[0];
   }
 }
 
-template <int RPL>
-__device__ __forceinline__ void st_rhs(double* p, const double (&v)[RPL]) {
+template <int RPL, typename VR>
+__device__ __forceinline__ void st_rhs(double* p, const VR (&v)[RPL]) {
   if constexpr (RPL == 1) {
-    p[0] = v[0];
+    p[0] = (double)v[0];
   } else {
 #pragma unroll
     for (int q = 0; q < RPL / 2; ++q)
-      reinterpret_cast<double2*>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+      reinterpret_cast<double2*>(p)[q] = make_double2((double)v[2 * q], (double)v[2 * q + 1]);
   }
 }
 
-template <int RPL>
-__device__ __forceinline__ void st_rhs(float* p, const double (&v)[RPL]) {
+template <int RPL, typename VR>
+__device__ __forceinline__ void st_rhs(float* p, const VR (&v)[RPL]) {
   if constexpr (RPL == 4) {
     *reinterpret_cast<float4*>(p) = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
   } else if constexpr (RPL == 2) {
@@ -485,8 +487,8 @@ __device__ __forceinline__ void lds(const T* p, T (&v)[N]) {
   }
 }
 
-template <typename T, int N>
-__device__ __forceinline__ void sts(T* p, const double (&v)[N]) {
+template <typename T, int N, typename VR>
+__device__ __forceinline__ void sts(T* p, const VR (&v)[N]) {
   if constexpr (sizeof(T) == 4 && N % 4 == 0) {
 #pragma unroll
     for (int q = 0; q < N / 4; ++q)
@@ -495,7 +497,7 @@ __device__ __forceinline__ void sts(T* p, const double (&v)[N]) {
   } else if constexpr (sizeof(T) == 8 && N % 2 == 0) {
 #pragma unroll
     for (int q = 0; q < N / 2; ++q)
-      reinterpret_cast<double2*>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+      reinterpret_cast<double2*>(p)[q] = make_double2((double)v[2 * q], (double)v[2 * q + 1]);
   } else {
 #pragma unroll
     for (int q = 0; q < N; ++q) p[q] = (T)v[q];
@@ -540,6 +542,9 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int rl = rc0 + lane * RPL;  // first right-hand side of this lane
   const bool lane_ok = rl < R;      // R is a multiple of RPL
+  // staging / output arithmetic in the sweep vectors' type (float for FP32
+  // panel banks: no FP64 work at all)
+  using VS = typename std::remove_cv<typename std::remove_pointer<decltype(st.y)>::type>::type;
   const int K = FWD ? s : f;
   const int ld = FWD ? f : s;
   const T* M = static_cast<const T*>(FWD ? B.G : B.H) + (((long long)I.c.y << 32) | (unsigned)I.c.x);
@@ -585,15 +590,15 @@ __global__ void __launch_bounds__(kSolveThreads)
     for (int k = warp; k < kc; k += NW) {
       const int p = k0 + k;
       const int sr = src_s[p];
-      double v[RPL];
+      VS v[RPL];
 #pragma unroll
-      for (int q = 0; q < RPL; ++q) v[q] = 0.0;
+      for (int q = 0; q < RPL; ++q) v[q] = VS(0);
       if (lane_ok) {
         if (FWD) {
           ld_rhs<RPL>(st.b + (size_t)sr * R + rl, v);
           for (int c = cp_s[p]; c < cp_s[p + 1]; ++c) {
             const int wi = c < cm_cap ? cm_s[c] : B.cmap_idx[cbase + c];
-            double u[RPL];
+            VS u[RPL];
             ld_rhs<RPL>(st.w + (size_t)wi * R + rl, u);
 #pragma unroll
             for (int q = 0; q < RPL; ++q) v[q] -= u[q];
@@ -618,7 +623,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     __syncthreads();
   }
   // row i of the item -> its destination
-  auto emit = [&](int i, double (&v)[RPL]) {
+  auto emit = [&](int i, VS (&v)[RPL]) {
     const int row = r0 + i;
     if (FWD) {
       if (row < s) {
@@ -626,7 +631,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       } else {
         for (int c = cp_s[row]; c < cp_s[row + 1]; ++c) {
           const int wi = c < cm_cap ? cm_s[c] : B.cmap_idx[cbase + c];
-          double u[RPL];
+          VS u[RPL];
           ld_rhs<RPL>(st.w + (size_t)wi * R + rl, u);
 #pragma unroll
           for (int q = 0; q < RPL; ++q) v[q] += u[q];
@@ -642,9 +647,9 @@ __global__ void __launch_bounds__(kSolveThreads)
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       if (4 * g + i < nrows) {
-        double v[RPL];
+        VS v[RPL];
 #pragma unroll
-        for (int q = 0; q < RPL; ++q) v[q] = (double)acc[i][q];
+        for (int q = 0; q < RPL; ++q) v[q] = (VS)acc[i][q];
         emit(4 * g + i, v);
       }
     }
@@ -658,12 +663,12 @@ __global__ void __launch_bounds__(kSolveThreads)
     __syncthreads();
     if (!lane_ok) return;
     for (int i = warp; i < nrows; i += NW) {
-      double v[RPL];
+      VS v[RPL];
 #pragma unroll
       for (int q = 0; q < RPL; ++q) {
         T t = T(0);
         for (int p = 0; p < wpr; ++p) t += red[((size_t)p * ri + i) * RC + lane * RPL + q];
-        v[q] = (double)t;
+        v[q] = (VS)t;
       }
       emit(i, v);
     }

@@ -78,12 +78,12 @@ struct IlSetsView {
 };
 
 // Interleaved layout with single-precision sweep vectors (FP32 factors on the
-// panel path): the right-hand sides stay double, y / update vectors / x are
-// float -- they carry the FP32 factors' results, and refinement adds the
-// correction to a double solution outside the sweep.
+// panel path): b, y, update vectors and x are float -- they carry the FP32
+// factors' results; refinement forms residuals in double-float and adds the
+// correction to the solution outside the sweep.
 struct IlSetViewF {
   int nrhs;
-  const double* b;
+  const float* b;
   float* y;
   float* w;
   float* x;
