@@ -406,6 +406,10 @@ void launch_rb(int rb, bool forward, const BankView& B, const SV& S, const Level
 // ---- panel path --------------------------------------------------------------
 constexpr int kPanelKcF32 = 128;  // staged columns per chunk, FP32 blocks
 constexpr int kPanelKcF64 = 64;   // staged columns per chunk, FP64 blocks
+// chunk sizes the launch may fall back to (per-level child-row counts are
+// precomputed for each)
+constexpr int kPanelKcSteps = 8;
+constexpr int kPanelKc[kPanelKcSteps] = {128, 64, 32, 16, 8, 4, 2, 1};
 constexpr size_t kPanelSmem = 160 * 1024;
 constexpr int kPanelCmMax = 4096;  // staged child-update rows per node (more: read from global)
 
@@ -511,24 +515,58 @@ __device__ __forceinline__ void sts(T* p, const VR (&v)[N]) {
 // 4g..4g+3 of the tile and the chunk columns k = part (mod 32 / ri); partial
 // sums of the column parts are added through shared memory.
 //
-// The kernel is bound by the latency of dependent loads, so it is written to
-// keep their chain short: the item record carries everything about its node
-// (sizes, offsets, the node's child-update list range); one round of loads by
-// all threads stages the node's index metadata (source rows, child-update
-// ranges and rows) and the block tile in shared memory; the next round gathers
-// the right-hand-side rows (lanes over right-hand sides, coalesced) and
-// subtracts the children's updates; then the register tiles accumulate and the
-// rows are written.
+// The kernel is bound by memory latency, so each column chunk is staged with
+// asynchronous copies (cp.async: global -> shared without registers): the
+// block tile, the chunk's right-hand-side rows (lanes over right-hand sides,
+// coalesced) and, in the forward sweep, the children's update rows that land
+// on the chunk's columns are all in flight at once, followed by one wait.
+// The item record carries everything about its node (sizes, offsets, the
+// node's child-map range), and the node's index metadata is staged once, so
+// the chain of dependent loads per item is: record -> metadata -> copies.
 template <typename T>
 __host__ __device__ constexpr size_t panel_smem_bytes(int ds_rows, int rc, int kc, int ri_max,
-                                                      int meta_ints) {
-  return ((size_t)ds_rows * rc + (size_t)kc * ri_max) * sizeof(T) + (size_t)meta_ints * sizeof(int);
+                                                      int sc_rows, int meta_ints) {
+  return ((size_t)ds_rows * rc + (size_t)kc * ri_max + (size_t)sc_rows * rc) * sizeof(T) +
+         (size_t)meta_ints * sizeof(int);
+}
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gmem), "n"(BYTES)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// RPL consecutive T of one interleaved row -> shared memory (16-byte pieces
+// where the row segment allows; zero fill for lanes past the last RHS)
+template <typename T, int RPL>
+__device__ __forceinline__ void stage_row(T* dst, const T* src, bool ok) {
+  constexpr int BYTES = RPL * (int)sizeof(T);
+  if (!ok) {
+#pragma unroll
+    for (int q = 0; q < RPL; ++q) dst[q] = T(0);
+    return;
+  }
+  if constexpr (BYTES <= 16) {
+    cp_async<BYTES>(dst, src);
+  } else {
+#pragma unroll
+    for (int o = 0; o < BYTES / 16; ++o) cp_async<16>(reinterpret_cast<char*>(dst) + 16 * o,
+                                                      reinterpret_cast<const char*>(src) + 16 * o);
+  }
 }
 
 template <typename T, int RPL, bool FWD, typename SVT>
 __global__ void __launch_bounds__(kSolveThreads)
     k_panel(BankView B, SVT S, const PanelItem* __restrict__ items, int kc_cap, int ds_rows,
-            int ri_max, int max_s, int max_f, int cm_cap) {
+            int ri_max, int sc_rows, int max_s, int max_f, int cm_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int RC = 32 * RPL;
   constexpr int NW = kSolveThreads / 32;
@@ -536,15 +574,15 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int r0 = I.a.y, r1 = I.a.z, ri = I.a.w;
   const int s = I.b.x, m = I.b.y, f = s + m, w_off = I.b.w;
   const auto st = S.set[I.b.z];
+  // the sweep vectors have the block's type (FP64 banks: double, FP32: float)
+  static_assert(std::is_same<typename std::remove_cv<typename std::remove_pointer<decltype(st.y)>::type>::type,
+                             T>::value, "sweep vectors must have the block's type");
   const int R = st.nrhs;
   const int rc0 = blockIdx.y * RC;
   if (rc0 >= R) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int rl = rc0 + lane * RPL;  // first right-hand side of this lane
   const bool lane_ok = rl < R;      // R is a multiple of RPL
-  // staging / output arithmetic in the sweep vectors' type (float for FP32
-  // panel banks: no FP64 work at all)
-  using VS = typename std::remove_cv<typename std::remove_pointer<decltype(st.y)>::type>::type;
   const int K = FWD ? s : f;
   const int ld = FWD ? f : s;
   const T* M = static_cast<const T*>(FWD ? B.G : B.H) + (((long long)I.c.y << 32) | (unsigned)I.c.x);
@@ -553,11 +591,12 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int g = warp / wpr, part = warp % wpr;
   T* Ds = reinterpret_cast<T*>(smem_raw);  // [ds_rows][RC], ds_rows >= 32 when ri < 32
   T* Gs = Ds + (size_t)ds_rows * RC;        // [kc_cap][ri]
+  T* Sc = Gs + (size_t)kc_cap * ri_max;     // [sc_rows][RC] child-update rows of a chunk
   // index metadata of the whole node:
   //   forward:  src_s[s] = own rows; cp_s[f + 1] = child-update ranges per front
   //             position (relative to the node's first entry); cm_s = child rows
   //   backward: src_s[f] = own rows (y) / ~update rows (x)
-  int* src_s = reinterpret_cast<int*>(Gs + (size_t)kc_cap * ri_max);
+  int* src_s = reinterpret_cast<int*>(Sc + (size_t)sc_rows * RC);
   int* cp_s = src_s + (FWD ? max_s : max_f);
   int* cm_s = cp_s + max_f + 1;
   const int cbase = I.d.y, ncm = I.d.z;
@@ -574,6 +613,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       for (int p = tid; p < f; p += kSolveThreads) src_s[p] = p < s ? own[p] : ~upd[p - s];
     }
   }
+  __syncthreads();
   T acc[4][RPL];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -581,36 +621,51 @@ __global__ void __launch_bounds__(kSolveThreads)
     for (int q = 0; q < RPL; ++q) acc[i][q] = T(0);
   for (int k0 = 0; k0 < K; k0 += kc_cap) {
     const int kc = min(kc_cap, K - k0);
+    // (A) asynchronous copies: block tile, right-hand-side rows, child rows
     for (int idx = tid; idx < kc * ri; idx += kSolveThreads) {
       const int k = idx / ri, i = idx - k * ri;
-      Gs[idx] = i < nrows ? __ldg(M + (size_t)(k0 + k) * ld + r0 + i) : T(0);
+      if (i < nrows)
+        cp_async<sizeof(T)>(Gs + idx, M + (size_t)(k0 + k) * ld + r0 + i);
+      else
+        Gs[idx] = T(0);
     }
-    __syncthreads();  // metadata (first chunk) and block tile staged
-#pragma unroll 4
     for (int k = warp; k < kc; k += NW) {
-      const int p = k0 + k;
-      const int sr = src_s[p];
-      VS v[RPL];
-#pragma unroll
-      for (int q = 0; q < RPL; ++q) v[q] = VS(0);
-      if (lane_ok) {
-        if (FWD) {
-          ld_rhs<RPL>(st.b + (size_t)sr * R + rl, v);
-          for (int c = cp_s[p]; c < cp_s[p + 1]; ++c) {
-            const int wi = c < cm_cap ? cm_s[c] : B.cmap_idx[cbase + c];
-            VS u[RPL];
-            ld_rhs<RPL>(st.w + (size_t)wi * R + rl, u);
+      const int sr = src_s[k0 + k];
+      const T* src = FWD ? st.b + (size_t)sr * R
+                         : (sr >= 0 ? st.y + (size_t)sr * R : st.x + (size_t)(~sr) * R);
+      stage_row<T, RPL>(Ds + (size_t)k * RC + lane * RPL, src + rl, lane_ok);
+    }
+    int cb = 0;
+    if (FWD) {
+      cb = cp_s[k0];
+      const int ne = cp_s[k0 + kc] - cb;  // <= sc_rows (plan)
+      for (int e = warp; e < ne; e += NW) {
+        const int c = cb + e;
+        const int wi = c < cm_cap ? cm_s[c] : B.cmap_idx[cbase + c];
+        stage_row<T, RPL>(Sc + (size_t)e * RC + lane * RPL, st.w + (size_t)wi * R + rl, lane_ok);
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (FWD) {
+      // (B) subtract the children's updates from the staged right-hand sides
+      for (int k = warp; k < kc; k += NW) {
+        const int p = k0 + k;
+        const int e0 = cp_s[p] - cb, e1 = cp_s[p + 1] - cb;
+        if (e1 > e0) {
+          T v[RPL], u[RPL];
+          lds<T, RPL>(Ds + (size_t)k * RC + lane * RPL, v);
+          for (int e = e0; e < e1; ++e) {
+            lds<T, RPL>(Sc + (size_t)e * RC + lane * RPL, u);
 #pragma unroll
             for (int q = 0; q < RPL; ++q) v[q] -= u[q];
           }
-        } else {
-          const auto* src = sr >= 0 ? st.y + (size_t)sr * R : st.x + (size_t)(~sr) * R;
-          ld_rhs<RPL>(src + rl, v);
+          sts<T, RPL>(Ds + (size_t)k * RC + lane * RPL, v);
         }
       }
-      sts<T, RPL>(Ds + (size_t)k * RC + lane * RPL, v);
+      __syncthreads();
     }
-    __syncthreads();
+    // (C) register tiles
     for (int k = part; k < kc; k += wpr) {
       T gv[4], dv[RPL];
       lds<T, 4>(Gs + k * ri + 4 * g, gv);
@@ -623,7 +678,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     __syncthreads();
   }
   // row i of the item -> its destination
-  auto emit = [&](int i, VS (&v)[RPL]) {
+  auto emit = [&](int i, T (&v)[RPL]) {
     const int row = r0 + i;
     if (FWD) {
       if (row < s) {
@@ -631,7 +686,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       } else {
         for (int c = cp_s[row]; c < cp_s[row + 1]; ++c) {
           const int wi = c < cm_cap ? cm_s[c] : B.cmap_idx[cbase + c];
-          VS u[RPL];
+          T u[RPL];
           ld_rhs<RPL>(st.w + (size_t)wi * R + rl, u);
 #pragma unroll
           for (int q = 0; q < RPL; ++q) v[q] += u[q];
@@ -645,14 +700,8 @@ __global__ void __launch_bounds__(kSolveThreads)
   if (wpr == 1) {
     if (!lane_ok) return;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (4 * g + i < nrows) {
-        VS v[RPL];
-#pragma unroll
-        for (int q = 0; q < RPL; ++q) v[q] = (VS)acc[i][q];
-        emit(4 * g + i, v);
-      }
-    }
+    for (int i = 0; i < 4; ++i)
+      if (4 * g + i < nrows) emit(4 * g + i, acc[i]);
   } else {
     T* red = Ds;  // [wpr][ri][RC] = 32 * RC values
 #pragma unroll
@@ -663,12 +712,12 @@ __global__ void __launch_bounds__(kSolveThreads)
     __syncthreads();
     if (!lane_ok) return;
     for (int i = warp; i < nrows; i += NW) {
-      VS v[RPL];
+      T v[RPL];
 #pragma unroll
       for (int q = 0; q < RPL; ++q) {
         T t = T(0);
         for (int p = 0; p < wpr; ++p) t += red[((size_t)p * ri + i) * RC + lane * RPL + q];
-        v[q] = (VS)t;
+        v[q] = t;
       }
       emit(i, v);
     }
@@ -703,18 +752,28 @@ template <typename T, int RPL, typename SVT>
 void launch_panel(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
                   const PanelTiles& P, int max_nrhs, int kcap, cudaStream_t st) {
   if (P.n_items == 0) return;
-  const int kc = std::min(kcap, std::max(1, L.max_k));
   constexpr int RC = 32 * RPL;
-  const int ds_rows = P.min_ri < 32 ? std::max(kc, 32) : kc;
   const int meta = forward ? L.max_s + L.max_f + 1 + L.cm_cap : L.max_f;
-  const size_t smem = panel_smem_bytes<T>(ds_rows, RC, kc, P.max_ri, meta);
+  // columns per chunk: the tuned cap, halved until the chunk's staging fits
+  int ci = 0;
+  while (ci + 1 < kPanelKcSteps && (kPanelKc[ci] > kcap || kPanelKc[ci + 1] >= std::max(1, L.max_k))) ++ci;
+  size_t smem = 0;
+  int kc = 1, ds_rows = 32, sc_rows = 0;
+  for (;; ++ci) {
+    kc = std::min(kPanelKc[ci], std::max(1, L.max_k));
+    ds_rows = P.min_ri < 32 ? std::max(kc, 32) : kc;
+    sc_rows = forward ? L.sc_rows[ci] : 0;
+    smem = panel_smem_bytes<T>(ds_rows, RC, kc, P.max_ri, sc_rows, meta);
+    if (smem <= kPanelSmem || ci + 1 == kPanelKcSteps) break;
+  }
+  if (smem > kPanelSmem) throw PecsError(PECS_E_ARG, "panel staging exceeds shared memory");
   const dim3 grid(P.n_items, (max_nrhs + RC - 1) / RC);
   if (forward)
-    k_panel<T, RPL, true, SVT><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows,
-                                                                  P.max_ri, L.max_s, L.max_f, L.cm_cap);
+    k_panel<T, RPL, true, SVT><<<grid, kSolveThreads, smem, st>>>(
+        B, S, P.items.p, kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap);
   else
-    k_panel<T, RPL, false, SVT><<<grid, kSolveThreads, smem, st>>>(B, S, P.items.p, kc, ds_rows,
-                                                                   P.max_ri, L.max_s, L.max_f, L.cm_cap);
+    k_panel<T, RPL, false, SVT><<<grid, kSolveThreads, smem, st>>>(
+        B, S, P.items.p, kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap);
   PECS_CUDA(cudaGetLastError());
 }
 
@@ -963,6 +1022,18 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
         out[l].max_s = max_s;
         out[l].max_f = max_f;
         out[l].cm_cap = std::min(max_cm, kPanelCmMax);
+        // forward: most child-update rows landing on one chunk of columns
+        for (int ci = 0; ci < kPanelKcSteps; ++ci) {
+          int mx = 0;
+          if (forward) {
+            const int kc = kPanelKc[ci];
+            for (int g : lv[l].nodes) {
+              const int* cp = cmap_ptr.data() + cm_off[g];
+              for (int k0 = 0; k0 < hs[g]; k0 += kc) mx = std::max(mx, cp[std::min(k0 + kc, hs[g])] - cp[k0]);
+            }
+          }
+          out[l].sc_rows[ci] = mx;
+        }
         for (int ci = 0; ci < 4; ++ci) {
           const int cap = 32 >> ci;
           std::vector<PanelItem> items;
@@ -999,12 +1070,10 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
     make_panel(bl, false, pbwd_);
     fwd_.clear();
     bwd_.clear();
-    if (prec_ == PECS_PREC_FP64) {
+    if (prec_ == PECS_PREC_FP64)
       set_panel_smem_limit<double, IlSetsView>();
-    } else {
-      set_panel_smem_limit<float, IlSetsView>();
+    else
       set_panel_smem_limit<float, IlSetsViewF>();
-    }
     return;
   }
   make(fl, true, fwd_);
@@ -1061,6 +1130,8 @@ void FactorBank::solve(const SetsView& sets, int max_nrhs, cudaStream_t st) cons
 }
 
 void FactorBank::solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const {
+  if (panel_ && prec_ != PECS_PREC_FP64)
+    throw PecsError(PECS_E_STATE, "FP32 panel banks take float sweep vectors");
   if (panel_)
     solve_panel(sets, max_nrhs, st);
   else
@@ -1077,14 +1148,10 @@ void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) con
   for (int pass = 0; pass < 2; ++pass) {
     const bool fwd = pass == 0;
     for (const PanelPlan& L : fwd ? pfwd_ : pbwd_) {
-      if constexpr (std::is_same<SVT, IlSetsViewF>::value) {
+      if constexpr (std::is_same<SVT, IlSetsViewF>::value)
         launch_panel_level<float, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
-      } else {
-        if (prec_ == PECS_PREC_FP64)
-          launch_panel_level<double, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
-        else
-          launch_panel_level<float, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
-      }
+      else
+        launch_panel_level<double, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
     }
   }
 }

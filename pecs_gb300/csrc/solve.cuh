@@ -117,6 +117,7 @@ struct PanelPlan {
   int max_k = 0;   // largest column count of the level's nodes
   int max_s = 1, max_f = 1;
   int cm_cap = 0;  // child-map entries staged per node (the level's largest, capped)
+  int sc_rows[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // forward: child rows per chunk, per chunk size
   PanelTiles tiles[4];
 };
 
