@@ -110,7 +110,7 @@ typedef struct pecs_options {
   int panel_chunk;     /* panel solve kernels (>= 32 right-hand sides per factor): staged
                           block columns per chunk (0 = default: 128 FP32, 64 FP64) */
   int panel_min_ctas;  /* panel solve kernels: CTAs a level must reach before shorter row
-                          tiles or fewer right-hand sides per CTA are used (0 = default 304) */
+                          tiles or fewer right-hand sides per CTA are used (0 = default 152) */
 } pecs_options;
 
 typedef struct pecs_info {

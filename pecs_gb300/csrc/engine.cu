@@ -116,6 +116,24 @@ __global__ void k_axpy_il(double* __restrict__ x, const V* __restrict__ d, size_
   if (i < n) x[i] += (double)d[i];
 }
 
+// dst_k[d] = (double) x32[d * R + k] + (double) d32[d * R + k]: the refined
+// solution of an FP32 sweep and its one correction, written to the state
+__global__ void k_scatter_sum_il(const float* __restrict__ x32, const float* __restrict__ d32,
+                                 double* const* __restrict__ dst, int n, int R) {
+  __shared__ double t[32][33];
+  const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
+    const int d = d0 + dd, k = k0 + threadIdx.x;
+    const size_t o = (size_t)d * R + k;
+    t[dd][threadIdx.x] = (d < n && k < R) ? (double)x32[o] + (double)d32[o] : 0.0;
+  }
+  __syncthreads();
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k = k0 + kk, d = d0 + threadIdx.x;
+    if (k < R && d < n) dst[k][d] = t[threadIdx.x][kk];
+  }
+}
+
 // x = (double) x32 + (double) d32
 __global__ void k_sum_il(const float* __restrict__ x32, const float* __restrict__ d32,
                          double* __restrict__ x, size_t n) {
@@ -398,7 +416,7 @@ struct Engine {
     int n = 2;
     for (int it = 0; it < iters; ++it) {
       if (il_f32(which))
-        n += mixed ? (it == 0 ? 2 : 3) : (it == 0 ? 3 : 2);
+        n += mixed ? (it == 0 ? (iters == 1 ? 1 : 2) : 3) : (it == 0 ? 3 : 2);
       else
         n += mixed ? 3 : 2;
     }
@@ -590,6 +608,8 @@ struct Engine {
       for (int si = 0; si < I.n_sets; ++si) {
         IlSet& S_ = I.set[si];
         const size_t nR = (size_t)S_.n * S_.R;
+        if (f32 && mixed && it == 0 && iters == 1)
+          continue;  // the scatter adds the correction
         if (f32 && mixed && it == 0)
           k_sum_il<<<egrid(nR), 256, 0, s>>>(S_.X32.p, S_.D32.p, S_.X.p, nR);
         else if (f32)
@@ -604,6 +624,8 @@ struct Engine {
       const dim3 sg((S_.n + 31) / 32, (S_.R + 31) / 32);
       if (f32 && iters == 0)
         k_scatter_il<float><<<sg, tb, 0, s>>>(S_.X32.p, S_.dst[target].p, S_.n, S_.R);
+      else if (f32 && mixed && iters == 1)
+        k_scatter_sum_il<<<sg, tb, 0, s>>>(S_.X32.p, S_.D32.p, S_.dst[target].p, S_.n, S_.R);
       else
         k_scatter_il<double><<<sg, tb, 0, s>>>(S_.X.p, S_.dst[target].p, S_.n, S_.R);
       PECS_CUDA(cudaGetLastError());

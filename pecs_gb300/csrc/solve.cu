@@ -412,6 +412,7 @@ constexpr int kPanelKcSteps = 8;
 constexpr int kPanelKc[kPanelKcSteps] = {128, 64, 32, 16, 8, 4, 2, 1};
 constexpr size_t kPanelSmem = 160 * 1024;
 constexpr int kPanelCmMax = 4096;  // staged child-update rows per node (more: read from global)
+constexpr size_t kWarpSmem = 48 * 1024;  // leaf levels: shared memory per CTA
 
 // RPL consecutive values of one interleaved row (offset a multiple of RPL),
 // double or float storage, registers of type VR (the storage type converts
@@ -724,6 +725,100 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
 }
 
+// Leaf levels: a warp per node (all of its rows) and right-hand-side chunk,
+// eight independent nodes per CTA and no CTA barrier.  A level qualifies when
+// its nodes are small (at most kWarpMaxK columns and kWarpMaxRows rows) and,
+// in the forward sweep, have no children (so the staged right-hand sides need
+// no update subtraction and the outputs no pass-through sums).  The warp
+// stages its node's whole block and right-hand-side rows with cp.async.
+constexpr int kWarpMaxK = 64;
+constexpr int kWarpMaxRows = 64;
+constexpr int kWarpNodesPerCta = kSolveThreads / 32;
+
+template <typename T>
+__host__ __device__ constexpr size_t panel_warp_bytes(int max_k, int rows_pad, int rc) {
+  // rounded to 16 bytes: every warp's slice starts 16-byte aligned
+  return ((((size_t)max_k * rc + (size_t)max_k * rows_pad) * sizeof(T) + (size_t)max_k * sizeof(int)) +
+          15) & ~(size_t)15;
+}
+
+template <typename T, int RPL, bool FWD, typename SVT>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_panel_warp(BankView B, SVT S, const PanelItem* __restrict__ items, int n_items, int max_k,
+                 int rows_pad) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int RC = 32 * RPL;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int idx = blockIdx.x * kWarpNodesPerCta + warp;
+  if (idx >= n_items) return;
+  const PanelItem I = items[idx];
+  const int s = I.b.x, m = I.b.y, f = s + m, w_off = I.b.w;
+  const auto st = S.set[I.b.z];
+  const int R = st.nrhs;
+  const int rc0 = blockIdx.y * RC;
+  if (rc0 >= R) return;
+  const int rl = rc0 + lane * RPL;
+  const bool lane_ok = rl < R;
+  const int K = FWD ? s : f;
+  const int rows = FWD ? f : s;  // = the leading dimension of the block
+  const T* M = static_cast<const T*>(FWD ? B.G : B.H) + (((long long)I.c.y << 32) | (unsigned)I.c.x);
+  unsigned char* base = smem_raw + (size_t)warp * panel_warp_bytes<T>(max_k, rows_pad, RC);
+  T* Ds = reinterpret_cast<T*>(base);        // [max_k][RC]
+  T* Gs = Ds + (size_t)max_k * RC;           // [max_k][rows_pad]
+  int* src_s = reinterpret_cast<int*>(Gs + (size_t)max_k * rows_pad);  // [max_k]
+  {
+    const int* own = B.own_idx + I.c.z;
+    const int* upd = B.upd_idx + I.c.w;
+    for (int p = lane; p < K; p += 32) src_s[p] = FWD ? own[p] : (p < s ? own[p] : ~upd[p - s]);
+  }
+  for (int e = lane; e < K * rows_pad; e += 32) {
+    const int k = e / rows_pad, r = e - k * rows_pad;
+    if (r < rows)
+      cp_async<sizeof(T)>(Gs + e, M + (size_t)k * rows + r);
+    else
+      Gs[e] = T(0);
+  }
+  __syncwarp();
+  for (int k = 0; k < K; ++k) {
+    const int sr = src_s[k];
+    const T* src = FWD ? st.b + (size_t)sr * R
+                       : (sr >= 0 ? st.y + (size_t)sr * R : st.x + (size_t)(~sr) * R);
+    stage_row<T, RPL>(Ds + (size_t)k * RC + lane * RPL, src + rl, lane_ok);
+  }
+  cp_async_wait_all();
+  __syncwarp();
+  if (!lane_ok) return;
+  for (int r4 = 0; r4 < rows; r4 += 4) {
+    T acc[4][RPL];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) acc[i][q] = T(0);
+    for (int k = 0; k < K; ++k) {
+      T gv[4], dv[RPL];
+      lds<T, 4>(Gs + (size_t)k * rows_pad + r4, gv);
+      lds<T, RPL>(Ds + (size_t)k * RC + lane * RPL, dv);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) acc[i][q] += gv[i] * dv[q];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int row = r4 + i;
+      if (row >= rows) break;
+      if (FWD) {
+        if (row < s)
+          st_rhs<RPL>(st.y + (size_t)src_s[row] * R + rl, acc[i]);
+        else
+          st_rhs<RPL>(st.w + (size_t)(w_off + row - s) * R + rl, acc[i]);
+      } else {
+        st_rhs<RPL>(st.x + (size_t)src_s[row] * R + rl, acc[i]);
+      }
+    }
+  }
+}
+
 // Tile shape of one level for nrhs right-hand sides: the longest row tiles and
 // the most right-hand sides per lane that still give the GPU two CTAs per SM.
 // Fewer right-hand sides per CTA is tried first (it keeps the staged columns
@@ -789,11 +884,46 @@ void set_panel_smem_limit() {
   set((const void*)k_panel<T, 1, false, SVT>);
   set((const void*)k_panel<T, 2, false, SVT>);
   set((const void*)k_panel<T, 4, false, SVT>);
+  set((const void*)k_panel_warp<T, 1, true, SVT>);
+  set((const void*)k_panel_warp<T, 2, true, SVT>);
+  set((const void*)k_panel_warp<T, 4, true, SVT>);
+  set((const void*)k_panel_warp<T, 1, false, SVT>);
+  set((const void*)k_panel_warp<T, 2, false, SVT>);
+  set((const void*)k_panel_warp<T, 4, false, SVT>);
+}
+
+template <typename T, int RPL, typename SVT>
+void launch_panel_warp(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
+                       int max_nrhs, cudaStream_t st) {
+  constexpr int RC = 32 * RPL;
+  const int rows_pad = (L.warp_rows + 3) & ~3;
+  const size_t smem = kWarpNodesPerCta * panel_warp_bytes<T>(L.max_k, rows_pad, RC);
+  const dim3 grid((L.warp.n_items + kWarpNodesPerCta - 1) / kWarpNodesPerCta, (max_nrhs + RC - 1) / RC);
+  if (forward)
+    k_panel_warp<T, RPL, true, SVT><<<grid, kSolveThreads, smem, st>>>(B, S, L.warp.items.p, L.warp.n_items,
+                                                                       L.max_k, rows_pad);
+  else
+    k_panel_warp<T, RPL, false, SVT><<<grid, kSolveThreads, smem, st>>>(B, S, L.warp.items.p, L.warp.n_items,
+                                                                        L.max_k, rows_pad);
+  PECS_CUDA(cudaGetLastError());
 }
 
 template <typename T, typename SVT>
 void launch_panel_level(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
                         int max_nrhs, int rpl_max, const PanelTuning& tu, cudaStream_t st) {
+  if (L.warp.n_items > 0) {
+    // leaf level: the most right-hand sides per lane that keep a CTA's eight
+    // warps within kWarpSmem
+    int rpl = rpl_max;
+    const int rows_pad = (L.warp_rows + 3) & ~3;
+    while (rpl > 1 && kWarpNodesPerCta * panel_warp_bytes<T>(L.max_k, rows_pad, 32 * rpl) > kWarpSmem) rpl /= 2;
+    switch (rpl) {
+      case 1: launch_panel_warp<T, 1, SVT>(forward, B, S, L, max_nrhs, st); break;
+      case 2: launch_panel_warp<T, 2, SVT>(forward, B, S, L, max_nrhs, st); break;
+      default: launch_panel_warp<T, 4, SVT>(forward, B, S, L, max_nrhs, st); break;
+    }
+    return;
+  }
   const PanelChoice c = choose_panel(L, max_nrhs, rpl_max, tu.min_ctas);
   const PanelTiles& P = L.tiles[c.cap_idx];
   switch (c.rpl) {
@@ -844,7 +974,7 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
     throw PecsError(PECS_E_ARG, "panel tuning out of range");
   if (tune_.chunk == 0) tune_.chunk = precision == PECS_PREC_FP64 ? kPanelKcF64 : kPanelKcF32;
   if (prec_ == PECS_PREC_FP64) tune_.chunk = std::min(tune_.chunk, kPanelKcF64);
-  if (tune_.min_ctas == 0) tune_.min_ctas = 2 * kTargetCtas;
+  if (tune_.min_ctas == 0) tune_.min_ctas = kTargetCtas;
   n_sets_ = (int)factors.size();
   std::vector<int> hs, hm, own_off, upd_off, w_off, cm_off, own_idx, upd_idx, cmap_ptr, cmap_idx,
       node_set;
@@ -1033,6 +1163,39 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
             }
           }
           out[l].sc_rows[ci] = mx;
+        }
+        // leaf level: every node small and, forward, without children
+        bool leaf = true;
+        int max_rows = 0;
+        for (int g : lv[l].nodes) {
+          const int f = hs[g] + hm[g];
+          const int rows = forward ? f : hs[g];
+          const int k = forward ? hs[g] : f;
+          const bool kids = cmap_ptr[cm_off[g] + f] > cmap_ptr[cm_off[g]];
+          if (k > kWarpMaxK || rows > kWarpMaxRows || (forward && kids)) leaf = false;
+          max_rows = std::max(max_rows, rows);
+        }
+        {
+          const size_t esz = prec_ == PECS_PREC_FP64 ? 8 : 4;
+          const size_t rows_pad = (size_t)((max_rows + 3) & ~3);
+          const size_t wb = (((size_t)max_k * 32 + (size_t)max_k * rows_pad) * esz + (size_t)max_k * 4 + 15) & ~(size_t)15;
+          if (kWarpNodesPerCta * wb > kWarpSmem) leaf = false;
+        }
+        if (leaf) {
+          std::vector<PanelItem> items;
+          for (int g : lv[l].nodes) {
+            const int rows = forward ? hs[g] + hm[g] : hs[g];
+            const long long off = forward ? goff[g] : hoff[g];
+            PanelItem it;
+            it.a = make_int4(g, 0, rows, 32);
+            it.b = make_int4(hs[g], hm[g], node_set[g], w_off[g]);
+            it.c = make_int4((int)(off & 0xffffffffll), (int)(off >> 32), own_off[g], upd_off[g]);
+            it.d = make_int4(cm_off[g], cmap_ptr[cm_off[g]], 0, 0);
+            items.push_back(it);
+          }
+          out[l].warp.n_items = (int)items.size();
+          out[l].warp.items.upload(items);
+          out[l].warp_rows = max_rows;
         }
         for (int ci = 0; ci < 4; ++ci) {
           const int cap = 32 >> ci;

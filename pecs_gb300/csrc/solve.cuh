@@ -119,6 +119,8 @@ struct PanelPlan {
   int cm_cap = 0;  // child-map entries staged per node (the level's largest, capped)
   int sc_rows[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // forward: child rows per chunk, per chunk size
   PanelTiles tiles[4];
+  PanelTiles warp;    // leaf levels: one item per node, a warp each (else empty)
+  int warp_rows = 0;  // leaf levels: most rows of a node
 };
 
 struct LevelPlan {
@@ -130,7 +132,7 @@ struct LevelPlan {
 
 struct PanelTuning {
   int chunk = 0;     // staged block columns per chunk (0: 128 FP32, 64 FP64)
-  int min_ctas = 0;  // CTAs a level must reach before shorter tiles are used (0: 2 x SMs)
+  int min_ctas = 0;  // CTAs a level must reach before shorter tiles are used (0: one per SM)
 };
 
 class FactorBank {
