@@ -408,9 +408,10 @@ def plain_point(pg, refine, local):
 
 
 def run_full(args):
-    """Learned + batched: held-out I-V points in batches of args.batch_inst
-    instances (FP32-mixed), each warm-started by the neural operator with the
-    first-step fallback; the plain FP64 single-instance path measured beside."""
+    """Learned + batched: held-out I-V points streamed through args.batch_inst
+    slots (FP32-mixed), each warm-started by the neural operator with the
+    first-step fallback, each slot refilled as soon as its point finishes; the
+    plain FP64 single-instance path measured beside."""
     import numpy as np
     import torch
 
@@ -421,9 +422,12 @@ def run_full(args):
     pg.build()
     B = args.batch_inst
     base = pg.config2(n_refine=args.refine)
-    # held-out draws (seed differs from the training seed), sharded by rank
-    n_batches = args.warmup + args.steps + 2
-    thetas = L.sample(B * n_batches * world, seed=777)[rank * B * n_batches:(rank + 1) * B * n_batches]
+    # held-out draws (seed differs from the training seed), sharded by rank:
+    # warm-up points, timed points, end-to-end points
+    n_w, n_t, n_e = args.warmup * B, args.steps * B, B
+    per_rank = n_w + n_t + n_e
+    thetas = L.sample(per_rank * world, seed=777)[rank * per_rank:(rank + 1) * per_rank]
+    th_w, th_t, th_e = thetas[:n_w], thetas[n_w:n_w + n_t], thetas[n_w + n_t:]
     ctx = pg.Context([L.instance_params(t, base) for t in thetas[:B]], precision=pg.PREC_FP32_MIXED,
                      device=local)
     info = ctx.info()
@@ -439,103 +443,103 @@ def run_full(args):
         trained_here = args.train_samples
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
-    batches = [thetas[b * B:(b + 1) * B] for b in range(n_batches)]
-
-    def params_of(rows):
-        return [L.instance_params(t, base) for t in rows]
-
-    for b in range(args.warmup):
-        L.warm_started_sweep(ctx, op, batches[b], base)
-    # ---- timed: device-resident inputs (parameters uploaded before each batch) -----
-    ms, steps_all, fb_all, executed = 0.0, [], [], 0
+    if n_w:
+        L.stream_warm_sweep(ctx, op, th_w, base, MAX_STEPS, TOL, CHECK_EVERY)
+    # ---- timed: predictions, fallback probes and the streamed sweep of
+    # args.steps x B points (parameters uploaded per slot refill; final fields
+    # stay on the device) -------------------------------------------------------
     barrier(world)
     torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        flush.zero_()
+    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for b in range(args.warmup, args.warmup + args.steps):
-            ctx.set_instances(params_of(batches[b]))
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            s_b, fb, cur = L.warm_started_sweep(ctx, op, batches[b], base, set_params=False)
-            e1.record(stream)
-            e1.synchronize()
-            ms += e0.elapsed_time(e1)
-            steps_all.extend(s_b.tolist())
-            fb_all.extend(fb.tolist())
-            executed += ctx.last_run_steps() + 2
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        steps_t, fb_t, cur_t, _ = L.stream_warm_sweep(ctx, op, th_t, base, MAX_STEPS, TOL, CHECK_EVERY)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        executed = ctx.last_run_steps()
         torch.cuda.synchronize()
     barrier(world)
     ms = max_over_ranks(ms, world)
-    points = B * args.steps * world
+    points = n_t * world
     value = points / (ms * 1e-3)
     clocks = clk.summary()
-    # ---- e2e: host parameters in, currents and fields out, through the public API ---
-    e2e_b = batches[args.warmup + args.steps]
+    # ---- e2e: host parameters in, currents and final fields out, through the
+    # public API (pecs_sweep_stream), B points --------------------------------------
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    s_e, fb_e, cur_e = L.warm_started_sweep(ctx, op, e2e_b, base)   # parameters host -> device
-    finals = {f: np.zeros(B * info.ndofs[f]) for f in range(5) if info.ndofs[f]}
-    for f, a in finals.items():
-        for i in range(B):
-            a[i * info.ndofs[f]:(i + 1) * info.ndofs[f]] = ctx.get_state(f, i)
-    e2e = B * world / max_over_ranks(time.perf_counter() - t0, world)
-    h2d = B * (sum(info.ndofs[f] for f in range(5)) * 8 + info.ndofs[4] * 8)   # constant RHS parts
-    d2h = B * 8 + sum(a.nbytes for a in finals.values())
-    # ---- accuracy: FP64 plain runs of a few instances of the e2e batch ------------
+    steps_e, fb_e, cur_e, fin_e = L.stream_warm_sweep(ctx, op, th_e, base, MAX_STEPS, TOL, CHECK_EVERY,
+                                                      want_fields=True)
+    e2e = n_e * world / max_over_ranks(time.perf_counter() - t0, world)
+    h2d = n_e * (sum(info.ndofs[f] for f in range(5)) * 8 + info.ndofs[4] * 8)  # per-point constant RHS parts
+    d2h = n_e * 8 + sum(a.nbytes for a in fin_e.values())
+    # ---- accuracy: the same points, same warm starts, FP64 throughout ---------------
     nchk = 4
-    ref = pg.Context(params_of(e2e_b[:nchk]), precision=pg.PREC_FP64, device=local)
-    ref.initialize()
-    ref.run_to_steady_state(MAX_STEPS, TOL, CHECK_EVERY)
-    cur_ref = ref.interface_current()
+    ref = pg.Context([L.instance_params(t, base) for t in th_e[:nchk]], precision=pg.PREC_FP64, device=local)
+    init_n, init_p, fb_chk, keep = L.warm_start_vectors(ctx, op, th_e[:nchk], base)
+    s64, cur64, fin64 = ref.sweep_stream([L.instance_params(t, base) for t in th_e[:nchk]], MAX_STEPS, TOL,
+                                         CHECK_EVERY, init_n=init_n, init_p=init_p, want_fields=True)
+    del keep
     err_fields, err_cur = 0.0, 0.0
     for i in range(nchk):
         for f in ref.fields():
-            a = finals[f][i * info.ndofs[f]:(i + 1) * info.ndofs[f]]
-            r = ref.get_state(f, i)
+            nd = info.ndofs[f]
+            a = fin_e[f][i * nd:(i + 1) * nd]
+            r = fin64[f][i * nd:(i + 1) * nd]
             err_fields = max(err_fields, float(np.linalg.norm(a - r) / np.linalg.norm(r)))
-        err_cur = max(err_cur, float(abs(cur_e[i] - cur_ref[i]) / abs(cur_ref[i])))
+        err_cur = max(err_cur, float(abs(cur_e[i] - cur64[i]) / abs(cur64[i])))
+    steps_diff = [int(a) - 2 - int(b) for a, b in zip(steps_e[:nchk], s64)]
     del ref
     # ---- plain path (config 2, FP64, single instance) ---------------------------------
     plain_value, plain_steps, pctx = plain_point(pg, args.refine, local)
     pinfo = pctx.info()
-    solve_ms = pctx.time_solve(0, reps=30)
-    nlaunch = pinfo.solve_launches[0]
-    achieved = pinfo.solve_bytes[0] / (solve_ms * 1e-3) / 1e9
-    fast_ms = ctx.time_solve(0, reps=10)
-    fast_gbs = info.solve_bytes[0] / (fast_ms * 1e-3) / 1e9
-    peak, peak_kind = load_peaks()
+    plain_ms = pctx.time_solve(0, reps=30)
+    plain_gbs = pinfo.solve_bytes[0] / (plain_ms * 1e-3) / 1e9
     del pctx
+    # ---- roofline: the carrier solve sweep of the batched path (panel kernels) --------
+    solve_ms = ctx.time_solve(0, reps=30)
+    nlaunch = info.solve_launches[0]
+    achieved = info.solve_bytes[0] / (solve_ms * 1e-3) / 1e9
+    peak, peak_kind = load_peaks()
     line = {
         "metric": "I-V points/sec to steady state", "value": value, "unit": "I-V points/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 factors/quadrature + double-float refinement (learned+batched); "
+        "vs_baseline": None, "dtype": "f32 factors/sweeps + double-float refinement (learned+batched); "
                                       "f64 plain",
         "data": "synthetic",
-        "config": {"workload": f"learned+batched: {B} held-out I-V points per batch on the half cell "
-                               f"2x{2**args.refine}x{2**args.refine}, LDG k=1, RT0xDGQ0 Poisson, dt=1e-3, "
+        "config": {"workload": f"learned+batched: held-out I-V points streamed through {B} slots on the half "
+                               f"cell 2x{2**args.refine}x{2**args.refine}, LDG k=1, RT0xDGQ0 Poisson, dt=1e-3, "
                                f"warm-started, to rel. change <= {TOL} (<= {MAX_STEPS} steps)",
-                   "bench_step": f"one batch of {B} I-V points", "instances_per_gpu": B,
+                   "bench_step": f"{B} I-V points", "points_timed": n_t, "slots": B,
                    "model": os.path.basename(args.model) if trained_here is None
                    else f"trained in-run on {trained_here} draws",
-                   "l2": "flushed (512 MB write) before each timed batch"},
+                   "l2": "flushed (512 MB write) before the timed sweep; the sweep streams ~"
+                         f"{info.factor_bytes / 1e6:.0f} MB of factors per step"},
         "plain": {"value": plain_value, "unit": "I-V points/s", "steps_to_steady_state": plain_steps,
                   "workload": "config 2: one instance, FP64, standard initial condition"},
         "speedup_vs_plain": value / plain_value,
-        "warm_start": {"median_steps": float(np.median(steps_all)), "fallback_rate": float(np.mean(fb_all)),
-                       "plain_steps": plain_steps},
+        "warm_start": {"median_steps": float(np.median(steps_t)), "mean_steps": float(np.mean(steps_t)),
+                       "capped": int(np.sum(steps_t >= MAX_STEPS + 2)),
+                       "fallback_rate": float(np.mean(fb_t)), "plain_steps": plain_steps,
+                       "executed_steps": executed},
         "accuracy_vs_fp64": {"fields_rel_l2_max": err_fields, "current_rel_max": err_cur,
-                             "instances_checked": nchk},
+                             "instances_checked": nchk, "steps_diff": steps_diff,
+                             "reference": "the same points and warm starts marched in FP64"},
         "e2e": {"value": e2e, "unit": "I-V points/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": load_traffic(f"carrier_solve_r{args.refine}_fp64"),
-                     "kernel": "k_forward/k_backward carrier solve sweep, plain FP64 single instance",
+                     "traffic": load_traffic(f"carrier_solve_r{args.refine}_mixed_b{B}"),
+                     "kernel": "k_panel / k_panel_warp (carrier multifrontal solve sweep, FP32, "
+                               f"{2 * B} right-hand sides per factor)",
                      "solve_ms": solve_ms, "launches_per_sweep": nlaunch,
-                     "batched_fp32": {"solve_ms": fast_ms, "achieved_gbs": fast_gbs,
-                                      "frac": fast_gbs / peak, "rhs_per_sweep": 2 * B}},
+                     "bytes_per_sweep": info.solve_bytes[0],
+                     "plain_fp64": {"solve_ms": plain_ms, "achieved_gbs": plain_gbs,
+                                    "frac": plain_gbs / peak,
+                                    "traffic": load_traffic(f"carrier_solve_r{args.refine}_fp64")}},
         "gpu_launches": executed * info.launches_per_step,
         "clocks": clocks,
     }

@@ -179,6 +179,21 @@ int pecs_interface_current(pecs_ctx* ctx, double* out);
  * interface currents and (optionally) the final densities. */
 int pecs_iv_sweep(pecs_ctx* ctx, const double* const* init_fields, int max_steps, double tol,
                   int check_every, double* currents, int* steps, double* const* final_fields);
+/* Streamed I-V sweep: n_points parameter sets (same meshes and fixed matrices
+ * as the context) marched through the context's n_inst slots.  Every
+ * check_every steps, slots whose point converged (relative change <= tol) or
+ * marched max_steps are harvested and refilled with the next points, so the
+ * batch stays full until the list runs out.  init_n / init_p: NULL, or
+ * n_points DEVICE pointers (entries may be NULL = built-in initial condition)
+ * to full electron / hole vectors, e.g. a learned warm start.  Outputs per
+ * point (host): steps (to convergence; max_steps when capped; negative when
+ * the state became non-finite), currents (interface current) and, when
+ * final_fields is not NULL, final_fields[f] -> n_points x ndofs[f] doubles
+ * (NULL entries skipped).  No reference counterpart: the reference marches
+ * one bias point per SolarCellProblem::run (source/SolarCell.cpp). */
+int pecs_sweep_stream(pecs_ctx* ctx, int n_points, const pecs_params* params,
+                      const double* const* init_n, const double* const* init_p, int max_steps, double tol,
+                      int check_every, int* steps, double* currents, double* const* final_fields);
 int pecs_synchronize(pecs_ctx* ctx);
 /* Time steps executed by the last pecs_run_to_steady_state / pecs_iv_sweep
  * (including steps of a polling interval after the last instance converged). */

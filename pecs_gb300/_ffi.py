@@ -95,6 +95,9 @@ SIGNATURES = [
     ("pecs_interface_current", C.c_int, [_vp, _dp]),
     ("pecs_iv_sweep", C.c_int, [_vp, C.POINTER(_dp), C.c_int, C.c_double, C.c_int, _dp, _ip,
                                 C.POINTER(_dp)]),
+    ("pecs_sweep_stream", C.c_int, [_vp, C.c_int, C.POINTER(pecs_params), C.POINTER(C.c_void_p),
+                                    C.POINTER(C.c_void_p), C.c_int, C.c_double, C.c_int, _ip, _dp,
+                                    C.POINTER(_dp)]),
     ("pecs_synchronize", C.c_int, [_vp]),
     ("pecs_get_stream", _vp, [_vp]),
     ("pecs_last_run_steps", C.c_int, [_vp]),

@@ -300,6 +300,36 @@ class Context:
                                   steps.ctypes.data_as(C.POINTER(C.c_int)), fptrs))
         return cur, steps, finals
 
+    def sweep_stream(self, params: Sequence[Params], max_steps: int, tol: float,
+                     check_every: int = 50, init_n: Optional[Sequence[int]] = None,
+                     init_p: Optional[Sequence[int]] = None, want_fields: bool = False):
+        """Streamed I-V sweep (pecs_sweep_stream): every parameter set marched
+        to steady state through this context's slots, each slot refilled as
+        soon as its point finishes.  init_n / init_p: per point a device
+        pointer (int, 0 = built-in initial condition) to a full electron /
+        hole vector.  Returns (steps, currents, fields or None)."""
+        n = len(params)
+        arr = (F.pecs_params * n)(*[p.to_c() for p in params])
+        def ptrs(lst):
+            if lst is None:
+                return None
+            a = (C.c_void_p * n)()
+            for k, v in enumerate(lst):
+                a[k] = C.c_void_p(int(v)) if v else None
+            return a
+        steps = np.zeros(n, dtype=np.int32)
+        cur = np.zeros(n)
+        finals = fptrs = None
+        if want_fields:
+            finals = {f: np.zeros(n * self.ndofs[f]) for f in range(5) if self.ndofs[f]}
+            fptrs = (C.POINTER(C.c_double) * 5)()
+            for f, a in finals.items():
+                fptrs[f] = _dptr(a)
+        check(lib().pecs_sweep_stream(self._h, n, arr, ptrs(init_n), ptrs(init_p), max_steps, tol,
+                                      check_every, steps.ctypes.data_as(C.POINTER(C.c_int)),
+                                      _dptr(cur), fptrs))
+        return steps, cur, finals
+
 
 class LU:
     """Drop-in direct solver: factor(set_solver) once, solve() every step."""

@@ -86,9 +86,10 @@ __global__ void k_gather_il(const double* const* __restrict__ src, double* __res
 }
 
 // dst_k[d] = src[d * R + k]
+// mask (optional): only columns of instances k / nf with mask[k / nf] != 0
 template <typename V>
 __global__ void k_scatter_il(const V* __restrict__ src, double* const* __restrict__ dst, int n,
-                             int R) {
+                             int R, const int* __restrict__ mask, int nf) {
   __shared__ double t[32][33];
   const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
@@ -98,7 +99,7 @@ __global__ void k_scatter_il(const V* __restrict__ src, double* const* __restric
   __syncthreads();
   for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
     const int k = k0 + kk, d = d0 + threadIdx.x;
-    if (k < R && d < n) dst[k][d] = t[threadIdx.x][kk];
+    if (k < R && d < n && (!mask || mask[k / nf])) dst[k][d] = t[threadIdx.x][kk];
   }
 }
 
@@ -119,7 +120,8 @@ __global__ void k_axpy_il(double* __restrict__ x, const V* __restrict__ d, size_
 // dst_k[d] = (double) x32[d * R + k] + (double) d32[d * R + k]: the refined
 // solution of an FP32 sweep and its one correction, written to the state
 __global__ void k_scatter_sum_il(const float* __restrict__ x32, const float* __restrict__ d32,
-                                 double* const* __restrict__ dst, int n, int R) {
+                                 double* const* __restrict__ dst, int n, int R,
+                                 const int* __restrict__ mask, int nf) {
   __shared__ double t[32][33];
   const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
@@ -130,7 +132,7 @@ __global__ void k_scatter_sum_il(const float* __restrict__ x32, const float* __r
   __syncthreads();
   for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
     const int k = k0 + kk, d = d0 + threadIdx.x;
-    if (k < R && d < n) dst[k][d] = t[threadIdx.x][kk];
+    if (k < R && d < n && (!mask || mask[k / nf])) dst[k][d] = t[threadIdx.x][kk];
   }
 }
 
@@ -231,10 +233,15 @@ __global__ void k_relchange_partial(FieldPtrs NEW, FieldPtrs OLD, int n_fields,
 }
 
 // per instance: rel = max_f sqrt(d2/n2); record first step with rel <= tol.
+// Per-instance convergence test after a step.  An active instance stops when
+// its relative change is <= tol (conv_step = the step), when its state is not
+// finite (conv_step = -step), or when it has marched max_steps since its start
+// step (conv_step = the step, capped = 1; streamed sweeps refill such slots).
 __global__ void k_converge(const double2* __restrict__ partial, int n_inst, int n_fields, double tol,
                            int* __restrict__ conv_step, double* __restrict__ rel,
                            int* __restrict__ step_ctr, int* __restrict__ active,
-                           int* __restrict__ n_active) {
+                           int* __restrict__ n_active, const int* __restrict__ start, int max_steps,
+                           int* __restrict__ capped) {
   const int step = *step_ctr + 1;
   __shared__ int cnt;
   if (threadIdx.x == 0) cnt = 0;
@@ -261,6 +268,10 @@ __global__ void k_converge(const double2* __restrict__ partial, int n_inst, int 
       } else if (r <= tol) {
         active[i] = 0;
         conv_step[i] = step;
+      } else if (step - start[i] >= max_steps) {
+        active[i] = 0;
+        conv_step[i] = step;
+        capped[i] = 1;
       }
     }
     if (active[i]) atomicAdd(&cnt, 1);
@@ -395,7 +406,9 @@ struct Engine {
   DBuf<double*> snap_ptrs;
   // steady state
   DBuf<double2> partial;
-  DBuf<int> conv_step, step_ctr, active, n_active;
+  DBuf<int> conv_step, step_ctr, active, n_active, start_step, capped, refill_mask;
+  int step_cap = 1 << 30;  // per-instance step cap seen by k_converge (streamed sweeps)
+  const int* scatter_mask = nullptr;  // solves write only these instances (slot refills)
   DBuf<double> rel;
   // graphs
   cudaGraphExec_t graph2[2] = {nullptr, nullptr};  // two steps starting from cur = 0 / 1
@@ -622,12 +635,14 @@ struct Engine {
     for (int si = 0; si < I.n_sets; ++si) {
       IlSet& S_ = I.set[si];
       const dim3 sg((S_.n + 31) / 32, (S_.R + 31) / 32);
+      const int nf = S_.R / n_inst;  // columns per instance
       if (f32 && iters == 0)
-        k_scatter_il<float><<<sg, tb, 0, s>>>(S_.X32.p, S_.dst[target].p, S_.n, S_.R);
+        k_scatter_il<float><<<sg, tb, 0, s>>>(S_.X32.p, S_.dst[target].p, S_.n, S_.R, scatter_mask, nf);
       else if (f32 && mixed && iters == 1)
-        k_scatter_sum_il<<<sg, tb, 0, s>>>(S_.X32.p, S_.D32.p, S_.dst[target].p, S_.n, S_.R);
+        k_scatter_sum_il<<<sg, tb, 0, s>>>(S_.X32.p, S_.D32.p, S_.dst[target].p, S_.n, S_.R, scatter_mask,
+                                           nf);
       else
-        k_scatter_il<double><<<sg, tb, 0, s>>>(S_.X.p, S_.dst[target].p, S_.n, S_.R);
+        k_scatter_il<double><<<sg, tb, 0, s>>>(S_.X.p, S_.dst[target].p, S_.n, S_.R, scatter_mask, nf);
       PECS_CUDA(cudaGetLastError());
     }
   }
@@ -762,6 +777,12 @@ struct Engine {
     partial.alloc((size_t)n_inst * 5 * kRedChunks);
     partial.zero();
     conv_step.alloc(n_inst);
+    start_step.alloc(n_inst);
+    start_step.zero();
+    capped.alloc(n_inst);
+    capped.zero();
+    refill_mask.alloc(n_inst);
+    refill_mask.zero();
     rel.alloc(n_inst);
     step_ctr.alloc(1);
     n_active.alloc(1);
@@ -991,7 +1012,7 @@ struct Engine {
                                                                                      partial.p);
     PECS_CUDA(cudaGetLastError());
     k_converge<<<1, 256, 0, s>>>(partial.p, n_inst, n_fields, tol, conv_step.p, rel.p, step_ctr.p,
-                                 active.p, n_active.p);
+                                 active.p, n_active.p, start_step.p, step_cap, capped.p);
     PECS_CUDA(cudaGetLastError());
     k_snapshot<<<dim3(32, 5, n_inst), 256, 0, s>>>(NEW, snap_ptrs.p, conv_step.p, step_ctr.p, 5);
     PECS_CUDA(cudaGetLastError());
@@ -1016,11 +1037,14 @@ struct Engine {
     std::vector<int> ones(n_inst, 1), zeros(n_inst, 0);
     PECS_CUDA(cudaMemcpyAsync(active.p, ones.data(), n_inst * 4, cudaMemcpyHostToDevice, st));
     PECS_CUDA(cudaMemcpyAsync(conv_step.p, zeros.data(), n_inst * 4, cudaMemcpyHostToDevice, st));
+    PECS_CUDA(cudaMemsetAsync(start_step.p, 0, n_inst * 4, st));
+    PECS_CUDA(cudaMemsetAsync(capped.p, 0, n_inst * 4, st));
     PECS_CUDA(cudaMemsetAsync(step_ctr.p, 0, 4, st));
     PECS_CUDA(cudaStreamSynchronize(st));
   }
 
   void capture_graph(double tol) {
+    graph_cap = step_cap;
     const int saved = cur;
     for (int par = 0; par < 2; ++par) {
       if (graph2[par]) {
@@ -1047,6 +1071,7 @@ struct Engine {
     graph_valid = true;
   }
   double graph_tol = -1.0;
+  int graph_cap = -1;
   int last_run_steps = 0;
 
   void run_to_steady(int max_steps, double tol, int check_every, int* steps, double* relc) {
@@ -1057,7 +1082,8 @@ struct Engine {
     reset_convergence();
     last_run_steps = 0;
     const bool use_graph = opt.use_graphs != 0 && max_steps >= 2;
-    if (use_graph && (!graph_valid || graph_tol != tol)) capture_graph(tol);
+    step_cap = 1 << 30;  // the host loop stops at max_steps
+    if (use_graph && (!graph_valid || graph_tol != tol || graph_cap != step_cap)) capture_graph(tol);
     int done = 0;
     int h_active = n_inst;
     while (done < max_steps && h_active > 0) {
@@ -1101,6 +1127,186 @@ struct Engine {
         throw PecsError(PECS_E_NONFINITE, "instance " + std::to_string(i) +
                                               " produced a non-finite state at step " +
                                               std::to_string(-cs[i]));
+  }
+
+  // ---- streamed sweep: slots refilled as they finish -------------------------
+  // New parameters for the given slots (host setup of their per-instance data,
+  // uploaded slice by slice), their initial state (standard, or the given
+  // device densities for electrons / holes), then one Poisson solve whose
+  // results are written to these slots only.
+  void refill(const std::vector<int>& slots, const std::vector<pecs_params>& P,
+              const std::vector<const double*>& init_n, const std::vector<const double*>& init_p) {
+    {
+      std::vector<pecs_params> chk(P);
+      chk.insert(chk.begin(), S->inst[0]);
+      std::string err = validate_params(chk.data(), (int)chk.size());
+      if (!err.empty()) throw PecsError(PECS_E_ARG, err);
+    }
+    std::vector<int> mask(n_inst, 0);
+    for (size_t t = 0; t < slots.size(); ++t) {
+      const int i = slots[t];
+      S->inst[i] = P[t];
+      S->compute_instance(i);
+      mask[i] = 1;
+      auto put = [&](DBuf<double>& d, const std::vector<double>& v) {
+        if (v.empty()) return;
+        PECS_CUDA(cudaMemcpyAsync(d.p + (size_t)i * v.size(), v.data(), v.size() * 8, cudaMemcpyHostToDevice, st));
+      };
+      for (int f = 0; f < 5; ++f)
+        if (nd[f]) put(bconst[f], S->bconst[f][i]);
+      for (int f = 0; f < 4; ++f)
+        if (nd[f]) put(init_dev[f], S->init[f][i]);
+      if (full) {
+        put(iface_ne, S->iface_ne[i]);
+        put(iface_pe, S->iface_pe[i]);
+      }
+      if (S->has_schottky) {
+        put(sch_ne, S->schottky_ne[i]);
+        put(sch_pe, S->schottky_pe[i]);
+      }
+      const pecs_params& p = S->inst[i];
+      const InstDev ip{p.k_et, p.k_ht, p.tau_n, p.tau_p, p.n_i, p.s_n, p.s_p, p.srh, 0};
+      PECS_CUDA(cudaMemcpyAsync(inst.p + i, &ip, sizeof(InstDev), cudaMemcpyHostToDevice, st));
+      for (int f = 0; f < 4; ++f) {
+        if (!nd[f]) continue;
+        const double* src = init_dev[f].p + (size_t)i * nd[f];
+        if (f == 0 && init_n[t]) src = init_n[t];
+        if (f == 1 && init_p[t]) src = init_p[t];
+        PECS_CUDA(cudaMemcpyAsync(state[cur][f].p + (size_t)i * nd[f], src, (size_t)nd[f] * 8,
+                                  cudaMemcpyDeviceToDevice, st));
+      }
+      // host data of this slot must stay alive until the copies ran
+      PECS_CUDA(cudaStreamSynchronize(st));
+    }
+    PECS_CUDA(cudaMemcpyAsync(refill_mask.p, mask.data(), n_inst * 4, cudaMemcpyHostToDevice, st));
+    scatter_mask = refill_mask.p;
+    try {
+      stage_poisson_rhs(st, nullptr);
+      stage_solve_poisson(st, nullptr);
+    } catch (...) {
+      scatter_mask = nullptr;
+      throw;
+    }
+    scatter_mask = nullptr;
+    PECS_CUDA(cudaStreamSynchronize(st));
+  }
+
+  // March n_points parameter sets through the n_inst slots.  Outputs per
+  // point: steps (to convergence; max_steps when capped; negative when the
+  // state became non-finite), interface current, optionally final fields.
+  void sweep_stream(int n_points, const pecs_params* params, const double* const* init_n,
+                    const double* const* init_p, int max_steps, double tol, int check_every,
+                    int* out_steps, double* out_current, double* const* out_fields) {
+    if (n_points <= 0) return;
+    if (max_steps < 1) throw PecsError(PECS_E_ARG, "max_steps < 1");
+    if (check_every <= 0) check_every = 50;
+    check_every += check_every & 1;
+    std::vector<int> slot_point(n_inst, -1);
+    int next = 0;
+    auto take = [&](std::vector<int>& slots) {
+      std::vector<pecs_params> P;
+      std::vector<const double*> in, ip;
+      for (int i : slots) {
+        slot_point[i] = next;
+        P.push_back(params[next]);
+        in.push_back(init_n ? init_n[next] : nullptr);
+        ip.push_back(init_p ? init_p[next] : nullptr);
+        ++next;
+      }
+      refill(slots, P, in, ip);
+    };
+    // first fill: every slot the points can occupy; idle slots are inactive
+    std::vector<int> first;
+    for (int i = 0; i < n_inst && next + (int)first.size() < n_points; ++i) first.push_back(i);
+    carriers_advanced = false;
+    initialized = true;
+    take(first);
+    {
+      std::vector<int> act(n_inst, 0), zeros(n_inst, 0);
+      for (int i : first) act[i] = 1;
+      PECS_CUDA(cudaMemcpyAsync(active.p, act.data(), n_inst * 4, cudaMemcpyHostToDevice, st));
+      PECS_CUDA(cudaMemcpyAsync(conv_step.p, zeros.data(), n_inst * 4, cudaMemcpyHostToDevice, st));
+      PECS_CUDA(cudaMemsetAsync(start_step.p, 0, n_inst * 4, st));
+      PECS_CUDA(cudaMemsetAsync(capped.p, 0, n_inst * 4, st));
+      PECS_CUDA(cudaMemsetAsync(step_ctr.p, 0, 4, st));
+      PECS_CUDA(cudaStreamSynchronize(st));
+    }
+    step_cap = max_steps;
+    const bool use_graph = opt.use_graphs != 0;
+    if (use_graph && (!graph_valid || graph_tol != tol || graph_cap != step_cap)) capture_graph(tol);
+    int done_steps = 0, harvested = 0;
+    last_run_steps = 0;
+    std::vector<int> cs(n_inst), act(n_inst);
+    DBuf<double> cur_dev;
+    cur_dev.alloc(n_inst);
+    std::vector<double> hcur(n_inst);
+    while (harvested < n_points) {
+      for (int k = 0; k < check_every; k += 2) {
+        if (use_graph) {
+          PECS_CUDA(cudaGraphLaunch(graph2[cur], st));
+        } else {
+          step_with_check(st, tol);
+          step_with_check(st, tol);
+        }
+      }
+      done_steps += check_every;
+      last_run_steps = done_steps;
+      PECS_CUDA(cudaMemcpyAsync(cs.data(), conv_step.p, n_inst * 4, cudaMemcpyDeviceToHost, st));
+      PECS_CUDA(cudaMemcpyAsync(act.data(), active.p, n_inst * 4, cudaMemcpyDeviceToHost, st));
+      PECS_CUDA(cudaStreamSynchronize(st));
+      std::vector<int> finished;
+      for (int i = 0; i < n_inst; ++i)
+        if (slot_point[i] >= 0 && !act[i]) finished.push_back(i);
+      if (finished.empty()) continue;
+      // harvest from the snapshots (state at each slot's final step)
+      if (full && !S->iface_semi.empty() && out_current) {
+        FieldPtrs F{};
+        for (int f = 0; f < 5; ++f) {
+          F.u[f] = snap[f].p;
+          F.bc[f] = bconst[f].p;
+          F.nd[f] = nd[f];
+        }
+        k_interface_current<<<n_inst, kRedThreads, 0, st>>>(T, R[0], R[1], F, inst.p, iface_ne.p, iface_pe.p,
+                                                           isemi.p, ielec.p, (int)S->iface_semi.size(),
+                                                           S->n1, S->nq1, cur_dev.p);
+        PECS_CUDA(cudaGetLastError());
+        PECS_CUDA(cudaMemcpyAsync(hcur.data(), cur_dev.p, n_inst * 8, cudaMemcpyDeviceToHost, st));
+      }
+      for (int i : finished) {
+        const int pt = slot_point[i];
+        if (out_fields)
+          for (int f = 0; f < 5; ++f)
+            if (nd[f] && out_fields[f])
+              PECS_CUDA(cudaMemcpyAsync(out_fields[f] + (size_t)pt * nd[f], snap[f].p + (size_t)i * nd[f],
+                                        (size_t)nd[f] * 8, cudaMemcpyDeviceToHost, st));
+      }
+      PECS_CUDA(cudaStreamSynchronize(st));
+      std::vector<int> start_h(n_inst);
+      PECS_CUDA(cudaMemcpy(start_h.data(), start_step.p, n_inst * 4, cudaMemcpyDeviceToHost));
+      std::vector<int> refills;
+      for (int i : finished) {
+        const int pt = slot_point[i];
+        if (out_steps) out_steps[pt] = cs[i] < 0 ? cs[i] + start_h[i] : cs[i] - start_h[i];
+        if (out_current) out_current[pt] = (full && !S->iface_semi.empty()) ? hcur[i] : 0.0;
+        ++harvested;
+        slot_point[i] = -1;
+        if (next < n_points) refills.push_back(i);
+      }
+      if (!refills.empty()) {
+        take(refills);
+        // restart the refilled slots at the current step
+        int step_now = 0;
+        PECS_CUDA(cudaMemcpy(&step_now, step_ctr.p, 4, cudaMemcpyDeviceToHost));
+        for (int i : refills) {
+          const int one = 1, zero = 0;
+          PECS_CUDA(cudaMemcpyAsync(active.p + i, &one, 4, cudaMemcpyHostToDevice, st));
+          PECS_CUDA(cudaMemcpyAsync(conv_step.p + i, &zero, 4, cudaMemcpyHostToDevice, st));
+          PECS_CUDA(cudaMemcpyAsync(capped.p + i, &zero, 4, cudaMemcpyHostToDevice, st));
+          PECS_CUDA(cudaMemcpyAsync(start_step.p + i, &step_now, 4, cudaMemcpyHostToDevice, st));
+          PECS_CUDA(cudaStreamSynchronize(st));
+        }
+      }
+    }
   }
 
   void interface_current(double* out) {
@@ -1422,6 +1628,19 @@ int pecs_interface_current(pecs_ctx* ctx, double* out) {
     if (!ctx || !out) throw PecsError(PECS_E_ARG, "NULL argument");
     need_device(ctx->e);
     ctx->e.interface_current(out);
+  })
+}
+
+int pecs_sweep_stream(pecs_ctx* ctx, int n_points, const pecs_params* params,
+                      const double* const* init_n, const double* const* init_p, int max_steps, double tol,
+                      int check_every, int* steps, double* currents, double* const* final_fields) {
+  PECS_TRY({
+    if (!ctx || !params || n_points < 0) throw PecsError(PECS_E_ARG, "invalid arguments");
+    need_device(ctx->e);
+    if (!(tol >= 0.0)) throw PecsError(PECS_E_ARG, "tol must be >= 0");
+    if (ctx->e.carriers_advanced) throw PecsError(PECS_E_STATE, "step in progress");
+    ctx->e.sweep_stream(n_points, params, init_n, init_p, max_steps, tol, check_every, steps, currents,
+                        final_fields);
   })
 }
 

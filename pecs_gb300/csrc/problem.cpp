@@ -567,17 +567,21 @@ Setup::Setup(const std::vector<pecs_params>& p)
 void Setup::compute_instances(const std::vector<pecs_params>& p) {
   inst = p;
   const int ninst = (int)p.size();
-  const int nloc = n_rt + n_phi;
   for (int fld = 0; fld < 5; ++fld) bconst[fld].assign(ninst, {});
   iface_ne.assign(ninst, {});
   iface_pe.assign(ninst, {});
   schottky_ne.assign(ninst, {});
   schottky_pe.assign(ninst, {});
   for (int fld = 0; fld < 4; ++fld) init[fld].assign(ninst, {});
+  for (int s = 0; s < ninst; ++s) compute_instance(s);
+}
+
+void Setup::compute_instance(int s) {
+  const int nloc = n_rt + n_phi;
   std::vector<double> g1, w1;
   gauss01(k + 1, g1, w1);
-  for (int s = 0; s < ninst; ++s) {
-    const pecs_params& Pi = p[s];
+  {
+    const pecs_params& Pi = inst[s];
     for (int reg = 0; reg < (full ? 2 : 1); ++reg) {
       const CarrierSystem& CS = reg == 0 ? semi : elec;
       const Grid& g = CS.grid;

@@ -77,6 +77,8 @@ struct Setup {
 
   explicit Setup(const std::vector<pecs_params>& p);
   void compute_instances(const std::vector<pecs_params>& p);
+  // recompute the per-instance data of instance s from inst[s]
+  void compute_instance(int s);
 };
 
 // Validates a parameter set; returns an empty string when it is usable.

@@ -325,3 +325,60 @@ def warm_started_sweep(ctx: Context, op: Optional[NeuralOperator], thetas: np.nd
     apply_prediction(ctx, pred, [k for k in range(B) if use_pred[k]], lay)
     steps, _ = ctx.run_to_steady_state(max_steps, tol, check_every)
     return steps + 2, fallback, ctx.interface_current()
+
+
+def warm_start_vectors(ctx: Context, op: NeuralOperator, thetas: np.ndarray, base: Params,
+                       chunk: Optional[int] = None):
+    """Learned initial densities for every row of ``thetas`` and the
+    first-step-residual fallback decision, for a streamed sweep.
+
+    Per batch of ctx.n_inst rows the context marches one step from the
+    standard initial condition and one from the prediction; a prediction is
+    used when its first-step relative change is finite and below the standard
+    one.  Returns (init_n, init_p, fallback, keep): per row a device pointer
+    (0 = standard initial condition) to a full electron / hole vector, the
+    fallback flags, and the tensors that own the vectors."""
+    import torch
+    B = ctx.n_inst
+    lay = Layout.of(ctx)
+    n = thetas.shape[0]
+    X = torch.from_numpy(normalize(thetas)).cuda()
+    pred = op.predict(X)
+    fallback = np.ones(n, dtype=bool)
+    for b0 in range(0, n, B):
+        rows = list(range(b0, min(n, b0 + B)))
+        pad = rows + [rows[-1]] * (B - len(rows))
+        ctx.set_instances([instance_params(thetas[r], base) for r in pad])
+        ctx.initialize()
+        _, rel_std = ctx.run_to_steady_state(1, 0.0, 1)
+        ctx.initialize()
+        apply_prediction(ctx, pred[pad], range(B), lay)
+        _, rel_pred = ctx.run_to_steady_state(1, 0.0, 1)
+        ok = np.isfinite(rel_pred) & (rel_pred < rel_std)
+        for k, r in enumerate(rows):
+            fallback[r] = not ok[k]
+    nd = lay.nd_carrier
+    vn = torch.zeros(n, nd, dtype=torch.float64, device="cuda")
+    vp = torch.zeros(n, nd, dtype=torch.float64, device="cuda")
+    vn[:, lay.u_off:lay.u_off + lay.n_u] = pred[:, :lay.n_u].exp()
+    vp[:, lay.u_off:lay.u_off + lay.n_u] = pred[:, lay.n_u:2 * lay.n_u].exp()
+    init_n = [0 if fallback[r] else vn[r].data_ptr() for r in range(n)]
+    init_p = [0 if fallback[r] else vp[r].data_ptr() for r in range(n)]
+    return init_n, init_p, fallback, (vn, vp, pred)
+
+
+def stream_warm_sweep(ctx: Context, op: Optional[NeuralOperator], thetas: np.ndarray, base: Params,
+                      max_steps=5000, tol=1e-8, check_every=50, want_fields: bool = False):
+    """All rows of ``thetas`` to steady state in one streamed sweep through
+    ctx's slots (pecs_sweep_stream), warm-started by ``op`` (None: standard
+    initial condition).  Returns (steps incl. the two probe steps of a
+    warm-started point, fallback flags, currents, fields or None)."""
+    params = [instance_params(t, base) for t in thetas]
+    if op is None:
+        steps, cur, fin = ctx.sweep_stream(params, max_steps, tol, check_every, want_fields=want_fields)
+        return steps, np.ones(len(params), dtype=bool), cur, fin
+    init_n, init_p, fallback, keep = warm_start_vectors(ctx, op, thetas, base)
+    steps, cur, fin = ctx.sweep_stream(params, max_steps, tol, check_every, init_n=init_n, init_p=init_p,
+                                       want_fields=want_fields)
+    del keep
+    return steps + 2, fallback, cur, fin
