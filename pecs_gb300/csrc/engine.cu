@@ -1290,7 +1290,7 @@ struct Engine {
         if (out_current) out_current[pt] = (full && !S->iface_semi.empty()) ? hcur[i] : 0.0;
         ++harvested;
         slot_point[i] = -1;
-        if (next < n_points) refills.push_back(i);
+        if (next + (int)refills.size() < n_points) refills.push_back(i);
       }
       if (!refills.empty()) {
         take(refills);
@@ -1636,6 +1636,13 @@ int pecs_sweep_stream(pecs_ctx* ctx, int n_points, const pecs_params* params,
                       int check_every, int* steps, double* currents, double* const* final_fields) {
   PECS_TRY({
     if (!ctx || !params || n_points < 0) throw PecsError(PECS_E_ARG, "invalid arguments");
+    {
+      // every point must share the context's meshes and fixed matrices
+      std::vector<pecs_params> chk(params, params + n_points);
+      chk.insert(chk.begin(), ctx->e.S->inst[0]);
+      std::string err = validate_params(chk.data(), (int)chk.size());
+      if (!err.empty()) throw PecsError(PECS_E_ARG, err);
+    }
     need_device(ctx->e);
     if (!(tol >= 0.0)) throw PecsError(PECS_E_ARG, "tol must be >= 0");
     if (ctx->e.carriers_advanced) throw PecsError(PECS_E_STATE, "step in progress");

@@ -290,17 +290,26 @@ std::string validate_params(const pecs_params* p, int n_inst) {
   }
   for (int i = 1; i < n_inst; ++i) {
     const pecs_params& b = p[i];
-    bool same = a.degree == b.degree && a.full_system == b.full_system && a.nx_semi == b.nx_semi &&
-                a.nx_elec == b.nx_elec && a.ny == b.ny && a.x_semi0 == b.x_semi0 &&
-                a.x_semi1 == b.x_semi1 && a.x_elec1 == b.x_elec1 && a.height == b.height &&
-                a.lambda2 == b.lambda2 && a.eps_semi == b.eps_semi && a.eps_elec == b.eps_elec &&
-                a.dt == b.dt && a.penalty == b.penalty &&
-                std::memcmp(a.mu, b.mu, sizeof(a.mu)) == 0 &&
-                std::memcmp(a.bc_semi, b.bc_semi, sizeof(a.bc_semi)) == 0 &&
-                std::memcmp(a.bc_elec, b.bc_elec, sizeof(a.bc_elec)) == 0 &&
-                std::memcmp(a.bc_poisson, b.bc_poisson, sizeof(a.bc_poisson)) == 0;
-    if (!same) {
-      e << "instance " << i << " differs from instance 0 in a matrix-defining field; ";
+    std::string diff;
+    auto chk = [&](bool eq, const char* name) {
+      if (!eq) diff += std::string(diff.empty() ? "" : ", ") + name;
+    };
+    chk(a.degree == b.degree, "degree");
+    chk(a.full_system == b.full_system, "full_system");
+    chk(a.nx_semi == b.nx_semi && a.nx_elec == b.nx_elec && a.ny == b.ny, "cell counts");
+    chk(a.x_semi0 == b.x_semi0 && a.x_semi1 == b.x_semi1 && a.x_elec1 == b.x_elec1 && a.height == b.height,
+        "geometry");
+    chk(a.lambda2 == b.lambda2, "lambda2");
+    chk(a.eps_semi == b.eps_semi && a.eps_elec == b.eps_elec, "permittivities");
+    chk(a.dt == b.dt, "dt");
+    chk(a.penalty == b.penalty, "penalty");
+    chk(std::memcmp(a.mu, b.mu, sizeof(a.mu)) == 0, "mobilities");
+    chk(std::memcmp(a.bc_semi, b.bc_semi, sizeof(a.bc_semi)) == 0 &&
+            std::memcmp(a.bc_elec, b.bc_elec, sizeof(a.bc_elec)) == 0 &&
+            std::memcmp(a.bc_poisson, b.bc_poisson, sizeof(a.bc_poisson)) == 0,
+        "boundary ids");
+    if (!diff.empty()) {
+      e << "instance " << i << " differs from instance 0 in a matrix-defining field (" << diff << "); ";
       break;
     }
   }
