@@ -66,13 +66,18 @@ def test_stream_warm_start_vectors(pecs_lib):
     n_slots, n_pts, max_steps, tol, every = 4, 9, 700, 1e-6, 10
     pts = _points(n_pts, seed=5)
     ctx = pg.Context(pts[:n_slots])
-    nd = ctx.ndofs[pg.FIELD_N]
-    # a perturbed standard initial condition as the "prediction"
-    ctx.set_instances(pts[:n_slots])
-    ctx.initialize()
-    base_n = torch.from_numpy(ctx.get_state(pg.FIELD_N, 0)).cuda()
-    base_p = torch.from_numpy(ctx.get_state(pg.FIELD_P, 0)).cuda()
-    warm = {k: (base_n * (1.0 + 0.01 * k), base_p * (1.0 - 0.01 * k)) for k in (1, 4, 8)}
+    # the "prediction": each point's own standard initial densities, scaled
+    lay = L.Layout.of(ctx)
+    warm = {}
+    for k in (1, 4, 8):
+        ctx.set_instances([pts[k]] * n_slots)
+        ctx.initialize()
+        vs = []
+        for f, fac in ((pg.FIELD_N, 1.02), (pg.FIELD_P, 0.98)):
+            v = torch.from_numpy(ctx.get_state(f, 0)).cuda()
+            v[lay.u_off:lay.u_off + lay.n_u] *= fac
+            vs.append(v)
+        warm[k] = tuple(vs)
     init_n = [warm[k][0].data_ptr() if k in warm else 0 for k in range(n_pts)]
     init_p = [warm[k][1].data_ptr() if k in warm else 0 for k in range(n_pts)]
     steps, cur, fin = ctx.sweep_stream(pts, max_steps, tol, every, init_n=init_n, init_p=init_p,
@@ -91,4 +96,3 @@ def test_stream_warm_start_vectors(pecs_lib):
             a = fin[f][k * ctx.ndofs[f]:(k + 1) * ctx.ndofs[f]]
             b = ctx.get_state(f, 0)
             assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(b), (f, k)
-    assert nd > 0
