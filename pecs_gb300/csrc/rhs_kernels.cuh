@@ -16,6 +16,7 @@
 // _for_electrolyte (SolarCell.cpp:487-815): -(v, sum q_i u_i) on the Phi rows
 // of the matching Poisson cell plus the constant doping/Dirichlet part.
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace pecs {
@@ -31,6 +32,9 @@ struct Tables {
   const double* mref;  // n1*n1  unit-square mass matrix
   // FP32 copies for the mixed-precision path
   const float *phi_f, *qw_f, *fphi_f, *fw_f, *psix_f, *psiy_f;
+  // drift tensors of the current equations, sum_q phi_a phi_b psi_c w_q on
+  // the unit square: [a][b][c], n1 * n1 * nrt each (x and y components)
+  const double *drift_x, *drift_y;
 };
 
 struct RegionDev {
@@ -81,11 +85,16 @@ template <>
 __device__ __forceinline__ const float* tab<float>(const double*, const float* f) { return f; }
 
 // grid: x over (cells of both regions) * 2 carriers, y over instances.
-// Tq is the arithmetic type of the quadrature terms (drift, SRH, interface,
-// Schottky).  Tq = double is the FP64 path.  Tq = float is the mixed path: the
-// dominant, time-integrating part of the RHS -- the constant part and
-// (1/dt) M u^{n-1} -- stays FP64, and only the O(|D| dt)-relative corrections
-// run on the FP32 pipe (GB300 issues FP32 FMAs ~60x faster than FP64).
+// Tq is the arithmetic type of the quadrature terms (SRH, interface, Schottky,
+// and in the FP64 path the drift).  Tq = double is the FP64 path.  Tq = float
+// is the mixed path: the constant part, (1/dt) M u^{n-1} and the drift term
+// of the current equations, (q/eps) u D, stay FP64 -- the drift is large
+// (|D|/h relative to the density terms) and its rounding would leave a
+// per-step noise of ~eps32 |D| dt / h in the densities, above a 1e-8
+// steady-state criterion; it is evaluated as the bilinear form
+// sum_bc T_abc u_b D_c with precomputed tensors -- while the small
+// recombination and interface terms run on the FP32 pipe (GB300 issues FP32
+// FMAs ~60x faster than FP64).
 template <int K, typename Tq>
 __global__ void __launch_bounds__(128)
     k_carrier_rhs(Tables T, RegionDev semi, RegionDev elec, int n_regions, FieldPtrs F,
@@ -136,6 +145,9 @@ __global__ void __launch_bounds__(128)
   const Tq inv_eps = (Tq)R.inv_eps;
   // quadrature-term accumulators: [Jx (n1) | Jy (n1) | u (n1)]
   Tq r[3 * n1];
+  double drift64[2 * n1];  // mixed path: FP64 drift of the current rows
+#pragma unroll
+  for (int a = 0; a < 2 * n1; ++a) drift64[a] = 0.0;
 #pragma unroll
   for (int a = 0; a < 3 * n1; ++a) r[a] = Tq(0);
   const bool srh = in_semi && P.srh;
@@ -163,9 +175,35 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
     for (int a = 0; a < n1; ++a) {
       const Tq ph = phi[a * Q + q];
-      r[a] += ph * Ex * w;
-      r[n1 + a] += ph * Ey * w;
+      if constexpr (std::is_same<Tq, double>::value) {
+        r[a] += ph * Ex * w;
+        r[n1 + a] += ph * Ey * w;
+      }
       r[2 * n1 + a] += ph * Rq;
+    }
+  }
+  if constexpr (!std::is_same<Tq, double>::value) {
+    // FP64 drift of the current equations: (q/eps) hx hy sum_bc T_abc u_b D_c
+    double Dv[nrt];
+#pragma unroll
+    for (int b = 0; b < nrt; ++b) Dv[b] = Pv[R.rt[c * nrt + b]];
+    const double sc = (which ? 1.0 : -1.0) * R.inv_eps * hxhy;
+#pragma unroll
+    for (int a = 0; a < n1; ++a) {
+      double sx = 0.0, sy = 0.0;
+#pragma unroll
+      for (int b = 0; b < n1; ++b) {
+        double tx = 0.0, ty = 0.0;
+#pragma unroll
+        for (int cc = 0; cc < nrt; ++cc) {
+          tx += T.drift_x[(a * n1 + b) * nrt + cc] * Dv[cc];
+          ty += T.drift_y[(a * n1 + b) * nrt + cc] * Dv[cc];
+        }
+        sx += tx * uown[b];
+        sy += ty * uown[b];
+      }
+      drift64[a] = sc * sx;
+      drift64[n1 + a] = sc * sy;
     }
   }
   // interface Robin transfer (SolarCell.cpp:1265-1347, 1630-1716)
@@ -234,7 +272,10 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
     for (int a = 0; a < n1; ++a) {
       const size_t o = (size_t)comp * nc * n1 + c * n1 + a;
-      outp[o] = bcp[o] + (double)r[comp * n1 + a];
+      if constexpr (std::is_same<Tq, double>::value)
+        outp[o] = bcp[o] + (double)r[comp * n1 + a];
+      else
+        outp[o] = bcp[o] + drift64[comp * n1 + a];
     }
 #pragma unroll
   for (int a = 0; a < n1; ++a) {
