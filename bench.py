@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiler mode: initialise the workload, run this many time steps "
                          "with direct (non-graph) launches, print one line and exit")
+    ap.add_argument("--profile-sweep", choices=["carrier", "poisson"], default=None,
+                    help="profiler mode: build the workload and run exactly two solve sweeps of "
+                         "one bank (a warm-up and a timed one), print one line and exit")
     return ap.parse_args()
 
 
@@ -250,9 +253,28 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_sweep:
+        return run_profile_sweep(args)
     if args.mode == "full" and not args.profile_steps:
         return run_full(args)
     return run_plain(args)
+
+
+def run_profile_sweep(args):
+    """Two sweeps of one factor bank over the workload's right-hand sides (the
+    launches an ncu capture of one sweep selects with -k regex:k_panel or
+    regex:"k_forward|k_backward" and -c <launches per sweep>)."""
+    import pecs_gb300 as pg
+    pg.build()
+    prec = {"fp64": pg.PREC_FP64, "fp32ir": pg.PREC_FP32_IR, "mixed": pg.PREC_FP32_MIXED}[args.precision]
+    ctx = pg.Context(workload_params(args, 0), precision=prec)
+    which = 0 if args.profile_sweep == "carrier" else 1
+    info = ctx.info()
+    ms = ctx.time_solve(which, reps=1)
+    print(json.dumps({"profile_sweep": args.profile_sweep, "n_inst": args.n_inst, "precision": args.precision,
+                      "sweep_ms": ms, "launches_per_sweep": info.solve_launches[which],
+                      "bytes_per_sweep": info.solve_bytes[which]}))
+    return 0
 
 
 def run_plain(args):
