@@ -302,12 +302,13 @@ class Context:
 
     def sweep_stream(self, params: Sequence[Params], max_steps: int, tol: float,
                      check_every: int = 50, init_n: Optional[Sequence[int]] = None,
-                     init_p: Optional[Sequence[int]] = None, want_fields: bool = False):
+                     init_p: Optional[Sequence[int]] = None, want_fields=False):
         """Streamed I-V sweep (pecs_sweep_stream): every parameter set marched
         to steady state through this context's slots, each slot refilled as
         soon as its point finishes.  init_n / init_p: per point a device
         pointer (int, 0 = built-in initial condition) to a full electron /
-        hole vector.  Returns (steps, currents, fields or None)."""
+        hole vector.  want_fields: False, True (every field) or a list of
+        field indices to return.  Returns (steps, currents, fields or None)."""
         n = len(params)
         arr = (F.pecs_params * n)(*[p.to_c() for p in params])
         def ptrs(lst):
@@ -321,7 +322,8 @@ class Context:
         cur = np.zeros(n)
         finals = fptrs = None
         if want_fields:
-            finals = {f: np.zeros(n * self.ndofs[f]) for f in range(5) if self.ndofs[f]}
+            sel = range(5) if want_fields is True else want_fields
+            finals = {f: np.zeros(n * self.ndofs[f]) for f in sel if self.ndofs[f]}
             fptrs = (C.POINTER(C.c_double) * 5)()
             for f, a in finals.items():
                 fptrs[f] = _dptr(a)

@@ -251,31 +251,27 @@ class NeuralOperator:
 # -- data generation and warm-started sweeps --------------------------------------
 
 def steady_states(ctx: Context, thetas: np.ndarray, base: Params, max_steps=5000, tol=1e-8,
-                  check_every=50):
-    """March every row of ``thetas`` (batches of ctx.n_inst) to steady state with
-    the plain method; returns (targets (n, n_out) torch float64 cuda, steps)."""
+                  check_every=50, chunk_batches: int = 8):
+    """March every row of ``thetas`` to steady state with the plain method,
+    streamed through ctx's slots (chunks of chunk_batches * ctx.n_inst points);
+    returns (targets (n, n_out) torch float64 cuda, steps)."""
     import torch
     lay = Layout.of(ctx)
-    B = ctx.n_inst
     n = thetas.shape[0]
     Y = torch.empty(n, lay.n_out, dtype=torch.float64, device="cuda")
     steps = np.zeros(n, dtype=np.int64)
-    bufs = {f: torch.empty(ctx.ndofs[f], dtype=torch.float64, device="cuda")
-            for f in (F.FIELD_N, F.FIELD_P, F.FIELD_POISSON)}
-    for b0 in range(0, n, B):
-        rows = list(range(b0, min(n, b0 + B)))
-        pad = rows + [rows[-1]] * (B - len(rows))
-        ctx.set_instances([instance_params(thetas[r], base) for r in pad])
-        ctx.initialize()
-        s, _ = ctx.run_to_steady_state(max_steps, tol, check_every)
-        for k, r in enumerate(rows):
-            for f, t in bufs.items():
-                ctx.get_state_device(f, k, t.data_ptr())
-            nu = bufs[F.FIELD_N][lay.u_off:lay.u_off + lay.n_u].clamp_min(DENSITY_FLOOR).log()
-            pu = bufs[F.FIELD_P][lay.u_off:lay.u_off + lay.n_u].clamp_min(DENSITY_FLOOR).log()
-            ph = bufs[F.FIELD_POISSON][lay.phi_off:lay.phi_off + lay.n_phi]
-            Y[r] = torch.cat([nu, pu, ph])
-            steps[r] = s[k]
+    step = chunk_batches * ctx.n_inst
+    for b0 in range(0, n, step):
+        rows = thetas[b0:b0 + step]
+        s, _, fin = ctx.sweep_stream([instance_params(t, base) for t in rows], max_steps, tol, check_every,
+                                     want_fields=[F.FIELD_N, F.FIELD_P, F.FIELD_POISSON])
+        m = rows.shape[0]
+        nd, ndp = lay.nd_carrier, lay.nd_poisson
+        nn = torch.from_numpy(fin[F.FIELD_N].reshape(m, nd)[:, lay.u_off:lay.u_off + lay.n_u]).cuda()
+        pp = torch.from_numpy(fin[F.FIELD_P].reshape(m, nd)[:, lay.u_off:lay.u_off + lay.n_u]).cuda()
+        ph = torch.from_numpy(fin[F.FIELD_POISSON].reshape(m, ndp)[:, lay.phi_off:lay.phi_off + lay.n_phi]).cuda()
+        Y[b0:b0 + m] = torch.cat([nn.clamp_min(DENSITY_FLOOR).log(), pp.clamp_min(DENSITY_FLOOR).log(), ph], dim=1)
+        steps[b0:b0 + m] = s
     return Y, steps
 
 

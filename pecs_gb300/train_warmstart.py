@@ -5,7 +5,7 @@
 1. Draws n_train + n_eval parameter sets (seeded) from the benchmark's
    distributions (pecs_gb300.learned.RANGES).
 2. Marches every training draw to steady state with the plain method
-   (batched, ``--precision``), 64 instances per context.
+   (streamed through 64 slots, ``--precision``).
 3. Builds the POD basis of [log n | log p | Phi] and trains the MLP with the
    library's BF16/FP32 kernels (Adam, cosine decay).
 4. On the held-out draws: prediction error, steps to steady state with and
@@ -70,20 +70,12 @@ def main():
     for nm, (a, b) in zip(names, blocks):
         d = (P[:, a:b] - Yev[:, a:b]).norm(dim=1) / Yev[:, a:b].norm(dim=1).clamp_min(1e-30)
         err[nm] = {"median": float(d.median()), "max": float(d.max())}
-    steps_warm, fallbacks, cur_warm, cur_plain = [], [], [], []
-    for b0 in range(0, len(ev), B):
-        rows = ev[b0:b0 + B]
-        if len(rows) < B:
-            break
-        s_w, fb, c_w = L.warm_started_sweep(ctx, op, rows, base)
-        s_p, _, c_p = L.warm_started_sweep(ctx, None, rows, base)
-        steps_warm.extend(s_w.tolist())
-        fallbacks.extend(fb.tolist())
-        cur_warm.extend(c_w.tolist())
-        cur_plain.extend(c_p.tolist())
-    steps_warm = np.array(steps_warm)
+    # held-out sweeps, streamed: warm-started and from the standard initial condition
+    steps_warm, fallbacks, cur_warm, _ = L.stream_warm_sweep(ctx, op, ev, base)
+    steps_std, _, cur_plain, _ = L.stream_warm_sweep(ctx, None, ev, base)
+    steps_warm = np.asarray(steps_warm)
     m = len(steps_warm)
-    cur_warm, cur_plain = np.array(cur_warm), np.array(cur_plain)
+    cur_warm, cur_plain = np.asarray(cur_warm), np.asarray(cur_plain)
     rep = {
         "n_train": args.n_train, "n_eval": args.n_eval, "refine": args.refine, "rank": args.rank,
         "hidden": args.hidden, "n_params": op.mlp.n_params, "epochs": args.epochs,
@@ -92,6 +84,7 @@ def main():
         "final_loss": float(hist[-1]) if hist else None, "first_loss": float(hist[0]) if hist else None,
         "prediction_rel_error": err,
         "steps_plain_median": float(np.median(steps_plain[:m])),
+        "steps_plain_streamed_median": float(np.median(steps_std)),
         "steps_warm_median": float(np.median(steps_warm)),
         "steps_saved_fraction": float(1.0 - steps_warm.sum() / steps_plain[:m].sum()),
         "fallback_rate": float(np.mean(fallbacks)),
