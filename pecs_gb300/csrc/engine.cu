@@ -718,11 +718,14 @@ struct Engine {
     for (int t = 0; t < n_fe; ++t) cf.push_back(&fe[t]);
     const int fprec = opt.precision == PECS_PREC_FP64 ? PECS_PREC_FP64 : PECS_PREC_FP32_IR;
     // many right-hand sides per set: panel kernels (lanes over right-hand sides)
-    int min_rc = 1 << 30;
-    for (auto& f : carrier_set_fields()) min_rc = std::min(min_rc, n_inst * (int)f.size());
+    int min_rc = 1 << 30, max_rc = 0;
+    for (auto& f : carrier_set_fields()) {
+      min_rc = std::min(min_rc, n_inst * (int)f.size());
+      max_rc = std::max(max_rc, n_inst * (int)f.size());
+    }
     const PanelTuning tu{opt.panel_chunk, opt.panel_min_ctas};
-    bank_c.build(cf, fprec, min_rc >= kPanelMinRhs, tu);
-    bank_p.build({&fp}, fprec, n_inst >= kPanelMinRhs, tu);
+    bank_c.build(cf, fprec, min_rc >= kPanelMinRhs, tu, max_rc);
+    bank_p.build({&fp}, fprec, n_inst >= kPanelMinRhs, tu, n_inst);
     // free host copies of the factor values (structure is kept for stats)
     for (auto* F : {&fs[0], &fs[1], &fe[0], &fe[1], &fp}) {
       std::vector<std::vector<double>>().swap(F->Gf);

@@ -412,6 +412,9 @@ constexpr int kPanelKcSteps = 8;
 constexpr int kPanelKc[kPanelKcSteps] = {128, 64, 32, 16, 8, 4, 2, 1};
 constexpr size_t kPanelSmem = 160 * 1024;
 constexpr int kPanelCmMax = 4096;  // staged child-update rows per node (more: read from global)
+constexpr int kSplitMaxParts = 8;  // split-K: at most this many column parts per tile
+constexpr int kSplitPart = 128;    // split-K: columns per part (a multiple of every chunk size)
+constexpr int kSplitMinK = 192;    // split-K: only nodes with at least this many columns
 constexpr size_t kWarpSmem = 48 * 1024;  // leaf levels: shared memory per CTA
 
 // RPL consecutive values of one interleaved row (offset a multiple of RPL),
@@ -567,7 +570,8 @@ __device__ __forceinline__ void stage_row(T* dst, const T* src, bool ok) {
 template <typename T, int RPL, bool FWD, typename SVT>
 __global__ void __launch_bounds__(kSolveThreads)
     k_panel(BankView B, SVT S, const PanelItem* __restrict__ items, int kc_cap, int ds_rows,
-            int ri_max, int sc_rows, int max_s, int max_f, int cm_cap) {
+            int ri_max, int sc_rows, int max_s, int max_f, int cm_cap, T* __restrict__ partials,
+            int* __restrict__ counters, int parts_ld, int ychunks) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int RC = 32 * RPL;
   constexpr int NW = kSolveThreads / 32;
@@ -590,6 +594,9 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int nrows = r1 - r0;
   const int wpr = 32 / ri;  // warps sharing a row group (column parts)
   const int g = warp / wpr, part = warp % wpr;
+  // split-K: this CTA covers columns [k_lo, k_hi) of a tile split in n_parts
+  const bool split = I.e.z >= 0;
+  const int k_lo = split ? I.e.x : 0, k_hi = split ? I.e.y : K;
   T* Ds = reinterpret_cast<T*>(smem_raw);  // [ds_rows][RC], ds_rows >= 32 when ri < 32
   T* Gs = Ds + (size_t)ds_rows * RC;        // [kc_cap][ri]
   T* Sc = Gs + (size_t)kc_cap * ri_max;     // [sc_rows][RC] child-update rows of a chunk
@@ -620,8 +627,8 @@ __global__ void __launch_bounds__(kSolveThreads)
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int q = 0; q < RPL; ++q) acc[i][q] = T(0);
-  for (int k0 = 0; k0 < K; k0 += kc_cap) {
-    const int kc = min(kc_cap, K - k0);
+  for (int k0 = k_lo; k0 < k_hi; k0 += kc_cap) {
+    const int kc = min(kc_cap, k_hi - k0);
     // (A) asynchronous copies: block tile, right-hand-side rows, child rows
     for (int idx = tid; idx < kc * ri; idx += kSolveThreads) {
       const int k = idx / ri, i = idx - k * ri;
@@ -698,11 +705,22 @@ __global__ void __launch_bounds__(kSolveThreads)
       st_rhs<RPL>(st.x + (size_t)src_s[row] * R + rl, v);
     }
   };
-  if (wpr == 1) {
-    if (!lane_ok) return;
+  // row totals -> destination, or (split-K) this part's slab of partials
+  auto finish = [&](int i, T (&v)[RPL]) {
+    if (!split) {
+      emit(i, v);
+    } else {
+      T* dst = partials + ((size_t)(I.e.z * kSplitMaxParts + I.d.w) * 32 + i) * parts_ld + rl;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if (4 * g + i < nrows) emit(4 * g + i, acc[i]);
+      for (int q = 0; q < RPL; ++q) dst[q] = v[q];
+    }
+  };
+  if (wpr == 1) {
+    if (lane_ok) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (4 * g + i < nrows) finish(4 * g + i, acc[i]);
+    }
   } else {
     T* red = Ds;  // [wpr][ri][RC] = 32 * RC values
 #pragma unroll
@@ -711,18 +729,44 @@ __global__ void __launch_bounds__(kSolveThreads)
       for (int q = 0; q < RPL; ++q)
         red[((size_t)part * ri + 4 * g + i) * RC + lane * RPL + q] = acc[i][q];
     __syncthreads();
-    if (!lane_ok) return;
+    if (lane_ok) {
+      for (int i = warp; i < nrows; i += NW) {
+        T v[RPL];
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) {
+          T t = T(0);
+          for (int p = 0; p < wpr; ++p) t += red[((size_t)p * ri + i) * RC + lane * RPL + q];
+          v[q] = t;
+        }
+        finish(i, v);
+      }
+    }
+  }
+  if (!split) return;
+  // split-K: the last CTA of the tile to arrive adds the parts in part order
+  // (the result does not depend on which CTA is last) and writes the rows
+  __shared__ int ticket;
+  __threadfence();
+  __syncthreads();
+  int* ctr = counters + (size_t)I.e.z * ychunks + blockIdx.y;
+  if (tid == 0) ticket = atomicAdd(ctr, 1);
+  __syncthreads();
+  if (ticket != I.e.w - 1) return;
+  __threadfence();
+  if (lane_ok) {
     for (int i = warp; i < nrows; i += NW) {
       T v[RPL];
 #pragma unroll
-      for (int q = 0; q < RPL; ++q) {
-        T t = T(0);
-        for (int p = 0; p < wpr; ++p) t += red[((size_t)p * ri + i) * RC + lane * RPL + q];
-        v[q] = t;
+      for (int q = 0; q < RPL; ++q) v[q] = T(0);
+      for (int p = 0; p < I.e.w; ++p) {
+        const T* src = partials + ((size_t)(I.e.z * kSplitMaxParts + p) * 32 + i) * parts_ld + rl;
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) v[q] += __ldcg(src + q);
       }
       emit(i, v);
     }
   }
+  if (tid == 0) *ctr = 0;
 }
 
 // Leaf levels: a warp per node (all of its rows) and right-hand-side chunk,
@@ -845,7 +889,8 @@ PanelChoice choose_panel(const PanelPlan& L, int max_nrhs, int rpl_max, int min_
 
 template <typename T, int RPL, typename SVT>
 void launch_panel(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
-                  const PanelTiles& P, int max_nrhs, int kcap, cudaStream_t st) {
+                  const PanelTiles& P, int max_nrhs, int kcap, int parts_ld, cudaStream_t st) {
+  const int ychunks = (parts_ld + 31) / 32;
   if (P.n_items == 0) return;
   constexpr int RC = 32 * RPL;
   const int meta = forward ? L.max_s + L.max_f + 1 + L.cm_cap : L.max_f;
@@ -865,10 +910,12 @@ void launch_panel(bool forward, const BankView& B, const SVT& S, const PanelPlan
   const dim3 grid(P.n_items, (max_nrhs + RC - 1) / RC);
   if (forward)
     k_panel<T, RPL, true, SVT><<<grid, kSolveThreads, smem, st>>>(
-        B, S, P.items.p, kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap);
+        B, S, P.items.p, kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap,
+        reinterpret_cast<T*>(L.partials.p), L.counters.p, parts_ld, ychunks);
   else
     k_panel<T, RPL, false, SVT><<<grid, kSolveThreads, smem, st>>>(
-        B, S, P.items.p, kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap);
+        B, S, P.items.p, kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap,
+        reinterpret_cast<T*>(L.partials.p), L.counters.p, parts_ld, ychunks);
   PECS_CUDA(cudaGetLastError());
 }
 
@@ -910,7 +957,8 @@ void launch_panel_warp(bool forward, const BankView& B, const SVT& S, const Pane
 
 template <typename T, typename SVT>
 void launch_panel_level(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
-                        int max_nrhs, int rpl_max, const PanelTuning& tu, cudaStream_t st) {
+                        int max_nrhs, int rpl_max, const PanelTuning& tu, int parts_ld,
+                        cudaStream_t st) {
   if (L.warp.n_items > 0) {
     // leaf level: the most right-hand sides per lane that keep a CTA's eight
     // warps within kWarpSmem
@@ -924,12 +972,26 @@ void launch_panel_level(bool forward, const BankView& B, const SVT& S, const Pan
     }
     return;
   }
+  const long long full_tiles = (long long)L.tiles[0].n_items * ((max_nrhs + 31) / 32);
+  if (L.split.n_items > 0 && full_tiles < tu.min_ctas && max_nrhs <= parts_ld) {
+    // long rows and too few full-height tiles: split along K, the most RHS per
+    // lane that still reaches the CTA target
+    int rpl = rpl_max;
+    while (rpl > 1 && (long long)L.split.n_items * ((max_nrhs + 32 * rpl - 1) / (32 * rpl)) < tu.min_ctas)
+      rpl /= 2;
+    switch (rpl) {
+      case 1: launch_panel<T, 1, SVT>(forward, B, S, L, L.split, max_nrhs, tu.chunk, parts_ld, st); break;
+      case 2: launch_panel<T, 2, SVT>(forward, B, S, L, L.split, max_nrhs, tu.chunk, parts_ld, st); break;
+      default: launch_panel<T, 4, SVT>(forward, B, S, L, L.split, max_nrhs, tu.chunk, parts_ld, st); break;
+    }
+    return;
+  }
   const PanelChoice c = choose_panel(L, max_nrhs, rpl_max, tu.min_ctas);
   const PanelTiles& P = L.tiles[c.cap_idx];
   switch (c.rpl) {
-    case 1: launch_panel<T, 1, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
-    case 2: launch_panel<T, 2, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
-    default: launch_panel<T, 4, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, st); break;
+    case 1: launch_panel<T, 1, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, parts_ld, st); break;
+    case 2: launch_panel<T, 2, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, parts_ld, st); break;
+    default: launch_panel<T, 4, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, parts_ld, st); break;
   }
 }
 }  // namespace
@@ -964,12 +1026,13 @@ int FactorBank::kernel_launches_per_solve() const {
 }
 
 void FactorBank::build(const std::vector<const MfFactor*>& factors, int precision, bool panel,
-                       PanelTuning tuning) {
+                       PanelTuning tuning, int max_nrhs) {
   if (factors.empty() || (int)factors.size() > kMaxSets)
     throw PecsError(PECS_E_ARG, "factor bank needs 1..4 factors");
   prec_ = precision;
   panel_ = panel;
   tune_ = tuning;
+  parts_ld_ = std::max(32, max_nrhs);
   if (tune_.chunk < 0 || tune_.chunk > 128 || tune_.min_ctas < 0)
     throw PecsError(PECS_E_ARG, "panel tuning out of range");
   if (tune_.chunk == 0) tune_.chunk = precision == PECS_PREC_FP64 ? kPanelKcF64 : kPanelKcF32;
@@ -1164,6 +1227,57 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
           }
           out[l].sc_rows[ci] = mx;
         }
+        // split-K items: nodes with long rows in 32-row tiles x column parts
+        // of kSplitPart (at most kSplitMaxParts); shorter nodes of the level
+        // as whole-row items
+        if (max_k >= kSplitMinK) {
+          std::vector<PanelItem> items;
+          int max_ri = 4, min_ri = 32, tiles = 0;
+          for (int g : lv[l].nodes) {
+            const int rows = forward ? hs[g] + hm[g] : hs[g];
+            const int K = forward ? hs[g] : hs[g] + hm[g];
+            const int nit = (rows + 31) / 32;
+            const int per = (rows + nit - 1) / nit;
+            int ri = 4;
+            while (ri < per) ri *= 2;
+            max_ri = std::max(max_ri, ri);
+            min_ri = std::min(min_ri, ri);
+            const long long off = forward ? goff[g] : hoff[g];
+            const int cb = cmap_ptr[cm_off[g]];
+            const int ncm = cmap_ptr[cm_off[g] + hs[g] + hm[g]] - cb;
+            int parts = 1, part_len = K;
+            if (K >= kSplitMinK) {
+              parts = std::min(kSplitMaxParts, (K + kSplitPart - 1) / kSplitPart);
+              part_len = ((K + parts - 1) / parts + kSplitPart - 1) / kSplitPart * kSplitPart;
+              parts = (K + part_len - 1) / part_len;
+            }
+            for (int r0 = 0; r0 < rows; r0 += per) {
+              const int tile = parts > 1 ? tiles++ : -1;
+              for (int p = 0; p < parts; ++p) {
+                PanelItem it;
+                it.a = make_int4(g, r0, std::min(rows, r0 + per), ri);
+                it.b = make_int4(hs[g], hm[g], node_set[g], w_off[g]);
+                it.c = make_int4((int)(off & 0xffffffffll), (int)(off >> 32), own_off[g], upd_off[g]);
+                it.d = make_int4(cm_off[g], cb, ncm, p);
+                it.e = make_int4(p * part_len, std::min(K, (p + 1) * part_len), tile, parts);
+                items.push_back(it);
+              }
+            }
+          }
+          if (tiles > 0) {
+            PanelTiles& P = out[l].split;
+            P.n_items = (int)items.size();
+            P.max_ri = max_ri;
+            P.min_ri = min_ri;
+            P.items.upload(items);
+            out[l].split_tiles = tiles;
+            const int ych = (parts_ld_ + 31) / 32;
+            out[l].counters.alloc((size_t)tiles * ych);
+            out[l].counters.zero();
+            const size_t esz = prec_ == PECS_PREC_FP64 ? 8 : 4;
+            out[l].partials.alloc((size_t)tiles * kSplitMaxParts * 32 * parts_ld_ * esz);
+          }
+        }
         // leaf level: every node small and, forward, without children
         bool leaf = true;
         int max_rows = 0;
@@ -1191,6 +1305,7 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
             it.b = make_int4(hs[g], hm[g], node_set[g], w_off[g]);
             it.c = make_int4((int)(off & 0xffffffffll), (int)(off >> 32), own_off[g], upd_off[g]);
             it.d = make_int4(cm_off[g], cmap_ptr[cm_off[g]], 0, 0);
+            it.e = make_int4(0, 0, -1, 1);
             items.push_back(it);
           }
           out[l].warp.n_items = (int)items.size();
@@ -1218,6 +1333,7 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
               it.b = make_int4(hs[g], hm[g], node_set[g], w_off[g]);
               it.c = make_int4((int)(off & 0xffffffffll), (int)(off >> 32), own_off[g], upd_off[g]);
               it.d = make_int4(cm_off[g], cb, ncm, 0);
+              it.e = make_int4(0, 0, -1, 1);  // no split
               items.push_back(it);
             }
           }
@@ -1312,9 +1428,9 @@ void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) con
     const bool fwd = pass == 0;
     for (const PanelPlan& L : fwd ? pfwd_ : pbwd_) {
       if constexpr (std::is_same<SVT, IlSetsViewF>::value)
-        launch_panel_level<float, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
+        launch_panel_level<float, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, parts_ld_, st);
       else
-        launch_panel_level<double, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, st);
+        launch_panel_level<double, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, parts_ld_, st);
     }
   }
 }

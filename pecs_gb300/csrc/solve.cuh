@@ -103,7 +103,8 @@ struct __align__(16) PanelItem {
   int4 a;  // node, row0, row1, rows per tile
   int4 b;  // s, m, RHS set, update-vector offset
   int4 c;  // block offset (low, high 32 bits), own-index offset, update-index offset
-  int4 d;  // child-map pointer offset, first child-map entry, child-map entries, 0
+  int4 d;  // child-map pointer offset, first child-map entry, child-map entries, K part
+  int4 e;  // split-K: first column, end column, tile (-1: no split), K parts of the tile
 };
 
 struct PanelTiles {
@@ -119,6 +120,10 @@ struct PanelPlan {
   int cm_cap = 0;  // child-map entries staged per node (the level's largest, capped)
   int sc_rows[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // forward: child rows per chunk, per chunk size
   PanelTiles tiles[4];
+  PanelTiles split;   // levels with long rows: 32-row tiles split along K (else empty)
+  int split_tiles = 0;
+  DBuf<int> counters;      // split-K: arrival counter per (tile, RHS chunk); reset by the last CTA
+  DBuf<unsigned char> partials;  // split-K: [tile][part][32 rows][max RHS] partial products
   PanelTiles warp;    // leaf levels: one item per node, a warp each (else empty)
   int warp_rows = 0;  // leaf levels: most rows of a node
 };
@@ -140,8 +145,10 @@ class FactorBank {
   // factors[i] is bound to RHS set i.  precision: PECS_PREC_FP64 or FP32_IR.
   // panel: store every block column-major and apply it with the panel
   // kernels (many right-hand sides per set, interleaved layout only).
+  // max_nrhs: the most right-hand sides any set will carry (panel banks size
+  // their split-K scratch with it)
   void build(const std::vector<const MfFactor*>& factors, int precision, bool panel = false,
-             PanelTuning tuning = PanelTuning());
+             PanelTuning tuning = PanelTuning(), int max_nrhs = 0);
   // y = forward(b), x = backward(y); w is workspace.  All sets must be bound.
   void solve(const SetsView& sets, int max_nrhs, cudaStream_t st) const;
   void solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) const;
@@ -169,6 +176,7 @@ class FactorBank {
   std::vector<PanelPlan> pfwd_, pbwd_;
   bool panel_ = false;
   PanelTuning tune_;
+  int parts_ld_ = 32;  // split-K scratch: right-hand sides per partial row
   int max_cols_ = 0, max_rb_ = 8;
   template <typename SVT>
   void solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) const;

@@ -215,3 +215,23 @@ def test_panel_mixed_batch_within_1e6(pecs_lib):
     for i in (3, 63):
         st, _, _ = oracle.Problem(Ps[i]).run(20)
         _compare_state(ctx, st, 1e-6, inst=i)
+
+
+def test_split_k_levels_match_oracle_and_unsplit(pecs_lib):
+    """Refinement 5 has root fronts with 256-512 columns, which the panel path
+    splits along K for 80 carrier right-hand sides (partials reduced by the
+    last CTA of each tile).  FP64: two instances against the oracle, and the
+    whole batch against the same context without splitting (a CTA target of
+    1 keeps every level unsplit)."""
+    Ps = _panel_instances(40, oracle.config2_params(n_refine=5))
+    split = pg.Context([to_lib(P) for P in Ps])
+    whole = pg.Context([to_lib(P) for P in Ps], panel_min_ctas=1)
+    for c in (split, whole):
+        c.initialize()
+        c.step(3)
+    for i in (0, 39):
+        st, _, _ = oracle.Problem(Ps[i]).run(3)
+        _compare_state(split, st, STEP_TOL, inst=i)
+    for i in range(40):
+        for f in split.fields():
+            assert rel_err(split.get_state(f, i), whole.get_state(f, i)) < 1e-12
