@@ -375,6 +375,7 @@ struct Engine {
   DBuf<double> t_phi, t_qw, t_fphi, t_fw, t_psix, t_psiy, t_phiP, t_mref;
   DBuf<float> tf_phi, tf_qw, tf_fphi, tf_fw, tf_psix, tf_psiy;
   DBuf<double> t_drift_x, t_drift_y;
+  DBuf<int> t_drift_cx, t_drift_cy;
   Tables T{};
   DBuf<double2> h_[2], ph_[2];
   DBuf<int4> bid_[2];
@@ -857,22 +858,39 @@ struct Engine {
     tf_fw.upload(f32(ct.fw));
     tf_psix.upload(f32(pt.psi_x));
     tf_psiy.upload(f32(pt.psi_y));
-    // drift tensors sum_q phi_a phi_b psi_c w_q
-    const int n1 = ct.n1, Q = ct.Q, nrt = pt.n_rt;
-    std::vector<double> dx((size_t)n1 * n1 * nrt, 0.0), dy((size_t)n1 * n1 * nrt, 0.0);
+    // drift tensors sum_q phi_a phi_b psi_c w_q over the RT functions with a
+    // non-zero x (y) component; on rectangles each RT function has one
+    // component only, nrt/2 of each
+    const int n1 = ct.n1, Q = ct.Q, nrt = pt.n_rt, NC = nrt / 2;
+    std::vector<int> cx, cy;
+    for (int c = 0; c < nrt; ++c) {
+      bool nx = false, ny = false;
+      for (int q = 0; q < Q; ++q) {
+        nx = nx || pt.psi_x[c * Q + q] != 0.0;
+        ny = ny || pt.psi_y[c * Q + q] != 0.0;
+      }
+      if (nx && ny) throw PecsError(PECS_E_STATE, "RT function with two components");
+      if (nx) cx.push_back(c);
+      if (ny) cy.push_back(c);
+    }
+    if ((int)cx.size() != NC || (int)cy.size() != NC)
+      throw PecsError(PECS_E_STATE, "RT functions not split evenly by component");
+    std::vector<double> dx((size_t)n1 * n1 * NC, 0.0), dy((size_t)n1 * n1 * NC, 0.0);
     for (int a = 0; a < n1; ++a)
       for (int b = 0; b < n1; ++b)
-        for (int c = 0; c < nrt; ++c)
+        for (int j = 0; j < NC; ++j)
           for (int q = 0; q < Q; ++q) {
             const double pw = ct.phi[a * Q + q] * ct.phi[b * Q + q] * ct.qw[q];
-            dx[((size_t)a * n1 + b) * nrt + c] += pw * pt.psi_x[c * Q + q];
-            dy[((size_t)a * n1 + b) * nrt + c] += pw * pt.psi_y[c * Q + q];
+            dx[((size_t)a * n1 + b) * NC + j] += pw * pt.psi_x[cx[j] * Q + q];
+            dy[((size_t)a * n1 + b) * NC + j] += pw * pt.psi_y[cy[j] * Q + q];
           }
     t_drift_x.upload(dx);
     t_drift_y.upload(dy);
+    t_drift_cx.upload(cx);
+    t_drift_cy.upload(cy);
     T = Tables{t_phi.p,  t_qw.p,  t_fphi.p,  t_fw.p,   t_psix.p,  t_psiy.p, t_phiP.p,
                t_mref.p, tf_phi.p, tf_qw.p, tf_fphi.p, tf_fw.p, tf_psix.p, tf_psiy.p,
-               t_drift_x.p, t_drift_y.p};
+               t_drift_x.p, t_drift_y.p, t_drift_cx.p, t_drift_cy.p};
   }
 
   void upload_regions() {

@@ -33,8 +33,10 @@ struct Tables {
   // FP32 copies for the mixed-precision path
   const float *phi_f, *qw_f, *fphi_f, *fw_f, *psix_f, *psiy_f;
   // drift tensors of the current equations, sum_q phi_a phi_b psi_c w_q on
-  // the unit square: [a][b][c], n1 * n1 * nrt each (x and y components)
+  // the unit square, over the RT basis functions with a non-zero x (y)
+  // component only -- nrt/2 of them on rectangles: [a][b][j], n1*n1*(nrt/2)
   const double *drift_x, *drift_y;
+  const int *drift_cx, *drift_cy;  // their RT indices, nrt/2 each
 };
 
 struct RegionDev {
@@ -183,24 +185,28 @@ __global__ void __launch_bounds__(128)
     }
   }
   if constexpr (!std::is_same<Tq, double>::value) {
-    // FP64 drift of the current equations: (q/eps) hx hy sum_bc T_abc u_b D_c
-    double Dv[nrt];
+    // FP64 drift of the current equations: (q/eps) hx hy sum_bj T_abj u_b D_j,
+    // with the products u_b D_j formed once (n1 * nrt/2 per component)
+    constexpr int NC = nrt / 2;
+    double px[n1 * NC], py[n1 * NC];
 #pragma unroll
-    for (int b = 0; b < nrt; ++b) Dv[b] = Pv[R.rt[c * nrt + b]];
+    for (int j = 0; j < NC; ++j) {
+      const double dx = Pv[R.rt[c * nrt + T.drift_cx[j]]];
+      const double dy = Pv[R.rt[c * nrt + T.drift_cy[j]]];
+#pragma unroll
+      for (int b = 0; b < n1; ++b) {
+        px[b * NC + j] = uown[b] * dx;
+        py[b * NC + j] = uown[b] * dy;
+      }
+    }
     const double sc = (which ? 1.0 : -1.0) * R.inv_eps * hxhy;
 #pragma unroll
     for (int a = 0; a < n1; ++a) {
       double sx = 0.0, sy = 0.0;
 #pragma unroll
-      for (int b = 0; b < n1; ++b) {
-        double tx = 0.0, ty = 0.0;
-#pragma unroll
-        for (int cc = 0; cc < nrt; ++cc) {
-          tx += T.drift_x[(a * n1 + b) * nrt + cc] * Dv[cc];
-          ty += T.drift_y[(a * n1 + b) * nrt + cc] * Dv[cc];
-        }
-        sx += tx * uown[b];
-        sy += ty * uown[b];
+      for (int t = 0; t < n1 * NC; ++t) {
+        sx += T.drift_x[a * n1 * NC + t] * px[t];
+        sy += T.drift_y[a * n1 * NC + t] * py[t];
       }
       drift64[a] = sc * sx;
       drift64[n1 + a] = sc * sy;
