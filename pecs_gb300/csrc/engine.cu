@@ -376,6 +376,7 @@ struct Engine {
   DBuf<float> tf_phi, tf_qw, tf_fphi, tf_fw, tf_psix, tf_psiy;
   DBuf<double> t_drift_x, t_drift_y;
   DBuf<int> t_drift_cx, t_drift_cy;
+  DBuf<double> t_charge;
   Tables T{};
   DBuf<double2> h_[2], ph_[2];
   DBuf<int4> bid_[2];
@@ -888,9 +889,16 @@ struct Engine {
     t_drift_y.upload(dy);
     t_drift_cx.upload(cx);
     t_drift_cy.upload(cy);
+    // Poisson charge matrix sum_q phiP_a phi_b w_q
+    const int nphi = pt.n_phi;
+    std::vector<double> chg((size_t)nphi * n1, 0.0);
+    for (int a = 0; a < nphi; ++a)
+      for (int b = 0; b < n1; ++b)
+        for (int q = 0; q < Q; ++q) chg[(size_t)a * n1 + b] += pt.phi[a * Q + q] * ct.phi[b * Q + q] * ct.qw[q];
+    t_charge.upload(chg);
     T = Tables{t_phi.p,  t_qw.p,  t_fphi.p,  t_fw.p,   t_psix.p,  t_psiy.p, t_phiP.p,
                t_mref.p, tf_phi.p, tf_qw.p, tf_fphi.p, tf_fw.p, tf_psix.p, tf_psiy.p,
-               t_drift_x.p, t_drift_y.p, t_drift_cx.p, t_drift_cy.p};
+               t_drift_x.p, t_drift_y.p, t_drift_cx.p, t_drift_cy.p, t_charge.p};
   }
 
   void upload_regions() {

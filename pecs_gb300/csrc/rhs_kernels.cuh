@@ -37,6 +37,8 @@ struct Tables {
   // component only -- nrt/2 of them on rectangles: [a][b][j], n1*n1*(nrt/2)
   const double *drift_x, *drift_y;
   const int *drift_cx, *drift_cy;  // their RT indices, nrt/2 each
+  // Poisson charge matrix sum_q phiP_a phi_b w_q on the unit square, nphi x n1
+  const double* charge;
 };
 
 struct RegionDev {
@@ -315,20 +317,20 @@ __global__ void __launch_bounds__(128)
   const double* u1 = F.u[f1] + (size_t)i * F.nd[f1] + 2 * R.nc * n1 + c * n1;
   const double* u2 = F.u[f1 + 1] + (size_t)i * F.nd[f1 + 1] + 2 * R.nc * n1 + c * n1;
   const double2 h = R.h[c];
+  // charge density (-u1 + u2) (charge numbers -1, +1) against the Poisson test
+  // functions: the quadrature folded into the nphi x n1 matrix T.charge, so
+  // each cell costs nphi * n1 FP64 FMAs
+  double du[n1];
+#pragma unroll
+  for (int b = 0; b < n1; ++b) du[b] = u2[b] - u1[b];
+  const double hxhy = h.x * h.y;
   double acc[nphi];
 #pragma unroll
-  for (int a = 0; a < nphi; ++a) acc[a] = 0.0;
-#pragma unroll 1
-  for (int q = 0; q < Q; ++q) {
-    double a1 = 0.0, a2 = 0.0;
+  for (int a = 0; a < nphi; ++a) {
+    double t = 0.0;
 #pragma unroll
-    for (int a = 0; a < n1; ++a) {
-      a1 += T.phi[a * Q + q] * u1[a];
-      a2 += T.phi[a * Q + q] * u2[a];
-    }
-    const double rho = (-a1 + a2) * T.qw[q] * h.x * h.y;  // charge numbers -1, +1
-#pragma unroll
-    for (int a = 0; a < nphi; ++a) acc[a] += T.phiP[a * Q + q] * rho;
+    for (int b = 0; b < n1; ++b) t += T.charge[a * n1 + b] * du[b];
+    acc[a] = t * hxhy;
   }
 #pragma unroll
   for (int a = 0; a < nphi; ++a) {
