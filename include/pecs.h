@@ -111,6 +111,9 @@ typedef struct pecs_options {
                           block columns per chunk (0 = default: 128 FP32, 64 FP64) */
   int panel_min_ctas;  /* panel solve kernels: CTAs a level must reach before shorter row
                           tiles or fewer right-hand sides per CTA are used (0 = default 152) */
+  int autotune;        /* panel solve kernels: at creation, time every tiling option of
+                          every tree level and keep the fastest (1 = yes, the default;
+                          0 = the heuristic above) */
 } pecs_options;
 
 typedef struct pecs_info {

@@ -48,6 +48,7 @@ class pecs_options(C.Structure):
         ("precision", C.c_int), ("leaf_cells", C.c_int), ("use_graphs", C.c_int),
         ("ir_max_iters", C.c_int), ("ir_tol", C.c_double), ("device", C.c_int),
         ("host_setup_only", C.c_int), ("panel_chunk", C.c_int), ("panel_min_ctas", C.c_int),
+        ("autotune", C.c_int),
     ]
 
 

@@ -779,6 +779,18 @@ struct Engine {
     }
     build_il(0, carrier_set_fields(), bank_c);
     build_il(1, {{4}}, bank_p);
+    if (opt.autotune) {
+      // panel banks: per level, the fastest tiling for these right-hand sides
+      for (int which = 0; which < 2; ++which) {
+        FactorBank& bk = which == 0 ? bank_c : bank_p;
+        if (!bk.panel()) continue;
+        if (il_f32(which))
+          bk.autotune(il_view_f(which, false), il[which].max_R, st);
+        else
+          bk.autotune(il_view(which, false), il[which].max_R, st);
+      }
+      PECS_CUDA(cudaStreamSynchronize(st));
+    }
     // steady-state buffers
     partial.alloc((size_t)n_inst * 5 * kRedChunks);
     partial.zero();
@@ -1436,6 +1448,7 @@ void pecs_default_options(pecs_options* opt) {
   opt->ir_max_iters = 2;
   opt->ir_tol = 1e-12;
   opt->device = 0;
+  opt->autotune = 1;
 }
 
 int pecs_create(const pecs_params* params, int n_inst, const pecs_options* opt, pecs_ctx** out) {

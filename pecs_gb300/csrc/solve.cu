@@ -955,44 +955,74 @@ void launch_panel_warp(bool forward, const BankView& B, const SVT& S, const Pane
   PECS_CUDA(cudaGetLastError());
 }
 
+// One tiling option of a level: kind 0 = whole-row items (row-tile cap
+// 32 >> cap_idx), 1 = split-K items, 2 = leaf warps; rpl = RHS per lane.
 template <typename T, typename SVT>
-void launch_panel_level(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
-                        int max_nrhs, int rpl_max, const PanelTuning& tu, int parts_ld,
-                        cudaStream_t st) {
-  if (L.warp.n_items > 0) {
-    // leaf level: the most right-hand sides per lane that keep a CTA's eight
-    // warps within kWarpSmem
-    int rpl = rpl_max;
-    const int rows_pad = (L.warp_rows + 3) & ~3;
-    while (rpl > 1 && kWarpNodesPerCta * panel_warp_bytes<T>(L.max_k, rows_pad, 32 * rpl) > kWarpSmem) rpl /= 2;
-    switch (rpl) {
+void launch_panel_option(const PanelOption& o, bool forward, const BankView& B, const SVT& S,
+                         const PanelPlan& L, int max_nrhs, const PanelTuning& tu, int parts_ld,
+                         cudaStream_t st) {
+  if (o.kind == 2) {
+    switch (o.rpl) {
       case 1: launch_panel_warp<T, 1, SVT>(forward, B, S, L, max_nrhs, st); break;
       case 2: launch_panel_warp<T, 2, SVT>(forward, B, S, L, max_nrhs, st); break;
       default: launch_panel_warp<T, 4, SVT>(forward, B, S, L, max_nrhs, st); break;
     }
     return;
   }
-  const long long full_tiles = (long long)L.tiles[0].n_items * ((max_nrhs + 31) / 32);
-  if (L.split.n_items > 0 && full_tiles < tu.min_ctas && max_nrhs <= parts_ld) {
-    // long rows and too few full-height tiles: split along K, the most RHS per
-    // lane that still reaches the CTA target
-    int rpl = rpl_max;
-    while (rpl > 1 && (long long)L.split.n_items * ((max_nrhs + 32 * rpl - 1) / (32 * rpl)) < tu.min_ctas)
-      rpl /= 2;
-    switch (rpl) {
-      case 1: launch_panel<T, 1, SVT>(forward, B, S, L, L.split, max_nrhs, tu.chunk, parts_ld, st); break;
-      case 2: launch_panel<T, 2, SVT>(forward, B, S, L, L.split, max_nrhs, tu.chunk, parts_ld, st); break;
-      default: launch_panel<T, 4, SVT>(forward, B, S, L, L.split, max_nrhs, tu.chunk, parts_ld, st); break;
-    }
-    return;
-  }
-  const PanelChoice c = choose_panel(L, max_nrhs, rpl_max, tu.min_ctas);
-  const PanelTiles& P = L.tiles[c.cap_idx];
-  switch (c.rpl) {
+  const PanelTiles& P = o.kind == 1 ? L.split : L.tiles[o.cap_idx];
+  switch (o.rpl) {
     case 1: launch_panel<T, 1, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, parts_ld, st); break;
     case 2: launch_panel<T, 2, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, parts_ld, st); break;
     default: launch_panel<T, 4, SVT>(forward, B, S, L, P, max_nrhs, tu.chunk, parts_ld, st); break;
   }
+}
+
+// The valid options of a level for rpl_max RHS per lane.
+template <typename T>
+std::vector<PanelOption> panel_options(const PanelPlan& L, int max_nrhs, int rpl_max, int parts_ld) {
+  std::vector<PanelOption> v;
+  for (int rpl = rpl_max; rpl >= 1; rpl /= 2) {
+    if (L.warp.n_items > 0) {
+      const int rows_pad = (L.warp_rows + 3) & ~3;
+      if (kWarpNodesPerCta * panel_warp_bytes<T>(L.max_k, rows_pad, 32 * rpl) <= kWarpSmem)
+        v.push_back(PanelOption{2, 0, rpl});
+    }
+    for (int ci = 0; ci < 4; ++ci) v.push_back(PanelOption{0, ci, rpl});
+    if (L.split.n_items > 0 && max_nrhs <= parts_ld) v.push_back(PanelOption{1, 0, rpl});
+  }
+  return v;
+}
+
+// Heuristic option (untuned banks): leaf warps where the level has them; else
+// split-K when full-height tiles give too few CTAs; else the row-tile height
+// and RHS per lane of choose_panel.
+template <typename T>
+PanelOption panel_default_option(const PanelPlan& L, int max_nrhs, int rpl_max, const PanelTuning& tu,
+                                 int parts_ld) {
+  if (L.warp.n_items > 0) {
+    int rpl = rpl_max;
+    const int rows_pad = (L.warp_rows + 3) & ~3;
+    while (rpl > 1 && kWarpNodesPerCta * panel_warp_bytes<T>(L.max_k, rows_pad, 32 * rpl) > kWarpSmem) rpl /= 2;
+    return PanelOption{2, 0, rpl};
+  }
+  const long long full_tiles = (long long)L.tiles[0].n_items * ((max_nrhs + 31) / 32);
+  if (L.split.n_items > 0 && full_tiles < tu.min_ctas && max_nrhs <= parts_ld) {
+    int rpl = rpl_max;
+    while (rpl > 1 && (long long)L.split.n_items * ((max_nrhs + 32 * rpl - 1) / (32 * rpl)) < tu.min_ctas)
+      rpl /= 2;
+    return PanelOption{1, 0, rpl};
+  }
+  const PanelChoice c = choose_panel(L, max_nrhs, rpl_max, tu.min_ctas);
+  return PanelOption{0, c.cap_idx, c.rpl};
+}
+
+template <typename T, typename SVT>
+void launch_panel_level(bool forward, const BankView& B, const SVT& S, const PanelPlan& L,
+                        int max_nrhs, int rpl_max, const PanelTuning& tu, int parts_ld,
+                        cudaStream_t st) {
+  PanelOption o = L.tuned;
+  if (o.kind < 0 || o.rpl > rpl_max) o = panel_default_option<T>(L, max_nrhs, rpl_max, tu, parts_ld);
+  launch_panel_option<T, SVT>(o, forward, B, S, L, max_nrhs, tu, parts_ld, st);
 }
 }  // namespace
 
@@ -1418,11 +1448,17 @@ void FactorBank::solve(const IlSetsView& sets, int max_nrhs, cudaStream_t st) co
 }
 
 template <typename SVT>
-void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) const {
+int FactorBank::panel_rpl(const SVT& sets, int max_nrhs) const {
   // right-hand sides per lane: at most as many as fill the lanes, dividing every set's count
   int rpl = max_nrhs >= 96 ? 4 : (max_nrhs >= 48 ? 2 : 1);
   for (int si = 0; si < n_sets_; ++si)
     while (rpl > 1 && sets.set[si].nrhs % rpl != 0) rpl /= 2;
+  return rpl;
+}
+
+template <typename SVT>
+void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) const {
+  const int rpl = panel_rpl(sets, max_nrhs);
   const BankView B = view();
   for (int pass = 0; pass < 2; ++pass) {
     const bool fwd = pass == 0;
@@ -1433,6 +1469,61 @@ void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) con
         launch_panel_level<double, SVT>(fwd, B, sets, L, max_nrhs, rpl, tune_, parts_ld_, st);
     }
   }
+}
+
+// Per level, time every valid tiling option on these right-hand sides (one
+// warm-up launch, then the mean of `reps`) and keep the fastest.  The sweep's
+// values are meaningless while tuning (levels run out of order); callers solve
+// again before using any result.
+template <typename SVT>
+void FactorBank::autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, int reps) {
+  using T = typename std::conditional<std::is_same<SVT, IlSetsViewF>::value, float, double>::type;
+  const int rpl = panel_rpl(sets, max_nrhs);
+  const BankView B = view();
+  cudaEvent_t e0, e1;
+  PECS_CUDA(cudaEventCreate(&e0));
+  PECS_CUDA(cudaEventCreate(&e1));
+  tuned_ms_ = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool fwd = pass == 0;
+    for (PanelPlan& L : fwd ? pfwd_ : pbwd_) {
+      L.tuned = PanelOption{};
+      const std::vector<PanelOption> opts = panel_options<T>(L, max_nrhs, rpl, parts_ld_);
+      float best = 1e30f;
+      for (const PanelOption& o : opts) {
+        try {
+          launch_panel_option<T, SVT>(o, fwd, B, sets, L, max_nrhs, tune_, parts_ld_, st);
+        } catch (const PecsError& err) {
+          if (err.code != PECS_E_ARG) throw;
+          continue;  // the option's staging does not fit in shared memory
+        }
+        PECS_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps; ++r)
+          launch_panel_option<T, SVT>(o, fwd, B, sets, L, max_nrhs, tune_, parts_ld_, st);
+        PECS_CUDA(cudaEventRecord(e1, st));
+        PECS_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PECS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+          best = ms;
+          L.tuned = o;
+        }
+      }
+      tuned_ms_ += best / reps;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+}
+
+void FactorBank::autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps) {
+  if (!panel_ || prec_ == PECS_PREC_FP64) throw PecsError(PECS_E_STATE, "autotune needs an FP32 panel bank");
+  autotune_panel(sets, max_nrhs, st, reps);
+}
+
+void FactorBank::autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps) {
+  if (!panel_ || prec_ != PECS_PREC_FP64) throw PecsError(PECS_E_STATE, "autotune needs an FP64 panel bank");
+  autotune_panel(sets, max_nrhs, st, reps);
 }
 
 void FactorBank::solve(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st) const {

@@ -114,6 +114,13 @@ struct PanelTiles {
   DBuf<PanelItem> items;
 };
 
+// A tiling option of one panel level (see launch_panel_option).
+struct PanelOption {
+  int kind = -1;  // -1 untuned, 0 whole-row tiles, 1 split-K tiles, 2 leaf warps
+  int cap_idx = 0;
+  int rpl = 1;
+};
+
 struct PanelPlan {
   int max_k = 0;   // largest column count of the level's nodes
   int max_s = 1, max_f = 1;
@@ -126,6 +133,7 @@ struct PanelPlan {
   DBuf<unsigned char> partials;  // split-K: [tile][part][32 rows][max RHS] partial products
   PanelTiles warp;    // leaf levels: one item per node, a warp each (else empty)
   int warp_rows = 0;  // leaf levels: most rows of a node
+  PanelOption tuned;  // the autotuner's choice (kind -1: heuristic)
 };
 
 struct LevelPlan {
@@ -161,6 +169,12 @@ class FactorBank {
   int n_bwd_levels() const { return (int)bwd_.size(); }
   int kernel_launches_per_solve() const;
   bool panel() const { return panel_; }
+  // Panel banks: time every tiling option of every level on these right-hand
+  // sides and keep the fastest per level (the sweep's outputs are garbage
+  // afterwards).  tuned_ms(): the sum of the chosen levels' times.
+  void autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps = 3);
+  void autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps = 3);
+  double tuned_ms() const { return tuned_ms_; }
 
  private:
   int prec_ = PECS_PREC_FP64;
@@ -180,6 +194,11 @@ class FactorBank {
   int max_cols_ = 0, max_rb_ = 8;
   template <typename SVT>
   void solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) const;
+  template <typename SVT>
+  void autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, int reps);
+  template <typename SVT>
+  int panel_rpl(const SVT& sets, int max_nrhs) const;
+  double tuned_ms_ = 0.0;
   BankView view() const;
   template <typename SV>
   void solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const;
