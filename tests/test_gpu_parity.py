@@ -222,11 +222,14 @@ def test_split_k_levels_match_oracle_and_unsplit(pecs_lib):
     splits along K for 80 carrier right-hand sides (partials reduced by the
     last CTA of each tile).  FP64: two instances against the oracle, and the
     whole batch against the same context without splitting (a CTA target of
-    1 keeps every level unsplit)."""
+    1 keeps every level unsplit).  Both use the tiling heuristic (no
+    autotuning), which splits the root-most levels here; a third, autotuned
+    context must agree as well."""
     Ps = _panel_instances(40, oracle.config2_params(n_refine=5))
-    split = pg.Context([to_lib(P) for P in Ps])
-    whole = pg.Context([to_lib(P) for P in Ps], panel_min_ctas=1)
-    for c in (split, whole):
+    split = pg.Context([to_lib(P) for P in Ps], autotune=False)
+    whole = pg.Context([to_lib(P) for P in Ps], panel_min_ctas=1, autotune=False)
+    tuned = pg.Context([to_lib(P) for P in Ps])
+    for c in (split, whole, tuned):
         c.initialize()
         c.step(3)
     for i in (0, 39):
@@ -235,3 +238,4 @@ def test_split_k_levels_match_oracle_and_unsplit(pecs_lib):
     for i in range(40):
         for f in split.fields():
             assert rel_err(split.get_state(f, i), whole.get_state(f, i)) < 1e-12
+            assert rel_err(tuned.get_state(f, i), whole.get_state(f, i)) < 1e-12
