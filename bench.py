@@ -300,7 +300,9 @@ def run_plain(args):
         out = {"profile_steps": args.profile_steps, "n_inst": args.n_inst,
                "precision": args.precision, "ms_per_time_step": ms_step,
                "launches_per_step": info.launches_per_step,
-               "launches_initialize": 1 + info.solve_launches[1],
+               "launches_setup": info.setup_launches,
+               "tuned_sweep_ms": list(info.tuned_sweep_ms),
+               "launches_initialize": info.initialize_launches,
                "carrier_sweep_ms": ctx.time_solve(0, reps=5),
                "poisson_sweep_ms": ctx.time_solve(1, reps=5)}
         if args.steady:

@@ -128,6 +128,9 @@ typedef struct pecs_info {
   int launches_per_step;   /* kernel launches of one step incl. steady-state test */
   double solve_bytes[2];   /* algorithmic bytes of one carrier / Poisson solve sweep */
   int solve_launches[2];   /* kernel launches of one carrier / Poisson solve sweep */
+  int setup_launches;      /* kernel launches issued by pecs_create (tiling autotuner) */
+  int initialize_launches; /* kernel launches of pecs_initialize */
+  double tuned_sweep_ms[2]; /* autotuner: sum of the chosen levels' times per sweep (0: untuned) */
 } pecs_info;
 
 typedef struct pecs_ctx pecs_ctx;

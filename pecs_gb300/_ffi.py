@@ -59,6 +59,8 @@ class pecs_info(C.Structure):
         ("factor_bytes", C.c_longlong), ("setup_seconds", C.c_double),
         ("n_distinct_carrier_factors", C.c_int), ("launches_per_step", C.c_int),
         ("solve_bytes", C.c_double * 2), ("solve_launches", C.c_int * 2),
+        ("setup_launches", C.c_int), ("initialize_launches", C.c_int),
+        ("tuned_sweep_ms", C.c_double * 2),
     ]
 
 

@@ -438,6 +438,10 @@ struct Engine {
     }
     return n;
   }
+  // Poisson RHS + Poisson solve
+  int initialize_launches() const {
+    return 1 + bank_p.kernel_launches_per_solve() * (1 + ir_iters()) + il[1].n_sets * set_launches_per_solve(1);
+  }
   int launches_per_step() const {
     const int it = ir_iters();
     const int lc = bank_c.kernel_launches_per_solve(), lp = bank_p.kernel_launches_per_solve();
@@ -1508,6 +1512,10 @@ int pecs_get_info(pecs_ctx* ctx, pecs_info* info) {
       info->solve_bytes[1] = e.solve_bytes(1);
       info->solve_launches[0] = e.bank_c.kernel_launches_per_solve();
       info->solve_launches[1] = e.bank_p.kernel_launches_per_solve();
+      info->setup_launches = e.bank_c.tune_launches() + e.bank_p.tune_launches();
+      info->initialize_launches = e.initialize_launches();
+      info->tuned_sweep_ms[0] = e.bank_c.tuned_ms();
+      info->tuned_sweep_ms[1] = e.bank_p.tuned_ms();
     }
   })
 }

@@ -1497,6 +1497,7 @@ void FactorBank::autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, 
           if (err.code != PECS_E_ARG) throw;
           continue;  // the option's staging does not fit in shared memory
         }
+        tune_launches_ += 1 + reps;
         PECS_CUDA(cudaEventRecord(e0, st));
         for (int r = 0; r < reps; ++r)
           launch_panel_option<T, SVT>(o, fwd, B, sets, L, max_nrhs, tune_, parts_ld_, st);

@@ -175,6 +175,7 @@ class FactorBank {
   void autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps = 3);
   void autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps = 3);
   double tuned_ms() const { return tuned_ms_; }
+  int tune_launches() const { return tune_launches_; }
 
  private:
   int prec_ = PECS_PREC_FP64;
@@ -199,6 +200,7 @@ class FactorBank {
   template <typename SVT>
   int panel_rpl(const SVT& sets, int max_nrhs) const;
   double tuned_ms_ = 0.0;
+  int tune_launches_ = 0;
   BankView view() const;
   template <typename SV>
   void solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const;
