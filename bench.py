@@ -273,7 +273,8 @@ def run_profile_sweep(args):
     ms = ctx.time_solve(which, reps=1)
     print(json.dumps({"profile_sweep": args.profile_sweep, "n_inst": args.n_inst, "precision": args.precision,
                       "sweep_ms": ms, "launches_per_sweep": info.solve_launches[which],
-                      "bytes_per_sweep": info.solve_bytes[which]}))
+                      "bytes_per_sweep": info.solve_bytes[which], "launches_setup": info.setup_launches,
+                      "tuned_sweep_ms": list(info.tuned_sweep_ms)}))
     return 0
 
 
