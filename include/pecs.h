@@ -111,8 +111,8 @@ typedef struct pecs_options {
                           block columns per chunk (0 = default: 128 FP32, 64 FP64) */
   int panel_min_ctas;  /* panel solve kernels: CTAs a level must reach before shorter row
                           tiles or fewer right-hand sides per CTA are used (0 = default 152) */
-  int autotune;        /* panel solve kernels: at creation, time every tiling option of
-                          every tree level and keep the fastest (1 = yes, the default;
+  int autotune;        /* panel solve kernels: at creation, choose every tree level's
+                          tiling by timing whole sweeps (1 = yes, the default;
                           0 = the heuristic above) */
 } pecs_options;
 
@@ -130,7 +130,7 @@ typedef struct pecs_info {
   int solve_launches[2];   /* kernel launches of one carrier / Poisson solve sweep */
   int setup_launches;      /* kernel launches issued by pecs_create (tiling autotuner) */
   int initialize_launches; /* kernel launches of pecs_initialize */
-  double tuned_sweep_ms[2]; /* autotuner: sum of the chosen levels' times per sweep (0: untuned) */
+  double tuned_sweep_ms[2]; /* autotuner: time of the tuned carrier / Poisson sweep (0: untuned) */
 } pecs_info;
 
 typedef struct pecs_ctx pecs_ctx;

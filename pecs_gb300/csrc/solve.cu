@@ -1471,48 +1471,63 @@ void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) con
   }
 }
 
-// Per level, time every valid tiling option on these right-hand sides (one
-// warm-up launch, then the mean of `reps`) and keep the fastest.  The sweep's
-// values are meaningless while tuning (levels run out of order); callers solve
-// again before using any result.
+// Per level, choose the tiling option that gives the fastest whole sweep:
+// starting from the heuristic choice everywhere, each level in turn tries all
+// of its valid options with the other levels fixed, timing complete sweeps
+// (minimum of `reps` after one warm-up), so every level is measured with the
+// cache state the real sweep gives it.  The sweep's values are meaningless
+// while tuning; callers solve again before using any result.
 template <typename SVT>
 void FactorBank::autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, int reps) {
   using T = typename std::conditional<std::is_same<SVT, IlSetsViewF>::value, float, double>::type;
   const int rpl = panel_rpl(sets, max_nrhs);
-  const BankView B = view();
   cudaEvent_t e0, e1;
   PECS_CUDA(cudaEventCreate(&e0));
   PECS_CUDA(cudaEventCreate(&e1));
-  tuned_ms_ = 0.0;
+  const int per_sweep = kernel_launches_per_solve();
+  for (int pass = 0; pass < 2; ++pass)
+    for (PanelPlan& L : pass == 0 ? pfwd_ : pbwd_)
+      L.tuned = panel_default_option<T>(L, max_nrhs, rpl, tune_, parts_ld_);
+  auto time_sweep = [&]() {
+    float best = 1e30f;
+    solve_panel(sets, max_nrhs, st);  // warm-up
+    tune_launches_ += per_sweep;
+    for (int r = 0; r < reps; ++r) {
+      PECS_CUDA(cudaEventRecord(e0, st));
+      solve_panel(sets, max_nrhs, st);
+      PECS_CUDA(cudaEventRecord(e1, st));
+      PECS_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      PECS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best = std::min(best, ms);
+      tune_launches_ += per_sweep;
+    }
+    return best;
+  };
+  float best_sweep = time_sweep();
   for (int pass = 0; pass < 2; ++pass) {
-    const bool fwd = pass == 0;
-    for (PanelPlan& L : fwd ? pfwd_ : pbwd_) {
-      L.tuned = PanelOption{};
-      const std::vector<PanelOption> opts = panel_options<T>(L, max_nrhs, rpl, parts_ld_);
-      float best = 1e30f;
-      for (const PanelOption& o : opts) {
+    for (PanelPlan& L : pass == 0 ? pfwd_ : pbwd_) {
+      const PanelOption keep = L.tuned;
+      PanelOption best = keep;
+      for (const PanelOption& o : panel_options<T>(L, max_nrhs, rpl, parts_ld_)) {
+        if (o.kind == keep.kind && o.cap_idx == keep.cap_idx && o.rpl == keep.rpl) continue;
+        L.tuned = o;
+        float ms;
         try {
-          launch_panel_option<T, SVT>(o, fwd, B, sets, L, max_nrhs, tune_, parts_ld_, st);
+          ms = time_sweep();
         } catch (const PecsError& err) {
           if (err.code != PECS_E_ARG) throw;
           continue;  // the option's staging does not fit in shared memory
         }
-        tune_launches_ += 1 + reps;
-        PECS_CUDA(cudaEventRecord(e0, st));
-        for (int r = 0; r < reps; ++r)
-          launch_panel_option<T, SVT>(o, fwd, B, sets, L, max_nrhs, tune_, parts_ld_, st);
-        PECS_CUDA(cudaEventRecord(e1, st));
-        PECS_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        PECS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best) {
-          best = ms;
-          L.tuned = o;
+        if (ms < best_sweep) {
+          best_sweep = ms;
+          best = o;
         }
       }
-      tuned_ms_ += best / reps;
+      L.tuned = best;
     }
   }
+  tuned_ms_ = best_sweep;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
 }

@@ -169,9 +169,9 @@ class FactorBank {
   int n_bwd_levels() const { return (int)bwd_.size(); }
   int kernel_launches_per_solve() const;
   bool panel() const { return panel_; }
-  // Panel banks: time every tiling option of every level on these right-hand
-  // sides and keep the fastest per level (the sweep's outputs are garbage
-  // afterwards).  tuned_ms(): the sum of the chosen levels' times.
+  // Panel banks: choose each level's tiling option by timing whole sweeps on
+  // these right-hand sides (the sweep's outputs are garbage afterwards).
+  // tuned_ms(): the tuned sweep's time.
   void autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps = 3);
   void autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps = 3);
   double tuned_ms() const { return tuned_ms_; }
