@@ -548,6 +548,14 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// Programmatic dependent launch: a sweep level is launched while the previous
+// level still runs; it stages what does not depend on that level (item
+// records, index metadata, its block tile) and then waits for the previous
+// grid's completion and memory (griddepcontrol.wait) before reading vectors.
+// A level lets the next one start once its CTAs are past their main loop.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 // RPL consecutive T of one interleaved row -> shared memory (16-byte pieces
 // where the row segment allows; zero fill for lanes past the last RHS)
 template <typename T, int RPL>
@@ -637,6 +645,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       else
         Gs[idx] = T(0);
     }
+    if (k0 == k_lo) pdl_wait();  // vectors below are written by the previous level
     for (int k = warp; k < kc; k += NW) {
       const int sr = src_s[k0 + k];
       const T* src = FWD ? st.b + (size_t)sr * R
@@ -685,6 +694,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     }
     __syncthreads();
   }
+  pdl_trigger();
   // row i of the item -> its destination
   auto emit = [&](int i, T (&v)[RPL]) {
     const int row = r0 + i;
@@ -823,6 +833,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       Gs[e] = T(0);
   }
   __syncwarp();
+  pdl_wait();  // vectors below are written by the previous level
   for (int k = 0; k < K; ++k) {
     const int sr = src_s[k];
     const T* src = FWD ? st.b + (size_t)sr * R
@@ -831,6 +842,7 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
   cp_async_wait_all();
   __syncwarp();
+  pdl_trigger();
   if (!lane_ok) return;
   for (int r4 = 0; r4 < rows; r4 += 4) {
     T acc[4][RPL];
@@ -908,15 +920,25 @@ void launch_panel(bool forward, const BankView& B, const SVT& S, const PanelPlan
   }
   if (smem > kPanelSmem) throw PecsError(PECS_E_ARG, "panel staging exceeds shared memory");
   const dim3 grid(P.n_items, (max_nrhs + RC - 1) / RC);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kSolveThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  T* parts = reinterpret_cast<T*>(L.partials.p);
   if (forward)
-    k_panel<T, RPL, true, SVT><<<grid, kSolveThreads, smem, st>>>(
-        B, S, P.items.p, kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap,
-        reinterpret_cast<T*>(L.partials.p), L.counters.p, parts_ld, ychunks);
+    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_panel<T, RPL, true, SVT>, B, S, (const PanelItem*)P.items.p, kc,
+                                 ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap, parts,
+                                 L.counters.p, parts_ld, ychunks));
   else
-    k_panel<T, RPL, false, SVT><<<grid, kSolveThreads, smem, st>>>(
-        B, S, P.items.p, kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap,
-        reinterpret_cast<T*>(L.partials.p), L.counters.p, parts_ld, ychunks);
-  PECS_CUDA(cudaGetLastError());
+    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_panel<T, RPL, false, SVT>, B, S, (const PanelItem*)P.items.p, kc,
+                                 ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap, parts,
+                                 L.counters.p, parts_ld, ychunks));
 }
 
 template <typename T, typename SVT>
@@ -946,13 +968,22 @@ void launch_panel_warp(bool forward, const BankView& B, const SVT& S, const Pane
   const int rows_pad = (L.warp_rows + 3) & ~3;
   const size_t smem = kWarpNodesPerCta * panel_warp_bytes<T>(L.max_k, rows_pad, RC);
   const dim3 grid((L.warp.n_items + kWarpNodesPerCta - 1) / kWarpNodesPerCta, (max_nrhs + RC - 1) / RC);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kSolveThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   if (forward)
-    k_panel_warp<T, RPL, true, SVT><<<grid, kSolveThreads, smem, st>>>(B, S, L.warp.items.p, L.warp.n_items,
-                                                                       L.max_k, rows_pad);
+    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_panel_warp<T, RPL, true, SVT>, B, S, (const PanelItem*)L.warp.items.p,
+                                 L.warp.n_items, L.max_k, rows_pad));
   else
-    k_panel_warp<T, RPL, false, SVT><<<grid, kSolveThreads, smem, st>>>(B, S, L.warp.items.p, L.warp.n_items,
-                                                                        L.max_k, rows_pad);
-  PECS_CUDA(cudaGetLastError());
+    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_panel_warp<T, RPL, false, SVT>, B, S, (const PanelItem*)L.warp.items.p,
+                                 L.warp.n_items, L.max_k, rows_pad));
 }
 
 // One tiling option of a level: kind 0 = whole-row items (row-tile cap
