@@ -9,6 +9,14 @@ namespace pecs {
 
 namespace {
 
+// Programmatic dependent launch: a sweep level is launched while the previous
+// level still runs; it stages what does not depend on that level (item
+// records, index metadata, its block tile) and then waits for the previous
+// grid's completion and memory (griddepcontrol.wait) before reading vectors.
+// A level lets the next one start once its CTAs are past their main loop.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 // Loads RB consecutive staged values (16-byte aligned) with vector loads.
 template <typename T, int RB>
 __device__ __forceinline__ void load_rhs(const T* p, T (&v)[RB]) {
@@ -335,6 +343,8 @@ __global__ void __launch_bounds__(kSolveThreads)
               const int4* __restrict__ thin, int n_thin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
+  pdl_trigger();  // the next level may start launching once every CTA here has started
+  pdl_wait();     // every access below may read the previous level's results
   if ((int)blockIdx.x < n_large) {
     fwd_large<T, RB, SV>(B, S, items[blockIdx.x], sm);
   } else {
@@ -350,6 +360,8 @@ __global__ void __launch_bounds__(kSolveThreads)
                const int4* __restrict__ thin, int n_thin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
+  pdl_trigger();
+  pdl_wait();
   if ((int)blockIdx.x < n_large) {
     bwd_large<T, RB, SV>(B, S, items[blockIdx.x], sm);
   } else {
@@ -369,13 +381,22 @@ void launch_level(bool forward, const BankView& B, const SV& S, const LevelPlan&
   size_t sm_thin = L.n_thin ? (size_t)warps * kThinCols * RB * sizeof(T) : 0;
   size_t smem = std::max(sm_large, sm_thin);
   const dim3 grid(nblk, (max_nrhs + RB - 1) / RB);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kSolveThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   if (forward)
-    k_forward<T, RB, SV><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
-                                                             L.n_thin);
+    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_forward<T, RB, SV>, B, S, (const int4*)L.items.p, L.n_large,
+                                 (const int4*)L.thin.p, L.n_thin));
   else
-    k_backward<T, RB, SV><<<grid, kSolveThreads, smem, st>>>(B, S, L.items.p, L.n_large, L.thin.p,
-                                                              L.n_thin);
-  PECS_CUDA(cudaGetLastError());
+    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_backward<T, RB, SV>, B, S, (const int4*)L.items.p, L.n_large,
+                                 (const int4*)L.thin.p, L.n_thin));
 }
 
 template <typename T, int RB>
@@ -548,13 +569,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
-// Programmatic dependent launch: a sweep level is launched while the previous
-// level still runs; it stages what does not depend on that level (item
-// records, index metadata, its block tile) and then waits for the previous
-// grid's completion and memory (griddepcontrol.wait) before reading vectors.
-// A level lets the next one start once its CTAs are past their main loop.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 
 // RPL consecutive T of one interleaved row -> shared memory (16-byte pieces
 // where the row segment allows; zero fill for lanes past the last RHS)
