@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "common.hpp"
+#include "fp_bits.cuh"
 #include "mf.hpp"
 #include "problem.hpp"
 #include "rhs_kernels.cuh"
@@ -127,7 +128,7 @@ __global__ void k_scatter_sum_il(const float* __restrict__ x32, const float* __r
   for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
     const int d = d0 + dd, k = k0 + threadIdx.x;
     const size_t o = (size_t)d * R + k;
-    t[dd][threadIdx.x] = (d < n && k < R) ? (double)x32[o] + (double)d32[o] : 0.0;
+    t[dd][threadIdx.x] = (d < n && k < R) ? f2d_exact(x32[o]) + f2d_exact(d32[o]) : 0.0;
   }
   __syncthreads();
   for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
@@ -179,6 +180,72 @@ __global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const X*
   r[o] = (RT)(b[o] - ((double)sh + (double)sl));
 }
 
+// Four right-hand sides per lane (128 per warp, R a multiple of 4): the row's
+// column indices and values are read once for all of them and every x row is
+// one 512 B (float) / 1 KB (pair) coalesced access.  Same arithmetic as above.
+__device__ __forceinline__ void ld_pairs4(const float* p, float2 (&v)[4]) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = make_float2(t.x, 0.f);
+  v[1] = make_float2(t.y, 0.f);
+  v[2] = make_float2(t.z, 0.f);
+  v[3] = make_float2(t.w, 0.f);
+}
+__device__ __forceinline__ void ld_pairs4(const float2* p, float2 (&v)[4]) {
+  const float4 t0 = reinterpret_cast<const float4*>(p)[0], t1 = reinterpret_cast<const float4*>(p)[1];
+  v[0] = make_float2(t0.x, t0.y);
+  v[1] = make_float2(t0.z, t0.w);
+  v[2] = make_float2(t1.x, t1.y);
+  v[3] = make_float2(t1.z, t1.w);
+}
+__device__ __forceinline__ void st4(float* p, const double (&v)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double (&v)[4]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+
+template <typename X, typename RT>
+__global__ void k_residual_df_il4(CsrDf A, const double* __restrict__ b, const X* __restrict__ xs,
+                                  RT* __restrict__ r, int n, int R) {
+  const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int k = blockIdx.y * 128 + (threadIdx.x & 31) * 4;
+  if (row >= n || k >= R) return;
+  float sh[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
+  const int p1 = A.rp[row + 1];
+  for (int p = A.rp[row]; p < p1; ++p) {
+    const float2 a = A.v[p];
+    float2 xv[4];
+    ld_pairs4(xs + (size_t)A.ci[p] * R + k, xv);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float ph = a.x * xv[q].x;
+      const float pe = fmaf(a.x, xv[q].x, -ph) + fmaf(a.x, xv[q].y, a.y * xv[q].x);
+      const float t = sh[q] + ph;
+      const float z = t - sh[q];
+      const float e = (sh[q] - (t - z)) + (ph - z);
+      sh[q] = t;
+      sl[q] += e + pe;
+    }
+  }
+  const size_t o = (size_t)row * R + k;
+  const double2 b0 = reinterpret_cast<const double2*>(b + o)[0], b1 = reinterpret_cast<const double2*>(b + o)[1];
+  const double bb[4] = {b0.x, b0.y, b1.x, b1.y};
+  double v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = bb[q] - ((double)sh[q] + (double)sl[q]);
+  st4(r + o, v);
+}
+
+template <typename X, typename RT>
+void launch_residual_df(const CsrDf& A, const double* b, const X* xs, RT* r, int n, int R, cudaStream_t s) {
+  if (R % 4 == 0 && R >= 96)
+    k_residual_df_il4<X, RT><<<dim3((n + 7) / 8, (R + 127) / 128), 256, 0, s>>>(A, b, xs, r, n, R);
+  else
+    k_residual_df_il<X, RT><<<dim3((n + 7) / 8, (R + 31) / 32), 256, 0, s>>>(A, b, xs, r, n, R);
+  PECS_CUDA(cudaGetLastError());
+}
+
 // FP64 variant (FP32_IR mode)
 template <typename RT>
 __global__ void k_residual_il(CsrDev A, const double* __restrict__ b, const double* __restrict__ x,
@@ -213,7 +280,14 @@ __global__ void k_relchange_partial(FieldPtrs NEW, FieldPtrs OLD, int n_fields,
     const int lo = chunk * per, hi = min(nd, lo + per);
     for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
       const double x = a[t], y = b[t];
-      const Acc d = (Acc)(x - y), xa = (Acc)x;
+      Acc d, xa;
+      if constexpr (sizeof(Acc) == 4) {
+        d = d2f_trunc(x - y);  // the one FP64 operation per element
+        xa = d2f_trunc(x);
+      } else {
+        d = x - y;
+        xa = x;
+      }
       d2 += d * d;
       n2 += xa * xa;
     }
@@ -232,8 +306,8 @@ __global__ void k_relchange_partial(FieldPtrs NEW, FieldPtrs OLD, int n_fields,
     partial[((size_t)i * 5 + fld) * kRedChunks + chunk] = make_double2(sd[0], sn[0]);
 }
 
-// per instance: rel = max_f sqrt(d2/n2); record first step with rel <= tol.
-// Per-instance convergence test after a step.  An active instance stops when
+// Per-instance convergence test after a step (rel = max over fields of
+// sqrt(d2 / n2)).  An active instance stops when
 // its relative change is <= tol (conv_step = the step), when its state is not
 // finite (conv_step = -step), or when it has marched max_steps since its start
 // step (conv_step = the step, capped = 1; streamed sweeps refill such slots).
@@ -600,13 +674,11 @@ struct Engine {
         if (f32) {
           // FP32 sweep vectors: the residual is stored in float for the next sweep
           if (mixed && it == 0) {
-            k_residual_df_il<float, float><<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.X32.p,
-                                                              S_.Rr32.p, S_.n, S_.R);
+            launch_residual_df(csr_df.m[S_.mat], S_.B.p, S_.X32.p, S_.Rr32.p, S_.n, S_.R, s);
           } else if (mixed) {
             k_split_il<<<egrid(nR), 256, 0, s>>>(S_.X.p, S_.Xs.p, nR);
             PECS_CUDA(cudaGetLastError());
-            k_residual_df_il<float2, float><<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.Xs.p,
-                                                               S_.Rr32.p, S_.n, S_.R);
+            launch_residual_df(csr_df.m[S_.mat], S_.B.p, S_.Xs.p, S_.Rr32.p, S_.n, S_.R, s);
           } else {
             if (it == 0) {
               k_widen_il<<<egrid(nR), 256, 0, s>>>(S_.X32.p, S_.X.p, nR);
@@ -617,8 +689,7 @@ struct Engine {
         } else if (mixed) {
           k_split_il<<<egrid(nR), 256, 0, s>>>(S_.X.p, S_.Xs.p, nR);
           PECS_CUDA(cudaGetLastError());
-          k_residual_df_il<float2, double><<<rg, 256, 0, s>>>(csr_df.m[S_.mat], S_.B.p, S_.Xs.p,
-                                                              S_.Rr.p, S_.n, S_.R);
+          launch_residual_df(csr_df.m[S_.mat], S_.B.p, S_.Xs.p, S_.Rr.p, S_.n, S_.R, s);
         } else {
           k_residual_il<double><<<rg, 256, 0, s>>>(csr.m[S_.mat], S_.B.p, S_.X.p, S_.Rr.p, S_.n, S_.R);
         }
