@@ -86,23 +86,33 @@ struct Carrier {
 struct CarrierPair {
   void set_name(const std::string& s) { material_name = s; }
   // CarrierPair::print_dofs / read_dofs (CarrierPair.cpp:89-121): the
-  // solution of each carrier as "<name>.dofs", size then raw doubles.
+  // solution of each carrier as "<name>.dofs" in the layout of deal.II's
+  // Vector::block_write -- the size in ASCII decimal, '\n', '[', the raw
+  // doubles, ']' -- so restart files move between the two codes.
   void print_dofs() const {
     for (const Carrier* c : {&carrier_1, &carrier_2}) {
       std::ofstream out(c->name + ".dofs", std::ios::binary);
-      const std::uint64_t n = c->solution.size();
-      out.write(reinterpret_cast<const char*>(&n), sizeof(n));
-      out.write(reinterpret_cast<const char*>(c->solution.data()), n * sizeof(double));
+      const std::string head = std::to_string(c->solution.size()) + "\n[";
+      out.write(head.data(), (std::streamsize)head.size());
+      out.write(reinterpret_cast<const char*>(c->solution.data()),
+                (std::streamsize)(c->solution.size() * sizeof(double)));
+      out.put(']');
+      if (!out) throw std::runtime_error("pecs: cannot write " + c->name + ".dofs");
     }
   }
   void read_dofs() {
     for (Carrier* c : {&carrier_1, &carrier_2}) {
       std::ifstream in(c->name + ".dofs", std::ios::binary);
-      std::uint64_t n = 0;
-      in.read(reinterpret_cast<char*>(&n), sizeof(n));
+      std::size_t n = 0;
+      char open = 0, close = 0;
+      in >> n;
+      in.get();  // '\n'
+      in.get(open);
       c->solution.resize(n);
-      in.read(reinterpret_cast<char*>(c->solution.data()), n * sizeof(double));
-      if (!in) throw std::runtime_error("pecs: cannot read " + c->name + ".dofs");
+      in.read(reinterpret_cast<char*>(c->solution.data()), (std::streamsize)(n * sizeof(double)));
+      in.get(close);
+      if (!in || open != '[' || close != ']')
+        throw std::runtime_error("pecs: cannot read " + c->name + ".dofs");
     }
   }
   Carrier carrier_1, carrier_2;

@@ -71,19 +71,43 @@ class CarrierPair:
         self.material_name = name
 
     def print_dofs(self, directory: str = "."):
-        """deal.II Vector::block_write layout: size_t n, then n raw doubles."""
+        """Each carrier's solution as "<name>.dofs" (CarrierPair.cpp:89-104)."""
         import os
         for c in (self.carrier_1, self.carrier_2):
             with open(os.path.join(directory, c.name + ".dofs"), "wb") as fh:
-                fh.write(np.uint64(c.solution.size).tobytes())
-                fh.write(np.ascontiguousarray(c.solution, dtype=np.float64).tobytes())
+                block_write(fh, c.solution)
 
     def read_dofs(self, directory: str = "."):
+        """(CarrierPair.cpp:106-121)"""
         import os
         for c in (self.carrier_1, self.carrier_2):
             with open(os.path.join(directory, c.name + ".dofs"), "rb") as fh:
-                n = int(np.frombuffer(fh.read(8), dtype=np.uint64)[0])
-                c.solution = np.frombuffer(fh.read(8 * n), dtype=np.float64).copy()
+                c.solution = block_read(fh)
+
+
+def block_write(fh, v) -> None:
+    """The binary vector layout the reference's restart files use (deal.II
+    Vector::block_write, called at CarrierPair.cpp:99-102): the size in ASCII
+    decimal, a newline, '[', the raw doubles, ']'."""
+    a = np.ascontiguousarray(v, dtype=np.float64)
+    fh.write(f"{a.size}\n[".encode("ascii"))
+    fh.write(a.tobytes())
+    fh.write(b"]")
+
+
+def block_read(fh) -> np.ndarray:
+    """Inverse of block_write (deal.II Vector::block_read)."""
+    head = b""
+    while not head.endswith(b"["):
+        ch = fh.read(1)
+        if not ch:
+            raise ValueError("truncated .dofs header")
+        head += ch
+    n = int(head[:-1].strip())
+    data = fh.read(8 * n)
+    if len(data) != 8 * n or fh.read(1) != b"]":
+        raise ValueError("truncated or malformed .dofs body")
+    return np.frombuffer(data, dtype=np.float64).copy()
 
 
 class PoissonData(Carrier):
