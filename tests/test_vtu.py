@@ -1,0 +1,59 @@
+"""Headless VTU output (pecs_gb300/vtu.py): per-cell patches with the
+post-processor's fields and scales (PostProcessor.cpp:6-124).  A stand-in
+context supplies known state vectors; the file is parsed back."""
+import xml.etree.ElementTree as ET
+
+import numpy as np
+
+import pecs_gb300 as pg
+from pecs_gb300 import vtu
+
+
+class FakeCtx:
+    def __init__(self, p, vecs):
+        self.params = [p]
+        self.ndofs = [len(vecs.get(f, [])) for f in range(5)]
+        self._v = vecs
+
+    def get_state(self, f, inst=0):
+        return self._v[f]
+
+
+def _arrays(path):
+    root = ET.parse(path).getroot()
+    piece = root.find("UnstructuredGrid/Piece")
+    out = {a.get("Name"): np.array(a.text.split(), dtype=float) for a in piece.iter("DataArray")}
+    return piece, out
+
+
+def test_carrier_patches_and_scaling(tmp_path):
+    p = pg.config2(n_refine=1)   # 2x2 cells per region, k = 1
+    nc, n1 = 4, 4
+    n = np.arange(3 * nc * n1, dtype=float)
+    vecs = {pg.FIELD_N: n, pg.FIELD_P: -n}
+    ctx = FakeCtx(p, vecs)
+    path = tmp_path / "semi.vtu"
+    vtu.write_carriers(ctx, str(path), scales=vtu.Scales(density=2.0, current=3.0))
+    piece, a = _arrays(path)
+    assert piece.get("NumberOfPoints") == str(nc * n1) and piece.get("NumberOfCells") == str(nc)
+    np.testing.assert_array_equal(a["Electrons Density"], 2.0 * n[2 * nc * n1:])
+    cur = a["Electrons Current"].reshape(-1, 3)
+    np.testing.assert_array_equal(cur[:, 0], 3.0 * n[:nc * n1])
+    np.testing.assert_array_equal(cur[:, 1], 3.0 * n[nc * n1:2 * nc * n1])
+    pts = a["Points"].reshape(-1, 3)
+    # cell 1 (i = 1, j = 0) spans x in [0.5, 1], y in [0, 0.5]; nodes x-fastest
+    np.testing.assert_allclose(pts[4:8, :2], [[0.5, 0], [1, 0], [0.5, 0.5], [1, 0.5]])
+    assert set(a["types"]) == {9.0}
+
+
+def test_potential_cell_data(tmp_path):
+    p = pg.config2(n_refine=1)
+    ncp = 8                      # 4 x 2 Poisson cells
+    n_rt = 22                    # whatever precedes the potential block
+    P = np.concatenate([np.zeros(n_rt), np.arange(ncp, dtype=float)])
+    ctx = FakeCtx(p, {pg.FIELD_N: np.zeros(48), pg.FIELD_POISSON: P})
+    path = tmp_path / "phi.vtu"
+    vtu.write_potential(ctx, str(path), scales=vtu.Scales(potential=0.5))
+    piece, a = _arrays(path)
+    assert piece.get("NumberOfCells") == str(ncp)
+    np.testing.assert_array_equal(a["Potential"], 0.5 * np.arange(ncp))
