@@ -50,3 +50,46 @@ def distributed_sweep(params: Sequence, compute: Callable[[list], list], group=N
         for k, r in enumerate(res):
             out[start + k] = r
     return out
+
+
+# fields of pecs_params that define the meshes and the fixed matrices: points
+# that agree on them can share a context (validate_params checks the same set)
+MATRIX_FIELDS = ("degree", "full_system", "nx_semi", "nx_elec", "ny", "x_semi0", "x_semi1", "x_elec1",
+                 "height", "lambda2", "eps_semi", "eps_elec", "mu", "dt", "penalty", "bc_semi",
+                 "bc_elec", "bc_poisson")
+
+
+def matrix_key(p) -> tuple:
+    return tuple(tuple(v) if isinstance(v, (list, tuple)) else v for v in
+                 (getattr(p, f) for f in MATRIX_FIELDS))
+
+
+def ragged_sweep(points: Sequence, slots: int = 64, precision: int = None, max_steps: int = 5000,
+                 tol: float = 1e-8, check_every: int = 50, want_fields: bool = False, **ctx_kw):
+    """I-V points of uneven size (different refinement levels, degrees or other
+    matrix-defining parameters) to steady state: the points are grouped by
+    their meshes and fixed matrices, and each group is streamed through one
+    context of at most ``slots`` slots (pecs_sweep_stream).  Results come back
+    in the order of ``points``: (steps, currents, fields or None), fields as
+    one array per point and field."""
+    import numpy as np
+
+    from .api import PREC_FP64, Context
+    prec = PREC_FP64 if precision is None else precision
+    groups = {}
+    for i, p in enumerate(points):
+        groups.setdefault(matrix_key(p), []).append(i)
+    steps = np.zeros(len(points), dtype=np.int64)
+    cur = np.zeros(len(points))
+    fields = [None] * len(points) if want_fields else None
+    for idx in groups.values():
+        pts = [points[i] for i in idx]
+        ctx = Context(pts[:min(slots, len(pts))], precision=prec, **ctx_kw)
+        s, c, fin = ctx.sweep_stream(pts, max_steps, tol, check_every, want_fields=want_fields)
+        for k, i in enumerate(idx):
+            steps[i] = s[k]
+            cur[i] = c[k]
+            if want_fields:
+                fields[i] = {f: fin[f][k * ctx.ndofs[f]:(k + 1) * ctx.ndofs[f]].copy() for f in fin}
+        ctx.close()
+    return steps, cur, fields
