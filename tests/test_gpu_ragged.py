@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import pecs_gb300 as pg
-from pecs_gb300.sweep import ragged_sweep
+from pecs_gb300.sweep import matrix_key, ragged_sweep
 
 pytestmark = pytest.mark.gpu
 
@@ -20,10 +20,13 @@ def test_ragged_sweep_matches_single_instances(pecs_lib):
                               G0=float(rng.uniform(0.5, 2.0))))
     steps, cur, fields = ragged_sweep(pts, slots=3, max_steps=400, tol=1e-6, check_every=10,
                                       want_fields=True)
+    gsize = {}
+    for p in pts:
+        gsize[matrix_key(p)] = gsize.get(matrix_key(p), 0) + 1
     for i, p in enumerate(pts):
-        # the reference runs the point alone in a context of the same slot
-        # count (same kernels), padded with copies of itself
-        ctx = pg.Context([p] * 3)
+        # the reference runs the point alone in a context with as many slots
+        # as its group got (same kernels), padded with copies of itself
+        ctx = pg.Context([p] * min(3, gsize[matrix_key(p)]))
         ctx.initialize()
         s, _ = ctx.run_to_steady_state(400, 1e-6, 10)
         assert int(steps[i]) == int(s[0]), i
