@@ -103,7 +103,8 @@ typedef struct pecs_options {
   int use_graphs;    /* capture a time step in a CUDA graph (1 = yes) */
   int ir_max_iters;  /* FP32 modes: refinement sweeps per solve (0 = default: 2 for
                         FP32_IR, 1 for FP32_MIXED; < 0 = none) */
-  double ir_tol;     /* FP32_IR: target relative residual (0 = default 1e-12) */
+  double ir_tol;     /* reserved: the refinement runs ir_max_iters sweeps; pecs_solve_residual
+                        reports the relative residual they reached */
   int device;        /* CUDA device ordinal */
   int host_setup_only; /* 1: build meshes, matrices and factors on the host only
                           (no device work; for inspecting the setup) */
@@ -201,6 +202,12 @@ int pecs_sweep_stream(pecs_ctx* ctx, int n_points, const pecs_params* params,
                       const double* const* init_n, const double* const* init_p, int max_steps, double tol,
                       int check_every, int* steps, double* currents, double* const* final_fields);
 int pecs_synchronize(pecs_ctx* ctx);
+/* Largest relative residual ||b - A x|| / ||b|| (FP64) over the instances and
+ * fields of the latest carrier (which = 0) or Poisson (1) solve: b the last
+ * assembled right-hand sides, x the state they were solved into.  Reports
+ * what the refinement of the FP32 modes reached.  No reference counterpart
+ * (UMFPACK's direct solves in Carrier.cpp:34-40 are not checked). */
+int pecs_solve_residual(pecs_ctx* ctx, int which, double* max_rel);
 /* Time steps executed by the last pecs_run_to_steady_state / pecs_iv_sweep
  * (including steps of a polling interval after the last instance converged). */
 int pecs_last_run_steps(pecs_ctx* ctx);

@@ -102,6 +102,7 @@ SIGNATURES = [
                                     C.POINTER(C.c_void_p), C.c_int, C.c_double, C.c_int, _ip, _dp,
                                     C.POINTER(_dp)]),
     ("pecs_synchronize", C.c_int, [_vp]),
+    ("pecs_solve_residual", C.c_int, [_vp, C.c_int, _dp]),
     ("pecs_get_stream", _vp, [_vp]),
     ("pecs_last_run_steps", C.c_int, [_vp]),
     ("pecs_time_solve", C.c_int, [_vp, C.c_int, C.c_int, _dp]),

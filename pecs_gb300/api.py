@@ -267,6 +267,12 @@ class Context:
         check(lib().pecs_time_solve(self._h, which, reps, C.byref(ms)))
         return ms.value
 
+    def solve_residual(self, which: int) -> float:
+        """Largest relative residual of the latest carrier (0) / Poisson (1) solve."""
+        out = C.c_double()
+        check(lib().pecs_solve_residual(self._h, which, C.byref(out)))
+        return out.value
+
     def synchronize(self):
         check(lib().pecs_synchronize(self._h))
 

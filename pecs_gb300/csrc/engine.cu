@@ -246,6 +246,31 @@ void launch_residual_df(const CsrDf& A, const double* b, const X* xs, RT* r, int
   PECS_CUDA(cudaGetLastError());
 }
 
+// ||b - A x||^2 and ||b||^2 of one instance-major vector pair (grid.y =
+// instance), accumulated in FP64 (diagnostic: the residual a solve reached)
+__global__ void k_residual_norms(CsrDev A, const double* __restrict__ b, const double* __restrict__ x, int n,
+                                 double* __restrict__ sums) {
+  const int i = blockIdx.y;
+  const double* bi = b + (size_t)i * n;
+  const double* xi = x + (size_t)i * n;
+  double r2 = 0.0, b2 = 0.0;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int p = A.rp[row]; p < A.rp[row + 1]; ++p) acc += A.v[p] * xi[A.ci[p]];
+    const double r = bi[row] - acc;
+    r2 += r * r;
+    b2 += bi[row] * bi[row];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+    b2 += __shfl_xor_sync(0xffffffffu, b2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(sums + 2 * i, r2);
+    atomicAdd(sums + 2 * i + 1, b2);
+  }
+}
+
 // FP64 variant (FP32_IR mode)
 template <typename RT>
 __global__ void k_residual_il(CsrDev A, const double* __restrict__ b, const double* __restrict__ x,
@@ -1260,6 +1285,28 @@ struct Engine {
                                               std::to_string(-cs[i]));
   }
 
+  // Largest ||b - A x|| / ||b|| over the instances and fields of one bank, for
+  // the latest solve: b = the last assembled right-hand sides, x = the state
+  // they were solved into (valid after a full step or a stage solve).
+  double solve_residual(int which) {
+    std::vector<int> flds = which == 0 ? carrier_fields() : std::vector<int>{4};
+    DBuf<double> sums;
+    sums.alloc((size_t)2 * n_inst);
+    double worst = 0.0;
+    for (int f : flds) {
+      sums.zero();
+      const DBuf<double>& x = which == 0 ? (carriers_advanced ? state[nxt()][f] : state[cur][f]) : state[cur][f];
+      k_residual_norms<<<dim3(64, n_inst), 256, 0, st>>>(csr.m[f], rhs[f].p, x.p, nd[f], sums.p);
+      PECS_CUDA(cudaGetLastError());
+      std::vector<double> h(2 * n_inst);
+      PECS_CUDA(cudaMemcpyAsync(h.data(), sums.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
+      PECS_CUDA(cudaStreamSynchronize(st));
+      for (int i = 0; i < n_inst; ++i)
+        if (h[2 * i + 1] > 0.0) worst = std::max(worst, std::sqrt(h[2 * i] / h[2 * i + 1]));
+    }
+    return worst;
+  }
+
   // ---- streamed sweep: slots refilled as they finish -------------------------
   // New parameters for the given slots (host setup of their per-instance data,
   // uploaded slice by slice), their initial state (standard, or the given
@@ -1756,6 +1803,14 @@ int pecs_run_to_steady_state(pecs_ctx* ctx, int max_steps, double tol, int check
     need_device(ctx->e);
     if (!(tol >= 0.0)) throw PecsError(PECS_E_ARG, "tol must be >= 0");
     ctx->e.run_to_steady(max_steps, tol, check_every, steps, rel_change);
+  })
+}
+
+int pecs_solve_residual(pecs_ctx* ctx, int which, double* max_rel) {
+  PECS_TRY({
+    if (!ctx || !max_rel || which < 0 || which > 1) throw PecsError(PECS_E_ARG, "invalid arguments");
+    need_device(ctx->e);
+    *max_rel = ctx->e.solve_residual(which);
   })
 }
 

@@ -239,3 +239,22 @@ def test_split_k_levels_match_oracle_and_unsplit(pecs_lib):
         for f in split.fields():
             assert rel_err(split.get_state(f, i), whole.get_state(f, i)) < 1e-12
             assert rel_err(tuned.get_state(f, i), whole.get_state(f, i)) < 1e-12
+
+
+def test_refinement_reaches_fp64_residuals(pecs_lib):
+    """FP32 factors + FP64-residual refinement: the relative residual the
+    solves reach (pecs_solve_residual), against plain FP64 factors."""
+    P = to_lib(oracle.config2_params(n_refine=4))
+    res = {}
+    for name, kw in (("fp64", {}), ("ir2", dict(precision=pg.PREC_FP32_IR)),
+                     ("ir4", dict(precision=pg.PREC_FP32_IR, ir_max_iters=4)),
+                     ("mixed", dict(precision=pg.PREC_FP32_MIXED))):
+        ctx = pg.Context(P, **kw)
+        ctx.initialize()
+        ctx.step(3)
+        res[name] = (ctx.solve_residual(0), ctx.solve_residual(1))
+    print(res)
+    assert max(res["fp64"]) < 1e-13
+    assert max(res["ir4"]) < 1e-12
+    assert max(res["ir2"]) < 1e-10
+    assert max(res["mixed"]) < 1e-9
