@@ -16,6 +16,7 @@
 // _for_electrolyte (SolarCell.cpp:487-815): -(v, sum q_i u_i) on the Phi rows
 // of the matching Poisson cell plus the constant doping/Dirichlet part.
 #pragma once
+#include "fp_bits.cuh"
 #include <type_traits>
 #include <cuda_runtime.h>
 
@@ -81,6 +82,17 @@ struct Dims {
   static constexpr int nphi = K * K;
 };
 
+// state values into the quadrature type, and quadrature sums back: on the
+// integer pipe for the FP32 path (fp_bits.cuh), plain for FP64
+template <typename Tq>
+__device__ __forceinline__ Tq to_q(double x) {
+  if constexpr (sizeof(Tq) == 4) return d2f_trunc(x); else return x;
+}
+template <typename Tq>
+__device__ __forceinline__ double from_q(Tq x) {
+  if constexpr (sizeof(Tq) == 4) return f2d_exact(x); else return x;
+}
+
 template <typename Tq>
 __device__ __forceinline__ const Tq* tab(const double* d, const float* f);
 template <>
@@ -135,8 +147,8 @@ __global__ void __launch_bounds__(128)
   for (int a = 0; a < n1; ++a) {
     const double x1 = u1p[a], x2 = u2p[a];
     uown[a] = which ? x2 : x1;
-    u1[a] = (Tq)x1;
-    u2[a] = (Tq)x2;
+    u1[a] = to_q<Tq>(x1);
+    u2[a] = to_q<Tq>(x2);
   }
   const double* Pv = F.u[4] + (size_t)i * F.nd[4];
   Tq Dd[nrt];
@@ -233,8 +245,8 @@ __global__ void __launch_bounds__(128)
         const Tq fp = fphi[(pf * n1 + a) * nq + q];
         a1 += fo * u1[a];
         a2 += fo * u2[a];
-        b1 += fp * (Tq)o1p[a];
-        b2 += fp * (Tq)o2p[a];
+        b1 += fp * to_q<Tq>(o1p[a]);
+        b2 += fp * to_q<Tq>(o2p[a]);
       }
       // semiconductor-side values n, p and electrolyte-side r, o
       const Tq n = in_semi ? a1 : b1, p = in_semi ? a2 : b2;
@@ -291,7 +303,7 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
     for (int b = 0; b < n1; ++b) s += T.mref[a * n1 + b] * uown[b];
     const size_t o = (size_t)2 * nc * n1 + c * n1 + a;
-    outp[o] = bcp[o] + s * hxhy * R.inv_dt + (double)r[2 * n1 + a];
+    outp[o] = bcp[o] + s * hxhy * R.inv_dt + from_q<Tq>(r[2 * n1 + a]);
   }
 }
 
