@@ -501,6 +501,14 @@ def run_full(args):
     e2e = n_e * world / max_over_ranks(time.perf_counter() - t0, world)
     h2d = n_e * (sum(info.ndofs[f] for f in range(5)) * 8 + info.ndofs[4] * 8)  # per-point constant RHS parts
     d2h = n_e * 8 + sum(a.nbytes for a in fin_e.values())
+    # ---- the same timed points, batched and streamed but without the warm start --
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    steps_nw, _, _, _ = L.stream_warm_sweep(ctx, None, th_t, base, MAX_STEPS, TOL, CHECK_EVERY)
+    e3.record(stream)
+    e3.synchronize()
+    nw_value = n_t * world / (max_over_ranks(e2.elapsed_time(e3), world) * 1e-3)
     # ---- accuracy: the same points, same warm starts, FP64 throughout ---------------
     nchk = 4
     ref = pg.Context([L.instance_params(t, base) for t in th_e[:nchk]], precision=pg.PREC_FP64, device=local)
@@ -547,6 +555,10 @@ def run_full(args):
         "plain": {"value": plain_value, "unit": "I-V points/s", "steps_to_steady_state": plain_steps,
                   "workload": "config 2: one instance, FP64, standard initial condition"},
         "speedup_vs_plain": value / plain_value,
+        "batched_without_warm_start": {"value": nw_value, "unit": "I-V points/s",
+                                       "median_steps": float(np.median(steps_nw)),
+                                       "mean_steps": float(np.mean(steps_nw)),
+                                       "capped": int(np.sum(steps_nw >= MAX_STEPS))},
         "warm_start": {"median_steps": float(np.median(steps_t)), "mean_steps": float(np.mean(steps_t)),
                        "capped": int(np.sum(steps_t >= MAX_STEPS + 2)),
                        "fallback_rate": float(np.mean(fb_t)), "plain_steps": plain_steps,
