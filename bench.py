@@ -188,7 +188,7 @@ def workload_params(args, rank):
         # each rank/instance one point of an I-V sweep (bias in thermal-voltage units)
         g = rank * n + i
         bias = 0.0 if n == 1 else -0.5 + (g % 64) / 63.0
-        ps.append(pg.config2(n_refine=args.refine, phi_app=bias))
+        ps.append(pg.half_cell(n_refine=args.refine, phi_app=bias))
     return ps
 
 
@@ -197,7 +197,7 @@ def cpu_baseline(args, steps_to_ss, sample_steps):
     same workload, extrapolated to I-V points/sec with the steps to steady
     state measured on the GPU."""
     import oracle
-    P = oracle.config2_params(n_refine=args.refine)
+    P = oracle.half_cell_params(n_refine=args.refine)
     pb = oracle.Problem(P)
     st = pb.initial_state()
     st = pb.step(st)  # first step builds the LU factors (setup, untimed)
@@ -216,7 +216,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     import oracle
-    P = oracle.config2_params(n_refine=args.refine)
+    P = oracle.half_cell_params(n_refine=args.refine)
     pb = oracle.Problem(P)
     st = pb.initial_state()
     st = pb.step(st)
@@ -417,8 +417,8 @@ def run_plain(args):
 
 
 def plain_point(pg, refine, local):
-    """The plain FP64 single-instance path (config 2): one I-V point."""
-    ctx = pg.Context([pg.config2(n_refine=refine)], precision=pg.PREC_FP64, device=local)
+    """The plain FP64 single-instance path (half cell 64x64+64x64, k=1): one I-V point."""
+    ctx = pg.Context([pg.half_cell(n_refine=refine)], precision=pg.PREC_FP64, device=local)
     ctx.initialize()
     ctx.run_to_steady_state(MAX_STEPS, TOL, CHECK_EVERY)   # warm
     import torch
@@ -446,7 +446,7 @@ def run_full(args):
     world, rank, local = dist_init(args)
     pg.build()
     B = args.batch_inst
-    base = pg.config2(n_refine=args.refine)
+    base = pg.half_cell(n_refine=args.refine)
     # held-out draws (seed differs from the training seed), sharded by rank:
     # warm-up points, timed points, end-to-end points
     n_w, n_t, n_e = args.warmup * B, args.steps * B, B
@@ -526,7 +526,7 @@ def run_full(args):
         err_cur = max(err_cur, float(abs(cur_e[i] - cur64[i]) / abs(cur64[i])))
     steps_diff = [int(a) - 2 - int(b) for a, b in zip(steps_e[:nchk], s64)]
     del ref
-    # ---- plain path (config 2, FP64, single instance) ---------------------------------
+    # ---- plain path (half cell 64x64+64x64, FP64, single instance) --------------------
     plain_value, plain_steps, pctx = plain_point(pg, args.refine, local)
     pinfo = pctx.info()
     plain_ms = pctx.time_solve(0, reps=30)
@@ -553,7 +553,7 @@ def run_full(args):
                    "l2": "flushed (512 MB write) before the timed sweep; the sweep streams ~"
                          f"{info.factor_bytes / 1e6:.0f} MB of factors per step"},
         "plain": {"value": plain_value, "unit": "I-V points/s", "steps_to_steady_state": plain_steps,
-                  "workload": "config 2: one instance, FP64, standard initial condition"},
+                  "workload": "half cell 64x64+64x64, k=1: one instance, FP64, standard initial condition"},
         "speedup_vs_plain": value / plain_value,
         "batched_without_warm_start": {"value": nw_value, "unit": "I-V points/s",
                                        "median_steps": float(np.median(steps_nw)),

@@ -340,7 +340,7 @@ class Params:
 
 
 def reference_params(n_refine: int = 4, degree: int = 1, **kw) -> Params:
-    """Reference-faithful physics: constant equilibria
+    """Reference-faithful physics (what the reference code hard-codes): constant equilibria
     2, 0, 30, 29 (source/InitialConditions.cpp:5-82), SRH returning 0
     (include/SolarCell.hpp:86-98), generation alpha*G0*exp(alpha*(y-H))
     (source/Generation.cpp:29-44), potential data Phi_bi - Phi_app on x==0
@@ -354,7 +354,7 @@ def reference_params(n_refine: int = 4, degree: int = 1, **kw) -> Params:
     return p.copy(**kw)
 
 
-def config1_params(**kw) -> Params:
+def pn_junction_params(**kw) -> Params:
     """Semiconductor-only p-n junction, unit square, 16x16, k=1, 100 steps."""
     n_i = 1e-2
     p = Params(degree=1, full_system=False, nx_semi=16, nx_elec=0, ny=16,
@@ -369,7 +369,7 @@ def config1_params(**kw) -> Params:
     return p.copy(**kw)
 
 
-def config2_params(n_refine: int = 6, **kw) -> Params:
+def half_cell_params(n_refine: int = 6, **kw) -> Params:
     """Coupled half cell: semi [0,1]^2, electrolyte [1,2]x[0,1], 2^r x 2^r each."""
     n_i = 1e-2
     n = 2 ** n_refine

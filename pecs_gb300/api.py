@@ -79,7 +79,7 @@ class Params:
         return p
 
 
-def config1(**kw) -> Params:
+def pn_junction(**kw) -> Params:
     """Semiconductor-only p-n junction on the unit square, 16x16 cells, k=1,
     dt=1e-3, 100 steps, initial densities = doping."""
     n_i = 1e-2
@@ -93,7 +93,7 @@ def config1(**kw) -> Params:
     return p.copy(**kw)
 
 
-def config2(n_refine: int = 6, **kw) -> Params:
+def half_cell(n_refine: int = 6, **kw) -> Params:
     """Coupled half cell: semiconductor [0,1]^2 and electrolyte [1,2]x[0,1],
     2^r x 2^r cells each, k=1, G = G0 exp(-alpha (1-x)), dt=1e-3."""
     n_i = 1e-2

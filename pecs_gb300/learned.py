@@ -26,7 +26,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _ffi as F
-from .api import Context, Params, config2
+from .api import Context, Params, half_cell
 from ._ffi import check, lib
 
 NAMES = ("bias", "G0", "alpha", "N_D", "tau", "k_et")

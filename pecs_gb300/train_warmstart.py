@@ -44,7 +44,7 @@ def main():
 
     pg.build()
     prec = pg.PREC_FP32_MIXED if args.precision == "mixed" else pg.PREC_FP64
-    base = pg.config2(n_refine=args.refine)
+    base = pg.half_cell(n_refine=args.refine)
     B = 64
     thetas = L.sample(args.n_train + args.n_eval, args.seed)
     tr, ev = thetas[:args.n_train], thetas[args.n_train:]

@@ -36,7 +36,7 @@ def test_no_device_is_a_clean_error(pecs_lib):
     if torch.cuda.is_available():
         pytest.skip("a GPU is present")
     with pytest.raises(pg.PecsError) as ei:
-        pg.Context(pg.config2(n_refine=2))
+        pg.Context(pg.half_cell(n_refine=2))
     assert ei.value.code == pg._ffi.PECS_E_NODEVICE
 
 
@@ -44,7 +44,7 @@ def test_sweep_stream_rejects_points_with_other_matrices(pecs_lib):
     """Every streamed point must share the context's fixed matrices; the
     check runs before any device work (host-only context here)."""
     import pecs_gb300 as pg
-    base = pg.config2(n_refine=2)
+    base = pg.half_cell(n_refine=2)
     ctx = pg.Context([base], host_setup_only=True)
     with pytest.raises(pg.PecsError, match="dt"):
         ctx.sweep_stream([base, base.copy(dt=2e-3)], 10, 1e-6)

@@ -29,7 +29,7 @@ def _compare_state(ctx, st, tol, inst=0):
 
 
 def test_lu_device_solve_matches_scipy(pecs_lib):
-    pb = oracle.Problem(oracle.config2_params(n_refine=3))
+    pb = oracle.Problem(oracle.half_cell_params(n_refine=3))
     rng = np.random.default_rng(1)
     dc, cl, xy = _maps_carrier(pb, pb.semi)
     lu = pg.LU(pb.A_n, dc, xy, cl)
@@ -46,10 +46,10 @@ def test_lu_device_solve_matches_scipy(pecs_lib):
     assert rel_err(lu32.solve(b), spla.spsolve(pb.A_P.tocsc(), b)) < 1e-4
 
 
-@pytest.mark.parametrize("P", [oracle.config2_params(n_refine=3), oracle.config1_params(),
+@pytest.mark.parametrize("P", [oracle.half_cell_params(n_refine=3), oracle.pn_junction_params(),
                                oracle.reference_params(3, 1, dt=1e-4),
-                               oracle.config2_params(n_refine=2, degree=2)],
-                         ids=["config2_r3", "config1", "reference_r3", "config2_r2_k2"])
+                               oracle.half_cell_params(n_refine=2, degree=2)],
+                         ids=["halfcell_r3", "pn_junction", "reference_r3", "halfcell_r2_k2"])
 def test_initial_state_and_rhs(pecs_lib, P):
     pb = oracle.Problem(P)
     st = pb.initial_state()
@@ -62,12 +62,12 @@ def test_initial_state_and_rhs(pecs_lib, P):
         assert max_rel(ctx.get_rhs(FIELD_OF[name]), v) < RHS_TOL, name
 
 
-@pytest.mark.parametrize("P,steps", [(oracle.config2_params(n_refine=3), 20),
-                                     (oracle.config1_params(), 100),
+@pytest.mark.parametrize("P,steps", [(oracle.half_cell_params(n_refine=3), 20),
+                                     (oracle.pn_junction_params(), 100),
                                      (oracle.reference_params(3, 1, dt=1e-4), 10),
-                                     (oracle.config2_params(n_refine=2, degree=2), 10),
-                                     (oracle.config2_params(n_refine=3, mu=(1.0, 0.5, 2.0, 1.0)), 10)],
-                         ids=["config2_r3", "config1_100", "reference_r3", "config2_r2_k2", "mu_distinct"])
+                                     (oracle.half_cell_params(n_refine=2, degree=2), 10),
+                                     (oracle.half_cell_params(n_refine=3, mu=(1.0, 0.5, 2.0, 1.0)), 10)],
+                         ids=["halfcell_r3", "pn_junction_100", "reference_r3", "halfcell_r2_k2", "mu_distinct"])
 def test_trajectory_matches_oracle(pecs_lib, P, steps):
     pb = oracle.Problem(P)
     st, _, _ = pb.run(steps)
@@ -81,7 +81,7 @@ def test_trajectory_matches_oracle(pecs_lib, P, steps):
 
 
 def test_stage_api_equals_step(pecs_lib):
-    P = oracle.config2_params(n_refine=3)
+    P = oracle.half_cell_params(n_refine=3)
     a = _ctx(P)
     a.initialize()
     for _ in range(3):
@@ -97,7 +97,7 @@ def test_stage_api_equals_step(pecs_lib):
 
 
 def test_batched_instances_match_single(pecs_lib):
-    base = oracle.config2_params(n_refine=3)
+    base = oracle.half_cell_params(n_refine=3)
     Ps = [base.copy(phi_app=v, G0=g, tau_n=t, tau_p=t)
           for v, g, t in ((0.0, 1.0, 1.0), (-0.3, 0.5, 0.3), (0.4, 2.0, 3.0))]
     ctx = pg.Context([to_lib(P) for P in Ps])
@@ -109,7 +109,7 @@ def test_batched_instances_match_single(pecs_lib):
 
 
 def test_steady_state_graph_and_eager_agree(pecs_lib):
-    P = oracle.config2_params(n_refine=2)
+    P = oracle.half_cell_params(n_refine=2)
     res = []
     for graphs in (True, False):
         ctx = _ctx(P, use_graphs=graphs)
@@ -128,7 +128,7 @@ def test_steady_state_graph_and_eager_agree(pecs_lib):
 
 
 def test_fp32_refined_matches_fp64_oracle(pecs_lib):
-    P = oracle.config2_params(n_refine=3)
+    P = oracle.half_cell_params(n_refine=3)
     pb = oracle.Problem(P)
     st, _, _ = pb.run(20)
     ctx = _ctx(P, precision=pg.PREC_FP32_IR, ir_max_iters=3)
@@ -141,7 +141,7 @@ def test_fp32_refined_matches_fp64_oracle(pecs_lib):
 def test_mixed_precision_within_1e6_of_fp64_oracle(pecs_lib, iters):
     """FP32 factors + double-float refinement + FP32 quadrature terms: the
     batched throughput mode must stay within 1e-6 of the FP64 oracle."""
-    P = oracle.config2_params(n_refine=3)
+    P = oracle.half_cell_params(n_refine=3)
     pb = oracle.Problem(P)
     st, _, _ = pb.run(20)
     ctx = _ctx(P, precision=pg.PREC_FP32_MIXED, ir_max_iters=iters)
@@ -156,7 +156,7 @@ def test_mixed_precision_steady_state_and_current(pecs_lib):
     1e-8 change sits ~rel_change/(decay rate * dt) ~ 3e-6 short of the fixed
     point, and the mixed mode's FP32 terms leave a per-step noise floor
     between 1e-10 and 1e-8, so stopping criteria cannot be compared)."""
-    base = oracle.config2_params(n_refine=3)
+    base = oracle.half_cell_params(n_refine=3)
     Ps = [base.copy(phi_app=v) for v in (-0.4, 0.0, 0.4)]
     res = {}
     for prec in (pg.PREC_FP32_MIXED, pg.PREC_FP64):
@@ -174,7 +174,7 @@ def test_mixed_precision_steady_state_and_current(pecs_lib):
 def test_mixed_precision_converges_at_the_benchmark_criterion(pecs_lib):
     """At the benchmark's 1e-8 criterion the mixed mode stops within a few
     percent of the FP64 step count."""
-    base = oracle.config2_params(n_refine=3)
+    base = oracle.half_cell_params(n_refine=3)
     Ps = [base.copy(phi_app=v) for v in (-0.4, 0.0, 0.4)]
     steps = {}
     for prec in (pg.PREC_FP32_MIXED, pg.PREC_FP64):
@@ -198,7 +198,7 @@ def test_panel_batches_match_oracle(pecs_lib, n_inst):
     (lanes over right-hand sides): 40 instances give 80 carrier and 40 Poisson
     right-hand sides (partial chunks, one and two per lane), 64 give 128 and
     64.  FP64 factors: every checked instance within the step tolerance."""
-    Ps = _panel_instances(n_inst, oracle.config2_params(n_refine=3))
+    Ps = _panel_instances(n_inst, oracle.half_cell_params(n_refine=3))
     ctx = pg.Context([to_lib(P) for P in Ps])
     ctx.initialize()
     ctx.step(5)
@@ -208,7 +208,7 @@ def test_panel_batches_match_oracle(pecs_lib, n_inst):
 
 
 def test_panel_mixed_batch_within_1e6(pecs_lib):
-    Ps = _panel_instances(64, oracle.config2_params(n_refine=3))
+    Ps = _panel_instances(64, oracle.half_cell_params(n_refine=3))
     ctx = pg.Context([to_lib(P) for P in Ps], precision=pg.PREC_FP32_MIXED)
     ctx.initialize()
     ctx.step(20)
@@ -225,7 +225,7 @@ def test_split_k_levels_match_oracle_and_unsplit(pecs_lib):
     1 keeps every level unsplit).  Both use the tiling heuristic (no
     autotuning), which splits the root-most levels here; a third, autotuned
     context must agree as well."""
-    Ps = _panel_instances(40, oracle.config2_params(n_refine=5))
+    Ps = _panel_instances(40, oracle.half_cell_params(n_refine=5))
     split = pg.Context([to_lib(P) for P in Ps], autotune=False)
     whole = pg.Context([to_lib(P) for P in Ps], panel_min_ctas=1, autotune=False)
     tuned = pg.Context([to_lib(P) for P in Ps])
@@ -244,7 +244,7 @@ def test_split_k_levels_match_oracle_and_unsplit(pecs_lib):
 def test_refinement_reaches_fp64_residuals(pecs_lib):
     """FP32 factors + FP64-residual refinement: the relative residual the
     solves reach (pecs_solve_residual), against plain FP64 factors."""
-    P = to_lib(oracle.config2_params(n_refine=4))
+    P = to_lib(oracle.half_cell_params(n_refine=4))
     res = {}
     for name, kw in (("fp64", {}), ("ir2", dict(precision=pg.PREC_FP32_IR)),
                      ("ir4", dict(precision=pg.PREC_FP32_IR, ir_max_iters=4)),

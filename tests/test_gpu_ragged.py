@@ -1,4 +1,4 @@
-"""Ragged I-V sweeps (BASELINE config 3 shape): points with different
+"""Ragged I-V sweeps (the batched sweep with uneven instances): points with different
 refinement levels and degrees are grouped by their meshes and streamed through
 one context per group; every point must end exactly where it ends alone."""
 import numpy as np
@@ -16,7 +16,7 @@ def test_ragged_sweep_matches_single_instances(pecs_lib):
     for _ in range(10):
         r = int(rng.integers(2, 4))          # refinement 2 or 3
         k = int(rng.integers(1, 3))          # degree 1 or 2
-        pts.append(pg.config2(n_refine=r, degree=k, phi_app=float(rng.uniform(-0.5, 0.5)),
+        pts.append(pg.half_cell(n_refine=r, degree=k, phi_app=float(rng.uniform(-0.5, 0.5)),
                               G0=float(rng.uniform(0.5, 2.0))))
     steps, cur, fields = ragged_sweep(pts, slots=3, max_steps=400, tol=1e-6, check_every=10,
                                       want_fields=True)

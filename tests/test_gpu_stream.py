@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _points(n, seed, refine=3):
-    base = pg.config2(n_refine=refine)
+    base = pg.half_cell(n_refine=refine)
     return [L.instance_params(t, base) for t in L.sample(n, seed)]
 
 

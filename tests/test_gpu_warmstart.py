@@ -51,7 +51,7 @@ def test_mlp_training_reduces_loss(pecs_lib):
 def test_warm_start_saves_steps_and_keeps_the_steady_state(pecs_lib):
     torch = _torch()
     from pecs_gb300 import learned as L
-    base = pg.config2(n_refine=3)
+    base = pg.half_cell(n_refine=3)
     thetas = L.sample(96, seed=5)
     tr, ev = thetas[:64], thetas[64:]
     ctx = pg.Context([L.instance_params(t, base) for t in tr[:32]], precision=pg.PREC_FP32_MIXED)

@@ -33,7 +33,7 @@ def _maps_poisson(pb):
     return dof_cell, np.stack([x0 + hx / 2, y0 + hy / 2], 1)
 
 
-@pytest.mark.parametrize("P", [oracle.config2_params(n_refine=3), oracle.config1_params(),
+@pytest.mark.parametrize("P", [oracle.half_cell_params(n_refine=3), oracle.pn_junction_params(),
                                oracle.reference_params(2, 2)])
 def test_host_factorisation_matches_scipy(pecs_lib, P):
     pb = oracle.Problem(P)
@@ -56,7 +56,7 @@ def test_host_factorisation_matches_scipy(pecs_lib, P):
 
 
 def test_class0_coupling_is_rejected(pecs_lib):
-    pb = oracle.Problem(oracle.config2_params(n_refine=2))
+    pb = oracle.Problem(oracle.half_cell_params(n_refine=2))
     dc, cl, xy = _maps_carrier(pb, pb.semi)
     bad = np.zeros_like(cl)   # every dof "cell-local": u dofs couple across cells
     with pytest.raises(pg.PecsError):

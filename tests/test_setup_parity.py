@@ -9,11 +9,11 @@ import pecs_gb300 as pg
 from helpers import to_lib
 
 CASES = [
-    ("config1", oracle.config1_params()),
-    ("config2_r3", oracle.config2_params(n_refine=3)),
+    ("pn_junction", oracle.pn_junction_params()),
+    ("halfcell_r3", oracle.half_cell_params(n_refine=3)),
     ("reference_r3_k1", oracle.reference_params(3, 1)),
     ("reference_r2_k2", oracle.reference_params(2, 2)),
-    ("config2_r2_k2_mu", oracle.config2_params(n_refine=2, degree=2, mu=(1.0, 0.5, 2.0, 1.0))),
+    ("halfcell_r2_k2_mu", oracle.half_cell_params(n_refine=2, degree=2, mu=(1.0, 0.5, 2.0, 1.0))),
 ]
 
 
@@ -42,18 +42,18 @@ def test_matrices_match_oracle(pecs_lib, name, P):
 
 
 def test_equal_mobilities_share_one_factor(pecs_lib):
-    ctx = pg.Context(pg.config2(n_refine=2), host_setup_only=True)
+    ctx = pg.Context(pg.half_cell(n_refine=2), host_setup_only=True)
     assert ctx.info().n_distinct_carrier_factors == 2
-    ctx = pg.Context(pg.config2(n_refine=2, mu=(1.0, 0.5, 1.0, 1.0)), host_setup_only=True)
+    ctx = pg.Context(pg.half_cell(n_refine=2, mu=(1.0, 0.5, 1.0, 1.0)), host_setup_only=True)
     assert ctx.info().n_distinct_carrier_factors == 3
 
 
 def test_invalid_params_are_rejected(pecs_lib):
     with pytest.raises(pg.PecsError):
-        pg.Context(pg.config2(n_refine=2, degree=3), host_setup_only=True)
+        pg.Context(pg.half_cell(n_refine=2, degree=3), host_setup_only=True)
     with pytest.raises(pg.PecsError):
-        pg.Context(pg.config2(n_refine=2, dt=0.0), host_setup_only=True)
-    a = pg.config2(n_refine=2)
-    b = pg.config2(n_refine=3)
+        pg.Context(pg.half_cell(n_refine=2, dt=0.0), host_setup_only=True)
+    a = pg.half_cell(n_refine=2)
+    b = pg.half_cell(n_refine=3)
     with pytest.raises(pg.PecsError):
         pg.Context([a, b], host_setup_only=True)

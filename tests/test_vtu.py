@@ -27,7 +27,7 @@ def _arrays(path):
 
 
 def test_carrier_patches_and_scaling(tmp_path):
-    p = pg.config2(n_refine=1)   # 2x2 cells per region, k = 1
+    p = pg.half_cell(n_refine=1)   # 2x2 cells per region, k = 1
     nc, n1 = 4, 4
     n = np.arange(3 * nc * n1, dtype=float)
     vecs = {pg.FIELD_N: n, pg.FIELD_P: -n}
@@ -47,7 +47,7 @@ def test_carrier_patches_and_scaling(tmp_path):
 
 
 def test_potential_cell_data(tmp_path):
-    p = pg.config2(n_refine=1)
+    p = pg.half_cell(n_refine=1)
     ncp = 8                      # 4 x 2 Poisson cells
     n_rt = 22                    # whatever precedes the potential block
     P = np.concatenate([np.zeros(n_rt), np.arange(ncp, dtype=float)])

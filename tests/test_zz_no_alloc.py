@@ -31,7 +31,7 @@ def _rel(a, b):
 @pytest.mark.parametrize("system", ["carrier", "poisson"])
 def test_noalloc_matches_allocating_solve_twice(pecs_lib, system):
     torch = pytest.importorskip("torch")
-    pb = oracle.Problem(oracle.config2_params(n_refine=4))
+    pb = oracle.Problem(oracle.half_cell_params(n_refine=4))
     if system == "carrier":
         dc, cl, xy = _maps_carrier(pb, pb.semi)
         lu = pg.LU(pb.A_n, dc, xy, cl)
@@ -55,7 +55,7 @@ def test_noalloc_matches_allocating_solve_twice(pecs_lib, system):
 
 def test_noalloc_limits_and_preconditions(pecs_lib):
     torch = pytest.importorskip("torch")
-    pb = oracle.Problem(oracle.config2_params(n_refine=6))
+    pb = oracle.Problem(oracle.half_cell_params(n_refine=6))
     dc, cl, xy = _maps_carrier(pb, pb.semi)
     lu = pg.LU(pb.A_n, dc, xy, cl)
     n = pb.A_n.shape[0]
