@@ -1,10 +1,13 @@
 // Multifrontal LU: ordering, symbolic analysis, numeric factorisation (see mf.hpp).
 #include "mf.hpp"
 
+#include "dense.hpp"
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <functional>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <sstream>
@@ -291,7 +294,7 @@ namespace {
 // Factor one node's front.  Returns the update matrix S (m x m).
 std::vector<double> factor_node(MfFactor& F, int j, const Csr& A, const Csr& AT,
                                 std::vector<std::vector<double>>& Sstore, std::vector<int>& fpos,
-                                double& flops) {
+                                double& flops, dense::Team* team) {
   MfNode& nd = F.nodes[j];
   const int s = nd.s, m = nd.m, f = s + m;
   std::vector<double> Fm((size_t)f * f, 0.0);
@@ -333,102 +336,35 @@ std::vector<double> factor_node(MfFactor& F, int j, const Csr& A, const Csr& AT,
   }
   // partial pivoting LU on the first s columns, pivots among the s fully-summed rows
   std::vector<int> perm(s);
-  std::iota(perm.begin(), perm.end(), 0);
   double colmax_all = 0.0;
   for (size_t t = 0; t < (size_t)s * f; ++t) colmax_all = std::max(colmax_all, std::fabs(Fm[t]));
-  for (int col = 0; col < s; ++col) {
-    int piv = col;
-    double best = std::fabs(Fm[(size_t)col * f + col]);
-    for (int r = col + 1; r < s; ++r) {
-      double v = std::fabs(Fm[(size_t)r * f + col]);
-      if (v > best) {
-        best = v;
-        piv = r;
-      }
-    }
-    if (!(best > 1e-14 * colmax_all) || !std::isfinite(best)) {
-      std::ostringstream e;
-      e << "singular pivot " << best << " at node " << j << " column " << col << " (front " << s
-        << "+" << m << ")";
-      throw std::runtime_error(e.str());
-    }
-    if (piv != col) {
-      for (int c2 = 0; c2 < f; ++c2) std::swap(Fm[(size_t)col * f + c2], Fm[(size_t)piv * f + c2]);
-      std::swap(perm[col], perm[piv]);
-    }
-    const double inv = 1.0 / Fm[(size_t)col * f + col];
-    const double* prow = &Fm[(size_t)col * f];
-    for (int r = col + 1; r < f; ++r) {
-      double* row = &Fm[(size_t)r * f];
-      double l = row[col];
-      if (l == 0.0) continue;
-      l *= inv;
-      row[col] = l;
-      for (int c2 = col + 1; c2 < f; ++c2) row[c2] -= l * prow[c2];
-    }
-    flops += 2.0 * (double)(f - col - 1) * (double)(f - col - 1);
+  double bad = 0.0;
+  const int badcol = dense::lu_front(f, s, Fm.data(), f, perm.data(), 1e-14 * colmax_all, &bad, team);
+  if (badcol >= 0) {
+    std::ostringstream e;
+    e << "singular pivot " << bad << " at node " << j << " column " << badcol << " (front " << s
+      << "+" << m << ")";
+    throw std::runtime_error(e.str());
   }
+  for (int col = 0; col < s; ++col) flops += 2.0 * (double)(f - col - 1) * (double)(f - col - 1);
   // update matrix
   std::vector<double> S((size_t)m * m);
   for (int a = 0; a < m; ++a)
-    for (int b = 0; b < m; ++b) S[(size_t)a * m + b] = Fm[(size_t)(s + a) * f + s + b];
-  // Linv = L11^-1 (unit lower)
-  std::vector<double> Linv((size_t)s * s, 0.0);
-  for (int r = 0; r < s; ++r) {
-    double* xr = &Linv[(size_t)r * s];
-    xr[r] = 1.0;
-    const double* lr = &Fm[(size_t)r * f];
-    for (int t = 0; t < r; ++t) {
-      double l = lr[t];
-      if (l == 0.0) continue;
-      const double* xt = &Linv[(size_t)t * s];
-      for (int c2 = 0; c2 <= t; ++c2) xr[c2] -= l * xt[c2];
-    }
-  }
-  // Gf = [Linv P ; L21 Linv P]
+    std::copy_n(&Fm[(size_t)(s + a) * f + s], m, &S[(size_t)a * m]);
+  // Gf = [L11^-1 P ; L21 L11^-1 P]
+  std::vector<double> X((size_t)f * s, 0.0);
+  dense::inv_unit_lower(s, Fm.data(), f, X.data(), s, team);
+  dense::gemm(m, s, s, 1.0, &Fm[(size_t)s * f], f, X.data(), s, &X[(size_t)s * s], s, team);
   std::vector<double>& G = F.Gf[j];
   G.assign((size_t)f * s, 0.0);
-  for (int r = 0; r < s; ++r)
-    for (int t = 0; t <= r; ++t) G[(size_t)r * s + perm[t]] = Linv[(size_t)r * s + t];
-  for (int r = 0; r < m; ++r) {
-    const double* l21 = &Fm[(size_t)(s + r) * f];
-    std::vector<double> acc(s, 0.0);
-    for (int u = 0; u < s; ++u) {
-      double l = l21[u];
-      if (l == 0.0) continue;
-      const double* xu = &Linv[(size_t)u * s];
-      for (int t = 0; t <= u; ++t) acc[t] += l * xu[t];
-    }
-    for (int t = 0; t < s; ++t) G[(size_t)(s + r) * s + perm[t]] = acc[t];
-  }
-  // Uinv = U11^-1 (upper), rows from the bottom
-  std::vector<double> Uinv((size_t)s * s, 0.0);
-  for (int r = s - 1; r >= 0; --r) {
-    const double* ur = &Fm[(size_t)r * f];
-    double* yr = &Uinv[(size_t)r * s];
-    const double dinv = 1.0 / ur[r];
-    yr[r] = dinv;
-    for (int t = r + 1; t < s; ++t) {
-      double u = ur[t];
-      if (u == 0.0) continue;
-      const double* yt = &Uinv[(size_t)t * s];
-      for (int c2 = t; c2 < s; ++c2) yr[c2] -= u * dinv * yt[c2];
-    }
-  }
-  // Hb = [Uinv | -Uinv U12]
+  for (int r = 0; r < f; ++r)
+    for (int t = 0; t < s; ++t) G[(size_t)r * s + perm[t]] = X[(size_t)r * s + t];
+  std::vector<double>().swap(X);
+  // Hb = [U11^-1 | -U11^-1 U12]
   std::vector<double>& H = F.Hb[j];
   H.assign((size_t)s * f, 0.0);
-  for (int r = 0; r < s; ++r) {
-    const double* yr = &Uinv[(size_t)r * s];
-    double* hr = &H[(size_t)r * f];
-    for (int c2 = r; c2 < s; ++c2) hr[c2] = yr[c2];
-    for (int u = r; u < s; ++u) {
-      double y = yr[u];
-      if (y == 0.0) continue;
-      const double* u12 = &Fm[(size_t)u * f + s];
-      for (int t = 0; t < m; ++t) hr[s + t] -= y * u12[t];
-    }
-  }
+  dense::inv_upper(s, Fm.data(), f, H.data(), f, team);
+  dense::gemm(s, m, s, -1.0, H.data(), f, &Fm[s], f, &H[s], f, team);
   for (int t = 0; t < s; ++t) fpos[nd.own[t]] = -1;
   for (int t = 0; t < m; ++t) fpos[nd.upd[t]] = -1;
   flops += 2.0 * s * s * (double)(s + m);
@@ -465,23 +401,30 @@ void mf_factorize(MfFactor& F, const Csr& A, int n_threads) {
     unsigned hc = std::thread::hardware_concurrency();
     n_threads = (int)std::max(1u, std::min(hc, 16u));
   }
-  // nodes of equal height are independent: factor them in parallel, height by height
+  // nodes of equal height are independent: factor them in parallel, height by
+  // height.  Wide levels run one node per thread; narrow levels (the top of the
+  // tree, few large fronts) give each node a team that shares its dense work.
   std::vector<std::vector<int>> by_h(F.n_heights);
   for (int j = 0; j < N; ++j) by_h[F.nodes[j].height].push_back(j);
   double flops = 0.0;
   std::string err;
   std::mutex mu;
   for (auto& lvl : by_h) {
+    const int L = (int)lvl.size();
+    const int nt = std::min(n_threads, L);
+    const int per_node = std::max(1, n_threads / std::max(1, L));
     std::atomic<size_t> next(0);
     auto worker = [&]() {
       std::vector<int> fpos(F.n, -1);
+      std::unique_ptr<dense::Team> team;
+      if (per_node > 1) team.reset(new dense::Team(per_node));
       double fl = 0.0;
       for (;;) {
         size_t t = next.fetch_add(1);
         if (t >= lvl.size()) break;
         int j = lvl[t];
         try {
-          Sstore[j] = factor_node(F, j, A, AT, Sstore, fpos, fl);
+          Sstore[j] = factor_node(F, j, A, AT, Sstore, fpos, fl, team.get());
         } catch (const std::exception& e) {
           std::lock_guard<std::mutex> g(mu);
           if (err.empty()) err = e.what();
@@ -490,7 +433,6 @@ void mf_factorize(MfFactor& F, const Csr& A, int n_threads) {
       std::lock_guard<std::mutex> g(mu);
       flops += fl;
     };
-    int nt = (int)std::min<size_t>(n_threads, lvl.size());
     if (nt <= 1) {
       worker();
     } else {

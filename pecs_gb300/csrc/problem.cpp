@@ -7,6 +7,7 @@
 #include <map>
 #include <numeric>
 #include <sstream>
+#include <thread>
 #include <stdexcept>
 #include <tuple>
 
@@ -316,15 +317,27 @@ std::string validate_params(const pecs_params* p, int n_inst) {
   return e.str();
 }
 
+// Carrier system matrices straight into CSR.  Row (K, i) couples to the dofs
+// of K and of its face neighbours; a row's columns are sorted by dof index
+// (component, then cell, then node) and exact zeros are not stored.  Each
+// entry of the diagonal block sums its terms in the order: cell matrix, face
+// below (K is its plus side), face on the left (plus side), face on the right
+// (minus side), face above (minus side) -- the order of the reference's
+// cell loop followed by its face loop over cells in index order.
 static void assemble_carrier(CarrierSystem& S, const CarrierTables& ct, const pecs_params& P,
                              double mu1, double mu2) {
   const Grid& g = S.grid;
-  const int n1 = ct.n1, nd = 3 * n1, nc = g.nc();
+  const int n1 = ct.n1, nd = 3 * n1, nc = g.nc(), nx = g.nx, ny = g.ny;
   S.ndofs = 3 * nc * n1;
   auto dof = [&](int K, int i) { return (i / n1) * nc * n1 + K * n1 + (i % n1); };
-  std::vector<int> r[2], c[2], mr, mc;
-  std::vector<double> v[2], mv;
+  // cell matrices (assemble_local_LDG_cell_and_bc_terms, source/LDG.cpp:85-281),
+  // shared between cells of equal size and boundary ids
   std::map<std::tuple<double, double, int, int, int, int>, std::vector<double>> cache[2];
+  std::vector<const std::vector<double>*> cellA[2];
+  cellA[0].resize(nc);
+  cellA[1].resize(nc);
+  std::vector<int> mr, mc;
+  std::vector<double> mv;
   for (int K = 0; K < nc; ++K) {
     double x0, y0, hx, hy;
     g.geom(K, x0, y0, hx, hy);
@@ -338,13 +351,7 @@ static void assemble_carrier(CarrierSystem& S, const CarrierTables& ct, const pe
         it = cache[s].emplace(key, ldg_cell_matrix(ct, hx, hy, s == 0 ? mu1 : mu2, P.dt, 1.0,
                                                    P.penalty / diam, bids))
                  .first;
-      const std::vector<double>& A = it->second;
-      for (int i = 0; i < nd; ++i)
-        for (int j = 0; j < nd; ++j) {
-          r[s].push_back(dof(K, i));
-          c[s].push_back(dof(K, j));
-          v[s].push_back(A[i * nd + j]);
-        }
+      cellA[s][K] = &it->second;
     }
     // (1/dt) mass, source/LDG.cpp:40-83
     for (int a = 0; a < n1; ++a)
@@ -357,24 +364,17 @@ static void assemble_carrier(CarrierSystem& S, const CarrierTables& ct, const pe
         mv.push_back(s);
       }
   }
-  // interior faces (assemble_flux_terms, source/LDG.cpp:283-426)
+  // interior-face blocks (assemble_flux_terms, source/LDG.cpp:283-426): for the
+  // face of K in direction dir (0: right, 1: top), blocks (K,K), (K,nb), (nb,K),
+  // (nb,nb); equal for both carriers
   std::map<std::tuple<int, double, double>, std::vector<std::vector<double>>> fcache;
+  std::vector<const std::vector<std::vector<double>>*> faceB(2 * (size_t)nc, nullptr);
   for (int K = 0; K < nc; ++K) {
-    int i = K % g.nx, j = K / g.nx;
+    const int i = K % nx, j = K / nx;
     for (int dir = 0; dir < 2; ++dir) {
-      int nb;
-      int fm, fp;
-      if (dir == 0) {
-        if (i >= g.nx - 1) continue;
-        nb = K + 1;
-        fm = kRight;
-        fp = kLeft;
-      } else {
-        if (j >= g.ny - 1) continue;
-        nb = K + g.nx;
-        fm = kTop;
-        fp = kBottom;
-      }
+      if (dir == 0 ? i >= nx - 1 : j >= ny - 1) continue;
+      const int nb = dir == 0 ? K + 1 : K + nx;
+      const int fm = dir == 0 ? kRight : kTop, fp = dir == 0 ? kLeft : kBottom;
       double x0, y0, hx, hy, x1, y1, hx1, hy1;
       g.geom(K, x0, y0, hx, hy);
       g.geom(nb, x1, y1, hx1, hy1);
@@ -387,20 +387,111 @@ static void assemble_carrier(CarrierSystem& S, const CarrierTables& ct, const pe
         ldg_flux_blocks(ct, fm, fp, flen, P.penalty / h, blk);
         it = fcache.emplace(key, std::vector<std::vector<double>>(blk, blk + 4)).first;
       }
-      const int cells[4][2] = {{K, K}, {K, nb}, {nb, K}, {nb, nb}};
-      for (int t = 0; t < 4; ++t) {
-        const std::vector<double>& B = it->second[t];
-        for (int a = 0; a < nd; ++a)
-          for (int b = 0; b < nd; ++b)
-            for (int s = 0; s < 2; ++s) {
-              r[s].push_back(dof(cells[t][0], a));
-              c[s].push_back(dof(cells[t][1], b));
-              v[s].push_back(B[a * nd + b]);
-            }
-      }
+      faceB[2 * (size_t)K + dir] = &it->second;
     }
   }
-  for (int s = 0; s < 2; ++s) S.A[s] = coo_to_csr(S.ndofs, r[s], c[s], v[s]);
+  // rows, cell range by cell range; per thread one buffer per (carrier, component)
+  struct Part {
+    std::vector<int> len[2][3], col[2][3];
+    std::vector<double> val[2][3];
+  };
+  unsigned hc = std::thread::hardware_concurrency();
+  const int nt = (int)std::max(1u, std::min({hc, 16u, (unsigned)std::max(1, nc / 64)}));
+  std::vector<Part> parts(nt);
+  auto work = [&](int t) {
+    const int K0 = (int)((long long)nc * t / nt), K1 = (int)((long long)nc * (t + 1) / nt);
+    Part& pt = parts[t];
+    std::vector<double> blk[5];
+    for (auto& b : blk) b.resize((size_t)nd * nd);
+    for (int K = K0; K < K1; ++K) {
+      const int i = K % nx, j = K / nx;
+      int cells[5], nb = 0;
+      if (j > 0) cells[nb++] = K - nx;
+      if (i > 0) cells[nb++] = K - 1;
+      cells[nb++] = K;
+      if (i < nx - 1) cells[nb++] = K + 1;
+      if (j < ny - 1) cells[nb++] = K + nx;
+      for (int s = 0; s < 2; ++s) {
+        for (int c = 0; c < nb; ++c) {
+          const int C = cells[c];
+          double* B = blk[c].data();
+          if (C == K) {
+            const std::vector<double>& A = *cellA[s][K];
+            for (int e = 0; e < nd * nd; ++e) B[e] = 0.0 + A[e];
+            if (j > 0) {
+              const std::vector<double>& F = (*faceB[2 * (size_t)(K - nx) + 1])[3];
+              for (int e = 0; e < nd * nd; ++e) B[e] += F[e];
+            }
+            if (i > 0) {
+              const std::vector<double>& F = (*faceB[2 * (size_t)(K - 1) + 0])[3];
+              for (int e = 0; e < nd * nd; ++e) B[e] += F[e];
+            }
+            if (i < nx - 1) {
+              const std::vector<double>& F = (*faceB[2 * (size_t)K + 0])[0];
+              for (int e = 0; e < nd * nd; ++e) B[e] += F[e];
+            }
+            if (j < ny - 1) {
+              const std::vector<double>& F = (*faceB[2 * (size_t)K + 1])[0];
+              for (int e = 0; e < nd * nd; ++e) B[e] += F[e];
+            }
+          } else {
+            const std::vector<double>* F;
+            if (C == K + 1) F = &(*faceB[2 * (size_t)K + 0])[1];
+            else if (C == K + nx) F = &(*faceB[2 * (size_t)K + 1])[1];
+            else if (C == K - 1) F = &(*faceB[2 * (size_t)(K - 1) + 0])[2];
+            else F = &(*faceB[2 * (size_t)(K - nx) + 1])[2];
+            for (int e = 0; e < nd * nd; ++e) B[e] = 0.0 + (*F)[e];
+          }
+        }
+        for (int r = 0; r < nd; ++r) {
+          const int rc = r / n1;
+          int cnt = 0;
+          for (int comp = 0; comp < 3; ++comp)
+            for (int c = 0; c < nb; ++c) {
+              const double* B = blk[c].data() + (size_t)r * nd + comp * n1;
+              const int base = comp * nc * n1 + cells[c] * n1;
+              for (int a = 0; a < n1; ++a) {
+                if (B[a] == 0.0) continue;  // structural zeros of the flux pattern are not stored
+                pt.col[s][rc].push_back(base + a);
+                pt.val[s][rc].push_back(B[a]);
+                ++cnt;
+              }
+            }
+          pt.len[s][rc].push_back(cnt);
+        }
+      }
+    }
+  };
+  {
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+  }
+  for (int s = 0; s < 2; ++s) {
+    Csr& A = S.A[s];
+    A.n = S.ndofs;
+    A.rowptr.assign(S.ndofs + 1, 0);
+    size_t nnz = 0;
+    for (auto& pt : parts)
+      for (int rc = 0; rc < 3; ++rc) nnz += pt.col[s][rc].size();
+    A.col.reserve(nnz);
+    A.val.reserve(nnz);
+    // rows of component rc, cell K, node a sit at rc*nc*n1 + K*n1 + a; within a
+    // part they were produced cell by cell, node by node (r = rc*n1 + a)
+    int row = 0;
+    for (int rc = 0; rc < 3; ++rc)
+      for (auto& pt : parts) {
+        A.col.insert(A.col.end(), pt.col[s][rc].begin(), pt.col[s][rc].end());
+        A.val.insert(A.val.end(), pt.val[s][rc].begin(), pt.val[s][rc].end());
+        for (int l : pt.len[s][rc]) {
+          A.rowptr[row + 1] = A.rowptr[row] + l;
+          ++row;
+        }
+        std::vector<int>().swap(pt.col[s][rc]);
+        std::vector<double>().swap(pt.val[s][rc]);
+      }
+  }
   S.M = coo_to_csr(S.ndofs, mr, mc, mv);
   S.dof_cell.resize(S.ndofs);
   S.dof_class.resize(S.ndofs);

@@ -34,7 +34,9 @@ def _maps_poisson(pb):
 
 
 @pytest.mark.parametrize("P", [oracle.half_cell_params(n_refine=3), oracle.pn_junction_params(),
-                               oracle.reference_params(2, 2)])
+                               oracle.reference_params(2, 2),
+                               # fronts of a few hundred dofs: blocked LU, recursive inverses
+                               oracle.half_cell_params(n_refine=4, degree=2)])
 def test_host_factorisation_matches_scipy(pecs_lib, P):
     pb = oracle.Problem(P)
     rng = np.random.default_rng(0)
