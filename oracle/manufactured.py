@@ -16,6 +16,11 @@ TEST INFRASTRUCTURE ONLY.
 
 The reference only prints its convergence tables; the rates asserted in
 ``tests/`` are the theoretical ones for these elements.
+
+Both studies solve with scipy's sparse LU unless ``solver`` is given: a
+factory ``solver(A, space, kind)`` (kind "poisson" or "carrier") returning a
+function b -> x, through which the tests run the same studies on the
+library's multifrontal solver.
 """
 from __future__ import annotations
 
@@ -48,7 +53,12 @@ def _fine_rule(nq=8):
     return np.tile(g, nq), np.repeat(g, nq), np.tile(w, nq) * np.repeat(w, nq)
 
 
-def poisson_mixed_errors(n_refine: int, k: int = 1):
+def _scipy_solver(A, space, kind):
+    lu = spla.splu(A.tocsc())
+    return lu.solve
+
+
+def poisson_mixed_errors(n_refine: int, k: int = 1, solver=None):
     """Returns (h, ||Phi-Phi_h||_L2, ||D-D_h||_L2)."""
     n = 2 ** n_refine
     grid = uniform_grid(0.0, 1.0, 0.0, 1.0, n, n, (DIRICHLET, DIRICHLET, NEUMANN, NEUMANN))
@@ -71,7 +81,7 @@ def poisson_mixed_errors(n_refine: int, k: int = 1):
             gD = np.cos(TWO_PI * fy) - np.sin(TWO_PI * fx) - fx
             np.add.at(b, ps.l2g[K, :pe.n_rt], -(pe.fpsi_n[fc] @ (gD * Jf)))
     b[ps.constrained] = 0.0
-    sol = spla.spsolve(A.tocsc(), b)
+    sol = (solver or _scipy_solver)(A, ps, "poisson")(b)
     sol[ps.constrained] = 0.0
     # errors on a fine Gauss rule
     qx, qy, qw = _fine_rule()
@@ -92,7 +102,7 @@ def poisson_mixed_errors(n_refine: int, k: int = 1):
     return math.sqrt(2.0) / n, e_phi, e_D
 
 
-def ldg_imex_errors(n_refine: int, k: int = 1, t_end: float = 1.0):
+def ldg_imex_errors(n_refine: int, k: int = 1, t_end: float = 1.0, solver=None):
     """Returns (h, ||u-u_h||_L2, ||J-J_h||_L2, n_steps) at the final time."""
     n = 2 ** n_refine
     grid = uniform_grid(0.0, 1.0, 0.0, 1.0, n, n, (DIRICHLET, INTERFACE, NEUMANN, NEUMANN))
@@ -102,7 +112,7 @@ def ldg_imex_errors(n_refine: int, k: int = 1, t_end: float = 1.0):
     dt = h ** (k + 1)
     penalty = 1.0
     A, M = assemble_ldg_matrices(cs, 1.0, dt, penalty, tos=1.0)
-    lu = spla.splu(A.tocsc())
+    solve = (solver or _scipy_solver)(A, cs, "carrier")
     x0, y0, hx, hy = grid.cell_geom()
     diam = np.sqrt(hx ** 2 + hy ** 2)
     X = x0[:, None] + hx[:, None] * ce.qx
@@ -148,7 +158,7 @@ def ldg_imex_errors(n_refine: int, k: int = 1, t_end: float = 1.0):
             else:
                 I = -math.exp(-time) - np.cos(TWO_PI * fy) - 1.0
                 b[cs.dofs(K)] += -(fv @ (I * Jf))
-        u = lu.solve(b)
+        u = solve(b)
         time += dt
         steps += 1
     qx, qy, qw = _fine_rule()
