@@ -95,6 +95,10 @@ typedef struct pecs_params {
   double tau_n, tau_p, n_i;
   double phi_bi, phi_app; /* potential data phi_bi - phi_app where x == 0 */
   double s_n, s_p;        /* Schottky recombination velocities */
+  double grading; /* widest / narrowest cell width of each region along x, cells narrowing
+                     geometrically toward the interface x = x_semi1 (a boundary layer on a
+                     tensor-product mesh in place of the reference's local refinement with
+                     hanging nodes, Grid.cpp:71-111); 0 or 1: uniform */
 } pecs_params;
 
 typedef struct pecs_options {

@@ -32,7 +32,7 @@ import scipy.sparse.linalg as spla
 from .pecs_oracle import (BOTTOM, DIRICHLET, FACE_NORMALS, INTERFACE, LEFT, NEUMANN, RIGHT, TOP,
                           _carrier_face_tables, assemble_ldg_matrices, assemble_poisson_matrix,
                           dgq_nodes, gauss01, lagrange1d, make_carrier_space, make_poisson_space,
-                          uniform_grid, CarrierElement, PoissonElement)
+                          region_grid, CarrierElement, PoissonElement)
 
 TWO_PI = 2.0 * math.pi
 
@@ -58,10 +58,12 @@ def _scipy_solver(A, space, kind):
     return lu.solve
 
 
-def poisson_mixed_errors(n_refine: int, k: int = 1, solver=None):
-    """Returns (h, ||Phi-Phi_h||_L2, ||D-D_h||_L2)."""
+def poisson_mixed_errors(n_refine: int, k: int = 1, solver=None, grading: float = 1.0):
+    """Returns (h, ||Phi-Phi_h||_L2, ||D-D_h||_L2).  grading > 1: cells graded
+    along x toward x = 1 (widest/narrowest = grading)."""
     n = 2 ** n_refine
-    grid = uniform_grid(0.0, 1.0, 0.0, 1.0, n, n, (DIRICHLET, DIRICHLET, NEUMANN, NEUMANN))
+    grid = region_grid(0.0, 1.0, 0.0, 1.0, n, n, (DIRICHLET, DIRICHLET, NEUMANN, NEUMANN), grading,
+                       True)
     ce = CarrierElement.make(k)
     ps = make_poisson_space(grid, k, ce)
     pe = ps.pe
@@ -102,10 +104,13 @@ def poisson_mixed_errors(n_refine: int, k: int = 1, solver=None):
     return math.sqrt(2.0) / n, e_phi, e_D
 
 
-def ldg_imex_errors(n_refine: int, k: int = 1, t_end: float = 1.0, solver=None):
-    """Returns (h, ||u-u_h||_L2, ||J-J_h||_L2, n_steps) at the final time."""
+def ldg_imex_errors(n_refine: int, k: int = 1, t_end: float = 1.0, solver=None,
+                    grading: float = 1.0):
+    """Returns (h, ||u-u_h||_L2, ||J-J_h||_L2, n_steps) at the final time.
+    grading > 1: cells graded along x toward x = 1."""
     n = 2 ** n_refine
-    grid = uniform_grid(0.0, 1.0, 0.0, 1.0, n, n, (DIRICHLET, INTERFACE, NEUMANN, NEUMANN))
+    grid = region_grid(0.0, 1.0, 0.0, 1.0, n, n, (DIRICHLET, INTERFACE, NEUMANN, NEUMANN), grading,
+                       True)
     cs = make_carrier_space(grid, k)
     ce = cs.ce
     h = math.sqrt(2.0) / n

@@ -285,6 +285,32 @@ def uniform_grid(x0, x1, y0, y1, nx, ny, bc, material=0) -> RectGrid:
     return g
 
 
+def graded_coords(x0: float, x1: float, n: int, grading: float, fine_at_x1: bool) -> np.ndarray:
+    """n + 1 points on [x0, x1] whose cell widths shrink by the constant factor
+    q = grading^(1/(n-1)) toward x1 (fine_at_x1) or toward x0: widest/narrowest
+    = grading.  grading <= 1 gives numpy.linspace's points."""
+    if not grading > 1.0:
+        return np.linspace(x0, x1, n + 1)
+    q = grading ** (1.0 / (n - 1))
+    w = np.empty(n)
+    w[0] = 1.0
+    for i in range(1, n):
+        w[i] = w[i - 1] / q
+    if not fine_at_x1:
+        w = w[::-1].copy()
+    S = np.concatenate([[0.0], np.cumsum(w)])
+    xs = x0 + (x1 - x0) * (S / S[n])
+    xs[n] = x1
+    return xs
+
+
+def region_grid(x0, x1, y0, y1, nx, ny, bc, grading, fine_at_x1, material=0) -> RectGrid:
+    g = RectGrid(graded_coords(x0, x1, nx, grading, fine_at_x1), np.linspace(y0, y1, ny + 1),
+                 tuple(bc))
+    g.material = np.full(g.nc, material, dtype=np.int64)
+    return g
+
+
 # ---------------------------------------------------------------------------
 # Parameters (already-scaled, restates the role of ParameterSpace::Parameters,
 # include/Parameters.hpp:27-289; the benchmark configurations override the
@@ -334,6 +360,11 @@ class Params:
     phi_app: float = 0.0
     s_n: float = 0.0             # Schottky recombination velocities (SolarCell.cpp:1386-1401)
     s_p: float = 0.0
+    # widest / narrowest cell width of each region along x, cells narrowing
+    # geometrically toward the interface x = x_semi1 (<= 1: uniform).  A
+    # boundary layer on a tensor-product mesh, in place of the reference's
+    # local refinement with hanging nodes (Grid.cpp:71-111).
+    grading: float = 1.0
 
     def copy(self, **kw) -> "Params":
         return dataclasses.replace(self, **kw)
@@ -719,14 +750,14 @@ class Problem:
     def __init__(self, P: Params):
         self.P = P
         k = P.degree
-        self.semi_grid = uniform_grid(P.x_semi0, P.x_semi1, 0.0, P.height, P.nx_semi, P.ny,
-                                      P.bc_semi, material=0)
+        self.semi_grid = region_grid(P.x_semi0, P.x_semi1, 0.0, P.height, P.nx_semi, P.ny,
+                                     P.bc_semi, P.grading, True, material=0)
         self.semi = make_carrier_space(self.semi_grid, k)
         ce = self.semi.ce
         self.ce = ce
         if P.full_system:
-            self.elec_grid = uniform_grid(P.x_semi1, P.x_elec1, 0.0, P.height, P.nx_elec, P.ny,
-                                          P.bc_elec, material=2)
+            self.elec_grid = region_grid(P.x_semi1, P.x_elec1, 0.0, P.height, P.nx_elec, P.ny,
+                                         P.bc_elec, P.grading, False, material=2)
             self.elec = make_carrier_space(self.elec_grid, k)
             xs = np.concatenate([self.semi_grid.xs, self.elec_grid.xs[1:]])
             pg = RectGrid(xs, self.semi_grid.ys.copy(), tuple(P.bc_poisson))

@@ -62,6 +62,7 @@ class Params:
     phi_app: float = 0.0
     s_n: float = 0.0
     s_p: float = 0.0
+    grading: float = 1.0  # widest/narrowest cell along x, finest at the interface (1: uniform)
 
     def copy(self, **kw) -> "Params":
         return dataclasses.replace(self, **kw)

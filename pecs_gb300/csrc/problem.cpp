@@ -67,19 +67,38 @@ void Grid::geom(int K, double& x0, double& y0, double& hx, double& hy) const {
   hy = ys[j + 1] - ys[j];
 }
 
-static Grid uniform(double x0, double x1, double y0, double y1, int nx, int ny, const int* bc,
-                    int material) {
+// Cell boundaries along one axis.  grading <= 1: uniform, with the arithmetic
+// of numpy.linspace (x0 + i*step, last point exact).  grading > 1: widths
+// shrinking by q = grading^(1/(n-1)) per cell toward x1 (fine_at_x1) or toward
+// x0, so widest / narrowest = grading; normalised prefix sums of the widths.
+static std::vector<double> axis_coords(double x0, double x1, int n, double grading,
+                                       bool fine_at_x1) {
+  std::vector<double> xs(n + 1);
+  if (!(grading > 1.0)) {
+    const double sx = (x1 - x0) / n;
+    for (int i = 0; i <= n; ++i) xs[i] = x0 + i * sx;
+  } else {
+    const double q = std::pow(grading, 1.0 / (n - 1));
+    std::vector<double> w(n);
+    w[0] = 1.0;
+    for (int i = 1; i < n; ++i) w[i] = w[i - 1] / q;
+    if (!fine_at_x1) std::reverse(w.begin(), w.end());
+    std::vector<double> S(n + 1, 0.0);
+    for (int i = 0; i < n; ++i) S[i + 1] = S[i] + w[i];
+    for (int i = 0; i <= n; ++i) xs[i] = x0 + (x1 - x0) * (S[i] / S[n]);
+  }
+  xs[n] = x1;
+  return xs;
+}
+
+// One carrier region: graded along x toward the interface, uniform along y.
+static Grid region(double x0, double x1, double y0, double y1, int nx, int ny, const int* bc,
+                   int material, double grading, bool fine_at_x1) {
   Grid g;
   g.nx = nx;
   g.ny = ny;
-  g.xs.resize(nx + 1);
-  g.ys.resize(ny + 1);
-  // same arithmetic as numpy.linspace: x0 + i*step, last point exact
-  double sx = (x1 - x0) / nx, sy = (y1 - y0) / ny;
-  for (int i = 0; i <= nx; ++i) g.xs[i] = x0 + i * sx;
-  for (int j = 0; j <= ny; ++j) g.ys[j] = y0 + j * sy;
-  g.xs[nx] = x1;
-  g.ys[ny] = y1;
+  g.xs = axis_coords(x0, x1, nx, grading, fine_at_x1);
+  g.ys = axis_coords(y0, y1, ny, 1.0, false);
   for (int f = 0; f < 4; ++f) g.bc[f] = bc[f];
   g.material.assign(g.nc(), material);
   return g;
@@ -284,6 +303,7 @@ std::string validate_params(const pecs_params* p, int n_inst) {
     if (!(a.mu[c] > 0)) e << "mobilities must be > 0; ";
   if (!(a.x_semi1 > a.x_semi0) || !(a.height > 0) || (a.full_system && !(a.x_elec1 > a.x_semi1)))
     e << "bad geometry; ";
+  if (!(a.grading >= 0.0 && a.grading <= 1e4)) e << "grading must be in [0, 1e4]; ";
   for (int f = 0; f < 4; ++f) {
     if (a.bc_semi[f] < 0 || a.bc_semi[f] > 3 || a.bc_elec[f] < 0 || a.bc_elec[f] > 3 ||
         a.bc_poisson[f] < 0 || a.bc_poisson[f] > 3)
@@ -304,6 +324,7 @@ std::string validate_params(const pecs_params* p, int n_inst) {
     chk(a.eps_semi == b.eps_semi && a.eps_elec == b.eps_elec, "permittivities");
     chk(a.dt == b.dt, "dt");
     chk(a.penalty == b.penalty, "penalty");
+    chk(a.grading == b.grading || (!(a.grading > 1.0) && !(b.grading > 1.0)), "grading");
     chk(std::memcmp(a.mu, b.mu, sizeof(a.mu)) == 0, "mobilities");
     chk(std::memcmp(a.bc_semi, b.bc_semi, sizeof(a.bc_semi)) == 0 &&
             std::memcmp(a.bc_elec, b.bc_elec, sizeof(a.bc_elec)) == 0 &&
@@ -620,8 +641,11 @@ Setup::Setup(const std::vector<pecs_params>& p)
   Q = ct.Q;
   nq1 = ct.nq1;
   full = P.full_system != 0;
-  semi.grid = uniform(P.x_semi0, P.x_semi1, 0.0, P.height, P.nx_semi, P.ny, P.bc_semi, 0);
-  if (full) elec.grid = uniform(P.x_semi1, P.x_elec1, 0.0, P.height, P.nx_elec, P.ny, P.bc_elec, 2);
+  semi.grid = region(P.x_semi0, P.x_semi1, 0.0, P.height, P.nx_semi, P.ny, P.bc_semi, 0, P.grading,
+                     true);
+  if (full)
+    elec.grid = region(P.x_semi1, P.x_elec1, 0.0, P.height, P.nx_elec, P.ny, P.bc_elec, 2, P.grading,
+                       false);
   // Poisson mesh: merged triangulation (Grid.cpp:320-336)
   Grid& pg = pois.grid;
   pg.nx = P.nx_semi + (full ? P.nx_elec : 0);

@@ -48,8 +48,10 @@ def test_lu_device_solve_matches_scipy(pecs_lib):
 
 @pytest.mark.parametrize("P", [oracle.half_cell_params(n_refine=3), oracle.pn_junction_params(),
                                oracle.reference_params(3, 1, dt=1e-4),
-                               oracle.half_cell_params(n_refine=2, degree=2)],
-                         ids=["halfcell_r3", "pn_junction", "reference_r3", "halfcell_r2_k2"])
+                               oracle.half_cell_params(n_refine=2, degree=2),
+                               oracle.half_cell_params(n_refine=3, ny=4, grading=8.0)],
+                         ids=["halfcell_r3", "pn_junction", "reference_r3", "halfcell_r2_k2",
+                              "halfcell_graded"])
 def test_initial_state_and_rhs(pecs_lib, P):
     pb = oracle.Problem(P)
     st = pb.initial_state()
@@ -66,8 +68,12 @@ def test_initial_state_and_rhs(pecs_lib, P):
                                      (oracle.pn_junction_params(), 100),
                                      (oracle.reference_params(3, 1, dt=1e-4), 10),
                                      (oracle.half_cell_params(n_refine=2, degree=2), 10),
-                                     (oracle.half_cell_params(n_refine=3, mu=(1.0, 0.5, 2.0, 1.0)), 10)],
-                         ids=["halfcell_r3", "pn_junction_100", "reference_r3", "halfcell_r2_k2", "mu_distinct"])
+                                     (oracle.half_cell_params(n_refine=3, mu=(1.0, 0.5, 2.0, 1.0)), 10),
+                                     # graded toward the interface, non-square cells
+                                     (oracle.half_cell_params(n_refine=3, ny=4, grading=8.0), 20),
+                                     (oracle.half_cell_params(n_refine=2, degree=2, ny=8, grading=4.0), 10)],
+                         ids=["halfcell_r3", "pn_junction_100", "reference_r3", "halfcell_r2_k2", "mu_distinct",
+                              "halfcell_graded", "halfcell_k2_graded"])
 def test_trajectory_matches_oracle(pecs_lib, P, steps):
     pb = oracle.Problem(P)
     st, _, _ = pb.run(steps)

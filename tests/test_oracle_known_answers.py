@@ -28,3 +28,19 @@ def test_ldg_imex_convergence():
     assert r_u[-1] == pytest.approx(2.0, abs=0.15)   # u: O(h^{k+1})
     assert r_j[-1] == pytest.approx(1.0, abs=0.15)   # J: O(h^k)
     assert E[-1][1] < 1.2e-2
+
+
+@pytest.mark.parametrize("k,levels,phi_rate,d_rate", [(1, range(3, 6), 1.0, 2.0),
+                                                      (2, range(2, 5), 2.0, 3.0)])
+def test_mixed_poisson_convergence_graded(k, levels, phi_rate, d_rate):
+    """Cells graded 4:1 along x (non-square, non-uniform): the element rates
+    still hold, which pins the oracle's per-cell geometry."""
+    E = [poisson_mixed_errors(n, k, grading=4.0) for n in levels]
+    assert rates([e[1] for e in E])[-1] == pytest.approx(phi_rate, abs=0.15)
+    assert rates([e[2] for e in E])[-1] == pytest.approx(d_rate, abs=0.2)
+
+
+def test_ldg_imex_convergence_graded():
+    E = [ldg_imex_errors(n, 1, grading=4.0) for n in range(2, 5)]
+    assert rates([e[1] for e in E])[-1] == pytest.approx(2.0, abs=0.2)
+    assert rates([e[2] for e in E])[-1] == pytest.approx(1.0, abs=0.2)

@@ -14,6 +14,11 @@ CASES = [
     ("reference_r3_k1", oracle.reference_params(3, 1)),
     ("reference_r2_k2", oracle.reference_params(2, 2)),
     ("halfcell_r2_k2_mu", oracle.half_cell_params(n_refine=2, degree=2, mu=(1.0, 0.5, 2.0, 1.0))),
+    # non-square cells, graded meshes (finest at the interface)
+    ("halfcell_8x16", oracle.half_cell_params(n_refine=3, ny=16)),
+    ("halfcell_r3_graded", oracle.half_cell_params(n_refine=3, grading=8.0)),
+    ("halfcell_r2_k2_graded", oracle.half_cell_params(n_refine=2, degree=2, ny=8, grading=4.0)),
+    ("pn_junction_graded", oracle.pn_junction_params(grading=5.0)),
 ]
 
 
@@ -57,3 +62,9 @@ def test_invalid_params_are_rejected(pecs_lib):
     b = pg.half_cell(n_refine=3)
     with pytest.raises(pg.PecsError):
         pg.Context([a, b], host_setup_only=True)
+    with pytest.raises(pg.PecsError, match="grading"):
+        pg.Context([a, a.copy(grading=4.0)], host_setup_only=True)
+    with pytest.raises(pg.PecsError, match="grading"):
+        pg.Context(a.copy(grading=-2.0), host_setup_only=True)
+    # 0 and 1 both mean uniform
+    pg.Context([a.copy(grading=0.0), a.copy(grading=1.0)], host_setup_only=True)
