@@ -99,6 +99,10 @@ typedef struct pecs_params {
                      geometrically toward the interface x = x_semi1 (a boundary layer on a
                      tensor-product mesh in place of the reference's local refinement with
                      hanging nodes, Grid.cpp:71-111); 0 or 1: uniform */
+  int bc_poisson_elec[4]; /* full system: ids of the Poisson mesh's outer faces over the
+                             electrolyte (left unused, right, bottom, top), for layouts whose
+                             sides change id at the interface (Grid.cpp:377-431); entries <= 0
+                             take bc_poisson's id */
 } pecs_params;
 
 typedef struct pecs_options {

@@ -240,6 +240,11 @@ class RectGrid:
     ys: np.ndarray   # (ny+1,) row edges
     bc: tuple        # boundary id of (left, right, bottom, top) sides
     material: np.ndarray = None  # (nc,) 0 semiconductor, 2 electrolyte (include/Grid.hpp:150-156)
+    # cells with i >= split take bc2's id (where > 0) on their outer faces: the
+    # Poisson mesh over the electrolyte, whose sides may change id at the
+    # interface (Grid.cpp:377-431); split < 0: one id per side
+    split: int = -1
+    bc2: tuple = (0, 0, 0, 0)
 
     @property
     def nx(self):
@@ -268,15 +273,13 @@ class RectGrid:
     def face_bid(self, K: int, f: int) -> Optional[int]:
         """Boundary id of face f of cell K, None for an interior face."""
         i, j = K % self.nx, K // self.nx
-        if f == LEFT and i == 0:
-            return self.bc[0]
-        if f == RIGHT and i == self.nx - 1:
-            return self.bc[1]
-        if f == BOTTOM and j == 0:
-            return self.bc[2]
-        if f == TOP and j == self.ny - 1:
-            return self.bc[3]
-        return None
+        outer = ((f == LEFT and i == 0) or (f == RIGHT and i == self.nx - 1)
+                 or (f == BOTTOM and j == 0) or (f == TOP and j == self.ny - 1))
+        if not outer:
+            return None
+        if self.split >= 0 and i >= self.split and self.bc2[f] > 0:
+            return self.bc2[f]
+        return self.bc[f]
 
 
 def uniform_grid(x0, x1, y0, y1, nx, ny, bc, material=0) -> RectGrid:
@@ -365,6 +368,9 @@ class Params:
     # boundary layer on a tensor-product mesh, in place of the reference's
     # local refinement with hanging nodes (Grid.cpp:71-111).
     grading: float = 1.0
+    # full system: ids of the Poisson mesh's outer faces over the electrolyte
+    # (left unused, right, bottom, top); entries <= 0 take bc_poisson's id
+    bc_poisson_elec: tuple = (0, 0, 0, 0)
 
     def copy(self, **kw) -> "Params":
         return dataclasses.replace(self, **kw)
@@ -760,7 +766,8 @@ class Problem:
                                          P.bc_elec, P.grading, False, material=2)
             self.elec = make_carrier_space(self.elec_grid, k)
             xs = np.concatenate([self.semi_grid.xs, self.elec_grid.xs[1:]])
-            pg = RectGrid(xs, self.semi_grid.ys.copy(), tuple(P.bc_poisson))
+            pg = RectGrid(xs, self.semi_grid.ys.copy(), tuple(P.bc_poisson), split=P.nx_semi,
+                          bc2=tuple(P.bc_poisson_elec))
             ci, cj = pg.cell_ij()
             pg.material = np.where(ci < P.nx_semi, 0, 2)
         else:

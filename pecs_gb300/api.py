@@ -63,6 +63,7 @@ class Params:
     s_n: float = 0.0
     s_p: float = 0.0
     grading: float = 1.0  # widest/narrowest cell along x, finest at the interface (1: uniform)
+    bc_poisson_elec: tuple = (0, 0, 0, 0)  # Poisson outer-face ids over the electrolyte (<= 0: bc_poisson)
 
     def copy(self, **kw) -> "Params":
         return dataclasses.replace(self, **kw)
@@ -105,6 +106,37 @@ def half_cell(n_refine: int = 6, **kw) -> Params:
                gen_kind=2, G0=1.0, alpha=5.0, srh=True, tau_n=1.0, tau_p=1.0, n_i=n_i,
                k_et=1e-2, k_ht=1e-2, phi_bi=0.0, phi_app=0.0)
     return p.copy(**kw)
+
+
+def boundary_layout(p: Params, insulated: bool = False, schottky: bool = False) -> Params:
+    """The reference's boundary layouts (Grid::make_grids, source/Grid.cpp:112-131)
+    on a copy of p.  Every outer side is Dirichlet, the semiconductor-electrolyte
+    interface keeps the Interface id (make_Dirichlet_boundaries, Grid.cpp:343-373).
+    insulated (make_Neumann_boundaries, Grid.cpp:377-431): the left side is
+    Neumann, and the top and bottom are Neumann over the electrolyte and
+    Dirichlet over the semiconductor -- on the Poisson mesh too, whose top and
+    bottom then change id at the interface.  schottky
+    (make_Schottky_boundaries, Grid.cpp:434-461): the top side of the
+    semiconductor and of the whole Poisson mesh is Schottky; the electrolyte
+    mesh keeps its ids."""
+    D, N, I, S = DIRICHLET, NEUMANN, INTERFACE, SCHOTTKY
+    semi = [D, I if p.full_system else D, D, D]
+    elec = [I, D, D, D]
+    pois = [D, D, D, D]
+    pois_elec = [0, 0, 0, 0]
+    if insulated:
+        semi[0] = N
+        pois[0] = N
+        if p.full_system:
+            elec[2] = elec[3] = N
+            pois_elec[2] = pois_elec[3] = N
+    if schottky:
+        semi[3] = S
+        pois[3] = S
+        if p.full_system:
+            pois_elec[3] = S
+    return p.copy(bc_semi=tuple(semi), bc_elec=tuple(elec), bc_poisson=tuple(pois),
+                  bc_poisson_elec=tuple(pois_elec))
 
 
 def reference_params(n_refine: int = 4, degree: int = 1, **kw) -> Params:

@@ -52,11 +52,11 @@ Csr coo_to_csr(int n, const std::vector<int>& r, const std::vector<int>& c,
 
 int Grid::face_bid(int K, int f) const {
   int i = K % nx, j = K / nx;
-  if (f == kLeft && i == 0) return bc[0];
-  if (f == kRight && i == nx - 1) return bc[1];
-  if (f == kBottom && j == 0) return bc[2];
-  if (f == kTop && j == ny - 1) return bc[3];
-  return -1;
+  const bool outer = (f == kLeft && i == 0) || (f == kRight && i == nx - 1) ||
+                     (f == kBottom && j == 0) || (f == kTop && j == ny - 1);
+  if (!outer) return -1;
+  if (split >= 0 && i >= split && bc2[f] > 0) return bc2[f];
+  return bc[f];
 }
 
 void Grid::geom(int K, double& x0, double& y0, double& hx, double& hy) const {
@@ -306,7 +306,8 @@ std::string validate_params(const pecs_params* p, int n_inst) {
   if (!(a.grading >= 0.0 && a.grading <= 1e4)) e << "grading must be in [0, 1e4]; ";
   for (int f = 0; f < 4; ++f) {
     if (a.bc_semi[f] < 0 || a.bc_semi[f] > 3 || a.bc_elec[f] < 0 || a.bc_elec[f] > 3 ||
-        a.bc_poisson[f] < 0 || a.bc_poisson[f] > 3)
+        a.bc_poisson[f] < 0 || a.bc_poisson[f] > 3 || a.bc_poisson_elec[f] < -1 ||
+        a.bc_poisson_elec[f] > 3)
       e << "bad boundary id; ";
   }
   for (int i = 1; i < n_inst; ++i) {
@@ -328,7 +329,8 @@ std::string validate_params(const pecs_params* p, int n_inst) {
     chk(std::memcmp(a.mu, b.mu, sizeof(a.mu)) == 0, "mobilities");
     chk(std::memcmp(a.bc_semi, b.bc_semi, sizeof(a.bc_semi)) == 0 &&
             std::memcmp(a.bc_elec, b.bc_elec, sizeof(a.bc_elec)) == 0 &&
-            std::memcmp(a.bc_poisson, b.bc_poisson, sizeof(a.bc_poisson)) == 0,
+            std::memcmp(a.bc_poisson, b.bc_poisson, sizeof(a.bc_poisson)) == 0 &&
+            std::memcmp(a.bc_poisson_elec, b.bc_poisson_elec, sizeof(a.bc_poisson_elec)) == 0,
         "boundary ids");
     if (!diff.empty()) {
       e << "instance " << i << " differs from instance 0 in a matrix-defining field (" << diff << "); ";
@@ -654,6 +656,10 @@ Setup::Setup(const std::vector<pecs_params>& p)
   if (full) pg.xs.insert(pg.xs.end(), elec.grid.xs.begin() + 1, elec.grid.xs.end());
   pg.ys = semi.grid.ys;
   for (int f = 0; f < 4; ++f) pg.bc[f] = P.bc_poisson[f];
+  if (full) {
+    pg.split = P.nx_semi;
+    for (int f = 0; f < 4; ++f) pg.bc2[f] = P.bc_poisson_elec[f];
+  }
   pg.material.resize(pg.nc());
   for (int K = 0; K < pg.nc(); ++K) pg.material[K] = (K % pg.nx) < P.nx_semi ? 0 : 2;
 

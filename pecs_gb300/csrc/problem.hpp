@@ -29,6 +29,10 @@ struct Grid {
   int nx = 0, ny = 0;
   std::vector<double> xs, ys;
   int bc[4] = {0, 0, 0, 0};
+  // cells with i >= split take bc2's id (where > 0) on their outer faces: the
+  // Poisson mesh over the electrolyte; split < 0: one id per side
+  int split = -1;
+  int bc2[4] = {0, 0, 0, 0};
   std::vector<int> material;  // 0 semiconductor, 2 electrolyte
   int nc() const { return nx * ny; }
   int face_bid(int K, int f) const;  // -1 for interior faces

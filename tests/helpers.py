@@ -14,6 +14,12 @@ def to_lib(P: "oracle.Params") -> pg.Params:
     return pg.Params(**dataclasses.asdict(P))
 
 
+def with_layout(P: "oracle.Params", insulated: bool, schottky: bool) -> "oracle.Params":
+    """Oracle parameters carrying the library's boundary_layout of P."""
+    lib = pg.boundary_layout(to_lib(P), insulated=insulated, schottky=schottky)
+    return oracle.Params(**dataclasses.asdict(lib))
+
+
 def rel_err(a, b) -> float:
     a = np.asarray(a)
     b = np.asarray(b)

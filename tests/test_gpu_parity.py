@@ -7,7 +7,7 @@ import scipy.sparse.linalg as spla
 
 import oracle
 import pecs_gb300 as pg
-from helpers import FIELD_OF, max_rel, rel_err, to_lib
+from helpers import FIELD_OF, max_rel, rel_err, to_lib, with_layout
 from test_lu_host import _maps_carrier, _maps_poisson
 
 pytestmark = pytest.mark.gpu
@@ -15,6 +15,10 @@ pytestmark = pytest.mark.gpu
 STEP_TOL = 1e-10     # FP64 path vs FP64 oracle, relative L2 per field (spec bound)
 SOLVE_TOL = 1e-11    # one direct solve: multifrontal LU vs SuperLU, both O(cond * eps)
 RHS_TOL = 1e-13
+
+# the reference's insulated + Schottky layout (its input file's choice,
+# input_file.prm:107,119), Schottky recombination on the semiconductor's top
+INSULATED_SCHOTTKY = with_layout(oracle.half_cell_params(n_refine=3, s_n=0.5, s_p=0.25), True, True)
 
 
 def _ctx(P, **kw):
@@ -49,9 +53,10 @@ def test_lu_device_solve_matches_scipy(pecs_lib):
 @pytest.mark.parametrize("P", [oracle.half_cell_params(n_refine=3), oracle.pn_junction_params(),
                                oracle.reference_params(3, 1, dt=1e-4),
                                oracle.half_cell_params(n_refine=2, degree=2),
-                               oracle.half_cell_params(n_refine=3, ny=4, grading=8.0)],
+                               oracle.half_cell_params(n_refine=3, ny=4, grading=8.0),
+                               INSULATED_SCHOTTKY],
                          ids=["halfcell_r3", "pn_junction", "reference_r3", "halfcell_r2_k2",
-                              "halfcell_graded"])
+                              "halfcell_graded", "insulated_schottky"])
 def test_initial_state_and_rhs(pecs_lib, P):
     pb = oracle.Problem(P)
     st = pb.initial_state()
@@ -71,9 +76,10 @@ def test_initial_state_and_rhs(pecs_lib, P):
                                      (oracle.half_cell_params(n_refine=3, mu=(1.0, 0.5, 2.0, 1.0)), 10),
                                      # graded toward the interface, non-square cells
                                      (oracle.half_cell_params(n_refine=3, ny=4, grading=8.0), 20),
-                                     (oracle.half_cell_params(n_refine=2, degree=2, ny=8, grading=4.0), 10)],
+                                     (oracle.half_cell_params(n_refine=2, degree=2, ny=8, grading=4.0), 10),
+                                     (INSULATED_SCHOTTKY, 20)],
                          ids=["halfcell_r3", "pn_junction_100", "reference_r3", "halfcell_r2_k2", "mu_distinct",
-                              "halfcell_graded", "halfcell_k2_graded"])
+                              "halfcell_graded", "halfcell_k2_graded", "insulated_schottky"])
 def test_trajectory_matches_oracle(pecs_lib, P, steps):
     pb = oracle.Problem(P)
     st, _, _ = pb.run(steps)

@@ -6,7 +6,7 @@ import pytest
 
 import oracle
 import pecs_gb300 as pg
-from helpers import to_lib
+from helpers import to_lib, with_layout
 
 CASES = [
     ("pn_junction", oracle.pn_junction_params()),
@@ -68,3 +68,61 @@ def test_invalid_params_are_rejected(pecs_lib):
         pg.Context(a.copy(grading=-2.0), host_setup_only=True)
     # 0 and 1 both mean uniform
     pg.Context([a.copy(grading=0.0), a.copy(grading=1.0)], host_setup_only=True)
+
+
+def _reference_id(mesh, x, y, P, insulated, schottky):
+    """The id the reference's Grid::make_grids gives the outer face with centre
+    (x, y) of a mesh ("semi", "elec", "poisson"): make_Dirichlet_boundaries
+    (Grid.cpp:343-373) on faces at x = 0, x = L, y = 0, y = H (the
+    semiconductor-electrolyte faces keep the default Interface id), then
+    make_Neumann_boundaries (Grid.cpp:377-431), then make_Schottky_boundaries
+    (Grid.cpp:434-461, semiconductor and Poisson meshes only)."""
+    L = P.x_elec1 if P.full_system else P.x_semi1
+    H = P.height
+    bid = oracle.INTERFACE
+    if x == 0.0 or x == L or y == 0.0 or y == H:
+        bid = oracle.DIRICHLET
+    if insulated:
+        if y == H or y == 0.0:
+            bid = oracle.NEUMANN if x > P.x_semi1 else oracle.DIRICHLET
+        if x == 0.0:
+            bid = oracle.NEUMANN
+    if schottky and mesh in ("semi", "poisson") and y == H:
+        bid = oracle.SCHOTTKY
+    return bid
+
+
+@pytest.mark.parametrize("full", [True, False])
+@pytest.mark.parametrize("insulated,schottky", [(False, False), (True, False), (False, True),
+                                                (True, True)])
+def test_boundary_layouts_follow_the_reference_rules(full, insulated, schottky):
+    base = (oracle.half_cell_params(n_refine=2, grading=3.0) if full
+            else oracle.pn_junction_params(nx_semi=4, ny=4))
+    P = with_layout(base, insulated, schottky)
+    pb = oracle.Problem(P)
+    meshes = [("semi", pb.semi_grid), ("poisson", pb.poisson_grid)]
+    if full:
+        meshes.append(("elec", pb.elec_grid))
+    for name, g in meshes:
+        x0, y0, hx, hy = g.cell_geom()
+        for K in range(g.nc):
+            for f in range(4):
+                bid = g.face_bid(K, f)
+                if bid is None:
+                    continue
+                cx = {oracle.LEFT: x0[K], oracle.RIGHT: x0[K] + hx[K]}.get(f, x0[K] + 0.5 * hx[K])
+                cy = {oracle.BOTTOM: y0[K], oracle.TOP: y0[K] + hy[K]}.get(f, y0[K] + 0.5 * hy[K])
+                assert bid == _reference_id(name, cx, cy, P, insulated, schottky), (name, K, f)
+
+
+LAYOUT_CASES = [(ins, sch) for ins in (False, True) for sch in (False, True)]
+
+
+@pytest.mark.parametrize("insulated,schottky", LAYOUT_CASES)
+def test_layout_matrices_match_oracle(pecs_lib, insulated, schottky):
+    P = with_layout(oracle.half_cell_params(n_refine=3, s_n=0.5, s_p=0.25), insulated, schottky)
+    ctx = pg.Context(to_lib(P), host_setup_only=True)
+    pb = oracle.Problem(P)
+    for which, ref in ((pg.MAT_N, pb.A_n), (pg.MAT_P, pb.A_p), (pg.MAT_R, pb.A_r),
+                       (pg.MAT_O, pb.A_o), (pg.MAT_POISSON, pb.A_P)):
+        assert _cmp(ctx.matrix(which), ref) < 1e-14, which
