@@ -72,6 +72,7 @@ constexpr int MC = 64;     // rows of A packed per block
 constexpr int NC = 1024;   // columns of B packed per block
 constexpr int kBase = 64;  // triangular inverses: scalar below this size
 constexpr int NB = 64;     // LU block-column width
+constexpr int kTrmmBase = 128;  // triangular products: dense GEMM below this size
 constexpr double kWorkPerThread = 2.5e5;  // multiply-adds that justify one more thread
 
 int team_size(const Team* team) { return team ? team->size() : 1; }
@@ -275,6 +276,55 @@ void gemm(int M, int N, int K, double alpha, const double* A, int lda, const dou
     });
 }
 
+void trmm(bool left, bool lower, int M, int N, double alpha, const double* T, int ldt,
+          const double* B, int ldb, double* C, int ldc, Team* team) {
+  if (M <= 0 || N <= 0) return;
+  const int n = left ? M : N;
+  if (n <= kTrmmBase) {
+    if (left)
+      gemm(M, N, M, alpha, T, ldt, B, ldb, C, ldc, team);
+    else
+      gemm(M, N, N, alpha, B, ldb, T, ldt, C, ldc, team);
+    return;
+  }
+  const int p = split_point(n), r = n - p;
+  const double* T11 = T;
+  const double* T12 = T + p;
+  const double* T21 = T + (size_t)p * ldt;
+  const double* T22 = T + (size_t)p * ldt + p;
+  if (left) {
+    // rows of C: [0, p) and [p, M)
+    const double* B1 = B;
+    const double* B2 = B + (size_t)p * ldb;
+    double* C1 = C;
+    double* C2 = C + (size_t)p * ldc;
+    if (lower) {  // C1 += T11 B1; C2 += T21 B1 + T22 B2
+      trmm(true, true, p, N, alpha, T11, ldt, B1, ldb, C1, ldc, team);
+      gemm(r, N, p, alpha, T21, ldt, B1, ldb, C2, ldc, team);
+      trmm(true, true, r, N, alpha, T22, ldt, B2, ldb, C2, ldc, team);
+    } else {      // C1 += T11 B1 + T12 B2; C2 += T22 B2
+      trmm(true, false, p, N, alpha, T11, ldt, B1, ldb, C1, ldc, team);
+      gemm(p, N, r, alpha, T12, ldt, B2, ldb, C1, ldc, team);
+      trmm(true, false, r, N, alpha, T22, ldt, B2, ldb, C2, ldc, team);
+    }
+  } else {
+    // columns of C: [0, p) and [p, N)
+    const double* B1 = B;
+    const double* B2 = B + p;
+    double* C1 = C;
+    double* C2 = C + p;
+    if (lower) {  // C1 += B1 T11 + B2 T21; C2 += B2 T22
+      trmm(false, true, M, p, alpha, T11, ldt, B1, ldb, C1, ldc, team);
+      gemm(M, p, r, alpha, B2, ldb, T21, ldt, C1, ldc, team);
+      trmm(false, true, M, r, alpha, T22, ldt, B2, ldb, C2, ldc, team);
+    } else {      // C1 += B1 T11; C2 += B1 T12 + B2 T22
+      trmm(false, false, M, p, alpha, T11, ldt, B1, ldb, C1, ldc, team);
+      gemm(M, r, p, alpha, B1, ldb, T12, ldt, C2, ldc, team);
+      trmm(false, false, M, r, alpha, T22, ldt, B2, ldb, C2, ldc, team);
+    }
+  }
+}
+
 void inv_unit_lower(int n, const double* L, int ldl, double* X, int ldx, Team* team) {
   if (n <= kBase) {
     inv_unit_lower_base(n, L, ldl, X, ldx);
@@ -287,11 +337,11 @@ void inv_unit_lower(int n, const double* L, int ldl, double* X, int ldx, Team* t
   for (int r = 0; r < n1; ++r)
     for (int c = n1; c < n; ++c) X[(size_t)r * ldx + c] = 0.0;
   std::vector<double> T((size_t)n2 * n1, 0.0);
-  gemm(n2, n1, n1, 1.0, L + (size_t)n1 * ldl, ldl, X, ldx, T.data(), n1, team);
+  trmm(false, true, n2, n1, 1.0, X, ldx, L + (size_t)n1 * ldl, ldl, T.data(), n1, team);
   double* Xb = X + (size_t)n1 * ldx;
   for (int r = 0; r < n2; ++r)
     for (int c = 0; c < n1; ++c) Xb[(size_t)r * ldx + c] = 0.0;
-  gemm(n2, n1, n2, -1.0, X + (size_t)n1 * ldx + n1, ldx, T.data(), n1, Xb, ldx, team);
+  trmm(true, true, n2, n1, -1.0, X + (size_t)n1 * ldx + n1, ldx, T.data(), n1, Xb, ldx, team);
 }
 
 void inv_upper(int n, const double* U, int ldu, double* Y, int ldy, Team* team) {
@@ -306,11 +356,11 @@ void inv_upper(int n, const double* U, int ldu, double* Y, int ldy, Team* team) 
   for (int r = n1; r < n; ++r)
     for (int c = 0; c < n1; ++c) Y[(size_t)r * ldy + c] = 0.0;
   std::vector<double> T((size_t)n1 * n2, 0.0);
-  gemm(n1, n2, n2, 1.0, U + n1, ldu, Y + (size_t)n1 * ldy + n1, ldy, T.data(), n2, team);
+  trmm(false, false, n1, n2, 1.0, Y + (size_t)n1 * ldy + n1, ldy, U + n1, ldu, T.data(), n2, team);
   double* Yb = Y + n1;
   for (int r = 0; r < n1; ++r)
     for (int c = 0; c < n2; ++c) Yb[(size_t)r * ldy + c] = 0.0;
-  gemm(n1, n2, n1, -1.0, Y, ldy, T.data(), n2, Yb, ldy, team);
+  trmm(true, false, n1, n2, -1.0, Y, ldy, T.data(), n2, Yb, ldy, team);
 }
 
 int lu_front(int f, int s, double* A, int lda, int* perm, double tiny, double* bad_pivot,

@@ -45,6 +45,13 @@ class Team {
 void gemm(int M, int N, int K, double alpha, const double* A, int lda, const double* B, int ldb,
           double* C, int ldc, Team* team);
 
+// C += alpha * T * B (left) or C += alpha * B * T (right), T triangular
+// (lower or upper; its other triangle must hold zeros, which the blocks below
+// the recursion's base size multiply through).  C is M x N; T is M x M (left)
+// or N x N (right).  About half a GEMM's work.
+void trmm(bool left, bool lower, int M, int N, double alpha, const double* T, int ldt,
+          const double* B, int ldb, double* C, int ldc, Team* team);
+
 // X = L^{-1} for a unit lower-triangular L (n x n, strictly lower part read
 // from L); X's strictly upper part is set to zero.
 void inv_unit_lower(int n, const double* L, int ldl, double* X, int ldx, Team* team);

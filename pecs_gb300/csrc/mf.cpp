@@ -354,7 +354,7 @@ std::vector<double> factor_node(MfFactor& F, int j, const Csr& A, const Csr& AT,
   // Gf = [L11^-1 P ; L21 L11^-1 P]
   std::vector<double> X((size_t)f * s, 0.0);
   dense::inv_unit_lower(s, Fm.data(), f, X.data(), s, team);
-  dense::gemm(m, s, s, 1.0, &Fm[(size_t)s * f], f, X.data(), s, &X[(size_t)s * s], s, team);
+  dense::trmm(false, true, m, s, 1.0, X.data(), s, &Fm[(size_t)s * f], f, &X[(size_t)s * s], s, team);
   std::vector<double>& G = F.Gf[j];
   G.assign((size_t)f * s, 0.0);
   for (int r = 0; r < f; ++r)
@@ -364,7 +364,7 @@ std::vector<double> factor_node(MfFactor& F, int j, const Csr& A, const Csr& AT,
   std::vector<double>& H = F.Hb[j];
   H.assign((size_t)s * f, 0.0);
   dense::inv_upper(s, Fm.data(), f, H.data(), f, team);
-  dense::gemm(s, m, s, -1.0, H.data(), f, &Fm[s], f, &H[s], f, team);
+  dense::trmm(true, false, s, m, -1.0, H.data(), f, &Fm[s], f, &H[s], f, team);
   for (int t = 0; t < s; ++t) fpos[nd.own[t]] = -1;
   for (int t = 0; t < m; ++t) fpos[nd.upd[t]] = -1;
   flops += 2.0 * s * s * (double)(s + m);

@@ -65,6 +65,33 @@ int main() {
     std::printf("gemm %.3e\n", e);
     if (!(e < 1e-12)) return fail("gemm", e);
   }
+  // triangular products (all four forms) against the naive loop
+  for (int left = 0; left < 2; ++left)
+    for (int lower = 0; lower < 2; ++lower) {
+      const int M = 301, N = 277, n = left ? M : N;
+      std::vector<double> T((size_t)n * n, 0.0), B((size_t)M * N), C((size_t)M * N), R;
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+          if (lower ? j <= i : j >= i) T[(size_t)i * n + j] = urand();
+      for (auto& x : B) x = urand();
+      for (auto& x : C) x = urand();
+      R = C;
+      std::vector<double> C1 = C;
+      trmm(left, lower, M, N, -1.0, T.data(), n, B.data(), N, C.data(), N, &t4);
+      trmm(left, lower, M, N, -1.0, T.data(), n, B.data(), N, C1.data(), N, &t1);
+      if (C != C1) return fail("trmm differs between 1 and 4 threads", 1.0);
+      double e = 0.0;
+      for (int i = 0; i < M; ++i)
+        for (int j = 0; j < N; ++j) {
+          double s = R[(size_t)i * N + j];
+          for (int k = 0; k < n; ++k)
+            s -= left ? T[(size_t)i * n + k] * B[(size_t)k * N + j]
+                      : B[(size_t)i * N + k] * T[(size_t)k * n + j];
+          e = std::max(e, std::fabs(s - C[(size_t)i * N + j]));
+        }
+      std::printf("trmm left=%d lower=%d %.3e\n", left, lower, e);
+      if (!(e < 1e-12)) return fail("trmm", e);
+    }
   const int sizes[][2] = {{1, 1}, {5, 3}, {65, 65}, {200, 130}, {700, 450}};
   for (const auto& fs : sizes) {
     const int f = fs[0], s = fs[1];
