@@ -19,6 +19,27 @@ def test_shard_covers_everything_once():
         shard(4, 2, 2)
 
 
+def test_matrix_key_groups_points_by_their_matrices(pecs_lib):
+    """Points share a context exactly when the library accepts them in one:
+    the grouping key of ragged sweeps covers every matrix-defining field,
+    grading and boundary layouts included."""
+    import pecs_gb300 as pg
+    from pecs_gb300.sweep import MATRIX_FIELDS, matrix_key
+    base = pg.half_cell(n_refine=2)
+    same = [base.copy(phi_app=0.3), base.copy(G0=2.0, alpha=3.0), base.copy(tau_n=0.5, k_et=1e-3)]
+    other = [base.copy(grading=4.0), pg.boundary_layout(base, insulated=True),
+             pg.boundary_layout(base, schottky=True), base.copy(ny=8), base.copy(dt=2e-3),
+             base.copy(degree=2)]
+    for p in same:
+        assert matrix_key(p) == matrix_key(base)
+        pg.Context([base, p], host_setup_only=True).close()
+    for p in other:
+        assert matrix_key(p) != matrix_key(base)
+        with pytest.raises(pg.PecsError):
+            pg.Context([base, p], host_setup_only=True)
+    assert set(MATRIX_FIELDS) <= set(base.__dataclass_fields__)
+
+
 def _free_port():
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
