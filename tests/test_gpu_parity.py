@@ -12,7 +12,7 @@ from test_lu_host import _maps_carrier, _maps_poisson
 
 pytestmark = pytest.mark.gpu
 
-STEP_TOL = 1e-10     # FP64 path vs FP64 oracle, relative L2 per field (spec bound)
+STEP_TOL = 1e-10     # FP64 path vs FP64 oracle, relative L2 per field (the FP64 parity bound)
 SOLVE_TOL = 1e-11    # one direct solve: multifrontal LU vs SuperLU, both O(cond * eps)
 RHS_TOL = 1e-13
 
