@@ -46,14 +46,19 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     obj = LIBDIR / "obj"
     obj.mkdir(parents=True, exist_ok=True)
     common = ["-O3", "-std=c++17", f"-I{INCLUDE}"]
+    # host arithmetic without fused multiply-adds: g++ fuses a*b+c by default
+    # in C++ on aarch64 but cannot on x86-64 without -mfma, so the host setup
+    # (matrices, factors, constant right-hand sides) would round differently
+    # on the two
+    host = "-ffp-contract=off"
     cmds = []
     for src in CUDA_SOURCES:
         o = obj / (src + ".o")
-        cmds.append([nvcc, *ARCH, *common, "-lineinfo", "-Xcompiler", "-fPIC", "-c",
+        cmds.append([nvcc, *ARCH, *common, "-lineinfo", "-Xcompiler", f"-fPIC,{host}", "-c",
                      str(CSRC / src), "-o", str(o)])
     for src in CXX_SOURCES:
         o = obj / (src + ".o")
-        cmds.append(["g++", *common, "-fPIC", "-c", str(CSRC / src), "-o", str(o)])
+        cmds.append(["g++", *common, host, "-fPIC", "-c", str(CSRC / src), "-o", str(o)])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -14,7 +14,7 @@ CSRC = ROOT / "pecs_gb300" / "csrc"
 
 def test_dense_front_kernels(tmp_path):
     exe = tmp_path / "dense_check"
-    r = subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", f"-I{CSRC}",
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", f"-I{CSRC}",
                         str(ROOT / "tests" / "dense_check.cpp"), str(CSRC / "dense.cpp"),
                         "-o", str(exe)], capture_output=True, text=True)
     if r.returncode != 0:
