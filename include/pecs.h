@@ -147,6 +147,17 @@ typedef struct pecs_ctx pecs_ctx;
 const char* pecs_last_error(void);
 void pecs_default_options(pecs_options* opt);
 
+/* The reference's boundary layouts on p, replacing Grid::make_grids' id
+ * assignment (Grid.cpp:112-131): every outer side Dirichlet and the
+ * semiconductor-electrolyte faces Interface (make_Dirichlet_boundaries,
+ * Grid.cpp:343-373); insulated != 0 adds make_Neumann_boundaries
+ * (Grid.cpp:377-431: left side Neumann, top and bottom Neumann over the
+ * electrolyte); schottky != 0 adds make_Schottky_boundaries (Grid.cpp:434-461:
+ * the top of the semiconductor and Poisson meshes).  Sets bc_semi, bc_elec,
+ * bc_poisson and bc_poisson_elec for p->full_system; no other field changes.
+ * Host only. */
+int pecs_apply_boundary_layout(pecs_params* p, int insulated, int schottky);
+
 /* Setup: meshes, DoF maps, LDG + mixed matrices, LU factors, upload.
  * `params` holds n_inst instances; all must share the fields that enter the
  * matrices (mesh, degree, boundary layout, lambda2, eps, mu, dt, penalty). */

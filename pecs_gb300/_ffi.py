@@ -79,6 +79,7 @@ _vp = C.c_void_p
 SIGNATURES = [
     ("pecs_last_error", C.c_char_p, []),
     ("pecs_default_options", None, [C.POINTER(pecs_options)]),
+    ("pecs_apply_boundary_layout", C.c_int, [C.POINTER(pecs_params), C.c_int, C.c_int]),
     ("pecs_create", C.c_int, [C.POINTER(pecs_params), C.c_int, C.POINTER(pecs_options), C.POINTER(_vp)]),
     ("pecs_destroy", None, [_vp]),
     ("pecs_get_info", C.c_int, [_vp, C.POINTER(pecs_info)]),

@@ -1573,6 +1573,26 @@ void pecs_default_options(pecs_options* opt) {
   opt->autotune = 1;
 }
 
+int pecs_apply_boundary_layout(pecs_params* p, int insulated, int schottky) {
+  PECS_TRY({
+    if (!p) throw PecsError(PECS_E_ARG, "params is NULL");
+    const int D = kDirichlet, N = kNeumann, I = kInterface, S = kSchottky;
+    const bool full = p->full_system != 0;
+    const int semi[4] = {insulated ? N : D, full ? I : D, D, schottky ? S : D};
+    const int elec_tb = (full && insulated) ? N : D;
+    const int elec[4] = {I, D, elec_tb, elec_tb};
+    const int pois[4] = {insulated ? N : D, D, D, schottky ? S : D};
+    const int pois_elec[4] = {0, 0, (full && insulated) ? N : 0,
+                              full && schottky ? S : ((full && insulated) ? N : 0)};
+    for (int f = 0; f < 4; ++f) {
+      p->bc_semi[f] = semi[f];
+      p->bc_elec[f] = elec[f];
+      p->bc_poisson[f] = pois[f];
+      p->bc_poisson_elec[f] = pois_elec[f];
+    }
+  })
+}
+
 int pecs_create(const pecs_params* params, int n_inst, const pecs_options* opt, pecs_ctx** out) {
   PECS_TRY({
     if (!out) throw PecsError(PECS_E_ARG, "out is NULL");

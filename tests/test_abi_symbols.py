@@ -50,3 +50,22 @@ def test_sweep_stream_rejects_points_with_other_matrices(pecs_lib):
         ctx.sweep_stream([base, base.copy(dt=2e-3)], 10, 1e-6)
     with pytest.raises(pg.PecsError, match="host_setup_only"):
         ctx.sweep_stream([base, base.copy(phi_app=0.3)], 10, 1e-6)
+
+
+@pytest.mark.parametrize("full", [True, False])
+def test_boundary_layout_abi_matches_python(pecs_lib, full):
+    """pecs_apply_boundary_layout (for C++ callers) and
+    pecs_gb300.boundary_layout set the same ids; other fields are untouched."""
+    import ctypes as C
+
+    import pecs_gb300 as pg
+    base = pg.half_cell(n_refine=2) if full else pg.pn_junction()
+    for insulated in (False, True):
+        for schottky in (False, True):
+            c = base.to_c()
+            assert pecs_lib.pecs_apply_boundary_layout(C.byref(c), int(insulated), int(schottky)) == 0
+            ref = pg.boundary_layout(base, insulated=insulated, schottky=schottky)
+            for f in ("bc_semi", "bc_elec", "bc_poisson", "bc_poisson_elec"):
+                assert tuple(getattr(c, f)) == tuple(getattr(ref, f)), (f, insulated, schottky)
+            assert c.nx_semi == base.nx_semi and c.phi_app == base.phi_app
+    assert pecs_lib.pecs_apply_boundary_layout(None, 0, 0) != 0
