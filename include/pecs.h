@@ -170,6 +170,18 @@ int pecs_get_info(pecs_ctx* ctx, pecs_info* info);
 int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowptr, int* col,
                     double* val);
 
+/* Host-computed per-instance vectors of the setup (also on host_setup_only
+ * contexts), ndofs[field] doubles into out:
+ *   PECS_SETUP_CONST_RHS: the time-independent right-hand-side part of a field
+ *     (generation and Dirichlet data of the carriers, SolarCell.cpp:1073-1401,
+ *     1451-1726; doping and potential data of Poisson, SolarCell.cpp:487-815);
+ *   PECS_SETUP_INITIAL: the projected initial density of a carrier field
+ *     (SolarCell.cpp:1996-2027; currents zero), before the initial Poisson
+ *     solve. */
+#define PECS_SETUP_CONST_RHS 0
+#define PECS_SETUP_INITIAL 1
+int pecs_get_setup_vector(pecs_ctx* ctx, int kind, int field, int inst, double* out);
+
 /* Initial conditions (SolarCell.cpp:1996-2034): L2 projection of the initial
  * profiles, then the initial Poisson solve. */
 int pecs_initialize(pecs_ctx* ctx);

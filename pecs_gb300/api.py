@@ -216,6 +216,13 @@ class Context:
         check(lib().pecs_get_info(self._h, C.byref(i)))
         return i
 
+    def setup_vector(self, kind: int, field: int, inst: int = 0) -> np.ndarray:
+        """Host-computed setup vector (SETUP_CONST_RHS or SETUP_INITIAL) of one
+        instance and field; also on host_setup_only contexts."""
+        out = np.zeros(self.ndofs[field])
+        check(lib().pecs_get_setup_vector(self._h, kind, field, inst, _dptr(out)))
+        return out
+
     def matrix(self, which: int):
         import scipy.sparse as sp
         n = C.c_int()

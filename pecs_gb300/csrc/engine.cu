@@ -1683,6 +1683,28 @@ int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowpt
   })
 }
 
+int pecs_get_setup_vector(pecs_ctx* ctx, int kind, int field, int inst, double* out) {
+  PECS_TRY({
+    if (!ctx || !out) throw PecsError(PECS_E_ARG, "NULL argument");
+    Engine& e = ctx->e;
+    Setup& S = *e.S;
+    if (field < 0 || field >= 5 || e.nd[field] == 0) throw PecsError(PECS_E_ARG, "no such field");
+    if (inst < 0 || inst >= e.n_inst) throw PecsError(PECS_E_ARG, "bad instance");
+    const std::vector<double>* v = nullptr;
+    if (kind == PECS_SETUP_CONST_RHS) {
+      v = &S.bconst[field][inst];
+    } else if (kind == PECS_SETUP_INITIAL) {
+      if (field == PECS_FIELD_POISSON)
+        throw PecsError(PECS_E_ARG, "the initial potential comes from a solve (pecs_initialize)");
+      v = &S.init[field][inst];
+    } else {
+      throw PecsError(PECS_E_ARG, "unknown kind");
+    }
+    if ((int)v->size() != e.nd[field]) throw PecsError(PECS_E_STATE, "setup vector not built");
+    std::copy(v->begin(), v->end(), out);
+  })
+}
+
 int pecs_initialize(pecs_ctx* ctx) {
   PECS_TRY({
     if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");

@@ -126,3 +126,33 @@ def test_layout_matrices_match_oracle(pecs_lib, insulated, schottky):
     for which, ref in ((pg.MAT_N, pb.A_n), (pg.MAT_P, pb.A_p), (pg.MAT_R, pb.A_r),
                        (pg.MAT_O, pb.A_o), (pg.MAT_POISSON, pb.A_P)):
         assert _cmp(ctx.matrix(which), ref) < 1e-14, which
+
+
+SETUP_VECTOR_CASES = CASES + [
+    ("halfcell_bias", oracle.half_cell_params(n_refine=3, phi_bi=0.7, phi_app=0.2)),
+    ("insulated_schottky", with_layout(oracle.half_cell_params(n_refine=3, s_n=0.5, phi_bi=0.3),
+                                       True, True)),
+]
+
+
+@pytest.mark.parametrize("name,P", SETUP_VECTOR_CASES, ids=[c[0] for c in SETUP_VECTOR_CASES])
+def test_constant_rhs_and_initial_state_match_oracle(pecs_lib, name, P):
+    """The host-computed per-instance vectors: time-independent RHS parts
+    (generation, Dirichlet and Schottky-face data, doping) and the projected
+    initial densities, against the oracle's, on the CPU."""
+    ctx = pg.Context(to_lib(P), host_setup_only=True)
+    pb = oracle.Problem(P)
+    fields = {"n": pg.FIELD_N, "p": pg.FIELD_P, "r": pg.FIELD_R, "o": pg.FIELD_O,
+              "P": pg.FIELD_POISSON}
+    for f, ref in pb.bconst.items():
+        v = ctx.setup_vector(pg.SETUP_CONST_RHS, fields[f])
+        assert np.abs(v - ref).max() <= 1e-13 * max(np.abs(ref).max(), 1e-300), f
+    st = pb.initial_state()
+    for f in ("n", "p", "r", "o"):
+        if f in st:
+            v = ctx.setup_vector(pg.SETUP_INITIAL, fields[f])
+            assert np.abs(v - st[f]).max() <= 1e-13 * np.abs(st[f]).max(), f
+    with pytest.raises(pg.PecsError):
+        ctx.setup_vector(pg.SETUP_INITIAL, pg.FIELD_POISSON)
+    with pytest.raises(pg.PecsError):
+        ctx.setup_vector(pg.SETUP_CONST_RHS, pg.FIELD_N, inst=1)
