@@ -182,6 +182,14 @@ int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowpt
 #define PECS_SETUP_INITIAL 1
 int pecs_get_setup_vector(pecs_ctx* ctx, int kind, int field, int inst, double* out);
 
+/* Cell edges of a mesh (the triangulations of Grid::make_grids, Grid.cpp:44-133):
+ * nx + 1 x-coordinates into xs and ny + 1 y-coordinates into ys; cells are
+ * numbered i + nx*j.  Call with NULL arrays to query nx and ny. */
+#define PECS_MESH_SEMI 0
+#define PECS_MESH_ELEC 1
+#define PECS_MESH_POISSON 2
+int pecs_get_mesh(pecs_ctx* ctx, int mesh, int* nx, int* ny, double* xs, double* ys);
+
 /* Initial conditions (SolarCell.cpp:1996-2034): L2 projection of the initial
  * profiles, then the initial Poisson solve. */
 int pecs_initialize(pecs_ctx* ctx);

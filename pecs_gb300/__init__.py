@@ -8,6 +8,7 @@ from ._build import build, LIB  # noqa: F401
 from ._ffi import (DIRICHLET, FIELD_N, FIELD_O, FIELD_P, FIELD_POISSON, FIELD_R,  # noqa: F401
                    INTERFACE, MAT_MASS_ELEC, MAT_MASS_SEMI, MAT_N, MAT_O, MAT_P, MAT_POISSON,
                    MAT_R, NEUMANN, PREC_FP32_IR, PREC_FP32_MIXED, PREC_FP64, SCHOTTKY,
-                   SETUP_CONST_RHS, SETUP_INITIAL, PecsError, lib)
+                   SETUP_CONST_RHS, SETUP_INITIAL, MESH_SEMI, MESH_ELEC, MESH_POISSON,
+                   PecsError, lib)
 from .api import (LU, Context, Params, boundary_layout, pn_junction, half_cell,  # noqa: F401
                   reference_params)

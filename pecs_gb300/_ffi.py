@@ -23,6 +23,7 @@ INTERFACE, DIRICHLET, NEUMANN, SCHOTTKY = 0, 1, 2, 3
 FIELD_N, FIELD_P, FIELD_R, FIELD_O, FIELD_POISSON = 0, 1, 2, 3, 4
 MAT_N, MAT_P, MAT_R, MAT_O, MAT_POISSON, MAT_MASS_SEMI, MAT_MASS_ELEC = range(7)
 SETUP_CONST_RHS, SETUP_INITIAL = 0, 1
+MESH_SEMI, MESH_ELEC, MESH_POISSON = 0, 1, 2
 PREC_FP64, PREC_FP32_IR, PREC_FP32_MIXED = 0, 1, 2
 
 
@@ -82,6 +83,8 @@ SIGNATURES = [
     ("pecs_default_options", None, [C.POINTER(pecs_options)]),
     ("pecs_apply_boundary_layout", C.c_int, [C.POINTER(pecs_params), C.c_int, C.c_int]),
     ("pecs_get_setup_vector", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    ("pecs_get_mesh", C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("pecs_create", C.c_int, [C.POINTER(pecs_params), C.c_int, C.POINTER(pecs_options), C.POINTER(_vp)]),
     ("pecs_destroy", None, [_vp]),
     ("pecs_get_info", C.c_int, [_vp, C.POINTER(pecs_info)]),

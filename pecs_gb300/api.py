@@ -223,6 +223,15 @@ class Context:
         check(lib().pecs_get_setup_vector(self._h, kind, field, inst, _dptr(out)))
         return out
 
+    def mesh(self, which: int):
+        """Cell edges (xs, ys) of a mesh (MESH_SEMI, MESH_ELEC, MESH_POISSON);
+        cells are numbered i + nx*j."""
+        nx, ny = C.c_int(), C.c_int()
+        check(lib().pecs_get_mesh(self._h, which, C.byref(nx), C.byref(ny), None, None))
+        xs, ys = np.zeros(nx.value + 1), np.zeros(ny.value + 1)
+        check(lib().pecs_get_mesh(self._h, which, None, None, _dptr(xs), _dptr(ys)))
+        return xs, ys
+
     def matrix(self, which: int):
         import scipy.sparse as sp
         n = C.c_int()

@@ -1705,6 +1705,22 @@ int pecs_get_setup_vector(pecs_ctx* ctx, int kind, int field, int inst, double* 
   })
 }
 
+int pecs_get_mesh(pecs_ctx* ctx, int mesh, int* nx, int* ny, double* xs, double* ys) {
+  PECS_TRY({
+    if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");
+    Setup& S = *ctx->e.S;
+    const Grid* g = nullptr;
+    if (mesh == PECS_MESH_SEMI) g = &S.semi.grid;
+    else if (mesh == PECS_MESH_ELEC && S.full) g = &S.elec.grid;
+    else if (mesh == PECS_MESH_POISSON) g = &S.pois.grid;
+    if (!g) throw PecsError(PECS_E_ARG, "no such mesh");
+    if (nx) *nx = g->nx;
+    if (ny) *ny = g->ny;
+    if (xs) std::copy(g->xs.begin(), g->xs.end(), xs);
+    if (ys) std::copy(g->ys.begin(), g->ys.end(), ys);
+  })
+}
+
 int pecs_initialize(pecs_ctx* ctx) {
   PECS_TRY({
     if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");

@@ -43,24 +43,18 @@ class Scales:
                       / characteristic_time)
 
 
-def _region_cells(p, region: str):
-    """(nx, ny, x0, x1) of a carrier region of the rectangular half cell."""
-    if region == "semi":
-        return p.nx_semi, p.ny, p.x_semi0, p.x_semi1
-    return p.nx_elec, p.ny, p.x_semi1, p.x_elec1
-
-
-def _patches(nx, ny, x0, x1, height, k):
-    """Points (cells*(k+1)^2, 3) and quads (cells*k*k, 4) of per-cell patches."""
+def _patches(xs, ys, k):
+    """Points (cells*(k+1)^2, 3) and quads (cells*k*k, 4) of per-cell patches
+    on the mesh with cell edges xs, ys (cells i + nx*j; graded meshes too)."""
     m = k + 1
-    hx, hy = (x1 - x0) / nx, height / ny
+    nx, ny = len(xs) - 1, len(ys) - 1
     t = np.linspace(0.0, 1.0, m)
     pts, quads = [], []
     base = 0
     for j in range(ny):
         for i in range(nx):
-            X = x0 + hx * (i + t)
-            Y = hy * (j + t)
+            X = xs[i] + (xs[i + 1] - xs[i]) * t
+            Y = ys[j] + (ys[j + 1] - ys[j]) * t
             for b in range(m):
                 for a in range(m):
                     pts.append((X[a], Y[b], 0.0))
@@ -114,10 +108,10 @@ def write_carriers(ctx, path: str, inst: int = 0, region: str = "semi",
     k = p.degree
     m = k + 1
     n1 = m * m
-    nx, ny, x0, x1 = _region_cells(p, region)
-    nc = nx * ny
+    xs, ys = ctx.mesh(F.MESH_SEMI if region == "semi" else F.MESH_ELEC)
+    nc = (len(xs) - 1) * (len(ys) - 1)
     fields = (F.FIELD_N, F.FIELD_P) if region == "semi" else (F.FIELD_R, F.FIELD_O)
-    pts, quads = _patches(nx, ny, x0, x1, p.height, k)
+    pts, quads = _patches(xs, ys, k)
     pdata = {}
     for f, name in zip(fields, names):
         v = ctx.get_state(f, inst)
@@ -136,13 +130,12 @@ def write_potential(ctx, path: str, inst: int = 0, scales: Scales = Scales()) ->
     p = ctx.params[inst]
     k = p.degree
     lay = Layout.of(ctx)
-    nx = p.nx_semi + (p.nx_elec if p.full_system else 0)
-    x1 = p.x_elec1 if p.full_system else p.x_semi1
+    xs, ys = ctx.mesh(F.MESH_POISSON)
     v = ctx.get_state(F.FIELD_POISSON, inst)
     phi = scales.potential * v[lay.phi_off:lay.phi_off + lay.n_phi]
     if k == 1:
-        pts, quads = _patches(nx, p.ny, p.x_semi0, x1, p.height, 1)
+        pts, quads = _patches(xs, ys, 1)
         _write(path, [_piece(pts, quads, {}, {"Potential": phi})])
     else:
-        pts, quads = _patches(nx, p.ny, p.x_semi0, x1, p.height, k - 1)
+        pts, quads = _patches(xs, ys, k - 1)
         _write(path, [_piece(pts, quads, {"Potential": phi}, {})])

@@ -4,19 +4,26 @@ context supplies known state vectors; the file is parsed back."""
 import xml.etree.ElementTree as ET
 
 import numpy as np
+import pytest
 
 import pecs_gb300 as pg
 from pecs_gb300 import vtu
 
 
 class FakeCtx:
+    """Known state vectors; the meshes come from a host-only library context."""
+
     def __init__(self, p, vecs):
         self.params = [p]
         self.ndofs = [len(vecs.get(f, [])) for f in range(5)]
         self._v = vecs
+        self._host = pg.Context(p, host_setup_only=True)
 
     def get_state(self, f, inst=0):
         return self._v[f]
+
+    def mesh(self, which):
+        return self._host.mesh(which)
 
 
 def _arrays(path):
@@ -26,7 +33,7 @@ def _arrays(path):
     return piece, out
 
 
-def test_carrier_patches_and_scaling(tmp_path):
+def test_carrier_patches_and_scaling(tmp_path, pecs_lib):
     p = pg.half_cell(n_refine=1)   # 2x2 cells per region, k = 1
     nc, n1 = 4, 4
     n = np.arange(3 * nc * n1, dtype=float)
@@ -46,7 +53,7 @@ def test_carrier_patches_and_scaling(tmp_path):
     assert set(a["types"]) == {9.0}
 
 
-def test_potential_cell_data(tmp_path):
+def test_potential_cell_data(tmp_path, pecs_lib):
     p = pg.half_cell(n_refine=1)
     ncp = 8                      # 4 x 2 Poisson cells
     n_rt = 22                    # whatever precedes the potential block
@@ -57,3 +64,33 @@ def test_potential_cell_data(tmp_path):
     piece, a = _arrays(path)
     assert piece.get("NumberOfCells") == str(ncp)
     np.testing.assert_array_equal(a["Potential"], 0.5 * np.arange(ncp))
+
+
+def test_graded_mesh_patches_follow_the_cell_edges(tmp_path, pecs_lib):
+    """On a mesh graded toward the interface every patch spans its own cell:
+    the library's cell edges (pecs_get_mesh) are the oracle's, and the
+    written points lie on them."""
+    import oracle
+    from helpers import to_lib
+    P = oracle.half_cell_params(n_refine=2, grading=6.0)
+    pb = oracle.Problem(P)
+    lib_p = to_lib(P)
+    host = pg.Context(lib_p, host_setup_only=True)
+    for which, g in ((pg.MESH_SEMI, pb.semi_grid), (pg.MESH_ELEC, pb.elec_grid),
+                     (pg.MESH_POISSON, pb.poisson_grid)):
+        xs, ys = host.mesh(which)
+        np.testing.assert_allclose(xs, g.xs, rtol=0, atol=1e-15)
+        np.testing.assert_allclose(ys, g.ys, rtol=0, atol=1e-15)
+    nc, n1 = 16, 4
+    vecs = {pg.FIELD_N: np.zeros(3 * nc * n1), pg.FIELD_P: np.zeros(3 * nc * n1)}
+    path = tmp_path / "graded.vtu"
+    vtu.write_carriers(FakeCtx(lib_p, vecs), str(path))
+    _, a = _arrays(path)
+    pts = a["Points"].reshape(nc, n1, 3)
+    x0, y0, hx, hy = pb.semi_grid.cell_geom()
+    np.testing.assert_allclose(pts[:, 0, 0], x0, atol=1e-15)
+    np.testing.assert_allclose(pts[:, 3, 0], x0 + hx, atol=1e-15)
+    np.testing.assert_allclose(pts[:, 3, 1], y0 + hy, atol=1e-15)
+    assert hx[3] < hx[0] / 4     # finest next to the interface
+    with pytest.raises(pg.PecsError):
+        pg.Context(pg.pn_junction(), host_setup_only=True).mesh(pg.MESH_ELEC)
