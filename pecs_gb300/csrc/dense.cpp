@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <exception>
 #include <utility>
 
 namespace pecs {
@@ -10,7 +11,31 @@ namespace dense {
 
 Team::Team(int n) : n_(std::max(1, n)) {
   th_.reserve(n_ - 1);
-  for (int i = 1; i < n_; ++i) th_.emplace_back([this, i]() { worker(i); });
+  try {
+    for (int i = 1; i < n_; ++i) th_.emplace_back([this, i]() { worker(i); });
+  } catch (...) {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+    throw;
+  }
+}
+
+void run_threads(int n, const std::function<void(int)>& fn) {
+  std::vector<std::thread> th;
+  th.reserve(n > 1 ? n - 1 : 0);
+  std::exception_ptr err;
+  try {
+    for (int t = 1; t < n; ++t) th.emplace_back(fn, t);
+    fn(0);
+  } catch (...) {
+    err = std::current_exception();
+  }
+  for (auto& x : th) x.join();
+  if (err) std::rethrow_exception(err);
 }
 
 Team::~Team() {

@@ -41,6 +41,10 @@ class Team {
   bool stop_ = false;
 };
 
+// Runs fn(t) for t in [0, n) on n threads (the caller takes t = 0) and joins
+// them; if starting a thread fails, joins the started ones and rethrows.
+void run_threads(int n, const std::function<void(int)>& fn);
+
 // C[M x N] += alpha * A[M x K] * B[K x N]; threads from `team` (may be null).
 void gemm(int M, int N, int K, double alpha, const double* A, int lda, const double* B, int ldb,
           double* C, int ldc, Team* team);

@@ -433,13 +433,7 @@ void mf_factorize(MfFactor& F, const Csr& A, int n_threads) {
       std::lock_guard<std::mutex> g(mu);
       flops += fl;
     };
-    if (nt <= 1) {
-      worker();
-    } else {
-      std::vector<std::thread> th;
-      for (int t = 0; t < nt; ++t) th.emplace_back(worker);
-      for (auto& x : th) x.join();
-    }
+    dense::run_threads(std::max(1, nt), [&](int) { worker(); });
     if (!err.empty()) throw std::runtime_error(err);
   }
   F.factor_flops = flops;

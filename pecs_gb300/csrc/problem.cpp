@@ -1,6 +1,8 @@
 // Host-side setup of the PECS problem (see problem.hpp).
 #include "problem.hpp"
 
+#include "dense.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -485,12 +487,7 @@ static void assemble_carrier(CarrierSystem& S, const CarrierTables& ct, const pe
       }
     }
   };
-  {
-    std::vector<std::thread> th;
-    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
-    work(0);
-    for (auto& x : th) x.join();
-  }
+  dense::run_threads(nt, work);
   for (int s = 0; s < 2; ++s) {
     Csr& A = S.A[s];
     A.n = S.ndofs;
