@@ -37,7 +37,9 @@ DENSITY_FLOOR = 1e-12
 
 
 def sample(n: int, seed: int) -> np.ndarray:
-    """n parameter draws (n x 6) from the benchmark's distributions."""
+    """n parameter draws (n x 6, columns NAMES): bias ~ U[-0.5, 0.5],
+    G0 ~ U[0.5, 2], alpha ~ U[1, 10], and N_D, tau, k_et log-uniform on
+    [0.3, 3], [0.1, 10], [1e-3, 1e-1]."""
     rng = np.random.default_rng(seed)
     out = np.zeros((n, 6))
     for j, (lo, hi, lg) in enumerate(RANGES):
@@ -56,7 +58,7 @@ def normalize(theta: np.ndarray) -> np.ndarray:
 
 
 def instance_params(theta_row, base: Params) -> Params:
-    """Parameters of one instance: config-2 physics with the six drawn values
+    """Parameters of one instance: the half cell's physics with the six drawn values
     (k_ht follows k_et; equilibrium densities follow the doping)."""
     bias, G0, alpha, nd, tau, ket = (float(v) for v in theta_row)
     ni = base.n_i
