@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--precision", choices=["fp64", "fp32ir", "mixed"], default="fp64")
     ap.add_argument("--n-inst", type=int, default=1, help="instances per GPU per bench step")
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
+    ap.add_argument("--ref-procs", type=int, default=0,
+                    help="--impl reference: oracle processes (0 = one per host core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", choices=["full", "plain"], default="full",
                     help="full: learned warm start + 64-instance batches (FP32-mixed) with the "
@@ -242,6 +244,8 @@ def run_reference(args):
     import multiprocessing as mp
     # one single-threaded oracle per host core: I-V points are independent
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    if args.ref_procs > 0:
+        cores = min(cores, args.ref_procs)
     for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
         os.environ[var] = "1"
     ctx = mp.get_context("spawn")
