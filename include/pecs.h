@@ -171,7 +171,7 @@ int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowpt
                     double* val);
 
 /* Host-computed per-instance vectors of the setup (also on host_setup_only
- * contexts), ndofs[field] doubles into out:
+ * contexts), ndofs[field] doubles into out (n: its capacity in doubles):
  *   PECS_SETUP_CONST_RHS: the time-independent right-hand-side part of a field
  *     (generation and Dirichlet data of the carriers, SolarCell.cpp:1073-1401,
  *     1451-1726; doping and potential data of Poisson, SolarCell.cpp:487-815);
@@ -180,7 +180,7 @@ int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowpt
  *     solve. */
 #define PECS_SETUP_CONST_RHS 0
 #define PECS_SETUP_INITIAL 1
-int pecs_get_setup_vector(pecs_ctx* ctx, int kind, int field, int inst, double* out);
+int pecs_get_setup_vector(pecs_ctx* ctx, int kind, int field, int inst, double* out, long long n);
 
 /* Cell edges of a mesh (the triangulations of Grid::make_grids, Grid.cpp:44-133):
  * nx + 1 x-coordinates into xs and ny + 1 y-coordinates into ys; cells are

@@ -82,7 +82,8 @@ SIGNATURES = [
     ("pecs_last_error", C.c_char_p, []),
     ("pecs_default_options", None, [C.POINTER(pecs_options)]),
     ("pecs_apply_boundary_layout", C.c_int, [C.POINTER(pecs_params), C.c_int, C.c_int]),
-    ("pecs_get_setup_vector", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    ("pecs_get_setup_vector", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                        C.c_longlong]),
     ("pecs_get_mesh", C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                 C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("pecs_create", C.c_int, [C.POINTER(pecs_params), C.c_int, C.POINTER(pecs_options), C.POINTER(_vp)]),

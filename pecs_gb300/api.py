@@ -220,7 +220,7 @@ class Context:
         """Host-computed setup vector (SETUP_CONST_RHS or SETUP_INITIAL) of one
         instance and field; also on host_setup_only contexts."""
         out = np.zeros(self.ndofs[field])
-        check(lib().pecs_get_setup_vector(self._h, kind, field, inst, _dptr(out)))
+        check(lib().pecs_get_setup_vector(self._h, kind, field, inst, _dptr(out), out.size))
         return out
 
     def mesh(self, which: int):

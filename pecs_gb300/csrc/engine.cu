@@ -1683,13 +1683,14 @@ int pecs_get_matrix(pecs_ctx* ctx, int which, int* n, long long* nnz, int* rowpt
   })
 }
 
-int pecs_get_setup_vector(pecs_ctx* ctx, int kind, int field, int inst, double* out) {
+int pecs_get_setup_vector(pecs_ctx* ctx, int kind, int field, int inst, double* out, long long n) {
   PECS_TRY({
     if (!ctx || !out) throw PecsError(PECS_E_ARG, "NULL argument");
     Engine& e = ctx->e;
     Setup& S = *e.S;
     if (field < 0 || field >= 5 || e.nd[field] == 0) throw PecsError(PECS_E_ARG, "no such field");
     if (inst < 0 || inst >= e.n_inst) throw PecsError(PECS_E_ARG, "bad instance");
+    if (n < e.nd[field]) throw PecsError(PECS_E_ARG, "output buffer too small");
     const std::vector<double>* v = nullptr;
     if (kind == PECS_SETUP_CONST_RHS) {
       v = &S.bconst[field][inst];

@@ -156,3 +156,8 @@ def test_constant_rhs_and_initial_state_match_oracle(pecs_lib, name, P):
         ctx.setup_vector(pg.SETUP_INITIAL, pg.FIELD_POISSON)
     with pytest.raises(pg.PecsError):
         ctx.setup_vector(pg.SETUP_CONST_RHS, pg.FIELD_N, inst=1)
+    import ctypes
+    short = np.zeros(3)
+    assert pg.lib().pecs_get_setup_vector(ctx._h, pg.SETUP_CONST_RHS, pg.FIELD_N, 0,
+                                          short.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                          short.size) != 0
