@@ -69,3 +69,25 @@ def test_boundary_layout_abi_matches_python(pecs_lib, full):
                 assert tuple(getattr(c, f)) == tuple(getattr(ref, f)), (f, insulated, schottky)
             assert c.nx_semi == base.nx_semi and c.phi_app == base.phi_app
     assert pecs_lib.pecs_apply_boundary_layout(None, 0, 0) != 0
+
+
+def test_headers_are_c99(pecs_lib, tmp_path):
+    """include/pecs.h and pecs_debug.h compile as strict C99 and a C program
+    links against the library (the ABI is plain C: no C++ types cross it)."""
+    import subprocess
+    from pecs_gb300._build import LIB
+    src = tmp_path / "abi.c"
+    src.write_text('#include <string.h>\n#include "pecs.h"\n#include "pecs_debug.h"\n'
+                   "int main(void) {\n"
+                   "  pecs_params p; pecs_options o;\n"
+                   "  memset(&p, 0, sizeof p); p.full_system = 1;\n"
+                   "  pecs_default_options(&o);\n"
+                   "  if (pecs_apply_boundary_layout(&p, 1, 1) != 0) return 1;\n"
+                   "  return p.bc_poisson_elec[3] == 3 && p.bc_semi[0] == 2 ? 0 : 2;\n"
+                   "}\n")
+    exe = tmp_path / "abi"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                        f"-I{ROOT / 'include'}", str(src), "-o", str(exe), f"-L{LIB.parent}",
+                        "-lpecs_gb300", f"-Wl,-rpath,{LIB.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(exe)]).returncode == 0
