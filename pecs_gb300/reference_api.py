@@ -14,7 +14,9 @@ reference project):
   source/Poisson.cpp:90-105).
 * ``SolarCellProblem`` -- the IMEX loop driver of
   SOLARCELL::SolarCellProblem::run_full_system (source/SolarCell.cpp:1898-2095)
-  with the stage methods it calls each step.
+  with the stage methods it calls each step, ``print_results`` (VTU files,
+  SolarCell.cpp:1823-1858) and the end-of-run ``print_dofs`` restart files
+  (SolarCell.cpp:2090-2092).
 
 Errors surface as ``PecsError`` (a RuntimeError), as the reference's
 exceptions reach ``main``'s ``catch (std::exception&)``.
@@ -151,8 +153,64 @@ class SolarCellProblem:
     def solve_Poisson(self):  # noqa: N802 (reference name)
         self.ctx.solve_poisson()
 
-    def run_full_system(self, n_steps: int):
+    # carrier names and pair names the reference sets (SolarCell.cpp:53-81)
+    CARRIERS = (("Semiconductor-", F.FIELD_N, "Electrons", F.FIELD_P, "Holes"),
+                ("Electrolyte-", F.FIELD_R, "Reductants", F.FIELD_O, "Oxidants"))
+
+    def _pairs(self):
+        full = bool(self.sim_params.full_system)
+        return self.CARRIERS if full else self.CARRIERS[:1]
+
+    def print_results(self, time_step_number: int, directory: str = ".", scales=None):
+        """print_results (SolarCell.cpp:1823-1858): "Poisson-NNN.vtu" and one
+        "<pair>NNN.vtu" per carrier pair, as output_rescaled_results names
+        them (MixedFEM.cpp:297-320, LDG.cpp:1195-1232; NNN the step number in
+        three digits), with the post-processor's scales (vtu.Scales)."""
+        import os
+
+        from . import vtu
+        sc = scales if scales is not None else vtu.Scales()
+        tag = f"{time_step_number:03d}"
+        vtu.write_potential(self.ctx, os.path.join(directory, f"Poisson-{tag}.vtu"), scales=sc)
+        for (pair, _, name1, _, name2), region in zip(self._pairs(), ("semi", "elec")):
+            vtu.write_carriers(self.ctx, os.path.join(directory, f"{pair}{tag}.vtu"), region=region,
+                               names=(name1, name2), scales=sc)
+
+    def print_dofs(self, directory: str = "."):
+        """The end-of-run restart files (SolarCell.cpp:2090-2092 through
+        CarrierPair::print_dofs): "<carrier name>.dofs" per carrier."""
+        for _, f1, name1, f2, name2 in self._pairs():
+            cp = CarrierPair()
+            cp.carrier_1.set_name(name1)
+            cp.carrier_2.set_name(name2)
+            cp.carrier_1.solution = self.ctx.get_state(f1)
+            cp.carrier_2.solution = self.ctx.get_state(f2)
+            cp.print_dofs(directory)
+
+    def read_dofs(self, directory: str = "."):
+        """Restart (SolarCell.cpp:1980-1995 through CarrierPair::read_dofs):
+        the carriers' states from their .dofs files, then the Poisson
+        right-hand side and solve for the potential they imply
+        (SolarCell.cpp:2032-2034)."""
         self.ctx.initialize()
+        for _, f1, name1, f2, name2 in self._pairs():
+            cp = CarrierPair()
+            cp.carrier_1.set_name(name1)
+            cp.carrier_2.set_name(name2)
+            cp.read_dofs(directory)
+            self.ctx.set_state(f1, cp.carrier_1.solution)
+            self.ctx.set_state(f2, cp.carrier_2.solution)
+        self.ctx.assemble_poisson_rhs()
+        self.ctx.solve_poisson()
+
+    def run_full_system(self, n_steps: int, restart_from: Optional[str] = None):
+        """n_steps IMEX steps from the initial condition, or, with
+        restart_from, from the .dofs files in that directory (the reference's
+        restart_status branch, SolarCell.cpp:1980-1995)."""
+        if restart_from is None:
+            self.ctx.initialize()
+        else:
+            self.read_dofs(restart_from)
         for _ in range(n_steps):
             self.assemble_semiconductor_rhs()
             self.assemble_electrolyte_rhs()
