@@ -203,6 +203,50 @@ class SolarCellProblem:
         self.ctx.assemble_poisson_rhs()
         self.ctx.solve_poisson()
 
+    def run(self, t_end: float, number_outputs: int, directory: str = ".",
+            restart_from: Optional[str] = None, t_end_2: Optional[float] = None, scales=None) -> int:
+        """run_full_system's time loop with its outputs (SolarCell.cpp:1968-2092):
+        the initial state (or, with restart_from, the .dofs files there) and
+        print_results for it; then for each of number_outputs time stamps the
+        IMEX steps while time < stamp, each stamp followed by print_results;
+        at the end print_dofs.  Stamps: (k+1) t_end / number_outputs from
+        time 0, or on a restart t_end + (k+1) (t_end_2 - t_end) / number_outputs
+        from time t_end with output numbers continuing at number_outputs.
+        Each interval's steps are counted with the reference's float
+        accumulation (time += dt) and marched as one pecs_step call, which
+        equals the stage-by-stage loop.  Returns the steps taken."""
+        if number_outputs < 1:
+            raise ValueError("number_outputs must be >= 1")
+        dt = self.sim_params.dt
+        if restart_from is None:
+            self.ctx.initialize()
+            stamps = [(k + 1) * t_end / number_outputs for k in range(number_outputs)]
+            number, time = 0, 0.0
+        else:
+            if t_end_2 is None:
+                raise ValueError("a restart needs t_end_2")
+            self.read_dofs(restart_from)
+            stamps = [t_end + (k + 1) * (t_end_2 - t_end) / number_outputs
+                      for k in range(number_outputs)]
+            number, time = number_outputs, t_end
+        self.print_results(number, directory, scales)
+        number += 1
+        steps = 0
+        for stamp in stamps:
+            n = 0
+            while time < stamp:
+                time += dt
+                n += 1
+            if n:
+                self.ctx.step(n)
+            steps += n
+            self.print_results(number, directory, scales)
+            number += 1
+        self.time = time
+        self.counter += steps
+        self.print_dofs(directory)
+        return steps
+
     def run_full_system(self, n_steps: int, restart_from: Optional[str] = None):
         """n_steps IMEX steps from the initial condition, or, with
         restart_from, from the .dofs files in that directory (the reference's

@@ -52,6 +52,10 @@ class OracleCtx:
     def mesh(self, which):
         return self._host.mesh(which)
 
+    def step(self, n):
+        self.calls.append(f"step {n}")
+        self.st, _, _ = self.pb.run(n, self.st)
+
 
 def _problem(ctx):
     sp = SolarCellProblem.__new__(SolarCellProblem)
@@ -111,3 +115,48 @@ def test_semiconductor_only_writes_one_pair(tmp_path, pecs_lib):
     sp.print_dofs(str(tmp_path))
     assert sorted(os.listdir(tmp_path)) == ["Electrons.dofs", "Holes.dofs", "Poisson-000.vtu",
                                             "Semiconductor-000.vtu"]
+
+
+def test_run_loop_outputs_and_restart(tmp_path, pecs_lib):
+    """The reference's loop: outputs 000..N at the stamps, steps counted by
+    float accumulation, restart files at the end; a restart continues the
+    output numbers and the time from t_end."""
+    P = oracle.half_cell_params(n_refine=2, dt=1e-3)
+    ctx = OracleCtx(P)
+    sp = _problem(ctx)
+    d1 = tmp_path / "first"
+    d1.mkdir()
+    steps = sp.run(0.010, 3, str(d1))
+    # stamps 0.00333.., 0.00666.., 0.01 with time += 1e-3 from 0
+    expected, time = [], 0.0
+    for stamp in (0.010 / 3, 2 * 0.010 / 3, 0.010):
+        n = 0
+        while time < stamp:
+            time += 1e-3
+            n += 1
+        expected.append(n)
+    assert steps == sum(expected)
+    assert [c for c in ctx.calls if c.startswith("step")] == [f"step {n}" for n in expected]
+    names = sorted(os.listdir(d1))
+    for i in range(4):
+        for pair in ("Poisson-", "Semiconductor-", "Electrolyte-"):
+            assert f"{pair}{i:03d}.vtu" in names
+    assert "Electrons.dofs" in names and "Oxidants.dofs" in names
+    ref, _, _ = oracle.Problem(P).run(steps)
+    for f in ("n", "p", "r", "o", "P"):
+        np.testing.assert_array_equal(ctx.st[f], ref[f])
+    # restart: the restart state printed as output 3, then outputs 4..6;
+    # time runs from t_end to t_end_2
+    ctx2 = OracleCtx(P)
+    sp2 = _problem(ctx2)
+    d2 = tmp_path / "second"
+    d2.mkdir()
+    more = sp2.run(0.010, 3, str(d2), restart_from=str(d1), t_end_2=0.016)
+    n, time = 0, 0.010
+    for stamp in (0.010 + k * 0.006 / 3 for k in (1, 2, 3)):
+        while time < stamp:
+            time += 1e-3
+            n += 1
+    assert more == n
+    names = sorted(os.listdir(d2))
+    assert [f"Poisson-{i:03d}.vtu" for i in range(3, 7)] == [x for x in names if x.startswith("Poisson")]
