@@ -158,6 +158,49 @@ void pecs_default_options(pecs_options* opt);
  * Host only. */
 int pecs_apply_boundary_layout(pecs_params* p, int insulated, int schottky);
 
+/* Physical parameters as input_file.prm gives them (the sections computational,
+ * mesh, physical, electrons, holes, reductants, oxidants that
+ * ParameterReader::declare_parameters declares, ParameterReader.cpp:29-208),
+ * in the reference's units. */
+typedef struct pecs_physical_params {
+  double time_step;   /* computational/time step size (already scaled) */
+  double mesh_height; /* mesh/mesh height (already scaled; the generation's incident line) */
+  int illuminated;    /* physical/illumination status */
+  double applied_bias, built_in_bias, schottky_bias; /* [V] */
+  double characteristic_length;  /* [cm] */
+  double characteristic_density; /* [cm^-3] */
+  double characteristic_time;    /* [s] */
+  double intrinsic_density;      /* [cm^-3] */
+  double photon_flux;            /* [cm^-2 s^-1] */
+  double absorption_coeff;       /* [cm^-1] */
+  double semiconductor_permittivity, electrolyte_permittivity; /* relative */
+  double electron_mobility, hole_mobility, reductant_mobility, oxidant_mobility; /* [cm^2/(V s)] */
+  double electron_recombination_time, hole_recombination_time;         /* [s] */
+  double electron_recombination_velocity, hole_recombination_velocity; /* [cm/s] */
+  double electron_transfer_rate, hole_transfer_rate;                   /* [cm^4/s] */
+} pecs_physical_params;
+
+/* Scale factors the reference keeps beside the scaled values. */
+typedef struct pecs_scales {
+  double mobility_scale;  /* T V_t / L^2 */
+  double rescale_current; /* q rho L / T: scaled current density -> [A cm^-2] */
+  double rescaled_k_et, rescaled_k_ht; /* q k rho^2 with the unscaled rate constants */
+  double schottky_bias;   /* scaled Schottky bias (no pecs_params field: the reference never
+                             places its Schottky data, SolarCell.cpp:49-50) */
+} pecs_scales;
+
+/* The values of the reference's input_file.prm. */
+void pecs_reference_physical_params(pecs_physical_params* ph);
+
+/* Parameters::parse_and_scale_parameters (include/Parameters.hpp:117-287,
+ * scaling 181-243) and the constructor's hand-off of the scaled values
+ * (SolarCell.cpp:44-92): writes into p the scaled n_i, tau_n, tau_p, s_n, s_p,
+ * G0, alpha and gen_kind (1 when illuminated, else 0 with G0 = alpha = 0),
+ * lambda2, mu[0..3], k_et, k_ht, phi_app, phi_bi, eps_semi, eps_elec, dt and
+ * height, evaluated in the reference's operation order; every other field of p
+ * is left as it is.  scales may be NULL.  Host only. */
+int pecs_scale_params(const pecs_physical_params* ph, pecs_params* p, pecs_scales* scales);
+
 /* Setup: meshes, DoF maps, LDG + mixed matrices, LU factors, upload.
  * `params` holds n_inst instances; all must share the fields that enter the
  * matrices (mesh, degree, boundary layout, lambda2, eps, mu, dt, penalty). */
@@ -276,15 +319,17 @@ void pecs_lu_destroy(pecs_lu* lu);
 /* Same solve as pecs_lu_solve_device for callers that cannot allocate device
  * memory when they solve (their own pool owns the GPU's memory, or they run
  * under a fixed memory budget).  It has no counterpart in the reference.  The
- * sweeps' scratch lives in one file-scope device array of 2^20 doubles (8 MiB)
- * that every GPU loading the library holds until exit; a solve needs
- * nrhs*(n + update-vector length) doubles of it and nrhs <= 8, larger requests
- * return PECS_E_ARG.  Nothing is allocated: the factors must already be on the
- * current device (any earlier pecs_lu_solve or pecs_lu_solve_device call on the
- * handle uploads them), else PECS_E_STATE.  The first call on a device looks
- * up the array's device address; make that first call before any stream
- * capture.  All calls share the array and leave their contents in it (every
- * value a sweep reads is written earlier in the same sweep, so nothing needs
+ * sweeps' scratch lives in one file-scope device array of 2^20 doubles (8 MiB);
+ * a solve needs nrhs*(n + update-vector length) doubles of it and nrhs <= 8,
+ * larger requests return PECS_E_ARG.  Nothing is allocated: the factors must
+ * already be on the current device (any earlier pecs_lu_solve or
+ * pecs_lu_solve_device call on the handle uploads them), else PECS_E_STATE.
+ * That upload also reserves the array on the device (CUDA loads the module
+ * holding it then) and looks up its device address, so this call never
+ * triggers a load; the device holds the array until the process exits.  The
+ * call is synchronous: it returns when the solve has finished on `stream`.
+ * All calls share the array and leave their contents in it (every value a
+ * sweep reads is written earlier in the same sweep, so nothing needs
  * clearing); calls that overlap on the GPU race on it. */
 int pecs_lu_solve_device_noalloc(pecs_lu* lu, int nrhs, const double* b_dev, double* x_dev,
                                  void* stream);

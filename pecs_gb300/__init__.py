@@ -10,5 +10,5 @@ from ._ffi import (DIRICHLET, FIELD_N, FIELD_O, FIELD_P, FIELD_POISSON, FIELD_R,
                    MAT_R, NEUMANN, PREC_FP32_IR, PREC_FP32_MIXED, PREC_FP64, SCHOTTKY,
                    SETUP_CONST_RHS, SETUP_INITIAL, MESH_SEMI, MESH_ELEC, MESH_POISSON,
                    PecsError, lib)
-from .api import (LU, Context, Params, boundary_layout, pn_junction, half_cell,  # noqa: F401
-                  reference_params)
+from .api import (LU, Context, Params, PhysicalParams, boundary_layout, pn_junction,  # noqa: F401
+                  half_cell, read_prm, reference_params, scale_params)

@@ -19,7 +19,7 @@ LIB = LIBDIR / "libpecs_gb300.so"
 INCLUDE = HERE.parent / "include"
 
 CUDA_SOURCES = ["engine.cu", "solve.cu", "nn.cu"]
-CXX_SOURCES = ["problem.cpp", "mf.cpp", "dense.cpp"]
+CXX_SOURCES = ["problem.cpp", "mf.cpp", "dense.cpp", "scaling.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

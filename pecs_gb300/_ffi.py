@@ -67,6 +67,29 @@ class pecs_info(C.Structure):
     ]
 
 
+class pecs_physical_params(C.Structure):
+    _fields_ = [
+        ("time_step", C.c_double), ("mesh_height", C.c_double), ("illuminated", C.c_int),
+        ("applied_bias", C.c_double), ("built_in_bias", C.c_double), ("schottky_bias", C.c_double),
+        ("characteristic_length", C.c_double), ("characteristic_density", C.c_double),
+        ("characteristic_time", C.c_double), ("intrinsic_density", C.c_double),
+        ("photon_flux", C.c_double), ("absorption_coeff", C.c_double),
+        ("semiconductor_permittivity", C.c_double), ("electrolyte_permittivity", C.c_double),
+        ("electron_mobility", C.c_double), ("hole_mobility", C.c_double),
+        ("reductant_mobility", C.c_double), ("oxidant_mobility", C.c_double),
+        ("electron_recombination_time", C.c_double), ("hole_recombination_time", C.c_double),
+        ("electron_recombination_velocity", C.c_double), ("hole_recombination_velocity", C.c_double),
+        ("electron_transfer_rate", C.c_double), ("hole_transfer_rate", C.c_double),
+    ]
+
+
+class pecs_scales(C.Structure):
+    _fields_ = [
+        ("mobility_scale", C.c_double), ("rescale_current", C.c_double),
+        ("rescaled_k_et", C.c_double), ("rescaled_k_ht", C.c_double), ("schottky_bias", C.c_double),
+    ]
+
+
 class PecsError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"pecs error {code}: {msg}")
@@ -82,6 +105,9 @@ SIGNATURES = [
     ("pecs_last_error", C.c_char_p, []),
     ("pecs_default_options", None, [C.POINTER(pecs_options)]),
     ("pecs_apply_boundary_layout", C.c_int, [C.POINTER(pecs_params), C.c_int, C.c_int]),
+    ("pecs_reference_physical_params", None, [C.POINTER(pecs_physical_params)]),
+    ("pecs_scale_params", C.c_int, [C.POINTER(pecs_physical_params), C.POINTER(pecs_params),
+                                    C.POINTER(pecs_scales)]),
     ("pecs_get_setup_vector", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
                                         C.c_longlong]),
     ("pecs_get_mesh", C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),

@@ -81,6 +81,148 @@ class Params:
         return p
 
 
+@dataclass
+class PhysicalParams:
+    """Physical parameters in the reference's units, as input_file.prm gives
+    them (sections computational, mesh, physical, electrons, holes,
+    reductants, oxidants of ParameterReader::declare_parameters,
+    source/ParameterReader.cpp:29-208).  The defaults are the reference's
+    input_file.prm values."""
+    time_step: float = 0.05
+    mesh_height: float = 1.0
+    illuminated: bool = True
+    applied_bias: float = 0.0
+    built_in_bias: float = 0.41
+    schottky_bias: float = 0.0
+    characteristic_length: float = 1.0e-4
+    characteristic_density: float = 1.0e16
+    characteristic_time: float = 1.0e-12
+    intrinsic_density: float = 2.564e9
+    photon_flux: float = 1.2e17
+    absorption_coeff: float = 1.74974e5
+    semiconductor_permittivity: float = 11.9
+    electrolyte_permittivity: float = 1000.0
+    electron_mobility: float = 1350.0
+    hole_mobility: float = 480.0
+    reductant_mobility: float = 1.0
+    oxidant_mobility: float = 1.0
+    electron_recombination_time: float = 5e-5
+    hole_recombination_time: float = 5e-5
+    electron_recombination_velocity: float = 3e5
+    hole_recombination_velocity: float = 2.9e5
+    electron_transfer_rate: float = 1e-19
+    hole_transfer_rate: float = 1e-14
+
+    @classmethod
+    def reference(cls) -> "PhysicalParams":
+        """The library's copy of the reference's input_file.prm values."""
+        c = F.pecs_physical_params()
+        lib().pecs_reference_physical_params(C.byref(c))
+        return cls(**{f.name: (bool(getattr(c, f.name)) if f.type in (bool, "bool")
+                               else getattr(c, f.name)) for f in dataclasses.fields(cls)})
+
+    def to_c(self) -> F.pecs_physical_params:
+        c = F.pecs_physical_params()
+        for f in dataclasses.fields(self):
+            v = getattr(self, f.name)
+            setattr(c, f.name, int(v) if isinstance(v, bool) else float(v))
+        return c
+
+
+# (subsection, key) of the reference's .prm files -> PhysicalParams field
+# (source/ParameterReader.cpp:29-208)
+_PRM_KEYS = {
+    ("computational", "time step size"): "time_step",
+    ("mesh", "mesh height"): "mesh_height",
+    ("physical", "illumination status"): "illuminated",
+    ("physical", "applied bias"): "applied_bias",
+    ("physical", "built in bias"): "built_in_bias",
+    ("physical", "schottky bias"): "schottky_bias",
+    ("physical", "characteristic length"): "characteristic_length",
+    ("physical", "characteristic density"): "characteristic_density",
+    ("physical", "characteristic time"): "characteristic_time",
+    ("physical", "intrinsic density"): "intrinsic_density",
+    ("physical", "photon flux"): "photon_flux",
+    ("physical", "absorption coefficient"): "absorption_coeff",
+    ("physical", "semiconductor permittivity"): "semiconductor_permittivity",
+    ("physical", "electrolyte permittivity"): "electrolyte_permittivity",
+    ("electrons", "mobility"): "electron_mobility",
+    ("electrons", "recombination time"): "electron_recombination_time",
+    ("electrons", "recombination velocity"): "electron_recombination_velocity",
+    ("electrons", "transfer rate"): "electron_transfer_rate",
+    ("holes", "mobility"): "hole_mobility",
+    ("holes", "recombination time"): "hole_recombination_time",
+    ("holes", "recombination velocity"): "hole_recombination_velocity",
+    ("holes", "transfer rate"): "hole_transfer_rate",
+    ("reductants", "mobility"): "reductant_mobility",
+    ("oxidants", "mobility"): "oxidant_mobility",
+}
+
+
+def read_prm(text: str, base: Optional[PhysicalParams] = None) -> PhysicalParams:
+    """Physical parameters from the text of a deal.II ParameterHandler file in
+    the layout of the reference's input_file.prm: ``subsection NAME`` ...
+    ``end`` blocks of ``set KEY = VALUE`` lines, ``#`` comments.  Entries this
+    library does not use (refinements, end times, mesh radii, switches of the
+    boundary layout) are skipped; missing entries keep base's value (default:
+    the reference's file).  Booleans are ``true``/``false``."""
+    out = dataclasses.replace(base) if base is not None else PhysicalParams()
+    types = {f.name: f.type for f in dataclasses.fields(PhysicalParams)}
+    stack = []
+    for lineno, raw in enumerate(text.splitlines(), 1):
+        line = raw.split("#", 1)[0].strip()
+        if not line:
+            continue
+        word = line.split(None, 1)
+        if word[0] == "subsection":
+            stack.append(word[1].strip() if len(word) > 1 else "")
+        elif word[0] == "end":
+            if not stack:
+                raise ValueError(f"line {lineno}: 'end' without a subsection")
+            stack.pop()
+        elif word[0] == "set":
+            if len(word) < 2 or "=" not in word[1]:
+                raise ValueError(f"line {lineno}: expected 'set KEY = VALUE'")
+            key, val = (t.strip() for t in word[1].split("=", 1))
+            name = _PRM_KEYS.get((stack[-1] if stack else "", key))
+            if name is None:
+                continue
+            if types[name] in (bool, "bool"):
+                if val not in ("true", "false"):
+                    raise ValueError(f"line {lineno}: {key} must be true or false")
+                setattr(out, name, val == "true")
+            else:
+                setattr(out, name, float(val))
+        else:
+            raise ValueError(f"line {lineno}: cannot read {raw!r}")
+    if stack:
+        raise ValueError(f"subsection {stack[-1]!r} is not closed")
+    return out
+
+
+def scale_params(phys: PhysicalParams, p: Optional[Params] = None):
+    """Parameters::parse_and_scale_parameters (include/Parameters.hpp:117-287)
+    through pecs_scale_params: returns (p with the scaled physical fields,
+    {mobility_scale, rescale_current, rescaled_k_et, rescaled_k_ht,
+    schottky_bias}).  Mesh, degree, layout and profile fields of p are kept."""
+    c = (p if p is not None else Params()).to_c()
+    sc = F.pecs_scales()
+    check(lib().pecs_scale_params(C.byref(phys.to_c()), C.byref(c), C.byref(sc)))
+    base = p if p is not None else Params()
+    kw = {}
+    for f in dataclasses.fields(Params):
+        v = getattr(c, f.name)
+        old = getattr(base, f.name)
+        if isinstance(old, tuple):
+            kw[f.name] = tuple(v[i] for i in range(len(old)))
+        elif isinstance(old, bool):
+            kw[f.name] = bool(v)
+        else:
+            kw[f.name] = v
+    scales = {name: getattr(sc, name) for name, _ in F.pecs_scales._fields_}
+    return dataclasses.replace(base, **kw), scales
+
+
 def pn_junction(**kw) -> Params:
     """Semiconductor-only p-n junction on the unit square, 16x16 cells, k=1,
     dt=1e-3, 100 steps, initial densities = doping."""
@@ -303,6 +445,21 @@ class Context:
         check(lib().pecs_run_to_steady_state(self._h, max_steps, tol, check_every,
                                              steps.ctypes.data_as(C.POINTER(C.c_int)), _dptr(rel)))
         return steps, rel
+
+    def probe_step(self) -> np.ndarray:
+        """One step of every instance; returns each instance's relative change.
+        An instance whose state became non-finite gets +inf instead of raising
+        (the warm start's fallback test treats it as the worse start)."""
+        steps = np.zeros(self.n_inst, dtype=np.int32)
+        rel = np.zeros(self.n_inst)
+        code = lib().pecs_run_to_steady_state(self._h, 1, 0.0, 1,
+                                              steps.ctypes.data_as(C.POINTER(C.c_int)), _dptr(rel))
+        if code == F.PECS_E_NONFINITE:
+            rel[steps < 0] = np.inf
+        else:
+            check(code)
+        rel[~np.isfinite(rel)] = np.inf
+        return rel
 
     def last_run_steps(self) -> int:
         return lib().pecs_last_run_steps(self._h)

@@ -1524,6 +1524,12 @@ struct LuHandle {
   }
 };
 
+namespace {
+// Loads this file's device module on device `dev` (current) and records the
+// device addresses of the no-alloc solve's static arrays; defined with them.
+void noalloc_reserve(int dev);
+}  // namespace
+
 }  // namespace pecs
 
 using namespace pecs;
@@ -1991,6 +1997,12 @@ static void lu_upload(LuHandle& h, int nrhs) {
       throw PecsError(PECS_E_NODEVICE, "no CUDA device available");
     PECS_CUDA(cudaStreamCreateWithFlags(&h.st, cudaStreamNonBlocking));
     h.bank.build({&h.F}, h.precision == PECS_PREC_FP64 ? PECS_PREC_FP64 : PECS_PREC_FP32_IR);
+    // The no-alloc solve's static scratch lives in this file's device module,
+    // which CUDA loads lazily; reserving it here, where allocation is allowed,
+    // means pecs_lu_solve_device_noalloc never triggers that load.
+    int dev = -1;
+    PECS_CUDA(cudaGetDevice(&dev));
+    noalloc_reserve(dev);
     h.uploaded = true;
   }
   if (nrhs > h.nrhs_cap) {
@@ -2075,8 +2087,10 @@ void pecs_lu_destroy(pecs_lu* lu) { delete lu; }
 // forward/backward sweeps as pecs_lu_solve_device, but keeps the sweeps'
 // scratch -- the forward-sweep slots and the per-node update vectors -- in the
 // fixed file-scope array below instead of memory owned by the handle, and
-// allocates nothing.  Every GPU that loads the library holds the array (8 MiB)
-// until the process exits.
+// allocates nothing.  CUDA loads this file's device module, and with it the
+// array (8 MiB), on a device when the factors are first uploaded there (the
+// first pecs_lu_solve / pecs_lu_solve_device call of a handle); the device
+// then holds it until the process exits.
 }  // extern "C"
 
 namespace pecs {
@@ -2094,9 +2108,10 @@ struct NoAllocSlot {
 std::mutex g_noalloc_mu;
 NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices];
 
-// Device addresses of the static arrays on the current device (looked up once
-// per device: the host-side names are only stand-ins for them).
-NoAllocSlot noalloc_slot(int dev) {
+// The host-side names of the static arrays are only stand-ins: their device
+// addresses are looked up once per device, with that device current.  Taking
+// the first address loads the module, so this runs at factor upload.
+void noalloc_reserve(int dev) {
   if (dev < 0 || dev >= kNoAllocMaxDevices) throw PecsError(PECS_E_ARG, "device ordinal too large");
   std::lock_guard<std::mutex> g(g_noalloc_mu);
   NoAllocSlot& s = g_noalloc_slot[dev];
@@ -2108,6 +2123,16 @@ NoAllocSlot noalloc_slot(int dev) {
     s.scratch = static_cast<double*>(a);
     s.ptrs = static_cast<double**>(b);
   }
+}
+
+// Addresses recorded by noalloc_reserve; never loads anything itself.
+NoAllocSlot noalloc_slot(int dev) {
+  if (dev < 0 || dev >= kNoAllocMaxDevices) throw PecsError(PECS_E_ARG, "device ordinal too large");
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  const NoAllocSlot s = g_noalloc_slot[dev];
+  if (!s.scratch)
+    throw PecsError(PECS_E_STATE, "the static scratch is not reserved on this device: upload the "
+                                  "factors there first (pecs_lu_solve or pecs_lu_solve_device)");
   return s;
 }
 }  // namespace

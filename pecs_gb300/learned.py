@@ -312,11 +312,11 @@ def warm_started_sweep(ctx: Context, op: Optional[NeuralOperator], thetas: np.nd
     pred = op.predict(X)
     # probe: one step from the standard initial condition ...
     ctx.initialize()
-    _, rel_std = ctx.run_to_steady_state(1, 0.0, 1)
+    rel_std = ctx.probe_step()
     # ... and one step from the prediction
     ctx.initialize()
     apply_prediction(ctx, pred, range(B), lay)
-    _, rel_pred = ctx.run_to_steady_state(1, 0.0, 1)
+    rel_pred = ctx.probe_step()
     use_pred = np.isfinite(rel_pred) & (rel_pred < rel_std)
     fallback = ~use_pred
     ctx.initialize()
@@ -348,10 +348,10 @@ def warm_start_vectors(ctx: Context, op: NeuralOperator, thetas: np.ndarray, bas
         pad = rows + [rows[-1]] * (B - len(rows))
         ctx.set_instances([instance_params(thetas[r], base) for r in pad])
         ctx.initialize()
-        _, rel_std = ctx.run_to_steady_state(1, 0.0, 1)
+        rel_std = ctx.probe_step()
         ctx.initialize()
         apply_prediction(ctx, pred[pad], range(B), lay)
-        _, rel_pred = ctx.run_to_steady_state(1, 0.0, 1)
+        rel_pred = ctx.probe_step()
         ok = np.isfinite(rel_pred) & (rel_pred < rel_std)
         for k, r in enumerate(rows):
             fallback[r] = not ok[k]

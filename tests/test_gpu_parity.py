@@ -272,3 +272,57 @@ def test_refinement_reaches_fp64_residuals(pecs_lib):
     assert max(res["ir2"]) < 1e-12    # the 1e-12 target of the FP32 variant
     assert max(res["ir4"]) < 1e-12
     assert max(res["mixed"]) < 1e-10
+
+
+# --- the benchmark's own mesh: half cell 64x64 + 64x64, k = 1 -------------------
+
+BENCH_STEPS = 60
+
+
+@pytest.fixture(scope="module")
+def bench_mesh_oracle():
+    """The oracle's trajectory on the benchmark mesh (~0.2-0.3 s per step after
+    a one-off SuperLU factorisation)."""
+    P = oracle.half_cell_params(n_refine=6)
+    pb = oracle.Problem(P)
+    st, _, _ = pb.run(BENCH_STEPS)
+    return P, st, pb.interface_current(st)
+
+
+def test_bench_mesh_fp64_trajectory_matches_oracle(pecs_lib, bench_mesh_oracle):
+    """Plain FP64 path, one instance, on the mesh the benchmark marches: every
+    field and the interface current within the FP64 parity bound after 60
+    steps."""
+    P, st, cur = bench_mesh_oracle
+    ctx = _ctx(P)
+    ctx.initialize()
+    ctx.step(BENCH_STEPS)
+    _compare_state(ctx, st, STEP_TOL)
+    assert abs(ctx.interface_current()[0] - cur) <= 1e-10 * abs(cur)
+
+
+def test_bench_mesh_batched_fp64_and_mixed(pecs_lib, bench_mesh_oracle):
+    """64 instances on the benchmark mesh (the panel kernels, 128 carrier
+    right-hand sides per factor): instance 0 carries the oracle's parameters
+    and must match it in FP64; every instance of the mixed-precision context
+    must stay within 1e-6 of the FP64 context's (the throughput mode's bound)."""
+    P, st, cur = bench_mesh_oracle
+    rng = np.random.default_rng(64)
+    Ps = [P] + [P.copy(phi_app=float(v), G0=float(g))
+                for v, g in zip(rng.uniform(-0.5, 0.5, 63), rng.uniform(0.5, 2.0, 63))]
+    lib_ps = [to_lib(q) for q in Ps]
+    c64 = pg.Context(lib_ps)
+    c64.initialize()
+    c64.step(BENCH_STEPS)
+    _compare_state(c64, st, STEP_TOL, inst=0)
+    assert abs(c64.interface_current()[0] - cur) <= 1e-10 * abs(cur)
+    cmx = pg.Context(lib_ps, precision=pg.PREC_FP32_MIXED)
+    cmx.initialize()
+    cmx.step(BENCH_STEPS)
+    I64, Imx = c64.interface_current(), cmx.interface_current()
+    worst = 0.0
+    for i in range(len(Ps)):
+        for f in c64.fields():
+            worst = max(worst, rel_err(cmx.get_state(f, i), c64.get_state(f, i)))
+    assert worst < 1e-6, worst
+    assert np.max(np.abs(Imx - I64) / np.abs(I64)) < 1e-6

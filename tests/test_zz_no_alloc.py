@@ -75,3 +75,56 @@ def test_noalloc_limits_and_preconditions(pecs_lib):
     lu.solve_device(b[0].data_ptr(), x1.data_ptr(), nrhs=1)
     pg._ffi.check(_noalloc(lu, 1, b[0].data_ptr(), x2.data_ptr()))
     assert _rel(x2, x1) < TOL
+
+
+def _block_diagonal(n_cells):
+    """2x2 blocks, one per cell, coupled to nothing else: the factor has no
+    update vectors, so a solve needs exactly nrhs * n doubles of scratch."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(11)
+    blocks = rng.uniform(-1.0, 1.0, (n_cells, 2, 2)) + 3.0 * np.eye(2)
+    A = sp.block_diag(list(blocks), format="csr")
+    dof_cell = np.repeat(np.arange(n_cells, dtype=np.int32), 2)
+    xy = np.stack([np.arange(n_cells) + 0.5, np.full(n_cells, 0.5)], axis=1)
+    return A, dof_cell, xy
+
+
+def test_noalloc_fills_scratch_exactly_on_a_caller_stream_without_allocating(pecs_lib):
+    """nrhs * n equal to the scratch's 2^20 doubles is accepted, one dof more
+    is refused; the call runs on the caller's stream and the device's free
+    memory is the same before and after it."""
+    torch = pytest.importorskip("torch")
+    cap = 1 << 20
+    nrhs = 8
+    A, dc, xy = _block_diagonal(cap // nrhs // 2)
+    n = A.shape[0]
+    assert nrhs * n == cap
+    lu = pg.LU(A, dc, xy)
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    b = torch.randn(nrhs, n, dtype=torch.float64, device="cuda", generator=gen)
+    x_ref = torch.zeros_like(b)
+    lu.solve_device(b.data_ptr(), x_ref.data_ptr(), nrhs=nrhs)    # uploads the factors
+    x = torch.full_like(b, float("nan"))
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        pg._ffi.check(pg.lib().pecs_lu_solve_device_noalloc(
+            lu._h, nrhs, C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()),
+            C.c_void_p(stream.cuda_stream)))
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert _rel(x, x_ref) < TOL
+    # the exact answer of the block-diagonal system, checked on the host
+    xb = np.linalg.solve(np.stack([A[2 * i:2 * i + 2, 2 * i:2 * i + 2].toarray() for i in range(4)]),
+                         b[:, :8].cpu().numpy().reshape(nrhs, 4, 2).transpose(1, 2, 0))
+    np.testing.assert_allclose(x[:, :8].cpu().numpy().reshape(nrhs, 4, 2).transpose(1, 2, 0), xb,
+                               rtol=1e-12, atol=1e-14)
+    # one dof more than fits: refused before any device work
+    A2, dc2, xy2 = _block_diagonal(cap // nrhs // 2 + 1)
+    lu2 = pg.LU(A2, dc2, xy2)
+    b2 = torch.ones(nrhs, A2.shape[0], dtype=torch.float64, device="cuda")
+    x2 = torch.zeros_like(b2)
+    lu2.solve_device(b2.data_ptr(), x2.data_ptr(), nrhs=1)
+    assert _noalloc(lu2, nrhs, b2.data_ptr(), x2.data_ptr()) == pg._ffi.PECS_E_ARG
+    assert _noalloc(lu2, nrhs - 1, b2.data_ptr(), x2.data_ptr()) == pg._ffi.PECS_OK
