@@ -53,17 +53,67 @@ def test_carrier_patches_and_scaling(tmp_path, pecs_lib):
     assert set(a["types"]) == {9.0}
 
 
-def test_potential_cell_data(tmp_path, pecs_lib):
+def test_potential_point_data(tmp_path, pecs_lib):
+    """k = 1: the potential is DGQ0, one value per cell, written (as DataOut
+    writes every quantity) at each of the cell's patch points."""
     p = pg.half_cell(n_refine=1)
     ncp = 8                      # 4 x 2 Poisson cells
-    n_rt = 22                    # whatever precedes the potential block
+    n_rt = 22                    # 10 vertical + 12 horizontal faces, one RT0 dof each
     P = np.concatenate([np.zeros(n_rt), np.arange(ncp, dtype=float)])
     ctx = FakeCtx(p, {pg.FIELD_N: np.zeros(48), pg.FIELD_POISSON: P})
     path = tmp_path / "phi.vtu"
-    vtu.write_potential(ctx, str(path), scales=vtu.Scales(potential=0.5))
+    vtu.write_poisson(ctx, str(path), scales=vtu.Scales(potential=0.5))
     piece, a = _arrays(path)
-    assert piece.get("NumberOfCells") == str(ncp)
-    np.testing.assert_array_equal(a["Potential"], 0.5 * np.arange(ncp))
+    assert piece.get("NumberOfCells") == str(ncp) and piece.get("NumberOfPoints") == str(4 * ncp)
+    np.testing.assert_array_equal(a["Potential"], 0.5 * np.repeat(np.arange(ncp), 4))
+    np.testing.assert_array_equal(a["Field"], 0.0)
+
+
+@pytest.mark.parametrize("degree,nref", [(1, 1), (2, 1)])
+def test_field_D_matches_a_field_in_the_RT_space(tmp_path, pecs_lib, degree, nref):
+    """The written "Field" is D evaluated from the RT_{k-1} coefficients: a
+    field that RT_{k-1} represents exactly (D_x of degree k in x and k-1 in y,
+    D_y the other way round) is put into a Poisson vector through the
+    oracle's own dof numbering and must come back at every patch point."""
+    import oracle
+    from helpers import to_lib
+    P = oracle.half_cell_params(n_refine=nref, degree=degree, grading=2.0)
+    pb = oracle.Problem(P)
+    sp, g = pb.pois, pb.poisson_grid
+    k = degree
+    fx = lambda x, y: x ** k + (y ** (k - 1) if k > 1 else 0.0) + 0.25   # noqa: E731
+    fy = lambda x, y: (x ** (k - 1) if k > 1 else 0.0) - 2.0 * y ** k   # noqa: E731
+    v = np.zeros(sp.ndofs)
+    nn = np.linspace(0.0, 1.0, k + 1)
+    tn = (np.arange(k) + 0.5) / k
+    x0, y0, hx, hy = g.cell_geom()
+    nxd = k * (k + 1)
+    for K in range(g.nc):
+        for b in range(k):
+            for a in range(k + 1):
+                v[sp.l2g[K, a + (k + 1) * b]] = fx(x0[K] + hx[K] * nn[a], y0[K] + hy[K] * tn[b])
+        for b in range(k + 1):
+            for a in range(k):
+                v[sp.l2g[K, nxd + a + k * b]] = fy(x0[K] + hx[K] * tn[a], y0[K] + hy[K] * nn[b])
+    lib_p = to_lib(P)
+    nd = 3 * pb.semi_grid.nc * (k + 1) ** 2
+    ctx = FakeCtx(lib_p, {pg.FIELD_N: np.zeros(nd), pg.FIELD_POISSON: v})
+    path = tmp_path / "poisson.vtu"
+    vtu.write_poisson(ctx, str(path), scales=vtu.Scales(field=3.0), subdivisions=3)
+    _, arr = _arrays(path)
+    pts = arr["Points"].reshape(-1, 3)
+    F = arr["Field"].reshape(-1, 3)
+    np.testing.assert_allclose(F[:, 0], 3.0 * fx(pts[:, 0], pts[:, 1]), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(F[:, 1], 3.0 * fy(pts[:, 0], pts[:, 1]), rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(F[:, 2], 0.0)
+
+
+def test_reference_scales(pecs_lib):
+    """PostProcessor.cpp:11-17: densities unscaled, field 0.2585 / L."""
+    s = vtu.Scales.physical(1e-4, 1e16, 1e-12)
+    assert s.density == 1.0 and s.potential == 0.02585
+    assert abs(s.field - 0.2585 / 1e-4) <= 1e-12 * s.field
+    assert abs(s.current - 1.6e-19 * 1e16 * 1e-4 / 1e-12) <= 1e-12 * s.current
 
 
 def test_graded_mesh_patches_follow_the_cell_edges(tmp_path, pecs_lib):

@@ -77,28 +77,34 @@ def test_noalloc_limits_and_preconditions(pecs_lib):
     assert _rel(x2, x1) < TOL
 
 
-def _block_diagonal(n_cells):
-    """2x2 blocks, one per cell, coupled to nothing else: the factor has no
-    update vectors, so a solve needs exactly nrhs * n doubles of scratch."""
+def _block_diagonal(n_cells, first_single=False):
+    """2x2 blocks, one per cell, coupled to nothing else (first_single: the
+    first cell has a 1x1 block).  No node of the factor has an update set, and
+    the sweeps keep one update-vector slot per right-hand side all the same,
+    so a solve needs exactly nrhs * (n + 1) doubles of scratch."""
     import scipy.sparse as sp
     rng = np.random.default_rng(11)
-    blocks = rng.uniform(-1.0, 1.0, (n_cells, 2, 2)) + 3.0 * np.eye(2)
-    A = sp.block_diag(list(blocks), format="csr")
-    dof_cell = np.repeat(np.arange(n_cells, dtype=np.int32), 2)
+    blocks = list(rng.uniform(-1.0, 1.0, (n_cells, 2, 2)) + 3.0 * np.eye(2))
+    sizes = [2] * n_cells
+    if first_single:
+        blocks[0] = np.array([[2.5]])
+        sizes[0] = 1
+    A = sp.block_diag(blocks, format="csr")
+    dof_cell = np.repeat(np.arange(n_cells, dtype=np.int32), sizes)
     xy = np.stack([np.arange(n_cells) + 0.5, np.full(n_cells, 0.5)], axis=1)
     return A, dof_cell, xy
 
 
 def test_noalloc_fills_scratch_exactly_on_a_caller_stream_without_allocating(pecs_lib):
-    """nrhs * n equal to the scratch's 2^20 doubles is accepted, one dof more
-    is refused; the call runs on the caller's stream and the device's free
-    memory is the same before and after it."""
+    """nrhs * (n + 1) equal to the scratch's 2^20 doubles is accepted, one dof
+    more is refused; the call runs on the caller's stream and the device's
+    free memory is the same before and after it."""
     torch = pytest.importorskip("torch")
     cap = 1 << 20
     nrhs = 8
-    A, dc, xy = _block_diagonal(cap // nrhs // 2)
+    A, dc, xy = _block_diagonal(cap // nrhs // 2, first_single=True)
     n = A.shape[0]
-    assert nrhs * n == cap
+    assert nrhs * (n + 1) == cap
     lu = pg.LU(A, dc, xy)
     gen = torch.Generator(device="cuda").manual_seed(3)
     b = torch.randn(nrhs, n, dtype=torch.float64, device="cuda", generator=gen)
@@ -115,16 +121,20 @@ def test_noalloc_fills_scratch_exactly_on_a_caller_stream_without_allocating(pec
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
     assert _rel(x, x_ref) < TOL
-    # the exact answer of the block-diagonal system, checked on the host
-    xb = np.linalg.solve(np.stack([A[2 * i:2 * i + 2, 2 * i:2 * i + 2].toarray() for i in range(4)]),
-                         b[:, :8].cpu().numpy().reshape(nrhs, 4, 2).transpose(1, 2, 0))
-    np.testing.assert_allclose(x[:, :8].cpu().numpy().reshape(nrhs, 4, 2).transpose(1, 2, 0), xb,
-                               rtol=1e-12, atol=1e-14)
+    # the exact answer of the first blocks, checked on the host
+    bh, xh = b.cpu().numpy(), x.cpu().numpy()
+    np.testing.assert_allclose(xh[:, 0], bh[:, 0] / 2.5, rtol=1e-14)
+    for c in range(1, 5):
+        i = 2 * c - 1
+        blk = A[i:i + 2, i:i + 2].toarray()
+        np.testing.assert_allclose(xh[:, i:i + 2], np.linalg.solve(blk, bh[:, i:i + 2].T).T,
+                                   rtol=1e-12, atol=1e-14)
     # one dof more than fits: refused before any device work
-    A2, dc2, xy2 = _block_diagonal(cap // nrhs // 2 + 1)
+    A2, dc2, xy2 = _block_diagonal(cap // nrhs // 2)
     lu2 = pg.LU(A2, dc2, xy2)
     b2 = torch.ones(nrhs, A2.shape[0], dtype=torch.float64, device="cuda")
     x2 = torch.zeros_like(b2)
     lu2.solve_device(b2.data_ptr(), x2.data_ptr(), nrhs=1)
     assert _noalloc(lu2, nrhs, b2.data_ptr(), x2.data_ptr()) == pg._ffi.PECS_E_ARG
+    assert b"scratch" in pg.lib().pecs_last_error()
     assert _noalloc(lu2, nrhs - 1, b2.data_ptr(), x2.data_ptr()) == pg._ffi.PECS_OK
