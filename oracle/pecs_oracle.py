@@ -805,11 +805,45 @@ class Problem:
 
     def lu(self, name):
         """SparseDirectUMFPACK::initialize restated by scipy's sparse LU
-        (Carrier.cpp:26-32, Poisson.cpp:90-96)."""
+        (Carrier.cpp:26-32, Poisson.cpp:90-96).  The LDG carrier matrices have
+        a symmetric pattern (flux sparsity, CarrierPair.cpp:44-48), for which
+        UMFPACK's default strategy is its symmetric one: a fill-reducing
+        ordering of A + A^T and diagonal pivots preferred down to a relative
+        tolerance of 0.001.  SuperLU's symmetric mode with the same tolerance
+        does that (a third of COLAMD's fill here).  The mixed Poisson matrix
+        keeps COLAMD with partial pivoting (its potential block has a zero
+        diagonal)."""
         if name not in self._lu:
-            A = getattr(self, "A_" + name)
-            self._lu[name] = spla.splu(A.tocsc(), permc_spec="COLAMD")
+            A = getattr(self, "A_" + name).tocsc()
+            if name == "P":
+                self._lu[name] = spla.splu(A, permc_spec="COLAMD")
+            else:
+                self._lu[name] = spla.splu(A, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.001,
+                                           options=dict(SymmetricMode=True))
         return self._lu[name]
+
+    def lu_solve(self, name, b):
+        """SparseDirectUMFPACK::solve / vmult (Carrier.cpp:34-40,
+        Poisson.cpp:98-105): deal.II hands UMFPACK the matrix with the
+        factors, and UMFPACK's default control then refines the solution (up
+        to UMFPACK_IRSTEP = 2 steps, stopping once the componentwise backward
+        error max_i |b - A x|_i / (|A| |x| + |b|)_i is at machine precision).
+        Restated with FP64 residuals."""
+        lu = self.lu(name)
+        A = getattr(self, "A_" + name)
+        if not hasattr(self, "_absA"):
+            self._absA = {}
+        if name not in self._absA:
+            self._absA[name] = abs(A).tocsr()
+        x = lu.solve(b)
+        for _ in range(2):
+            r = b - A @ x
+            den = self._absA[name] @ np.abs(x) + np.abs(b)
+            omega = np.max(np.abs(r)[den > 0] / den[den > 0]) if np.any(den > 0) else 0.0
+            if omega <= np.finfo(np.float64).eps:
+                break
+            x = x + lu.solve(r)
+        return x
 
     def _cell_points(self, grid):
         x0, y0, hx, hy = grid.cell_geom()
@@ -1038,7 +1072,7 @@ class Problem:
     def solve_poisson(self, b):
         """PoissonData::solve (Poisson.cpp:98-105): LU apply, then distribute
         (homogeneous constraints -> 0)."""
-        x = self.lu("P").solve(b)
+        x = self.lu_solve("P", b)
         x[self.pois.constrained] = 0.0
         return x
 
@@ -1048,7 +1082,7 @@ class Problem:
         new = {}
         for c in ("n", "p", "r", "o"):
             if c in rhs:
-                new[c] = self.lu(c).solve(rhs[c])
+                new[c] = self.lu_solve(c, rhs[c])
         new["P"] = self.solve_poisson(self.poisson_rhs(new))
         return new
 

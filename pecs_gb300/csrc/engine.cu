@@ -515,13 +515,17 @@ struct Engine {
   // graphs
   cudaGraphExec_t graph2[2] = {nullptr, nullptr};  // two steps starting from cur = 0 / 1
   bool graph_valid = false;
-  // refinement sweeps per solve: none for FP64 factors; ir_max_iters > 0 sets
-  // the count, < 0 disables refinement, 0 selects the default
+  // refinement sweeps per solve: ir_max_iters > 0 sets the count, < 0 disables
+  // refinement, 0 selects the default -- one for FP64 factors (the step
+  // UMFPACK's default control takes in SparseDirectUMFPACK::solve, which the
+  // reference's Carrier::solve / PoissonData::solve call, Carrier.cpp:34-40,
+  // Poisson.cpp:98-105: without it the explicit-inverse sweeps leave the
+  // Poisson field of a coupled trajectory ~1e-9 from exact arithmetic at
+  // 64x64 cells), two for FP32_IR, one for FP32_MIXED
   int ir_iters() const {
-    if (opt.precision == PECS_PREC_FP64) return 0;
     if (opt.ir_max_iters < 0) return 0;
     if (opt.ir_max_iters > 0) return opt.ir_max_iters;
-    return opt.precision == PECS_PREC_FP32_MIXED ? 1 : 2;
+    return opt.precision == PECS_PREC_FP32_IR ? 2 : 1;
   }
   // element-wise launches per set of one solve: gather, scatter and, per
   // refinement sweep, the residual and its helpers (split / widen, axpy / sum)
@@ -622,7 +626,7 @@ struct Engine {
         S_.W.alloc((size_t)bank.set_wtotal(si) * S_.R);
         S_.W.zero();
       }
-      if (opt.precision != PECS_PREC_FP64) {
+      if (ir_iters() > 0) {
         if (S_.f32) {
           S_.Rr32.alloc(nR);
           S_.D32.alloc(nR);
@@ -1573,7 +1577,7 @@ void pecs_default_options(pecs_options* opt) {
   opt->precision = PECS_PREC_FP64;
   opt->leaf_cells = 8;
   opt->use_graphs = 1;
-  opt->ir_max_iters = 2;
+  opt->ir_max_iters = 0;
   opt->ir_tol = 1e-12;
   opt->device = 0;
   opt->autotune = 1;
