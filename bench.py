@@ -22,8 +22,13 @@ Default (full) mode, one bench step = 64 held-out points:
 
 --impl reference times the CPU oracle (the restatement of the reference's
 numerics; the deal.II reference itself cannot be built here): one oracle
-process per host core, each marching a bounded sample of time steps of the
-workload, their throughputs summed.
+process per host core, each marching the plain point's time steps from the
+standard initial condition; every bench step is `--cpu-sample-steps` IMEX
+steps of every process, timed together, and `ms_per_step` is that measured
+time.  Points/sec is derived from the measured time per IMEX step and the
+plain point's steps to steady state (`profiles/steps_to_steady_state.json`,
+measured on the GPU's plain FP64 path, which marches the same discrete
+scheme).
 
 Multi-GPU: I-V points are independent, so each rank marches its own instances
 (weak scaling, no data-path collective); the barrier and max-over-ranks time
@@ -46,9 +51,6 @@ if ROOT not in sys.path:
 
 MAX_STEPS = 5000
 TOL = 1e-8
-# steps to steady state of the half cell at refinement r (measured by the GPU
-# arm; the oracle marches the same discrete scheme, so the count carries over)
-STEPS_TO_SS = {6: 3886}
 CHECK_EVERY = 50
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
 
@@ -62,7 +64,8 @@ def parse():
     ap.add_argument("--refine", type=int, default=6)
     ap.add_argument("--precision", choices=["fp64", "fp32ir", "mixed"], default="fp64")
     ap.add_argument("--n-inst", type=int, default=1, help="instances per GPU per bench step")
-    ap.add_argument("--cpu-sample-steps", type=int, default=20)
+    ap.add_argument("--cpu-sample-steps", type=int, default=8,
+                    help="IMEX steps of every oracle process per bench step of --impl reference")
     ap.add_argument("--ref-procs", type=int, default=0,
                     help="--impl reference: oracle processes (0 = one per host core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -70,6 +73,10 @@ def parse():
                     help="full: learned warm start + 64-instance batches (FP32-mixed) with the "
                          "plain FP64 path measured beside it; plain: one configuration only")
     ap.add_argument("--batch-inst", type=int, default=64)
+    ap.add_argument("--e2e-waves", type=int, default=4,
+                    help="full mode: end-to-end points = this many times --batch-inst")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="full mode: skip the FP64 accuracy references (profiling runs)")
     ap.add_argument("--model", default=os.path.join(ROOT, "pecs_gb300", "models", "warmstart_r6.npz"))
     ap.add_argument("--train-samples", type=int, default=256,
                     help="training draws when no trained model file is present")
@@ -84,9 +91,19 @@ def parse():
     return ap.parse_args()
 
 
+def check_world(args):
+    """--gpus N must match the launcher's world size (torchrun for N > 1)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world != args.gpus:
+        sys.stderr.write(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}; launch N > 1 with "
+                         f"torchrun --nproc-per-node N bench.py --gpus N\n")
+        sys.exit(2)
+    return world
+
+
 def dist_init(args):
     import torch
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    world = check_world(args)
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
@@ -187,6 +204,18 @@ def load_traffic(key: str):
         return None
 
 
+def load_steps_to_ss(refine: int):
+    """Steps to steady state of the plain point (half cell, standard initial
+    condition, FP64) at this refinement, measured by this benchmark on the GPU
+    (profiles/steps_to_steady_state.json), or None."""
+    p = os.path.join(ROOT, "profiles", "steps_to_steady_state.json")
+    try:
+        with open(p) as fh:
+            return int(json.load(fh)["steps"][str(refine)])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def workload_params(args, rank):
     import pecs_gb300 as pg
     n = args.n_inst
@@ -199,82 +228,95 @@ def workload_params(args, rank):
     return ps
 
 
-def cpu_baseline(args, steps_to_ss, sample_steps):
-    """The oracle on the host cores: a bounded sample of time steps of the
-    same workload, extrapolated to I-V points/sec with the steps to steady
-    state measured on the GPU."""
-    import oracle
-    P = oracle.half_cell_params(n_refine=args.refine)
-    pb = oracle.Problem(P)
-    st = pb.initial_state()
-    st = pb.step(st)  # first step builds the LU factors (setup, untimed)
-    t0 = time.perf_counter()
-    for _ in range(sample_steps):
-        st = pb.step(st)
-    dt = (time.perf_counter() - t0) / sample_steps
-    return {"value": 1.0 / (steps_to_ss * dt), "unit": "I-V points/s", "cores": 1, "kind": "port",
-            "sample": f"{sample_steps} IMEX steps of the 64x64+64x64 half cell on the numpy/SuperLU "
-                      f"oracle ({dt * 1e3:.1f} ms/step) x {steps_to_ss} steps to steady state"}
-
-
-def _reference_worker(refine, warmup, steps, sample_steps, barrier, out):
+def _reference_worker(refine, n_samples, sample_steps, barrier, out):
     """One oracle process: builds the problem and its LU factors (untimed),
-    then times `steps` samples of `sample_steps` IMEX steps, each sample
-    started together with the other processes."""
+    then marches the plain point from its standard initial condition, timing
+    `n_samples` samples of `sample_steps` IMEX steps, each sample started
+    together with the other processes at the barrier."""
     import oracle
     pb = oracle.Problem(oracle.half_cell_params(n_refine=refine))
-    st = pb.step(pb.initial_state())
-    for _ in range(warmup):
-        st = pb.step(st)
+    st = pb.step(pb.initial_state())   # the first step builds the factors
     per = []
-    for _ in range(steps):
+    for _ in range(n_samples):
         barrier.wait()
         t0 = time.perf_counter()
         for _ in range(sample_steps):
             st = pb.step(st)
-        per.append((time.perf_counter() - t0) / sample_steps)
+        per.append(time.perf_counter() - t0)
     out.put(per)
 
 
-def run_reference(args):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return 0
+def oracle_pool(refine, n_samples, sample_steps, procs):
+    """`procs` oracle processes (spawned; BLAS single-threaded), each timing
+    n_samples samples of sample_steps IMEX steps.  Returns (per-process
+    lists of sample seconds, wall seconds of each sample: the slowest
+    process's, since the samples start together)."""
     import multiprocessing as mp
-    # one single-threaded oracle per host core: I-V points are independent
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    if args.ref_procs > 0:
-        cores = min(cores, args.ref_procs)
     for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
         os.environ[var] = "1"
     ctx = mp.get_context("spawn")
-    barrier = ctx.Barrier(cores)
+    bar = ctx.Barrier(procs)
     out = ctx.Queue()
-    procs = [ctx.Process(target=_reference_worker,
-                         args=(args.refine, args.warmup, args.steps, args.cpu_sample_steps, barrier, out))
-             for _ in range(cores)]
-    for p in procs:
+    ps = [ctx.Process(target=_reference_worker, args=(refine, n_samples, sample_steps, bar, out))
+          for _ in range(procs)]
+    for p in ps:
         p.start()
-    per = [out.get() for _ in procs]
-    for p in procs:
+    per = [out.get() for _ in ps]
+    for p in ps:
         p.join()
-    # the oracle cannot march thousands of steps in a bounded sample
-    steps_to_ss = STEPS_TO_SS.get(args.refine, MAX_STEPS)
-    rates = [sum(1.0 / (steps_to_ss * w[k]) for w in per) for k in range(args.steps)]
-    value = statistics.mean(rates)
-    dt = statistics.mean(x for w in per for x in w)
+    wall = [max(w[k] for w in per) for k in range(n_samples)]
+    return per, wall
+
+
+def host_cores():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+def cpu_baseline(args, steps_to_ss, sample_steps=4, samples=2):
+    """The oracle on every host core (one process per core, each marching the
+    plain point), a bounded sample of IMEX steps; I-V points/sec from the
+    measured time per step and the steps to steady state that the GPU's plain
+    FP64 path measured in this run (the same discrete scheme)."""
+    procs = host_cores() if args.ref_procs <= 0 else min(host_cores(), args.ref_procs)
+    per, wall = oracle_pool(args.refine, samples, sample_steps, procs)
+    t_step = statistics.mean(wall) / sample_steps
+    return {"value": procs / (steps_to_ss * t_step), "unit": "I-V points/s", "cores": procs, "kind": "port",
+            "sample": f"{procs} oracle processes (one per host core), {samples} x {sample_steps} IMEX steps "
+                      f"each of the {2**args.refine}x{2**args.refine}+{2**args.refine}x{2**args.refine} "
+                      f"half cell ({t_step * 1e3:.1f} ms per step with all cores busy) x {steps_to_ss} "
+                      "steps to steady state"}
+
+
+def run_reference(args):
+    world = check_world(args)
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    procs = host_cores() if args.ref_procs <= 0 else min(host_cores(), args.ref_procs)
+    per, wall = oracle_pool(args.refine, args.warmup + args.steps, args.cpu_sample_steps, procs)
+    timed = wall[args.warmup:]
+    ms_step = 1e3 * statistics.mean(timed)                 # one bench step, measured
+    t_imex = statistics.mean(timed) / args.cpu_sample_steps
+    steps_to_ss = load_steps_to_ss(args.refine)
+    source = "measured on the GPU plain FP64 path (profiles/steps_to_steady_state.json)"
+    if steps_to_ss is None:
+        steps_to_ss, source = MAX_STEPS, "the step cap (no measurement for this mesh)"
+    value = procs / (steps_to_ss * t_imex)
     line = {
         "impl": "reference", "metric": "I-V points/sec to steady state", "value": value,
-        "unit": "I-V points/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "unit": "I-V points/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"half cell 2x{2**args.refine}x{2**args.refine}, k=1, dt=1e-3, "
-                               f"to steady state (<= {MAX_STEPS} steps)"},
-        "cpu_baseline": {"value": value, "unit": "I-V points/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} oracle processes, each {args.steps} x {args.cpu_sample_steps} "
-                                   f"IMEX steps ({dt * 1e3:.1f} ms/step on average), extrapolated to "
-                                   f"{steps_to_ss} steps per point"},
+                               f"to steady state (<= {MAX_STEPS} steps)",
+                   "bench_step": f"{args.cpu_sample_steps} IMEX steps of each of {procs} oracle processes",
+                   "ms_per_imex_step": t_imex * 1e3, "steps_to_steady_state": steps_to_ss,
+                   "steps_to_steady_state_source": source,
+                   "derived": "value = processes / (steps_to_steady_state x measured time per IMEX step)"},
+        "cpu_baseline": {"value": value, "unit": "I-V points/s", "cores": procs, "kind": "port",
+                         "sample": f"{procs} oracle processes, each {args.warmup} + {args.steps} x "
+                                   f"{args.cpu_sample_steps} IMEX steps of the plain point "
+                                   f"({t_imex * 1e3:.1f} ms per step with all cores busy)"},
         "e2e": {"value": value, "unit": "I-V points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -465,6 +507,67 @@ def plain_point(pg, refine, local):
     return 1.0 / (e0.elapsed_time(e1) * 1e-3), int(steps[0]), ctx
 
 
+def _fields_of(ctx, i):
+    return {f: ctx.get_state(f, i) for f in ctx.fields()}
+
+
+def _max_rel(a_list, b_list):
+    """max over points and fields of ||a - b|| / ||b||"""
+    import numpy as np
+    worst = 0.0
+    for a, b in zip(a_list, b_list):
+        for f in b:
+            worst = max(worst, float(np.linalg.norm(a[f] - b[f]) / np.linalg.norm(b[f])))
+    return worst
+
+
+def accuracy_block(pg, L, base, thetas, fin, cur, ndofs, local, op, mixed_ctx):
+    """The learned + batched answers of `thetas` (fields fin, currents cur)
+    against FP64 answers of the same points:
+      (i)  the plain method: FP64 from the standard initial condition, stopped
+           by the same relative-change rule;
+      (ii) the FP64 fixed point: (i) continued to relative change <= 1e-12;
+      (iii) precision only: the same warm starts marched in FP64.
+    Each is the max over points and fields of the relative L2 error, and the
+    max relative error of the interface current."""
+    import numpy as np
+    n = len(thetas)
+    params = [L.instance_params(t, base) for t in thetas]
+    ref = pg.Context(params, precision=pg.PREC_FP64, device=local)
+    learned = [{f: fin[f][k * ndofs[f]:(k + 1) * ndofs[f]] for f in fin} for k in range(n)]
+    ref.initialize()
+    s1, _ = ref.run_to_steady_state(MAX_STEPS, TOL, CHECK_EVERY)
+    plain = [_fields_of(ref, k) for k in range(n)]
+    I1 = ref.interface_current()
+    s2, rel2 = ref.run_to_steady_state(2 * MAX_STEPS, 1e-12, CHECK_EVERY)
+    fixed = [_fields_of(ref, k) for k in range(n)]
+    I2 = ref.interface_current()
+    # (iii) the same warm starts in FP64
+    init_n, init_p, _, keep = L.warm_start_vectors(mixed_ctx, op, thetas, base)
+    s3, I3, fin3 = ref.sweep_stream(params, MAX_STEPS, TOL, CHECK_EVERY, init_n=init_n, init_p=init_p,
+                                    want_fields=True)
+    del keep
+    same = [{f: fin3[f][k * ndofs[f]:(k + 1) * ndofs[f]] for f in fin3} for k in range(n)]
+    cur = np.asarray(cur)
+    rel = lambda a, b: float(np.max(np.abs(a - b) / np.abs(b)))   # noqa: E731
+    out = {
+        "points": n,
+        "vs_plain_fp64": {"fields_rel_l2_max": _max_rel(learned, plain), "current_rel_max": rel(cur, I1),
+                          "reference": "FP64 from the standard initial condition, same stop rule "
+                                       f"(rel. change <= {TOL})"},
+        "vs_fp64_fixed_point": {"fields_rel_l2_max": _max_rel(learned, fixed), "current_rel_max": rel(cur, I2),
+                                "reference": "FP64 marched on to rel. change <= 1e-12",
+                                "max_rel_change_reached": float(np.max(rel2))},
+        "plain_fp64_vs_fixed_point": {"fields_rel_l2_max": _max_rel(plain, fixed),
+                                      "current_rel_max": rel(I1, I2)},
+        "precision_only": {"fields_rel_l2_max": _max_rel(learned, same), "current_rel_max": rel(cur, I3),
+                           "reference": "the same warm starts marched in FP64"},
+        "plain_steps_median": float(np.median(s1)),
+    }
+    del ref
+    return out
+
+
 def run_full(args):
     """Learned + batched: held-out I-V points streamed through args.batch_inst
     slots (FP32-mixed), each warm-started by the neural operator with the
@@ -482,7 +585,7 @@ def run_full(args):
     base = pg.half_cell(n_refine=args.refine)
     # held-out draws (seed differs from the training seed), sharded by rank:
     # warm-up points, timed points, end-to-end points
-    n_w, n_t, n_e = args.warmup * B, args.steps * B, B
+    n_w, n_t, n_e = args.warmup * B, args.steps * B, args.e2e_waves * B
     per_rank = n_w + n_t + n_e
     thetas = L.sample(per_rank * world, seed=777)[rank * per_rank:(rank + 1) * per_rank]
     th_w, th_t, th_e = thetas[:n_w], thetas[n_w:n_w + n_t], thetas[n_w + n_t:]
@@ -526,7 +629,7 @@ def run_full(args):
     value = points / (ms * 1e-3)
     clocks = clk.summary()
     # ---- e2e: host parameters in, currents and final fields out, through the
-    # public API (pecs_sweep_stream), B points --------------------------------------
+    # public API (pecs_sweep_stream): e2e_waves x B points, slots refilled ----------
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     steps_e, fb_e, cur_e, fin_e = L.stream_warm_sweep(ctx, op, th_e, base, MAX_STEPS, TOL, CHECK_EVERY,
@@ -534,36 +637,30 @@ def run_full(args):
     e2e = n_e * world / max_over_ranks(time.perf_counter() - t0, world)
     h2d = n_e * (sum(info.ndofs[f] for f in range(5)) * 8 + info.ndofs[4] * 8)  # per-point constant RHS parts
     d2h = n_e * 8 + sum(a.nbytes for a in fin_e.values())
-    # ---- the same timed points, batched and streamed but without the warm start --
+    # ---- a sample of the timed points, batched and streamed without the warm start
+    n_nw = min(n_t, 4 * B)
     torch.cuda.synchronize()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2.record(stream)
-    steps_nw, _, _, _ = L.stream_warm_sweep(ctx, None, th_t, base, MAX_STEPS, TOL, CHECK_EVERY)
+    steps_nw, _, _, _ = L.stream_warm_sweep(ctx, None, th_t[:n_nw], base, MAX_STEPS, TOL, CHECK_EVERY)
     e3.record(stream)
     e3.synchronize()
-    nw_value = n_t * world / (max_over_ranks(e2.elapsed_time(e3), world) * 1e-3)
-    # ---- accuracy: the same points, same warm starts, FP64 throughout ---------------
-    nchk = 4
-    ref = pg.Context([L.instance_params(t, base) for t in th_e[:nchk]], precision=pg.PREC_FP64, device=local)
-    init_n, init_p, fb_chk, keep = L.warm_start_vectors(ctx, op, th_e[:nchk], base)
-    s64, cur64, fin64 = ref.sweep_stream([L.instance_params(t, base) for t in th_e[:nchk]], MAX_STEPS, TOL,
-                                         CHECK_EVERY, init_n=init_n, init_p=init_p, want_fields=True)
-    del keep
-    err_fields, err_cur = 0.0, 0.0
-    for i in range(nchk):
-        for f in ref.fields():
-            nd = info.ndofs[f]
-            a = fin_e[f][i * nd:(i + 1) * nd]
-            r = fin64[f][i * nd:(i + 1) * nd]
-            err_fields = max(err_fields, float(np.linalg.norm(a - r) / np.linalg.norm(r)))
-        err_cur = max(err_cur, float(abs(cur_e[i] - cur64[i]) / abs(cur64[i])))
-    steps_diff = [int(a) - 2 - int(b) for a, b in zip(steps_e[:nchk], s64)]
-    del ref
+    nw_value = n_nw * world / (max_over_ranks(e2.elapsed_time(e3), world) * 1e-3)
+    # ---- accuracy of the first B end-to-end points against FP64 answers ------------
+    acc = None
+    if not args.no_accuracy:
+        fin_b = {f: a[:B * info.ndofs[f]] for f, a in fin_e.items()}
+        acc = accuracy_block(pg, L, base, th_e[:B], fin_b, cur_e[:B], list(info.ndofs), local, op, ctx)
+    # ---- per-stage split of a time step (the reference's TimerOutput sections) ------
+    ctx.initialize()
+    stages_batched = ctx.time_stages(20)
     # ---- plain path (half cell 64x64+64x64, FP64, single instance) --------------------
     plain_value, plain_steps, pctx = plain_point(pg, args.refine, local)
     pinfo = pctx.info()
     plain_ms = pctx.time_solve(0, reps=30)
     plain_gbs = pinfo.solve_bytes[0] / (plain_ms * 1e-3) / 1e9
+    pctx.initialize()
+    stages_plain = pctx.time_stages(20)
     del pctx
     # ---- roofline: the carrier solve sweep of the batched path (panel kernels) --------
     solve_ms = ctx.time_solve(0, reps=30)
@@ -586,9 +683,10 @@ def run_full(args):
                    "l2": "flushed (512 MB write) before the timed sweep; the sweep streams ~"
                          f"{info.factor_bytes / 1e6:.0f} MB of factors per step"},
         "plain": {"value": plain_value, "unit": "I-V points/s", "steps_to_steady_state": plain_steps,
-                  "workload": "half cell 64x64+64x64, k=1: one instance, FP64, standard initial condition"},
+                  "workload": "half cell 64x64+64x64, k=1: one instance, FP64 (+1 FP64 refinement sweep per "
+                              "solve), standard initial condition"},
         "speedup_vs_plain": value / plain_value,
-        "batched_without_warm_start": {"value": nw_value, "unit": "I-V points/s",
+        "batched_without_warm_start": {"value": nw_value, "unit": "I-V points/s", "points": n_nw,
                                        "median_steps": float(np.median(steps_nw)),
                                        "mean_steps": float(np.mean(steps_nw)),
                                        "capped": int(np.sum(steps_nw >= MAX_STEPS))},
@@ -596,10 +694,12 @@ def run_full(args):
                        "capped": int(np.sum(steps_t >= MAX_STEPS + 2)),
                        "fallback_rate": float(np.mean(fb_t)), "plain_steps": plain_steps,
                        "executed_steps": executed},
-        "accuracy_vs_fp64": {"fields_rel_l2_max": err_fields, "current_rel_max": err_cur,
-                             "instances_checked": nchk, "steps_diff": steps_diff,
-                             "reference": "the same points and warm starts marched in FP64"},
-        "e2e": {"value": e2e, "unit": "I-V points/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "accuracy_vs_fp64": acc,
+        "stage_ms_per_step": {"batched_mixed": stages_batched, "plain_fp64": stages_plain,
+                              "sections": "carrier RHS, carrier solves, Poisson RHS, Poisson solve "
+                                          "(SolarCell.cpp:2057-2075 TimerOutput sections); CUDA events"},
+        "e2e": {"value": e2e, "unit": "I-V points/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "points": n_e},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": load_traffic(f"carrier_solve_r{args.refine}_mixed_b{B}"),
@@ -614,7 +714,9 @@ def run_full(args):
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args, plain_steps, args.cpu_sample_steps)
+        cb = cpu_baseline(args, plain_steps)
+        line["cpu_baseline"] = cb
+        line["plain_fp64_vs_cpu_baseline"] = plain_value / cb["value"]
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

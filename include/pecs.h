@@ -299,6 +299,13 @@ void* pecs_get_stream(pecs_ctx* ctx);
 /* Mean device time (CUDA events on the context's stream) of `reps` back-to-back
  * applications of the carrier (which = 0) or Poisson (1) factors to all RHS. */
 int pecs_time_solve(pecs_ctx* ctx, int which, int reps, double* ms_per_solve);
+/* Mean device time (CUDA events on the context's stream) of the four stages of
+ * `reps` full time steps, launched back to back after one untimed step: ms[0]
+ * carrier right-hand sides, ms[1] carrier solves, ms[2] Poisson right-hand
+ * side, ms[3] Poisson solve -- the sections the reference's TimerOutput times
+ * inside its time loop (SolarCell.cpp:2057-2075).  The steps advance the
+ * state. */
+int pecs_time_stages(pecs_ctx* ctx, int reps, double* ms);
 
 /* ---- drop-in direct solver for an externally assembled matrix ------------
  * Carrier::set_solver / PoissonData::set_solver (Carrier.cpp:26-32,

@@ -140,6 +140,7 @@ SIGNATURES = [
     ("pecs_get_stream", _vp, [_vp]),
     ("pecs_last_run_steps", C.c_int, [_vp]),
     ("pecs_time_solve", C.c_int, [_vp, C.c_int, C.c_int, _dp]),
+    ("pecs_time_stages", C.c_int, [_vp, C.c_int, _dp]),
     ("pecs_lu_factor", C.c_int, [C.c_int, _ip, _ip, _dp, _ip, _ip, C.c_int, _dp, C.c_int, C.c_int,
                                  C.POINTER(_vp)]),
     ("pecs_lu_solve", C.c_int, [_vp, C.c_int, _dp, _dp]),

@@ -467,6 +467,14 @@ class Context:
     def stream(self) -> int:
         return lib().pecs_get_stream(self._h) or 0
 
+    def time_stages(self, reps: int = 10) -> dict:
+        """Mean device milliseconds per stage of a time step (pecs_time_stages):
+        carrier RHS, carrier solves, Poisson RHS, Poisson solve.  Advances the
+        state by reps + 1 steps."""
+        ms = (C.c_double * 4)()
+        check(lib().pecs_time_stages(self._h, reps, ms))
+        return dict(zip(("carrier_rhs", "carrier_solve", "poisson_rhs", "poisson_solve"), list(ms)))
+
     def time_solve(self, which: int, reps: int = 20) -> float:
         """Mean device milliseconds of one carrier (0) / Poisson (1) solve sweep."""
         ms = C.c_double()

@@ -1852,6 +1852,39 @@ int pecs_solve_poisson(pecs_ctx* ctx) {
   })
 }
 
+int pecs_time_stages(pecs_ctx* ctx, int reps, double* ms) {
+  PECS_TRY({
+    if (!ctx || !ms || reps <= 0) throw PecsError(PECS_E_ARG, "invalid arguments");
+    Engine& e = ctx->e;
+    need_device(e);
+    if (!e.initialized) throw PecsError(PECS_E_STATE, "pecs_initialize must be called first");
+    if (e.carriers_advanced) throw PecsError(PECS_E_STATE, "a step is half done (carriers advanced)");
+    cudaEvent_t ev[5];
+    for (auto& v : ev) PECS_CUDA(cudaEventCreate(&v));
+    double acc[4] = {0, 0, 0, 0};
+    for (int r = 0; r <= reps; ++r) {  // the first step warms up, untimed
+      PECS_CUDA(cudaEventRecord(ev[0], e.st));
+      e.stage_carrier_rhs(e.st, nullptr);
+      PECS_CUDA(cudaEventRecord(ev[1], e.st));
+      e.stage_solve_carriers(e.st, nullptr);
+      PECS_CUDA(cudaEventRecord(ev[2], e.st));
+      e.stage_poisson_rhs(e.st, nullptr);
+      PECS_CUDA(cudaEventRecord(ev[3], e.st));
+      e.stage_solve_poisson(e.st, nullptr);
+      PECS_CUDA(cudaEventRecord(ev[4], e.st));
+      PECS_CUDA(cudaEventSynchronize(ev[4]));
+      if (r == 0) continue;
+      for (int k = 0; k < 4; ++k) {
+        float t = 0.f;
+        PECS_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+        acc[k] += t;
+      }
+    }
+    for (auto& v : ev) cudaEventDestroy(v);
+    for (int k = 0; k < 4; ++k) ms[k] = acc[k] / reps;
+  })
+}
+
 int pecs_step(pecs_ctx* ctx, int n_steps) {
   PECS_TRY({
     if (!ctx) throw PecsError(PECS_E_ARG, "ctx is NULL");

