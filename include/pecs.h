@@ -75,7 +75,7 @@ extern "C" {
  * value[0] applies where x < junction_x, value[1] elsewhere.
  */
 typedef struct pecs_params {
-  int degree;      /* LDG degree k (1 or 2); Poisson uses RT_{k-1} x DGQ_{k-1} */
+  int degree;      /* LDG degree k (1 or 2); Poisson element: see poisson_pairing */
   int full_system; /* 1: semiconductor + electrolyte; 0: semiconductor only */
   int nx_semi, nx_elec, ny;
   double x_semi0, x_semi1, x_elec1, height;
@@ -103,6 +103,9 @@ typedef struct pecs_params {
                              electrolyte (left unused, right, bottom, top), for layouts whose
                              sides change id at the interface (Grid.cpp:377-431); entries <= 0
                              take bc_poisson's id */
+  int poisson_pairing;    /* Poisson element: 0 = RT_{k-1} x DGQ_{k-1}, the reference's pairing
+                             (SolarCell.cpp:23-24); 1 = RT_k x DGQ_k, the pairing the benchmark
+                             configurations name */
 } pecs_params;
 
 typedef struct pecs_options {

@@ -371,6 +371,10 @@ class Params:
     # full system: ids of the Poisson mesh's outer faces over the electrolyte
     # (left unused, right, bottom, top); entries <= 0 take bc_poisson's id
     bc_poisson_elec: tuple = (0, 0, 0, 0)
+    # Poisson element: 0 = RT_{k-1} x DGQ_{k-1}, the reference's pairing
+    # (source/SolarCell.cpp:23-24); 1 = RT_k x DGQ_k, the pairing the benchmark
+    # configurations name
+    poisson_pairing: int = 0
 
     def copy(self, **kw) -> "Params":
         return dataclasses.replace(self, **kw)
@@ -776,7 +780,7 @@ class Problem:
             pg = RectGrid(self.semi_grid.xs.copy(), self.semi_grid.ys.copy(), tuple(P.bc_poisson))
             pg.material = np.zeros(pg.nc, dtype=np.int64)
         self.poisson_grid = pg
-        self.pois = make_poisson_space(pg, k, ce)
+        self.pois = make_poisson_space(pg, k + P.poisson_pairing, ce)
         # carrier cell -> Poisson cell maps (setup_mappings, SolarCell.cpp:264-372)
         si, sj = self.semi_grid.cell_ij()
         self.s2p = si + pg.nx * sj

@@ -42,7 +42,7 @@ class pecs_params(C.Structure):
         ("ic_kind", C.c_int), ("gen_kind", C.c_int), ("G0", C.c_double), ("alpha", C.c_double),
         ("srh", C.c_int), ("tau_n", C.c_double), ("tau_p", C.c_double), ("n_i", C.c_double),
         ("phi_bi", C.c_double), ("phi_app", C.c_double), ("s_n", C.c_double), ("s_p", C.c_double),
-        ("grading", C.c_double), ("bc_poisson_elec", C.c_int * 4),
+        ("grading", C.c_double), ("bc_poisson_elec", C.c_int * 4), ("poisson_pairing", C.c_int),
     ]
 
 

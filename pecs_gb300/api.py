@@ -64,6 +64,7 @@ class Params:
     s_p: float = 0.0
     grading: float = 1.0  # widest/narrowest cell along x, finest at the interface (1: uniform)
     bc_poisson_elec: tuple = (0, 0, 0, 0)  # Poisson outer-face ids over the electrolyte (<= 0: bc_poisson)
+    poisson_pairing: int = 0  # 0: RT_{k-1} x DGQ_{k-1} (the reference's), 1: RT_k x DGQ_k (the configurations')
 
     def copy(self, **kw) -> "Params":
         return dataclasses.replace(self, **kw)

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -1101,18 +1102,25 @@ struct Engine {
     const double* spe = S->has_schottky ? sch_pe.p : nullptr;
     const bool mixed = opt.precision == PECS_PREC_FP32_MIXED;
     const int nreg = full ? 2 : 1;
-    if (S->k == 1 && !mixed)
-      k_carrier_rhs<1, double><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
-                                                    iface_pe.p, nif, sne, spe, act);
-    else if (S->k == 1)
-      k_carrier_rhs<1, float><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
-                                                   iface_pe.p, nif, sne, spe, act);
-    else if (!mixed)
-      k_carrier_rhs<2, double><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
-                                                    iface_pe.p, nif, sne, spe, act);
+    // (LDG degree, Poisson table degree): the reference's RT_{k-1} x DGQ_{k-1}
+    // pairing has KP = k, the configurations' RT_k x DGQ_k KP = k + 1
+    auto go = [&](auto kk, auto kp) {
+      constexpr int K = decltype(kk)::value, KP = decltype(kp)::value;
+      if (mixed)
+        k_carrier_rhs<K, KP, float><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
+                                                         iface_pe.p, nif, sne, spe, act);
+      else
+        k_carrier_rhs<K, KP, double><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
+                                                          iface_pe.p, nif, sne, spe, act);
+    };
+    using I1 = std::integral_constant<int, 1>;
+    using I2 = std::integral_constant<int, 2>;
+    using I3 = std::integral_constant<int, 3>;
+    const int kp = S->pt.k;
+    if (S->k == 1)
+      kp == 1 ? go(I1{}, I1{}) : go(I1{}, I2{});
     else
-      k_carrier_rhs<2, float><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, inst.p, iface_ne.p,
-                                                   iface_pe.p, nif, sne, spe, act);
+      kp == 2 ? go(I2{}, I2{}) : go(I2{}, I3{});
     PECS_CUDA(cudaGetLastError());
   }
 
@@ -1121,10 +1129,15 @@ struct Engine {
     const int ncells = R[0].nc + (full ? R[1].nc : 0);
     const int n = std::max(ncells, S->pois.n_rt_total);
     dim3 grid((n + 127) / 128, n_inst);
-    if (S->k == 1)
-      k_poisson_rhs<1><<<grid, 128, 0, s>>>(T, R[0], R[1], full ? 2 : 1, F, S->pois.n_rt_total, act);
+    const int kp = S->pt.k, nreg = full ? 2 : 1, nrt = S->pois.n_rt_total;
+    if (S->k == 1 && kp == 1)
+      k_poisson_rhs<1, 1><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, nrt, act);
+    else if (S->k == 1)
+      k_poisson_rhs<1, 2><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, nrt, act);
+    else if (kp == 2)
+      k_poisson_rhs<2, 2><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, nrt, act);
     else
-      k_poisson_rhs<2><<<grid, 128, 0, s>>>(T, R[0], R[1], full ? 2 : 1, F, S->pois.n_rt_total, act);
+      k_poisson_rhs<2, 3><<<grid, 128, 0, s>>>(T, R[0], R[1], nreg, F, nrt, act);
     PECS_CUDA(cudaGetLastError());
   }
 

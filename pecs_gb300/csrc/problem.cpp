@@ -297,6 +297,7 @@ std::string validate_params(const pecs_params* p, int n_inst) {
   if (n_inst < 1) return "n_inst must be >= 1";
   const pecs_params& a = p[0];
   if (a.degree < 1 || a.degree > 2) e << "degree must be 1 or 2; ";
+  if (a.poisson_pairing != 0 && a.poisson_pairing != 1) e << "poisson_pairing must be 0 or 1; ";
   if (a.nx_semi < 2 || a.ny < 2 || (a.full_system && a.nx_elec < 2)) e << "mesh too small; ";
   if (a.nx_semi > 4096 || a.ny > 4096 || a.nx_elec > 4096) e << "mesh too large; ";
   if (!(a.dt > 0) || !(a.lambda2 > 0) || !(a.eps_semi > 0) || (a.full_system && !(a.eps_elec > 0)))
@@ -319,6 +320,7 @@ std::string validate_params(const pecs_params* p, int n_inst) {
       if (!eq) diff += std::string(diff.empty() ? "" : ", ") + name;
     };
     chk(a.degree == b.degree, "degree");
+    chk(a.poisson_pairing == b.poisson_pairing, "poisson_pairing");
     chk(a.full_system == b.full_system, "full_system");
     chk(a.nx_semi == b.nx_semi && a.nx_elec == b.nx_elec && a.ny == b.ny, "cell counts");
     chk(a.x_semi0 == b.x_semi0 && a.x_semi1 == b.x_semi1 && a.x_elec1 == b.x_elec1 && a.height == b.height,
@@ -631,7 +633,7 @@ static void setup_poisson(PoissonSystem& S, const PoissonTables& pt, const Carri
 }
 
 Setup::Setup(const std::vector<pecs_params>& p)
-    : inst(p), ct(p[0].degree), pt(p[0].degree, ct) {
+    : inst(p), ct(p[0].degree), pt(p[0].degree + p[0].poisson_pairing, ct) {
   const pecs_params& P = p[0];
   k = P.degree;
   n1 = ct.n1;

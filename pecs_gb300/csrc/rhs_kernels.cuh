@@ -73,13 +73,16 @@ struct FieldPtrs {
   int nd[5];
 };
 
-template <int K>
+// K: LDG degree; KP - 1: degree of the Poisson element RT_{KP-1} x DGQ_{KP-1}
+// (KP = K: the reference's pairing, SolarCell.cpp:23-24; KP = K + 1: the
+// RT_K x DGQ_K pairing of the benchmark configurations)
+template <int K, int KP>
 struct Dims {
   static constexpr int n1 = (K + 1) * (K + 1);
   static constexpr int nq = K + 2;
   static constexpr int Q = nq * nq;
-  static constexpr int nrt = 2 * K * (K + 1);
-  static constexpr int nphi = K * K;
+  static constexpr int nrt = 2 * KP * (KP + 1);
+  static constexpr int nphi = KP * KP;
 };
 
 // state values into the quadrature type, and quadrature sums back: on the
@@ -111,13 +114,13 @@ __device__ __forceinline__ const float* tab<float>(const double*, const float* f
 // sum_bc T_abc u_b D_c with precomputed tensors -- while the small
 // recombination and interface terms run on the FP32 pipe (GB300 issues FP32
 // FMAs ~60x faster than FP64).
-template <int K, typename Tq>
+template <int K, int KP, typename Tq>
 __global__ void __launch_bounds__(128)
     k_carrier_rhs(Tables T, RegionDev semi, RegionDev elec, int n_regions, FieldPtrs F,
                   const InstDev* __restrict__ inst, const double* __restrict__ iface_ne,
                   const double* __restrict__ iface_pe, int n_iface, const double* __restrict__ sch_ne,
                   const double* __restrict__ sch_pe, const int* __restrict__ active) {
-  using D = Dims<K>;
+  using D = Dims<K, KP>;
   constexpr int n1 = D::n1, nq = D::nq, Q = D::Q, nrt = D::nrt;
   const int i = blockIdx.y;
   if (active && !active[i]) return;
@@ -308,11 +311,11 @@ __global__ void __launch_bounds__(128)
 }
 
 // grid: x over max(n_rt_total, cells of both regions), y over instances
-template <int K>
+template <int K, int KP>
 __global__ void __launch_bounds__(128)
     k_poisson_rhs(Tables T, RegionDev semi, RegionDev elec, int n_regions, FieldPtrs F,
                   int n_rt_total, const int* __restrict__ active) {
-  using D = Dims<K>;
+  using D = Dims<K, KP>;
   constexpr int n1 = D::n1, Q = D::Q, nphi = D::nphi;
   const int i = blockIdx.y;
   if (active && !active[i]) return;

@@ -88,7 +88,8 @@ class Layout:
         ndp = ctx.ndofs[F.FIELD_POISSON]
         p0 = ctx.params[0]
         ncell_p = (p0.nx_semi + (p0.nx_elec if p0.full_system else 0)) * p0.ny
-        n_phi = ncell_p * (p0.degree * p0.degree)
+        kp = p0.degree + int(getattr(p0, "poisson_pairing", 0))   # DGQ_{kp-1} potential
+        n_phi = ncell_p * kp * kp
         return Layout(nd, n_u, 2 * n_u, ndp, n_phi, ndp - n_phi)
 
 

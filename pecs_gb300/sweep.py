@@ -56,7 +56,7 @@ def distributed_sweep(params: Sequence, compute: Callable[[list], list], group=N
 # that agree on them can share a context (validate_params checks the same set)
 MATRIX_FIELDS = ("degree", "full_system", "nx_semi", "nx_elec", "ny", "x_semi0", "x_semi1", "x_elec1",
                  "height", "lambda2", "eps_semi", "eps_elec", "mu", "dt", "penalty", "bc_semi",
-                 "bc_elec", "bc_poisson", "grading", "bc_poisson_elec")
+                 "bc_elec", "bc_poisson", "grading", "bc_poisson_elec", "poisson_pairing")
 
 
 def matrix_key(p) -> tuple:

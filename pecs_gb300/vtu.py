@@ -157,8 +157,9 @@ def write_carriers(ctx, path: str, inst: int = 0, region: str = "semi",
 
 
 def poisson_field_at(v, nx: int, ny: int, k: int, t) -> np.ndarray:
-    """The displacement D of a Poisson vector v (RT_{k-1} x DGQ_{k-1} for LDG
-    degree k, layout above) at the points t x t of every cell of the nx x ny
+    """The displacement D of a Poisson vector v (RT_{k-1} x DGQ_{k-1}: k is the
+    LDG degree for the reference's pairing, the LDG degree + 1 for RT_k x DGQ_k;
+    layout above) at the points t x t of every cell of the nx x ny
     Poisson mesh -> (nc * len(t)^2, 2), points x fastest."""
     nc = nx * ny
     nvert, nhor = (nx + 1) * ny, nx * (ny + 1)
@@ -202,7 +203,7 @@ def write_poisson(ctx, path: str, inst: int = 0, scales: Scales = Scales(),
     "Field" (D, a vector) and "Potential", point data on per-cell patches."""
     from .learned import Layout
     p = ctx.params[inst]
-    k = p.degree
+    k = p.degree + int(getattr(p, "poisson_pairing", 0))   # RT_{k-1} x DGQ_{k-1}
     lay = Layout.of(ctx)
     xs, ys = ctx.mesh(F.MESH_POISSON)
     nx, ny = len(xs) - 1, len(ys) - 1

@@ -54,9 +54,11 @@ def test_lu_device_solve_matches_scipy(pecs_lib):
                                oracle.reference_params(3, 1, dt=1e-4),
                                oracle.half_cell_params(n_refine=2, degree=2),
                                oracle.half_cell_params(n_refine=3, ny=4, grading=8.0),
-                               INSULATED_SCHOTTKY],
+                               INSULATED_SCHOTTKY,
+                               oracle.half_cell_params(n_refine=3, poisson_pairing=1),
+                               oracle.half_cell_params(n_refine=2, degree=2, poisson_pairing=1)],
                          ids=["halfcell_r3", "pn_junction", "reference_r3", "halfcell_r2_k2",
-                              "halfcell_graded", "insulated_schottky"])
+                              "halfcell_graded", "insulated_schottky", "halfcell_r3_rt1", "halfcell_r2_k2_rt2"])
 def test_initial_state_and_rhs(pecs_lib, P):
     pb = oracle.Problem(P)
     st = pb.initial_state()
@@ -77,9 +79,14 @@ def test_initial_state_and_rhs(pecs_lib, P):
                                      # graded toward the interface, non-square cells
                                      (oracle.half_cell_params(n_refine=3, ny=4, grading=8.0), 20),
                                      (oracle.half_cell_params(n_refine=2, degree=2, ny=8, grading=4.0), 10),
-                                     (INSULATED_SCHOTTKY, 20)],
+                                     (INSULATED_SCHOTTKY, 20),
+                                     # the configurations' RT_k x DGQ_k Poisson pairing
+                                     (oracle.half_cell_params(n_refine=3, poisson_pairing=1), 20),
+                                     (oracle.half_cell_params(n_refine=2, degree=2, poisson_pairing=1), 10),
+                                     (oracle.pn_junction_params(poisson_pairing=1), 100)],
                          ids=["halfcell_r3", "pn_junction_100", "reference_r3", "halfcell_r2_k2", "mu_distinct",
-                              "halfcell_graded", "halfcell_k2_graded", "insulated_schottky"])
+                              "halfcell_graded", "halfcell_k2_graded", "insulated_schottky", "halfcell_r3_rt1",
+                              "halfcell_r2_k2_rt2", "pn_junction_rt1_100"])
 def test_trajectory_matches_oracle(pecs_lib, P, steps):
     pb = oracle.Problem(P)
     st, _, _ = pb.run(steps)
@@ -342,9 +349,20 @@ def test_bench_mesh_batched_fp64_and_mixed(pecs_lib, bench_mesh_oracle):
     cmx.initialize()
     cmx.step(BENCH_STEPS)
     I64, Imx = c64.interface_current(), cmx.interface_current()
-    worst = 0.0
+    nc, n1, nrt = pb.semi.nc, pb.semi.n1, pb.pois.n_rt
+    w = {"densities": 0.0, "J": 0.0, "potential": 0.0, "D": 0.0}
     for i in range(len(Ps)):
         for f in c64.fields():
-            worst = max(worst, rel_err(cmx.get_state(f, i), c64.get_state(f, i)))
-    assert worst < 1e-6, worst
-    assert np.max(np.abs(Imx - I64) / np.abs(I64)) < 1e-6
+            a, b = cmx.get_state(f, i), c64.get_state(f, i)
+            if f == pg.FIELD_POISSON:
+                w["potential"] = max(w["potential"], rel_err(a[nrt:], b[nrt:]))
+                w["D"] = max(w["D"], rel_err(a[:nrt], b[:nrt]))
+            else:
+                w["densities"] = max(w["densities"], rel_err(a[2 * nc * n1:], b[2 * nc * n1:]))
+                w["J"] = max(w["J"], rel_err(a[:2 * nc * n1], b[:2 * nc * n1]))
+    w["current"] = float(np.max(np.abs(Imx - I64) / np.abs(I64)))
+    print("mixed vs FP64, 64 instances after", BENCH_STEPS, "steps:", {k: f"{v:.2e}" for k, v in w.items()})
+    # the throughput mode's bound on the quantities the metric reads; the
+    # derived fluxes J and D amplify rounding (see BENCH_TOL) and get 10x
+    for k, v in w.items():
+        assert v < (1e-5 if k in ("J", "D") else 1e-6), (k, w)

@@ -11,6 +11,8 @@ from oracle.manufactured import ldg_imex_errors, poisson_mixed_errors, rates
 @pytest.mark.parametrize("k,levels,phi_rate,d_rate", [
     (1, range(2, 6), 1.0, 2.0),   # DGQ0 potential O(h); RT0 flux (x/y-separable solution) O(h^2)
     (2, range(1, 5), 2.0, 3.0),   # DGQ1 potential O(h^2); RT1 flux O(h^3)
+    (3, range(1, 5), 3.0, 4.0),   # DGQ2 potential O(h^3); RT2 flux O(h^4): the RT_k x DGQ_k
+                                  # pairing of the configurations at LDG degree 2
 ])
 def test_mixed_poisson_convergence(k, levels, phi_rate, d_rate):
     E = [poisson_mixed_errors(n, k) for n in levels]

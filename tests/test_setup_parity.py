@@ -19,6 +19,10 @@ CASES = [
     ("halfcell_r3_graded", oracle.half_cell_params(n_refine=3, grading=8.0)),
     ("halfcell_r2_k2_graded", oracle.half_cell_params(n_refine=2, degree=2, ny=8, grading=4.0)),
     ("pn_junction_graded", oracle.pn_junction_params(grading=5.0)),
+    # the configurations' RT_k x DGQ_k Poisson pairing
+    ("halfcell_r3_rt1", oracle.half_cell_params(n_refine=3, poisson_pairing=1)),
+    ("halfcell_r2_k2_rt2", oracle.half_cell_params(n_refine=2, degree=2, poisson_pairing=1)),
+    ("pn_junction_rt1_graded", oracle.pn_junction_params(poisson_pairing=1, grading=3.0)),
 ]
 
 
@@ -58,6 +62,12 @@ def test_invalid_params_are_rejected(pecs_lib):
         pg.Context(pg.half_cell(n_refine=2, degree=3), host_setup_only=True)
     with pytest.raises(pg.PecsError):
         pg.Context(pg.half_cell(n_refine=2, dt=0.0), host_setup_only=True)
+    with pytest.raises(pg.PecsError):
+        pg.Context(pg.half_cell(n_refine=2, poisson_pairing=2), host_setup_only=True)
+    with pytest.raises(pg.PecsError) as e:   # the pairing defines the Poisson matrix
+        pg.Context([pg.half_cell(n_refine=2), pg.half_cell(n_refine=2, poisson_pairing=1)],
+                   host_setup_only=True)
+    assert "poisson_pairing" in str(e.value)
     a = pg.half_cell(n_refine=2)
     b = pg.half_cell(n_refine=3)
     with pytest.raises(pg.PecsError):
