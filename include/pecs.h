@@ -310,6 +310,45 @@ int pecs_time_solve(pecs_ctx* ctx, int which, int reps, double* ms_per_solve);
  * state. */
 int pecs_time_stages(pecs_ctx* ctx, int reps, double* ms);
 
+/* ---- element matrices of the reference's local assembly members ----------
+ * Host only.  One axis-aligned cell (the data a deal.II cell iterator gives
+ * the reference's assembly): its size, the boundary id of each face (left,
+ * right, bottom, top; -1 = interior) and its material id (0, 1
+ * semiconductor, 2, 3 electrolyte).  Outputs are row-major; carrier local
+ * dofs [J_x (n1) | J_y (n1) | u (n1)], n1 = (k+1)^2; Poisson local dofs
+ * [D_x | D_y | Phi] of the library's nodal RT basis.  pecs_element_sizes
+ * gives the block sizes. */
+typedef struct pecs_cell {
+  double hx, hy;
+  int boundary_id[4];
+  int material_id;
+} pecs_cell;
+int pecs_element_sizes(int degree, int poisson_pairing, int* carrier_dofs, int* poisson_rt_dofs,
+                       int* poisson_phi_dofs);
+/* LDG::assemble_local_LDG_mass_matrix (LDG.cpp:40-83): (1/delta_t) v u on the
+ * density block, zero elsewhere. */
+int pecs_ldg_local_mass_matrix(int degree, const pecs_cell* cell, double delta_t, double* out);
+/* LDG::assemble_local_LDG_cell_and_bc_terms (LDG.cpp:85-281) for both carriers
+ * of a pair: (transient_or_steady/delta_t) v u + (1/mu) p.q - div(p) u -
+ * grad(v).q, Dirichlet faces v (n.q + penalty/h u), other boundary faces
+ * (p.n) u; h = the cell diagonal (cell->diameter(), LDG.cpp:117). */
+int pecs_ldg_local_cell_and_bc_terms(int degree, const pecs_cell* cell, double mobility_1,
+                                     double mobility_2, double delta_t, double transient_or_steady,
+                                     double penalty, double* out_1, double* out_2);
+/* LDG::assemble_local_flux_terms (LDG.cpp:429-622) on the face `face` of cell
+ * (interior side i) shared with neighbor (exterior side e, its opposite
+ * face): the blocks vi_ui, vi_ue, ve_ui, ve_ue with the reference's flux --
+ * averages of p.n and v, beta.p with beta = (1,1)/sqrt(2) (LDG.cpp:455-501)
+ * and penalty / min(h_i, h_e) -- as its assemble_flux_terms loop calls it
+ * from the lower-numbered cell (the left / bottom one on these meshes). */
+int pecs_ldg_local_flux_terms(int degree, const pecs_cell* cell, int face, const pecs_cell* neighbor,
+                              double penalty, double* vi_ui, double* vi_ue, double* ve_ui, double* ve_ue);
+/* MixedFEM::assemble_local_Poisson_matrix (MixedFEM.cpp:29-164):
+ * p.(1/eps) D - div(p) Phi - lambda^2 v div(D), eps by the cell's material. */
+int pecs_mixed_local_poisson_matrix(int degree, int poisson_pairing, const pecs_cell* cell,
+                                    double semi_permittivity, double elec_permittivity,
+                                    double scaled_debye_length, double* out);
+
 /* ---- drop-in direct solver for an externally assembled matrix ------------
  * Carrier::set_solver / PoissonData::set_solver (Carrier.cpp:26-32,
  * Poisson.cpp:90-96) and their solve() (Carrier.cpp:34-40, Poisson.cpp:98-105).

@@ -141,6 +141,13 @@ SIGNATURES = [
     ("pecs_last_run_steps", C.c_int, [_vp]),
     ("pecs_time_solve", C.c_int, [_vp, C.c_int, C.c_int, _dp]),
     ("pecs_time_stages", C.c_int, [_vp, C.c_int, _dp]),
+    ("pecs_element_sizes", C.c_int, [C.c_int, C.c_int, _ip, _ip, _ip]),
+    ("pecs_ldg_local_mass_matrix", C.c_int, [C.c_int, _vp, C.c_double, _dp]),
+    ("pecs_ldg_local_cell_and_bc_terms", C.c_int, [C.c_int, _vp, C.c_double, C.c_double, C.c_double,
+                                                   C.c_double, C.c_double, _dp, _dp]),
+    ("pecs_ldg_local_flux_terms", C.c_int, [C.c_int, _vp, C.c_int, _vp, C.c_double, _dp, _dp, _dp, _dp]),
+    ("pecs_mixed_local_poisson_matrix", C.c_int, [C.c_int, C.c_int, _vp, C.c_double, C.c_double,
+                                                  C.c_double, _dp]),
     ("pecs_lu_factor", C.c_int, [C.c_int, _ip, _ip, _dp, _ip, _ip, C.c_int, _dp, C.c_int, C.c_int,
                                  C.POINTER(_vp)]),
     ("pecs_lu_solve", C.c_int, [_vp, C.c_int, _dp, _dp]),

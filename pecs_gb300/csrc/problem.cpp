@@ -884,3 +884,132 @@ void Setup::compute_instance(int s) {
 }
 
 }  // namespace pecs
+
+// ---------------------------------------------------------------------------
+// Element matrices for the drop-in assembly classes (host only): what the
+// reference's local assembly members compute for one cell, on the library's
+// element tables.  Matrices are row-major; carrier local dofs are
+// [J_x (n1) | J_y (n1) | u (n1)], n1 = (k+1)^2; Poisson local dofs
+// [D_x | D_y | Phi] of the nodal RT basis (fe.hpp).
+// ---------------------------------------------------------------------------
+namespace pecs {
+void set_error_external(const std::string& m);
+}
+
+namespace {
+
+bool cell_ok(const pecs_cell* c, std::string& err) {
+  if (!c) {
+    err = "cell is NULL";
+    return false;
+  }
+  if (!(c->hx > 0.0) || !(c->hy > 0.0) || !std::isfinite(c->hx) || !std::isfinite(c->hy)) {
+    err = "cell sizes must be positive and finite";
+    return false;
+  }
+  for (int f = 0; f < 4; ++f)
+    if (c->boundary_id[f] < -1 || c->boundary_id[f] > 3) {
+      err = "boundary ids must be -1 (interior) or 0..3";
+      return false;
+    }
+  return true;
+}
+
+int fail(const std::string& m) {
+  pecs::set_error_external(m);
+  return PECS_E_ARG;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pecs_ldg_local_mass_matrix(int degree, const pecs_cell* cell, double delta_t, double* out) {
+  using namespace pecs;
+  std::string err;
+  if (degree < 1 || degree > 2) return fail("degree must be 1 or 2");
+  if (!cell_ok(cell, err)) return fail(err);
+  if (!(delta_t > 0.0) || !out) return fail("delta_t must be > 0 and out not NULL");
+  CarrierTables ct(degree);
+  const int n1 = ct.n1, nd = 3 * n1;
+  std::fill(out, out + nd * nd, 0.0);
+  for (int a = 0; a < n1; ++a)
+    for (int b = 0; b < n1; ++b) {
+      double s = 0.0;
+      for (int q = 0; q < ct.Q; ++q)
+        s += (1.0 / delta_t) * ct.phi[a * ct.Q + q] * ct.phi[b * ct.Q + q] * ct.qw[q] * cell->hx * cell->hy;
+      out[(2 * n1 + a) * nd + 2 * n1 + b] = s;
+    }
+  return PECS_OK;
+}
+
+int pecs_ldg_local_cell_and_bc_terms(int degree, const pecs_cell* cell, double mobility_1,
+                                     double mobility_2, double delta_t, double transient_or_steady,
+                                     double penalty, double* out_1, double* out_2) {
+  using namespace pecs;
+  std::string err;
+  if (degree < 1 || degree > 2) return fail("degree must be 1 or 2");
+  if (!cell_ok(cell, err)) return fail(err);
+  if (!(mobility_1 > 0.0) || !(mobility_2 > 0.0) || !(delta_t > 0.0) || !out_1 || !out_2)
+    return fail("mobilities and delta_t must be > 0, outputs not NULL");
+  CarrierTables ct(degree);
+  const double diam = std::sqrt(cell->hx * cell->hx + cell->hy * cell->hy);  // cell->diameter()
+  const std::vector<double> A1 = ldg_cell_matrix(ct, cell->hx, cell->hy, mobility_1, delta_t,
+                                                 transient_or_steady, penalty / diam, cell->boundary_id);
+  const std::vector<double> A2 = ldg_cell_matrix(ct, cell->hx, cell->hy, mobility_2, delta_t,
+                                                 transient_or_steady, penalty / diam, cell->boundary_id);
+  std::copy(A1.begin(), A1.end(), out_1);
+  std::copy(A2.begin(), A2.end(), out_2);
+  return PECS_OK;
+}
+
+int pecs_ldg_local_flux_terms(int degree, const pecs_cell* cell, int face, const pecs_cell* neighbor,
+                              double penalty, double* vi_ui, double* vi_ue, double* ve_ui, double* ve_ue) {
+  using namespace pecs;
+  std::string err;
+  if (degree < 1 || degree > 2) return fail("degree must be 1 or 2");
+  if (!cell_ok(cell, err) || !cell_ok(neighbor, err)) return fail(err);
+  if (face < 0 || face > 3) return fail("face must be 0..3");
+  if (!vi_ui || !vi_ue || !ve_ui || !ve_ue) return fail("outputs must not be NULL");
+  CarrierTables ct(degree);
+  const double flen = (face == kLeft || face == kRight) ? cell->hy : cell->hx;
+  const double h = std::min(std::sqrt(cell->hx * cell->hx + cell->hy * cell->hy),
+                            std::sqrt(neighbor->hx * neighbor->hx + neighbor->hy * neighbor->hy));
+  std::vector<double> blk[4];
+  ldg_flux_blocks(ct, face, face ^ 1, flen, penalty / h, blk);
+  double* outs[4] = {vi_ui, vi_ue, ve_ui, ve_ue};
+  for (int t = 0; t < 4; ++t) std::copy(blk[t].begin(), blk[t].end(), outs[t]);
+  return PECS_OK;
+}
+
+int pecs_mixed_local_poisson_matrix(int degree, int poisson_pairing, const pecs_cell* cell,
+                                    double semi_permittivity, double elec_permittivity,
+                                    double scaled_debye_length, double* out) {
+  using namespace pecs;
+  std::string err;
+  if (degree < 1 || degree > 2) return fail("degree must be 1 or 2");
+  if (poisson_pairing != 0 && poisson_pairing != 1) return fail("poisson_pairing must be 0 or 1");
+  if (!cell_ok(cell, err)) return fail(err);
+  if (!out || !(semi_permittivity > 0.0) || !(elec_permittivity > 0.0) || !(scaled_debye_length > 0.0))
+    return fail("permittivities and the Debye length must be > 0, out not NULL");
+  CarrierTables ct(degree);
+  PoissonTables pt(degree + poisson_pairing, ct);
+  // material ids 0, 1: semiconductor; 2, 3: electrolyte (MixedFEM.hpp:226-236)
+  const double eps = cell->material_id <= 1 ? semi_permittivity : elec_permittivity;
+  const std::vector<double> A = poisson_cell_matrix(pt, ct, cell->hx, cell->hy, eps, scaled_debye_length);
+  std::copy(A.begin(), A.end(), out);
+  return PECS_OK;
+}
+
+int pecs_element_sizes(int degree, int poisson_pairing, int* carrier_dofs, int* poisson_rt_dofs,
+                       int* poisson_phi_dofs) {
+  if (degree < 1 || degree > 2) return fail("degree must be 1 or 2");
+  if (poisson_pairing != 0 && poisson_pairing != 1) return fail("poisson_pairing must be 0 or 1");
+  const int kp = degree + poisson_pairing;
+  if (carrier_dofs) *carrier_dofs = 3 * (degree + 1) * (degree + 1);
+  if (poisson_rt_dofs) *poisson_rt_dofs = 2 * kp * (kp + 1);
+  if (poisson_phi_dofs) *poisson_phi_dofs = kp * kp;
+  return PECS_OK;
+}
+
+}  // extern "C"
