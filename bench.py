@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiler mode: initialise the workload, run this many time steps "
                          "with direct (non-graph) launches, print one line and exit")
+    ap.add_argument("--level-times", action="store_true",
+                    help="with --profile-sweep (FP32 sweeps): also time every level of the sweep")
     ap.add_argument("--profile-sweep", choices=["carrier", "poisson"], default=None,
                     help="profiler mode: build the workload and run exactly two solve sweeps of "
                          "one bank (a warm-up and a timed one), print one line and exit")
@@ -346,10 +348,19 @@ def run_profile_sweep(args):
     which = 0 if args.profile_sweep == "carrier" else 1
     info = ctx.info()
     ms = ctx.time_solve(which, reps=1)
-    print(json.dumps({"profile_sweep": args.profile_sweep, "n_inst": args.n_inst, "precision": args.precision,
-                      "sweep_ms": ms, "launches_per_sweep": info.solve_launches[which],
-                      "bytes_per_sweep": info.solve_bytes[which], "launches_setup": info.setup_launches,
-                      "tuned_sweep_ms": list(info.tuned_sweep_ms)}))
+    out = {"profile_sweep": args.profile_sweep, "n_inst": args.n_inst, "precision": args.precision,
+           "sweep_ms": ms, "launches_per_sweep": info.solve_launches[which],
+           "bytes_per_sweep": info.solve_bytes[which], "launches_setup": info.setup_launches,
+           "tuned_sweep_ms": list(info.tuned_sweep_ms)}
+    if args.level_times and args.precision != "fp64":
+        import ctypes as C
+        buf = (C.c_double * 64)()
+        n = pg.lib().pecs_debug_time_levels(ctx._h, which, 20, buf, 64)
+        if n < 0:
+            pg._ffi.check(n)
+        out["level_ms"] = [round(buf[k], 4) for k in range(n)]
+        out["sweep_ms_20"] = ctx.time_solve(which, reps=20)
+    print(json.dumps(out))
     return 0
 
 

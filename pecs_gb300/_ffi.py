@@ -156,6 +156,7 @@ SIGNATURES = [
     ("pecs_lu_destroy", None, [_vp]),
     ("pecs_lu_solve_device_noalloc", C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     ("pecs_lu_host_apply", C.c_int, [_vp, _dp, _dp]),
+    ("pecs_debug_time_levels", C.c_int, [_vp, C.c_int, C.c_int, _dp, C.c_int]),
     ("pecs_mlp_create", C.c_int, [C.c_int, _ip, C.c_ulonglong, C.POINTER(_vp)]),
     ("pecs_mlp_destroy", None, [_vp]),
     ("pecs_mlp_n_params", C.c_int, [_vp, C.POINTER(C.c_longlong)]),

@@ -2231,6 +2231,26 @@ int pecs_lu_solve_device_noalloc(pecs_lu* lu, int nrhs, const double* b_dev, dou
   })
 }
 
+// diagnostic: per-level device times of one carrier (which = 0) or Poisson (1)
+// sweep of an FP32 panel bank; returns the number of levels written
+int pecs_debug_time_levels(pecs_ctx* ctx, int which, int reps, double* ms, int cap) {
+  int n = 0;
+  const int rc = [&]() -> int {
+    PECS_TRY({
+      if (!ctx || !ms || cap <= 0 || reps <= 0 || (which != 0 && which != 1))
+        throw PecsError(PECS_E_ARG, "invalid arguments");
+      Engine& e = ctx->e;
+      need_device(e);
+      if (!e.il_f32(which)) throw PecsError(PECS_E_STATE, "level timing needs FP32 panel sweeps");
+      const FactorBank& B = which == 0 ? e.bank_c : e.bank_p;
+      const std::vector<double> t = B.time_levels(e.il_view_f(which, false), e.il[which].max_R, e.st, reps);
+      n = std::min(cap, (int)t.size());
+      for (int k = 0; k < n; ++k) ms[k] = t[k];
+    })
+  }();
+  return rc == PECS_OK ? n : rc;
+}
+
 // diagnostic: apply the host copy of the factors (no GPU involved)
 int pecs_lu_host_apply(pecs_lu* lu, const double* b, double* x) {
   PECS_TRY({

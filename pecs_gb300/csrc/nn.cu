@@ -5,8 +5,8 @@
 // the reference: it is the warm-start component the benchmark adds.
 //
 // Arithmetic: GEMM operands are BF16 (weights stored in BF16, activations
-// rounded to BF16 when staged), accumulation FP32; FP32 master weights and
-// Adam moments.  Layers: z = x W^T + b, y = tanh(z) for hidden layers, linear
+// rounded to BF16 when staged), accumulation FP32 on the tensor cores
+// (tcgen05.mma into TMEM); FP32 master weights and Adam moments.  Layers: z = x W^T + b, y = tanh(z) for hidden layers, linear
 // output; loss = mean squared error.  The decoder (mean + V c) is an FP32 GEMM.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -107,6 +107,171 @@ void gemm(int M, int N, int K, const TAe* A, int lda, const TBe* B, int ldb, flo
   PECS_CUDA(cudaGetLastError());
 }
 
+// ---- tensor-core GEMM: tcgen05.mma, BF16 operands, FP32 accumulator in TMEM ----
+// The layers' GEMMs C = act(alpha op(A) op(B) + beta C + bias) with BF16-rounded
+// operands run on the 5th-generation tensor cores: each CTA owns a 128 x 128
+// tile of C, whose FP32 accumulator lives in 128 TMEM columns.  Per K chunk of
+// 64, the CTA's threads stage op(A) (128 x 64) and op(B)^T (128 x 64) as BF16
+// in shared memory in the canonical K-major layout without swizzle (8-row x
+// 16-byte core matrices; K-adjacent core matrices 128 B apart, 8-row groups
+// 1024 B apart), one thread issues four tcgen05.mma (K = 16 each) and commits
+// them to an mbarrier, and every thread waits on it -- with a bounded number of
+// polls: a wait that runs out sets the error flag, the tile is skipped and the
+// TMEM is still freed -- before the buffers are refilled.  The epilogue reads
+// the accumulator with tcgen05.ld (warp w: TMEM lanes 32w..32w+31 = rows).
+constexpr int kTcM = 128, kTcN = 128, kTcK = 64, kTcThreads = 128;
+constexpr uint32_t kTcCols = 128;
+constexpr long long kTcPollLimit = 1LL << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// byte offset of element (row, k) of a 128 x 64 K-major tile
+__device__ __forceinline__ uint32_t tc_off(int row, int k) {
+  return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start address, leading-dimension byte
+// offset (K direction, 128 B), stride byte offset (8-row groups, 1024 B),
+// descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) |
+         ((uint64_t)(1024u >> 4) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+  for (long long i = 0; i < kTcPollLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <typename TAe, typename TBe, bool TA, bool TB>
+__global__ void __launch_bounds__(kTcThreads)
+    k_gemm_tc(int M, int N, int K, const TAe* __restrict__ A, int lda, const TBe* __restrict__ B, int ldb,
+              float* __restrict__ C, int ldc, float alpha, float beta, const float* __restrict__ bias,
+              int act, int* __restrict__ err) {
+  __shared__ __align__(1024) unsigned char As[kTcM * kTcK * 2];
+  __shared__ __align__(1024) unsigned char Bs[kTcN * kTcK * 2];
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+  const uint32_t mbar_a = smem_u32(&mbar);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar_a) : "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  // instruction descriptor (kind::f16): FP32 accumulator, BF16 A and B, both
+  // K-major, N = 128, M = 128
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                         ((uint32_t)(kTcM >> 4) << 24);
+  uint32_t parity = 0;
+  bool failed = false;
+  const int nk = (K + kTcK - 1) / kTcK;
+  for (int kc = 0; kc < nk && !failed; ++kc) {
+    const int k0 = kc * kTcK;
+    for (int t = tid; t < kTcM * kTcK; t += kTcThreads) {
+      int r, k;
+      if (TA) { r = t % kTcM; k = t / kTcM; } else { k = t % kTcK; r = t / kTcK; }
+      const int m = m0 + r, kk = k0 + k;
+      float v = 0.f;
+      if (m < M && kk < K) v = to_f(TA ? A[(size_t)kk * lda + m] : A[(size_t)m * lda + kk]);
+      *reinterpret_cast<__nv_bfloat16*>(As + tc_off(r, k)) = __float2bfloat16_rn(v);
+    }
+    for (int t = tid; t < kTcN * kTcK; t += kTcThreads) {
+      int r, k;
+      if (TB) { k = t % kTcK; r = t / kTcK; } else { r = t % kTcN; k = t / kTcN; }
+      const int n = n0 + r, kk = k0 + k;
+      float v = 0.f;
+      if (n < N && kk < K) v = to_f(TB ? B[(size_t)n * ldb + kk] : B[(size_t)kk * ldb + n]);
+      *reinterpret_cast<__nv_bfloat16*>(Bs + tc_off(r, k)) = __float2bfloat16_rn(v);
+    }
+    // the staged tiles are read by the tensor cores (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (tid == 0) {
+#pragma unroll
+      for (int s = 0; s < kTcK / 16; ++s) {
+        const uint64_t ad = tc_desc(smem_u32(As) + s * 256);
+        const uint64_t bd = tc_desc(smem_u32(Bs) + s * 256);
+        const uint32_t accumulate = (kc > 0 || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar_a)
+                   : "memory");
+    }
+    const bool ok = tc_wait(mbar_a, parity);
+    parity ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    failed = __syncthreads_or(!ok) != 0;
+  }
+  if (failed) {
+    if (tid == 0) atomicExch(err, 1);
+    // let MMAs still in flight finish (bounded) before the TMEM is freed
+    tc_wait(mbar_a, parity ^ 1u);
+  } else {
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kTcN; c0 += 32) {
+      if (n0 + c0 >= N) break;
+      uint32_t v[32];
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                   : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                   : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0)
+                   : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int n = n0 + c0 + j;
+          if (n >= N) break;
+          float x = alpha * __uint_as_float(v[j]);
+          if (beta != 0.f) x += beta * C[(size_t)row * ldc + n];
+          if (bias) x += bias[n];
+          if (act == 1) x = tanhf(x);
+          C[(size_t)row * ldc + n] = x;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTcCols) : "memory");
+}
+
+// BF16-operand GEMMs of the network: on the tensor cores
+template <typename TAe, typename TBe, bool TA, bool TB>
+void gemm_tc(int M, int N, int K, const TAe* A, int lda, const TBe* B, int ldb, float* C, int ldc,
+             float alpha, float beta, const float* bias, int act, int* err, cudaStream_t st) {
+  dim3 grid((N + kTcN - 1) / kTcN, (M + kTcM - 1) / kTcM);
+  k_gemm_tc<TAe, TBe, TA, TB><<<grid, kTcThreads, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, beta,
+                                                           bias, act, err);
+  PECS_CUDA(cudaGetLastError());
+}
+
 // dz = dy * (1 - y^2)   (tanh backward), in place on dy
 __global__ void k_tanh_bwd(float* __restrict__ dy, const float* __restrict__ y, size_t n) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -179,6 +344,7 @@ struct Mlp {
   std::vector<DBuf<float>> act;  // act[l]: batch x w[l] (act[0] = input copy)
   std::vector<DBuf<float>> dact;
   DBuf<float> loss_part;
+  DBuf<int> err;  // set by a tensor-core GEMM whose MMA-completion wait ran out
   int adam_t = 0;
   cudaStream_t st = nullptr;
   ~Mlp() {
@@ -207,9 +373,9 @@ struct Mlp {
     PECS_CUDA(cudaMemcpyAsync(act[0].p, x, (size_t)B * w[0] * 4, cudaMemcpyDeviceToDevice, s));
     for (int l = 0; l < L; ++l) {
       // act[l+1] = act(act[l] W_l^T + b_l); W_l stored out x in (row-major)
-      gemm<float, __nv_bfloat16, false, true, true>(B, w[l + 1], w[l], act[l].p, w[l], Wb(l), w[l],
-                                                    act[l + 1].p, w[l + 1], 1.f, 0.f, bias(l),
-                                                    l < L - 1 ? 1 : 0, s);
+      gemm_tc<float, __nv_bfloat16, false, true>(B, w[l + 1], w[l], act[l].p, w[l], Wb(l), w[l],
+                                                 act[l + 1].p, w[l + 1], 1.f, 0.f, bias(l),
+                                                 l < L - 1 ? 1 : 0, err.p, s);
     }
   }
 
@@ -229,15 +395,25 @@ struct Mlp {
         PECS_CUDA(cudaGetLastError());
       }
       // dW_l (out x in) = dz^T (out x B) * act[l] (B x in)
-      gemm<float, float, true, false, true>(w[l + 1], w[l], B, dz, w[l + 1], act[l].p, w[l],
-                                            G.p + woff[l], w[l], 1.f, 0.f, nullptr, 0, s);
+      gemm_tc<float, float, true, false>(w[l + 1], w[l], B, dz, w[l + 1], act[l].p, w[l],
+                                         G.p + woff[l], w[l], 1.f, 0.f, nullptr, 0, err.p, s);
       k_colsum<<<(w[l + 1] + 127) / 128, 128, 0, s>>>(dz, G.p + boff[l], B, w[l + 1]);
       PECS_CUDA(cudaGetLastError());
       if (l > 0) {
         // d act[l] (B x in) = dz (B x out) * W_l (out x in)
-        gemm<float, __nv_bfloat16, false, false, true>(B, w[l], w[l + 1], dz, w[l + 1], Wb(l), w[l],
-                                                       dact[l].p, w[l], 1.f, 0.f, nullptr, 0, s);
+        gemm_tc<float, __nv_bfloat16, false, false>(B, w[l], w[l + 1], dz, w[l + 1], Wb(l), w[l],
+                                                    dact[l].p, w[l], 1.f, 0.f, nullptr, 0, err.p, s);
       }
+    }
+  }
+
+  // after the stream has synchronised: report (and clear) a GEMM that gave up
+  void check_err() {
+    int h = 0;
+    PECS_CUDA(cudaMemcpy(&h, err.p, 4, cudaMemcpyDeviceToHost));
+    if (h) {
+      err.zero();
+      throw PecsError(PECS_E_CUDA, "a tensor-core GEMM gave up waiting for its MMAs; outputs are invalid");
     }
   }
 
@@ -322,6 +498,8 @@ int pecs_mlp_create(int n_layers, const int* widths, unsigned long long seed, pe
     m.P.upload(init);
     m.G.alloc(off);
     m.G.zero();
+    m.err.alloc(1);
+    m.err.zero();
     m.Mo.alloc(off);
     m.Mo.zero();
     m.Vo.alloc(off);
@@ -372,6 +550,7 @@ int pecs_mlp_forward(pecs_mlp* h, int batch, const float* x_dev, float* y_dev, v
     PECS_CUDA(cudaMemcpyAsync(y_dev, m.act.back().p, (size_t)batch * m.w.back() * 4,
                               cudaMemcpyDeviceToDevice, s));
     PECS_CUDA(cudaStreamSynchronize(s));
+    m.check_err();
   })
 }
 
@@ -386,6 +565,7 @@ int pecs_mlp_gradients(pecs_mlp* h, int batch, const float* x_dev, const float* 
     if (loss) *loss = m.read_loss(m.st, batch);
     if (grad_host) PECS_CUDA(cudaMemcpy(grad_host, m.G.p, m.n_params * 4, cudaMemcpyDeviceToHost));
     PECS_CUDA(cudaStreamSynchronize(m.st));
+    m.check_err();
   })
 }
 
@@ -402,6 +582,7 @@ int pecs_mlp_train_step(pecs_mlp* h, int batch, const float* x_dev, const float*
       *loss = m.read_loss(m.st, batch);
     else
       PECS_CUDA(cudaStreamSynchronize(m.st));
+    m.check_err();
   })
 }
 

@@ -1578,6 +1578,35 @@ void FactorBank::autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, 
   cudaEventDestroy(e1);
 }
 
+std::vector<double> FactorBank::time_levels(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st,
+                                            int reps) const {
+  if (!panel_ || prec_ == PECS_PREC_FP64) throw PecsError(PECS_E_STATE, "level timing needs an FP32 panel bank");
+  const int rpl = panel_rpl(sets, max_nrhs);
+  const BankView B = view();
+  const int nl = (int)(pfwd_.size() + pbwd_.size());
+  std::vector<cudaEvent_t> ev(nl + 1);
+  for (auto& e : ev) PECS_CUDA(cudaEventCreate(&e));
+  std::vector<double> ms(nl, 0.0);
+  for (int r = 0; r <= reps; ++r) {
+    int l = 0;
+    PECS_CUDA(cudaEventRecord(ev[0], st));
+    for (int pass = 0; pass < 2; ++pass)
+      for (const PanelPlan& L : pass == 0 ? pfwd_ : pbwd_) {
+        launch_panel_level<float, IlSetsViewF>(pass == 0, B, sets, L, max_nrhs, rpl, tune_, parts_ld_, st);
+        PECS_CUDA(cudaEventRecord(ev[++l], st));
+      }
+    PECS_CUDA(cudaEventSynchronize(ev[nl]));
+    if (r == 0) continue;
+    for (int k = 0; k < nl; ++k) {
+      float t = 0.f;
+      PECS_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+      ms[k] += t / reps;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return ms;
+}
+
 void FactorBank::autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps) {
   if (!panel_ || prec_ == PECS_PREC_FP64) throw PecsError(PECS_E_STATE, "autotune needs an FP32 panel bank");
   autotune_panel(sets, max_nrhs, st, reps);

@@ -175,6 +175,11 @@ class FactorBank {
   void autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps = 3);
   void autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps = 3);
   double tuned_ms() const { return tuned_ms_; }
+  // Diagnostic: device time of each level launch of one sweep (forward levels,
+  // then backward), CUDA events recorded between the launches, mean of reps
+  // sweeps after one warm-up; the events keep consecutive levels from
+  // overlapping, so the times are upper bounds of the in-sweep ones.
+  std::vector<double> time_levels(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps) const;
   int tune_launches() const { return tune_launches_; }
 
  private:

@@ -36,6 +36,31 @@ def test_mlp_gradients_match_cpu_oracle(pecs_lib):
     assert np.max(np.abs(y.cpu().numpy() - y_ref)) < 1e-3 * np.max(np.abs(y_ref))
 
 
+def test_mlp_tensor_core_gemms_across_tiles(pecs_lib):
+    """Widths and batch that are not multiples of the tensor-core tile (128 x
+    128, K chunks of 64): several tiles and chunks per GEMM, ragged edges in
+    M, N and K, for the forward GEMM and both backward GEMMs."""
+    torch = _torch()
+    from pecs_gb300.learned import Mlp
+    widths = [6, 200, 300, 70]
+    m = Mlp(widths, seed=4)
+    rng = np.random.default_rng(1)
+    p = (rng.standard_normal(m.n_params) * 0.1).astype(np.float32)
+    m.set_params(p)
+    B = 150
+    x = rng.uniform(-1, 1, (B, 6)).astype(np.float32)
+    t = rng.standard_normal((B, 70)).astype(np.float32)
+    xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+    y = torch.empty(B, 70, device="cuda")
+    m.forward(xd.data_ptr(), y.data_ptr(), B)
+    y_ref = nn_oracle.forward(p, widths, x)[-1]
+    assert np.max(np.abs(y.cpu().numpy() - y_ref)) < 1e-3 * np.max(np.abs(y_ref))
+    g, loss = m.gradients(xd.data_ptr(), td.data_ptr(), B)
+    loss_ref, g_ref = nn_oracle.loss_and_grad(p, widths, x, t)
+    assert abs(loss - loss_ref) <= 1e-4 * abs(loss_ref)
+    assert np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref) < 2e-3
+
+
 def test_mlp_training_reduces_loss(pecs_lib):
     torch = _torch()
     from pecs_gb300.learned import Mlp
