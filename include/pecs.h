@@ -62,7 +62,7 @@ extern "C" {
 #define PECS_MAT_MASS_ELEC 6
 
 /* solver precision */
-#define PECS_PREC_FP64 0    /* FP64 factors and arithmetic; the Poisson solve refined once */
+#define PECS_PREC_FP64 0    /* FP64 factors and arithmetic, every solve refined once */
 #define PECS_PREC_FP32_IR 1 /* FP32 factors + FP64-residual iterative refinement */
 /* FP32 factors + refinement with FP32-pair ("double-float") residuals, RHS
  * quadrature terms in FP32 (constant and mass terms FP64), FP32 convergence
@@ -113,8 +113,8 @@ typedef struct pecs_options {
   int leaf_cells;    /* nested-dissection leaf size in cells (0 = default) */
   int use_graphs;    /* capture a time step in a CUDA graph (1 = yes) */
   int ir_max_iters;  /* refinement sweeps per solve: FP64 residual, correction sweep
-                        (0 = default: FP64 one on the Poisson solve, none on the
-                        carriers; FP32_MIXED one, FP32_IR two; < 0 = none) */
+                        (0 = default: one for FP64 and FP32_MIXED, two for FP32_IR;
+                        < 0 = none) */
   double ir_tol;     /* reserved: the refinement runs ir_max_iters sweeps; pecs_solve_residual
                         reports the relative residual they reached */
   int device;        /* CUDA device ordinal */

@@ -518,19 +518,20 @@ struct Engine {
   bool graph_valid = false;
   // refinement sweeps per solve of bank `which` (0 carriers, 1 Poisson):
   // ir_max_iters > 0 sets the count, < 0 disables refinement, 0 selects the
-  // default -- two for FP32_IR and one for FP32_MIXED on both banks; for FP64
-  // factors one on the Poisson solve and none on the carriers.  That FP64
-  // step is what UMFPACK's default control does in SparseDirectUMFPACK::solve,
-  // which the reference's PoissonData::solve calls (Poisson.cpp:98-105):
-  // without it the explicit-inverse sweeps leave the Poisson field of a
-  // coupled trajectory ~1e-9 from exact arithmetic at 64x64 cells (the net
-  // charge on its right-hand side nearly cancels), and the carriers follow
-  // through the drift; with it both stay within ~2e-12 after 60 steps, the
-  // carrier solves needing no refinement of their own
+  // default -- two for FP32_IR, one for FP32_MIXED and for FP64 factors.  The
+  // FP64 step is what UMFPACK's default control does in
+  // SparseDirectUMFPACK::solve, which the reference's Carrier::solve and
+  // PoissonData::solve call (Carrier.cpp:34-40, Poisson.cpp:98-105): without
+  // it the explicit-inverse sweeps leave the Poisson field of a coupled
+  // trajectory ~1e-9 from exact arithmetic at 64x64 cells after 60 steps (the
+  // net charge on its right-hand side nearly cancels, so the carrier solves'
+  // errors are amplified there, and the same on the single-instance and the
+  // batched paths: it is the stored factors' rounding, not the sweeps'); with
+  // it, ~2e-12
   int ir_iters(int which) const {
+    (void)which;
     if (opt.ir_max_iters < 0) return 0;
     if (opt.ir_max_iters > 0) return opt.ir_max_iters;
-    if (opt.precision == PECS_PREC_FP64) return which == 1 ? 1 : 0;
     return opt.precision == PECS_PREC_FP32_IR ? 2 : 1;
   }
   // element-wise launches per set of one solve: gather, scatter and, per
