@@ -77,7 +77,7 @@ def parse():
                     help="full mode: end-to-end points = this many times --batch-inst")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="full mode: skip the FP64 accuracy references (profiling runs)")
-    ap.add_argument("--model", default=os.path.join(ROOT, "pecs_gb300", "models", "warmstart_r6.npz"))
+    ap.add_argument("--model", default=os.path.join(ROOT, "pecs_gb300", "models", "warmstart_ref6.npz"))
     ap.add_argument("--train-samples", type=int, default=256,
                     help="training draws when no trained model file is present")
     ap.add_argument("--steady", action="store_true",
@@ -485,7 +485,7 @@ def run_plain(args):
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": load_traffic(f"carrier_solve_r{args.refine}_{args.precision}"),
+                     "traffic": load_traffic(f"carrier_solve_ref{args.refine}_{args.precision}"),
                      "kernel": "k_forward/k_backward (carrier multifrontal solve sweep)",
                      "solve_ms": solve_ms, "poisson_solve_ms": pois_ms,
                      "bytes_per_sweep": info.solve_bytes[0], "launches_per_sweep": nlaunch},
@@ -713,14 +713,14 @@ def run_full(args):
                 "points": n_e},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": load_traffic(f"carrier_solve_r{args.refine}_mixed_b{B}"),
+                     "traffic": load_traffic(f"carrier_solve_ref{args.refine}_mixed_b{B}"),
                      "kernel": "k_panel / k_panel_warp (carrier multifrontal solve sweep, FP32, "
                                f"{2 * B} right-hand sides per factor)",
                      "solve_ms": solve_ms, "launches_per_sweep": nlaunch,
                      "bytes_per_sweep": info.solve_bytes[0],
                      "plain_fp64": {"solve_ms": plain_ms, "achieved_gbs": plain_gbs,
                                     "frac": plain_gbs / peak,
-                                    "traffic": load_traffic(f"carrier_solve_r{args.refine}_fp64")}},
+                                    "traffic": load_traffic(f"carrier_solve_ref{args.refine}_fp64")}},
         "gpu_launches": executed * info.launches_per_step,
         "clocks": clocks,
     }

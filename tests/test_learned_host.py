@@ -98,7 +98,7 @@ def test_pod_fit_reproduces_low_rank_snapshots():
 
 
 def test_committed_model_file_is_consistent():
-    d = np.load(os.path.join(ROOT, "pecs_gb300", "models", "warmstart_r6.npz"))
+    d = np.load(os.path.join(ROOT, "pecs_gb300", "models", "warmstart_ref6.npz"))
     widths = [int(w) for w in d["widths"]]
     assert widths[0] == 6 and widths[-1] == int(d["rank"])
     n_params = sum(a * b + b for a, b in zip(widths[:-1], widths[1:]))
