@@ -406,6 +406,13 @@ int pecs_mlp_train_step(pecs_mlp* m, int batch, const float* x_dev, const float*
 /* y (batch x n) = mean + c (batch x r) V^T with V (n x r); FP32 */
 int pecs_decode(int batch, int r, int n, const float* c_dev, const float* V_dev, const float* mean_dev,
                 float* y_dev, void* stream);
+/* Warm-start carrier vectors from the network's coefficients c (batch x r):
+ * y = mean + V c over the 2 n_u log-density outputs (V: 2 n_u x r, FP32), and
+ * per row full electron / hole vectors (batch x nd doubles, device) with
+ * exp(y) in the density block at u_off and zero currents.  Synchronous. */
+int pecs_warm_start_vectors(int batch, int r, int n_u, const float* c_dev, const float* V_dev,
+                            const float* mean_dev, int nd, int u_off, double* vn_dev, double* vp_dev,
+                            void* stream);
 
 #ifdef __cplusplus
 }

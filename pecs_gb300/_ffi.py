@@ -166,6 +166,8 @@ SIGNATURES = [
     ("pecs_mlp_gradients", C.c_int, [_vp, C.c_int, _vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("pecs_mlp_train_step", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_float, C.POINTER(C.c_float)]),
     ("pecs_decode", C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    ("pecs_warm_start_vectors", C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, _vp,
+                                          _vp, _vp]),
 ]
 
 _lib = None

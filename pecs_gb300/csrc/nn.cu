@@ -11,6 +11,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -586,6 +587,34 @@ int pecs_mlp_train_step(pecs_mlp* h, int batch, const float* x_dev, const float*
   })
 }
 
+// Warm-start carrier vectors straight from the network's coefficients: for
+// each row b, y_i = mean_i + sum_j V_ij c_bj (FP32) over the 2 n_u density
+// outputs, and the full carrier vectors (nd doubles, currents zero) get
+// exp(y) in their density block at u_off: electrons from y_0..y_{n_u-1},
+// holes from y_{n_u}..y_{2 n_u - 1}.
+__global__ void k_warm_start(int batch, int r, int n_u, const float* __restrict__ c, const float* __restrict__ V,
+                             const float* __restrict__ mean, int nd, int u_off, double* __restrict__ vn,
+                             double* __restrict__ vp) {
+  const int b = blockIdx.y;
+  extern __shared__ float cs[];
+  for (int j = threadIdx.x; j < r; j += blockDim.x) cs[j] = c[(size_t)b * r + j];
+  __syncthreads();
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * nd; t += gridDim.x * blockDim.x) {
+    const int which = t / nd, d = t - which * nd;
+    double* out = (which ? vp : vn) + (size_t)b * nd;
+    const int i = d - u_off;
+    if (i < 0 || i >= n_u) {
+      out[d] = 0.0;
+      continue;
+    }
+    const int o = which * n_u + i;
+    const float* v = V + (size_t)o * r;
+    float y = mean[o];
+    for (int j = 0; j < r; ++j) y = fmaf(v[j], cs[j], y);
+    out[d] = (double)expf(y);
+  }
+}
+
 // FP32 decoder: y (batch x n) = mean (n) + c (batch x r) V^T, V stored n x r (row-major)
 int pecs_decode(int batch, int r, int n, const float* c_dev, const float* V_dev, const float* mean_dev,
                 float* y_dev, void* stream) {
@@ -597,6 +626,22 @@ int pecs_decode(int batch, int r, int n, const float* c_dev, const float* V_dev,
                                            0, s);
     const size_t tot = (size_t)batch * n;
     k_add_rowvec<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(y_dev, mean_dev, batch, n);
+    PECS_CUDA(cudaGetLastError());
+    PECS_CUDA(cudaStreamSynchronize(s));
+  })
+}
+
+int pecs_warm_start_vectors(int batch, int r, int n_u, const float* c_dev, const float* V_dev,
+                            const float* mean_dev, int nd, int u_off, double* vn_dev, double* vp_dev,
+                            void* stream) {
+  NN_TRY({
+    if (batch < 1 || r < 1 || n_u < 1 || nd < 1 || u_off < 0 || u_off + n_u > nd || !c_dev || !V_dev ||
+        !mean_dev || !vn_dev || !vp_dev)
+      throw PecsError(PECS_E_ARG, "invalid arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    const dim3 grid((unsigned)std::min<long long>(((long long)2 * nd + 255) / 256, 1024), batch);
+    k_warm_start<<<grid, 256, (size_t)r * sizeof(float), s>>>(batch, r, n_u, c_dev, V_dev, mean_dev, nd, u_off,
+                                                               vn_dev, vp_dev);
     PECS_CUDA(cudaGetLastError());
     PECS_CUDA(cudaStreamSynchronize(s));
   })

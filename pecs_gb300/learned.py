@@ -250,6 +250,27 @@ class NeuralOperator:
                                 C.c_void_p(y.data_ptr()), C.c_void_p(0)))
         return y.double()
 
+    def predict_vectors(self, X, lay: Layout):
+        """Full electron and hole vectors (n x nd float64 cuda, currents zero)
+        from the network: the MLP forward and pecs_warm_start_vectors (decode of
+        the 2 n_u log-density outputs, exp, scatter into the density block) --
+        library kernels only."""
+        import torch
+        if getattr(self, "_ws", None) is None or self._ws[0] != lay.n_u:
+            m = 2 * lay.n_u
+            V = (self.basis[:m] * self.scale[:m, None] * self.cscale[None, :]).float().contiguous()
+            self._ws = (lay.n_u, V, self.mean[:m].float().contiguous())
+        _, V, mean = self._ws
+        c = self.predict_coeffs(X)
+        n = X.shape[0]
+        vn = torch.empty(n, lay.nd_carrier, dtype=torch.float64, device=X.device)
+        vp = torch.empty_like(vn)
+        check(lib().pecs_warm_start_vectors(n, self.rank, lay.n_u, C.c_void_p(c.data_ptr()),
+                                            C.c_void_p(V.data_ptr()), C.c_void_p(mean.data_ptr()),
+                                            lay.nd_carrier, lay.u_off, C.c_void_p(vn.data_ptr()),
+                                            C.c_void_p(vp.data_ptr()), C.c_void_p(0)))
+        return vn, vp
+
 
 # -- data generation and warm-started sweeps --------------------------------------
 
@@ -278,16 +299,13 @@ def steady_states(ctx: Context, thetas: np.ndarray, base: Params, max_steps=5000
     return Y, steps
 
 
-def apply_prediction(ctx: Context, pred, rows_k: Sequence[int], lay: Layout):
-    """Write predicted densities of instances rows_k into ctx (currents 0,
-    electrolyte fields untouched) and re-solve Poisson from them."""
-    import torch
-    for k in rows_k:
-        y = pred[k]
-        for f, blk in ((F.FIELD_N, y[:lay.n_u]), (F.FIELD_P, y[lay.n_u:2 * lay.n_u])):
-            v = torch.zeros(lay.nd_carrier, dtype=torch.float64, device="cuda")
-            v[lay.u_off:lay.u_off + lay.n_u] = blk.exp()
-            ctx.set_state_device(f, k, v.data_ptr())
+def apply_prediction(ctx: Context, vn, vp, rows, slots: Sequence[int]):
+    """Write the predicted electron / hole vectors vn[rows[k]], vp[rows[k]]
+    (full carrier vectors, currents zero) into instance slots[k] of ctx
+    (electrolyte fields untouched) and re-solve Poisson from them."""
+    for r, k in zip(rows, slots):
+        ctx.set_state_device(F.FIELD_N, k, vn[r].data_ptr())
+        ctx.set_state_device(F.FIELD_P, k, vp[r].data_ptr())
     ctx.assemble_poisson_rhs()
     ctx.solve_poisson()
 
@@ -310,18 +328,19 @@ def warm_started_sweep(ctx: Context, op: Optional[NeuralOperator], thetas: np.nd
         steps, _ = ctx.run_to_steady_state(max_steps, tol, check_every)
         return steps, fallback, ctx.interface_current()
     X = torch.from_numpy(normalize(thetas)).cuda()
-    pred = op.predict(X)
+    vn, vp = op.predict_vectors(X, lay)
     # probe: one step from the standard initial condition ...
     ctx.initialize()
     rel_std = ctx.probe_step()
     # ... and one step from the prediction
     ctx.initialize()
-    apply_prediction(ctx, pred, range(B), lay)
+    apply_prediction(ctx, vn, vp, range(B), range(B))
     rel_pred = ctx.probe_step()
     use_pred = np.isfinite(rel_pred) & (rel_pred < rel_std)
     fallback = ~use_pred
     ctx.initialize()
-    apply_prediction(ctx, pred, [k for k in range(B) if use_pred[k]], lay)
+    keep = [k for k in range(B) if use_pred[k]]
+    apply_prediction(ctx, vn, vp, keep, keep)
     steps, _ = ctx.run_to_steady_state(max_steps, tol, check_every)
     return steps + 2, fallback, ctx.interface_current()
 
@@ -342,7 +361,7 @@ def warm_start_vectors(ctx: Context, op: NeuralOperator, thetas: np.ndarray, bas
     lay = Layout.of(ctx)
     n = thetas.shape[0]
     X = torch.from_numpy(normalize(thetas)).cuda()
-    pred = op.predict(X)
+    vn, vp = op.predict_vectors(X, lay)
     fallback = np.ones(n, dtype=bool)
     for b0 in range(0, n, B):
         rows = list(range(b0, min(n, b0 + B)))
@@ -351,19 +370,14 @@ def warm_start_vectors(ctx: Context, op: NeuralOperator, thetas: np.ndarray, bas
         ctx.initialize()
         rel_std = ctx.probe_step()
         ctx.initialize()
-        apply_prediction(ctx, pred[pad], range(B), lay)
+        apply_prediction(ctx, vn, vp, pad, range(B))
         rel_pred = ctx.probe_step()
         ok = np.isfinite(rel_pred) & (rel_pred < rel_std)
         for k, r in enumerate(rows):
             fallback[r] = not ok[k]
-    nd = lay.nd_carrier
-    vn = torch.zeros(n, nd, dtype=torch.float64, device="cuda")
-    vp = torch.zeros(n, nd, dtype=torch.float64, device="cuda")
-    vn[:, lay.u_off:lay.u_off + lay.n_u] = pred[:, :lay.n_u].exp()
-    vp[:, lay.u_off:lay.u_off + lay.n_u] = pred[:, lay.n_u:2 * lay.n_u].exp()
     init_n = [0 if fallback[r] else vn[r].data_ptr() for r in range(n)]
     init_p = [0 if fallback[r] else vp[r].data_ptr() for r in range(n)]
-    return init_n, init_p, fallback, (vn, vp, pred)
+    return init_n, init_p, fallback, (vn, vp)
 
 
 def stream_warm_sweep(ctx: Context, op: Optional[NeuralOperator], thetas: np.ndarray, base: Params,

@@ -65,20 +65,23 @@ def test_streamed_point_with_a_nan_start_is_marked_and_the_others_are_unchanged(
 
 
 class _PoisonedOperator:
-    """Stands in for the trained operator: rows 0-1 predict NaN, row 2 predicts
-    densities of 1e30, row 3 the plain method's own steady state (a perfect
+    """Stands in for the trained operator: rows 0-1 predict NaN densities, row
+    2 densities of 1e30, row 3 the plain method's own steady state (a perfect
     prediction)."""
 
-    def __init__(self, good_row):
-        self.good = good_row
+    def __init__(self, good_n, good_p):
+        self.good = (good_n, good_p)
 
-    def predict(self, X):
+    def predict_vectors(self, X, lay):
         import torch
-        out = torch.empty(X.shape[0], self.good.numel(), dtype=torch.float64, device="cuda")
-        out[0:2] = float("nan")
-        out[2] = float(np.log(1e30))
-        out[3] = self.good
-        return out
+        out = []
+        for g in self.good:
+            v = torch.zeros(X.shape[0], lay.nd_carrier, dtype=torch.float64, device="cuda")
+            v[0:2, lay.u_off:lay.u_off + lay.n_u] = float("nan")
+            v[2, lay.u_off:lay.u_off + lay.n_u] = 1e30
+            v[3] = g
+            out.append(v)
+        return tuple(out)
 
 
 def test_poisoned_predictions_fall_back_to_the_standard_start(pecs_lib):
@@ -89,10 +92,12 @@ def test_poisoned_predictions_fall_back_to_the_standard_start(pecs_lib):
     lay = L.Layout.of(ctx)
     steps_p, _, cur_p, fin = L.stream_warm_sweep(ctx, None, thetas, base, 3000, 1e-8, 25,
                                                  want_fields=True)
-    nd, ndp = lay.nd_carrier, lay.nd_poisson
-    good = L.fields_to_targets(fin[pg.FIELD_N].reshape(4, nd)[3], fin[pg.FIELD_P].reshape(4, nd)[3],
-                               fin[pg.FIELD_POISSON].reshape(4, ndp)[3], lay)
-    op = _PoisonedOperator(torch.from_numpy(good).cuda())
+    nd = lay.nd_carrier
+    gn = torch.from_numpy(fin[pg.FIELD_N].reshape(4, nd)[3].copy()).cuda()
+    gp = torch.from_numpy(fin[pg.FIELD_P].reshape(4, nd)[3].copy()).cuda()
+    gn[:lay.u_off] = 0.0       # a prediction carries densities only
+    gp[:lay.u_off] = 0.0
+    op = _PoisonedOperator(gn, gp)
     steps_w, fb, cur_w, _ = L.stream_warm_sweep(ctx, op, thetas, base, 3000, 1e-8, 25)
     assert list(fb) == [True, True, True, False]
     for k in range(3):   # fallbacks: exactly the plain march, plus the two probe steps

@@ -87,6 +87,14 @@ def test_warm_start_saves_steps_and_keeps_the_steady_state(pecs_lib):
     X = torch.from_numpy(L.normalize(tr)).cuda()
     hist = op.train(X, T, epochs=300, batch=32, lr=2e-3)
     assert hist[-1] < 0.2 * hist[0]
+    # the fused library kernel (decode, exp, scatter) against the decode + torch
+    Xe = torch.from_numpy(L.normalize(ev)).cuda()
+    vn, vp = op.predict_vectors(Xe, lay)
+    y = op.predict(Xe)
+    u = slice(lay.u_off, lay.u_off + lay.n_u)
+    assert torch.allclose(vn[:, u], y[:, :lay.n_u].exp(), rtol=1e-5, atol=0)
+    assert torch.allclose(vp[:, u], y[:, lay.n_u:2 * lay.n_u].exp(), rtol=1e-5, atol=0)
+    assert (vn[:, :lay.u_off] == 0).all() and (vp[:, :lay.u_off] == 0).all()
     s_w, fb, c_w = L.warm_started_sweep(ctx, op, ev, base)
     s_p, _, c_p = L.warm_started_sweep(ctx, None, ev, base)
     assert s_w.sum() < s_p.sum()                      # fewer steps overall
