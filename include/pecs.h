@@ -127,6 +127,9 @@ typedef struct pecs_options {
   int autotune;        /* panel solve kernels: at creation, choose every tree level's
                           tiling by timing whole sweeps (1 = yes, the default;
                           0 = the heuristic above) */
+  int gpu_factor_min_front; /* factorisation: fronts with at least this many rows are
+                               factored in FP64 on the GPU (0 = default 1024; < 0 = all
+                               on the host); host_setup_only contexts factor on the host */
 } pecs_options;
 
 typedef struct pecs_info {
@@ -361,6 +364,10 @@ typedef struct pecs_lu pecs_lu;
 int pecs_lu_factor(int n, const int* rowptr, const int* col, const double* val,
                    const int* dof_cell, const int* dof_class, int n_cells, const double* cell_xy,
                    int precision, int leaf_cells, pecs_lu** out);
+/* Fronts of at least this many rows are factored in FP64 on the current GPU
+ * by later pecs_lu_factor calls of this process (default 1024; < 0: always on
+ * the host, as without a GPU).  Returns the previous value. */
+int pecs_lu_set_gpu_factor_min_front(int rows);
 int pecs_lu_solve(pecs_lu* lu, int nrhs, const double* b, double* x); /* host arrays, nrhs*n */
 int pecs_lu_solve_device(pecs_lu* lu, int nrhs, const double* b_dev, double* x_dev, void* stream);
 int pecs_lu_stats(pecs_lu* lu, long long* entries, int* levels, int* nodes, int* max_front);

@@ -20,6 +20,11 @@ int pecs_lu_host_apply(pecs_lu* lu, const double* b, double* x);
  * warm-up.  Returns the number of levels written to ms (at most cap), or a
  * negative error code.  The sweep's outputs are overwritten. */
 int pecs_debug_time_levels(pecs_ctx* ctx, int which, int reps, double* ms, int cap);
+/* The stored factor values of a pecs_lu handle (before its first solve
+ * uploads them): every node's Gf then Hb, nodes in elimination order, into
+ * out (capacity n doubles); returns the count via *count (out may be NULL to
+ * query it). */
+int pecs_debug_lu_values(pecs_lu* lu, double* out, long long n, long long* count);
 #ifdef __cplusplus
 }
 #endif

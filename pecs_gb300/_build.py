@@ -18,7 +18,7 @@ LIBDIR = HERE / "_lib"
 LIB = LIBDIR / "libpecs_gb300.so"
 INCLUDE = HERE.parent / "include"
 
-CUDA_SOURCES = ["engine.cu", "solve.cu", "nn.cu"]
+CUDA_SOURCES = ["engine.cu", "solve.cu", "nn.cu", "front.cu"]
 CXX_SOURCES = ["problem.cpp", "mf.cpp", "dense.cpp", "scaling.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -72,7 +72,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         list(ex.map(run, cmds))
     objs = [str(obj / (s + ".o")) for s in CUDA_SOURCES + CXX_SOURCES]
     tmp = LIB.with_suffix(".so.tmp")
-    run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lpthread"])
+    run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcublas", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

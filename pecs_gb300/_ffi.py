@@ -51,7 +51,7 @@ class pecs_options(C.Structure):
         ("precision", C.c_int), ("leaf_cells", C.c_int), ("use_graphs", C.c_int),
         ("ir_max_iters", C.c_int), ("ir_tol", C.c_double), ("device", C.c_int),
         ("host_setup_only", C.c_int), ("panel_chunk", C.c_int), ("panel_min_ctas", C.c_int),
-        ("autotune", C.c_int),
+        ("autotune", C.c_int), ("gpu_factor_min_front", C.c_int),
     ]
 
 
@@ -151,6 +151,8 @@ SIGNATURES = [
     ("pecs_lu_factor", C.c_int, [C.c_int, _ip, _ip, _dp, _ip, _ip, C.c_int, _dp, C.c_int, C.c_int,
                                  C.POINTER(_vp)]),
     ("pecs_lu_solve", C.c_int, [_vp, C.c_int, _dp, _dp]),
+    ("pecs_lu_set_gpu_factor_min_front", C.c_int, [C.c_int]),
+    ("pecs_debug_lu_values", C.c_int, [_vp, _dp, C.c_longlong, C.POINTER(C.c_longlong)]),
     ("pecs_lu_solve_device", C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     ("pecs_lu_stats", C.c_int, [_vp, C.POINTER(C.c_longlong), _ip, _ip, _ip]),
     ("pecs_lu_destroy", None, [_vp]),

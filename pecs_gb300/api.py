@@ -297,7 +297,7 @@ def reference_params(n_refine: int = 4, degree: int = 1, **kw) -> Params:
 def default_options(precision: int = PREC_FP64, use_graphs: bool = True, leaf_cells: int = 8,
                     ir_max_iters: int = 0, device: int = 0, host_setup_only: bool = False,
                     panel_chunk: int = 0, panel_min_ctas: int = 0,
-                    autotune: bool = True) -> F.pecs_options:
+                    autotune: bool = True, gpu_factor_min_front: int = 0) -> F.pecs_options:
     o = F.pecs_options()
     lib().pecs_default_options(C.byref(o))
     o.precision = precision
@@ -309,6 +309,7 @@ def default_options(precision: int = PREC_FP64, use_graphs: bool = True, leaf_ce
     o.panel_chunk = panel_chunk
     o.panel_min_ctas = panel_min_ctas
     o.autotune = int(autotune)
+    o.gpu_factor_min_front = gpu_factor_min_front
     return o
 
 
@@ -322,13 +323,14 @@ class Context:
     def __init__(self, params: Sequence[Params] | Params, precision: int = PREC_FP64,
                  use_graphs: bool = True, leaf_cells: int = 8, ir_max_iters: int = 0,
                  device: int = 0, host_setup_only: bool = False, panel_chunk: int = 0,
-                 panel_min_ctas: int = 0, autotune: bool = True):
+                 panel_min_ctas: int = 0, autotune: bool = True, gpu_factor_min_front: int = 0):
         if isinstance(params, Params):
             params = [params]
         self.params = list(params)
         arr = (F.pecs_params * len(self.params))(*[p.to_c() for p in self.params])
         opt = default_options(precision, use_graphs, leaf_cells, ir_max_iters, device,
-                              host_setup_only, panel_chunk, panel_min_ctas, autotune)
+                              host_setup_only, panel_chunk, panel_min_ctas, autotune,
+                              gpu_factor_min_front)
         h = C.c_void_p()
         check(lib().pecs_create(arr, len(self.params), C.byref(opt), C.byref(h)))
         self._h = h
@@ -601,6 +603,15 @@ class LU:
         """b, x: device pointers (e.g. torch.Tensor.data_ptr()) of nrhs*n doubles."""
         check(lib().pecs_lu_solve_device(self._h, nrhs, C.c_void_p(b), C.c_void_p(x),
                                          C.c_void_p(stream)))
+
+    def factor_values(self) -> np.ndarray:
+        """The stored factor values (every node's Gf then Hb), before the
+        first solve uploads them (pecs_debug_lu_values)."""
+        n = C.c_longlong()
+        check(lib().pecs_debug_lu_values(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        check(lib().pecs_debug_lu_values(self._h, _dptr(out), n.value, C.byref(n)))
+        return out
 
     def host_apply(self, b: np.ndarray) -> np.ndarray:
         """Diagnostic host application of the factors (no GPU)."""

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -803,11 +804,17 @@ struct Engine {
     auto same = [](const Csr& a, const Csr& b) {
       return a.rowptr == b.rowptr && a.col == b.col && a.val == b.val;
     };
+    // the largest fronts (near the root) are factored in FP64 on the GPU
+    std::shared_ptr<FrontOffload> off;
+    if (!host_only && opt.gpu_factor_min_front >= 0)
+      off = make_gpu_front_offload(opt.device, opt.gpu_factor_min_front > 0 ? opt.gpu_factor_min_front : 1024);
     auto factor = [&](const Csr& A, const std::vector<int>& dc, const std::vector<int>* cls, int nc,
                       const std::vector<double>& xy, MfFactor& F) {
       F = mf_analyze(A, dc.data(), cls ? cls->data() : nullptr, nc, xy.data(), leaf);
       try {
-        mf_factorize(F, A);
+        mf_factorize(F, A, 0, off.get());
+      } catch (const PecsError&) {
+        throw;
       } catch (const std::exception& e) {
         throw PecsError(PECS_E_SINGULAR, e.what());
       }
@@ -1581,6 +1588,9 @@ struct pecs_lu {
     return PECS_E_ARG;                                  \
   }
 
+// pecs_lu_factor: fronts with at least this many rows go to the GPU
+static std::atomic<int> g_lu_gpu_min_front{1024};
+
 static void need_device(Engine& e) {
   if (e.host_only) throw PecsError(PECS_E_STATE, "context was created with host_setup_only");
 }
@@ -2036,12 +2046,42 @@ int pecs_lu_factor(int n, const int* rowptr, const int* col, const double* val, 
     std::unique_ptr<pecs_lu> h(new pecs_lu());
     h->h.precision = precision;
     h->h.F = mf_analyze(A, dof_cell, dof_class, n_cells, cell_xy, leaf_cells);
+    std::shared_ptr<FrontOffload> off;
+    int ndev = 0, dev = 0;
+    const int min_front = g_lu_gpu_min_front.load();
+    if (min_front >= 0 && cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0 && cudaGetDevice(&dev) == cudaSuccess)
+      off = make_gpu_front_offload(dev, min_front);
     try {
-      mf_factorize(h->h.F, A);
+      mf_factorize(h->h.F, A, 0, off.get());
+    } catch (const PecsError&) {
+      throw;
     } catch (const std::exception& ex) {
       throw PecsError(PECS_E_SINGULAR, ex.what());
     }
     *out = h.release();
+  })
+}
+
+int pecs_lu_set_gpu_factor_min_front(int rows) { return g_lu_gpu_min_front.exchange(rows); }
+
+int pecs_debug_lu_values(pecs_lu* lu, double* out, long long n, long long* count) {
+  PECS_TRY({
+    if (!lu) throw PecsError(PECS_E_ARG, "lu is NULL");
+    const MfFactor& F = lu->h.F;
+    if (F.Gf.empty()) throw PecsError(PECS_E_STATE, "host factors were released");
+    long long tot = 0;
+    for (size_t j = 0; j < F.Gf.size(); ++j) tot += (long long)(F.Gf[j].size() + F.Hb[j].size());
+    if (count) *count = tot;
+    if (out) {
+      if (n < tot) throw PecsError(PECS_E_ARG, "output too small");
+      long long o = 0;
+      for (size_t j = 0; j < F.Gf.size(); ++j) {
+        std::copy(F.Gf[j].begin(), F.Gf[j].end(), out + o);
+        o += (long long)F.Gf[j].size();
+        std::copy(F.Hb[j].begin(), F.Hb[j].end(), out + o);
+        o += (long long)F.Hb[j].size();
+      }
+    }
   })
 }
 

@@ -294,7 +294,7 @@ namespace {
 // Factor one node's front.  Returns the update matrix S (m x m).
 std::vector<double> factor_node(MfFactor& F, int j, const Csr& A, const Csr& AT,
                                 std::vector<std::vector<double>>& Sstore, std::vector<int>& fpos,
-                                double& flops, dense::Team* team) {
+                                double& flops, dense::Team* team, const FrontOffload* off) {
   MfNode& nd = F.nodes[j];
   const int s = nd.s, m = nd.m, f = s + m;
   std::vector<double> Fm((size_t)f * f, 0.0);
@@ -339,6 +339,23 @@ std::vector<double> factor_node(MfFactor& F, int j, const Csr& A, const Csr& AT,
   double colmax_all = 0.0;
   for (size_t t = 0; t < (size_t)s * f; ++t) colmax_all = std::max(colmax_all, std::fabs(Fm[t]));
   double bad = 0.0;
+  if (off && off->factor && f >= off->min_front) {
+    // the same factorisation on the device
+    std::vector<double> S;
+    const int bc = off->factor(off->ctx, f, s, Fm.data(), 1e-14 * colmax_all, perm.data(), &bad, F.Gf[j],
+                               F.Hb[j], S);
+    if (bc >= 0) {
+      std::ostringstream e;
+      e << "singular pivot " << bad << " at node " << j << " column " << bc << " (front " << s << "+" << m
+        << ")";
+      throw std::runtime_error(e.str());
+    }
+    for (int col = 0; col < s; ++col) flops += 2.0 * (double)(f - col - 1) * (double)(f - col - 1);
+    flops += 2.0 * s * s * (double)(s + m);
+    for (int t = 0; t < s; ++t) fpos[nd.own[t]] = -1;
+    for (int t = 0; t < m; ++t) fpos[nd.upd[t]] = -1;
+    return S;
+  }
   const int badcol = dense::lu_front(f, s, Fm.data(), f, perm.data(), 1e-14 * colmax_all, &bad, team);
   if (badcol >= 0) {
     std::ostringstream e;
@@ -391,7 +408,7 @@ Csr transpose(const Csr& A) {
 
 }  // namespace
 
-void mf_factorize(MfFactor& F, const Csr& A, int n_threads) {
+void mf_factorize(MfFactor& F, const Csr& A, int n_threads, const FrontOffload* off) {
   const int N = (int)F.nodes.size();
   Csr AT = transpose(A);
   F.Gf.assign(N, {});
@@ -424,7 +441,7 @@ void mf_factorize(MfFactor& F, const Csr& A, int n_threads) {
         if (t >= lvl.size()) break;
         int j = lvl[t];
         try {
-          Sstore[j] = factor_node(F, j, A, AT, Sstore, fpos, fl, team.get());
+          Sstore[j] = factor_node(F, j, A, AT, Sstore, fpos, fl, team.get(), off);
         } catch (const std::exception& e) {
           std::lock_guard<std::mutex> g(mu);
           if (err.empty()) err = e.what();

@@ -24,6 +24,7 @@
 // substitution inside a node).
 #pragma once
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -53,11 +54,27 @@ struct MfFactor {
   double factor_flops = 0.0;
 };
 
+// Dense work of one front handed to another device (front.cu): given the
+// assembled front Fm (f x f, row-major; s fully-summed rows/columns) and the
+// pivot threshold, returns -1 (or the first bad column, with its pivot
+// magnitude in *bad) and fills perm (s), Gf (f x s, permuted), Hb (s x f) and
+// the Schur complement S (m x m) exactly as the host path defines them.
+struct FrontOffload {
+  int min_front = 0;  // fronts with at least this many rows go to the device
+  void* ctx = nullptr;
+  int (*factor)(void* ctx, int f, int s, const double* Fm, double tiny, int* perm, double* bad,
+                std::vector<double>& G, std::vector<double>& H, std::vector<double>& S) = nullptr;
+};
+
+// The GPU implementation (front.cu) on `device`; fronts of min_front rows and up.
+std::shared_ptr<FrontOffload> make_gpu_front_offload(int device, int min_front);
+
 // Ordering + symbolic analysis.  Throws std::runtime_error on invalid input.
 MfFactor mf_analyze(const Csr& A, const int* dof_cell, const int* dof_class, int n_cells,
                     const double* cell_xy, int leaf_cells);
-// Numeric factorisation (FP64, host).  Throws std::runtime_error("singular ...").
-void mf_factorize(MfFactor& F, const Csr& A, int n_threads = 0);
+// Numeric factorisation (FP64, host; the largest fronts on a device when
+// `off` is given).  Throws std::runtime_error("singular ...").
+void mf_factorize(MfFactor& F, const Csr& A, int n_threads = 0, const FrontOffload* off = nullptr);
 // Host application of the stored factors (diagnostic; the product path runs on the GPU).
 void mf_apply_host(const MfFactor& F, const double* b, double* x);
 
