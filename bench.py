@@ -73,6 +73,8 @@ def parse():
                     help="full: learned warm start + 64-instance batches (FP32-mixed) with the "
                          "plain FP64 path measured beside it; plain: one configuration only")
     ap.add_argument("--batch-inst", type=int, default=64)
+    ap.add_argument("--leaf-cells", type=int, default=8,
+                    help="nested-dissection leaf size in cells (the solve tree's height)")
     ap.add_argument("--e2e-waves", type=int, default=4,
                     help="full mode: end-to-end points = this many times --batch-inst")
     ap.add_argument("--no-accuracy", action="store_true",
@@ -344,11 +346,13 @@ def run_profile_sweep(args):
     import pecs_gb300 as pg
     pg.build()
     prec = {"fp64": pg.PREC_FP64, "fp32ir": pg.PREC_FP32_IR, "mixed": pg.PREC_FP32_MIXED}[args.precision]
-    ctx = pg.Context(workload_params(args, 0), precision=prec)
+    ctx = pg.Context(workload_params(args, 0), precision=prec, leaf_cells=args.leaf_cells)
     which = 0 if args.profile_sweep == "carrier" else 1
     info = ctx.info()
     ms = ctx.time_solve(which, reps=1)
     out = {"profile_sweep": args.profile_sweep, "n_inst": args.n_inst, "precision": args.precision,
+           "leaf_cells": args.leaf_cells, "factor_entries": list(info.factor_entries),
+           "factor_levels": list(info.factor_levels),
            "sweep_ms": ms, "launches_per_sweep": info.solve_launches[which],
            "bytes_per_sweep": info.solve_bytes[which], "launches_setup": info.setup_launches,
            "tuned_sweep_ms": list(info.tuned_sweep_ms)}
