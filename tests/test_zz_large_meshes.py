@@ -70,6 +70,27 @@ def test_refine7_k2_fp32_refined_matches_fp64(pecs_lib):
     assert np.linalg.norm(phi[0] - phi[2]) > 1e-6 * np.linalg.norm(phi[1])
 
 
+@pytest.mark.parametrize("refine", [7, pytest.param(8, marks=pytest.mark.skipif(
+    os.environ.get("PECS_LARGE_TESTS") != "1", reason="refinement 8 with k=2: PECS_LARGE_TESTS=1"))])
+def test_setup_with_gpu_fronts_matches_host_setup(pecs_lib, refine):
+    """The factorisation with the large fronts on the GPU (the default) gives
+    the trajectory of the all-host factorisation; prints both setup times."""
+    times, states = {}, {}
+    for label, mf in (("gpu fronts", 0), ("host", -1)):
+        t0 = time.perf_counter()
+        ctx = pg.Context(_instances(refine), precision=pg.PREC_FP64, gpu_factor_min_front=mf)
+        times[label] = time.perf_counter() - t0
+        ctx.initialize()
+        ctx.step(2)
+        states[label] = [ctx.state(i) for i in range(len(BIASES))]
+        ctx.close()
+    print(f"refine {refine} k=2 setup: {times['gpu fronts']:.1f} s with the large fronts on the GPU, "
+          f"{times['host']:.1f} s on the host")
+    for a, b in zip(states["gpu fronts"], states["host"]):
+        for f in b:
+            assert np.linalg.norm(a[f] - b[f]) / np.linalg.norm(b[f]) < 1e-11, f
+
+
 @pytest.mark.skipif(os.environ.get("PECS_LARGE_TESTS") != "1",
                     reason="refinement 8 with k=2 takes minutes of host setup; PECS_LARGE_TESTS=1")
 def test_refine8_k2_fp32_refined_residuals(pecs_lib):
