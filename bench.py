@@ -75,6 +75,9 @@ def parse():
     ap.add_argument("--batch-inst", type=int, default=64)
     ap.add_argument("--leaf-cells", type=int, default=8,
                     help="nested-dissection leaf size in cells (the solve tree's height)")
+    ap.add_argument("--flow", type=int, choices=[-1, 0, 1], default=0,
+                    help="batched solve sweeps: 1 = one persistent launch per direction, "
+                         "-1 = one launch per tree level, 0 = whichever the autotuner times faster")
     ap.add_argument("--e2e-waves", type=int, default=4,
                     help="full mode: end-to-end points = this many times --batch-inst")
     ap.add_argument("--no-accuracy", action="store_true",
@@ -346,7 +349,8 @@ def run_profile_sweep(args):
     import pecs_gb300 as pg
     pg.build()
     prec = {"fp64": pg.PREC_FP64, "fp32ir": pg.PREC_FP32_IR, "mixed": pg.PREC_FP32_MIXED}[args.precision]
-    ctx = pg.Context(workload_params(args, 0), precision=prec, leaf_cells=args.leaf_cells)
+    ctx = pg.Context(workload_params(args, 0), precision=prec, leaf_cells=args.leaf_cells,
+                     flow_sweep=args.flow)
     which = 0 if args.profile_sweep == "carrier" else 1
     info = ctx.info()
     ms = ctx.time_solve(which, reps=1)
@@ -355,8 +359,8 @@ def run_profile_sweep(args):
            "factor_levels": list(info.factor_levels),
            "sweep_ms": ms, "launches_per_sweep": info.solve_launches[which],
            "bytes_per_sweep": info.solve_bytes[which], "launches_setup": info.setup_launches,
-           "tuned_sweep_ms": list(info.tuned_sweep_ms)}
-    if args.level_times and args.precision != "fp64":
+           "tuned_sweep_ms": list(info.tuned_sweep_ms), "flow_rpl": list(info.flow_rpl), "flow_top": list(info.flow_top)}
+    if args.level_times and args.precision != "fp64" and info.flow_rpl[which] == 0:
         import ctypes as C
         buf = (C.c_double * 64)()
         n = pg.lib().pecs_debug_time_levels(ctx._h, which, 20, buf, 64)
@@ -378,7 +382,8 @@ def run_plain(args):
     pg.build()
     prec = {"fp64": pg.PREC_FP64, "fp32ir": pg.PREC_FP32_IR, "mixed": pg.PREC_FP32_MIXED}[args.precision]
     params = workload_params(args, rank)
-    ctx = pg.Context(params, precision=prec, device=local, use_graphs=args.profile_steps == 0)
+    ctx = pg.Context(params, precision=prec, device=local, use_graphs=args.profile_steps == 0,
+                     flow_sweep=args.flow)
     info = ctx.info()
     if args.profile_steps:
         ctx.initialize()
@@ -392,7 +397,7 @@ def run_plain(args):
                "precision": args.precision, "ms_per_time_step": ms_step,
                "launches_per_step": info.launches_per_step,
                "launches_setup": info.setup_launches,
-               "tuned_sweep_ms": list(info.tuned_sweep_ms),
+               "tuned_sweep_ms": list(info.tuned_sweep_ms), "flow_rpl": list(info.flow_rpl), "flow_top": list(info.flow_top),
                "launches_initialize": info.initialize_launches,
                "carrier_sweep_ms": ctx.time_solve(0, reps=5),
                "poisson_sweep_ms": ctx.time_solve(1, reps=5)}
@@ -605,7 +610,7 @@ def run_full(args):
     thetas = L.sample(per_rank * world, seed=777)[rank * per_rank:(rank + 1) * per_rank]
     th_w, th_t, th_e = thetas[:n_w], thetas[n_w:n_w + n_t], thetas[n_w + n_t:]
     ctx = pg.Context([L.instance_params(t, base) for t in thetas[:B]], precision=pg.PREC_FP32_MIXED,
-                     device=local)
+                     device=local, leaf_cells=args.leaf_cells, flow_sweep=args.flow)
     info = ctx.info()
     trained_here = None
     if os.path.exists(args.model):
@@ -718,8 +723,11 @@ def run_full(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": load_traffic(f"carrier_solve_ref{args.refine}_mixed_b{B}"),
-                     "kernel": "k_panel / k_panel_warp (carrier multifrontal solve sweep, FP32, "
-                               f"{2 * B} right-hand sides per factor)",
+                     "kernel": ("k_panel_flow (carrier multifrontal solve sweep, one persistent "
+                                "launch per direction, FP32, " if info.flow_rpl[0] else
+                                "k_panel / k_panel_warp (carrier multifrontal solve sweep, one launch "
+                                "per tree level, FP32, ") + f"{2 * B} right-hand sides per factor)",
+                     "flow_rpl": info.flow_rpl[0], "flow_top": info.flow_top[0],
                      "solve_ms": solve_ms, "launches_per_sweep": nlaunch,
                      "bytes_per_sweep": info.solve_bytes[0],
                      "plain_fp64": {"solve_ms": plain_ms, "achieved_gbs": plain_gbs,

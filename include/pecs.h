@@ -130,6 +130,18 @@ typedef struct pecs_options {
   int gpu_factor_min_front; /* factorisation: fronts with at least this many rows are
                                factored in FP64 on the GPU (0 = default 1024; < 0 = all
                                on the host); host_setup_only contexts factor on the host */
+  int flow_sweep;      /* panel solve kernels: one persistent launch per sweep direction,
+                          nodes started as soon as their children (forward) or parent
+                          (backward) finish, instead of one launch per tree level
+                          (0 = default: when the autotuner times it faster; 1 = wherever
+                          a flow plan applies; -1 = never).  A flow plan applies to banks
+                          whose sweep vector rows are whole 128-byte lines */
+  int increment_solves; /* PECS_PREC_FP32_MIXED: time steps solve for the increment from the
+                           previous step's solution -- the residual b - K u_prev in FP32 pairs,
+                           one FP32 sweep, u = u_prev + increment -- instead of a sweep and a
+                           refinement sweep from zero; the fixed point is the FP64 system's
+                           (the residual vanishes there).  Initial and refill solves keep
+                           the refinement.  (1 = on, 0 = default: off) */
 } pecs_options;
 
 typedef struct pecs_info {
@@ -147,6 +159,10 @@ typedef struct pecs_info {
   int setup_launches;      /* kernel launches issued by pecs_create (tiling autotuner) */
   int initialize_launches; /* kernel launches of pecs_initialize */
   double tuned_sweep_ms[2]; /* autotuner: time of the tuned carrier / Poisson sweep (0: untuned) */
+  int flow_rpl[2];         /* carrier / Poisson sweeps: right-hand sides per lane of the flow
+                              sweep in use (0: one launch per tree level) */
+  int flow_top[2];         /* carrier / Poisson sweeps: tree levels (from the root side) the
+                              flow launches cover; the others are launched level by level */
 } pecs_info;
 
 typedef struct pecs_ctx pecs_ctx;

@@ -1,11 +1,12 @@
 /*
- * pecs_debug.h -- diagnostics of the pecs C ABI that involve no GPU.
+ * pecs_debug.h -- diagnostics of the pecs C ABI; no product path calls them.
  *
  * pecs_lu_host_apply applies, on the host, the multifrontal factors that
  * pecs_lu_factor computed (before they are uploaded to the device by the
- * first pecs_lu_solve*).  It exists so that the ordering and factorisation
- * logic can be checked on machines without a GPU; no product path calls it.
- * pecs_debug_time_levels times the levels of a solve sweep for profiling.
+ * first pecs_lu_solve*), so that the ordering and factorisation logic can be
+ * checked on machines without a GPU; pecs_debug_lu_values exports them.
+ * pecs_debug_time_levels times the levels of a solve sweep for profiling, and
+ * pecs_debug_flow_stall exercises the bounded waits of the flow sweeps.
  */
 #ifndef PECS_DEBUG_H
 #define PECS_DEBUG_H
@@ -25,6 +26,13 @@ int pecs_debug_time_levels(pecs_ctx* ctx, int which, int reps, double* ms, int c
  * out (capacity n doubles); returns the count via *count (out may be NULL to
  * query it). */
 int pecs_debug_lu_values(pecs_lu* lu, double* out, long long n, long long* count);
+/* Contexts whose carrier (which = 0) or Poisson (1) bank uses the flow sweep:
+ * sets the first factor's root counter of the next forward flow sweep far
+ * below its target, runs one solve sweep of that bank (the root's waits run
+ * out after their poll limit), and returns in *flag the bank's flow error
+ * flag (1: a wait ran out and that sweep wrote NaN), clearing it.  The
+ * sweep's outputs are overwritten; the context stays usable. */
+int pecs_debug_flow_stall(pecs_ctx* ctx, int which, int* flag);
 #ifdef __cplusplus
 }
 #endif

@@ -51,7 +51,8 @@ class pecs_options(C.Structure):
         ("precision", C.c_int), ("leaf_cells", C.c_int), ("use_graphs", C.c_int),
         ("ir_max_iters", C.c_int), ("ir_tol", C.c_double), ("device", C.c_int),
         ("host_setup_only", C.c_int), ("panel_chunk", C.c_int), ("panel_min_ctas", C.c_int),
-        ("autotune", C.c_int), ("gpu_factor_min_front", C.c_int),
+        ("autotune", C.c_int), ("gpu_factor_min_front", C.c_int), ("flow_sweep", C.c_int),
+        ("increment_solves", C.c_int),
     ]
 
 
@@ -63,7 +64,7 @@ class pecs_info(C.Structure):
         ("n_distinct_carrier_factors", C.c_int), ("launches_per_step", C.c_int),
         ("solve_bytes", C.c_double * 2), ("solve_launches", C.c_int * 2),
         ("setup_launches", C.c_int), ("initialize_launches", C.c_int),
-        ("tuned_sweep_ms", C.c_double * 2),
+        ("tuned_sweep_ms", C.c_double * 2), ("flow_rpl", C.c_int * 2), ("flow_top", C.c_int * 2),
     ]
 
 
@@ -159,6 +160,7 @@ SIGNATURES = [
     ("pecs_lu_solve_device_noalloc", C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     ("pecs_lu_host_apply", C.c_int, [_vp, _dp, _dp]),
     ("pecs_debug_time_levels", C.c_int, [_vp, C.c_int, C.c_int, _dp, C.c_int]),
+    ("pecs_debug_flow_stall", C.c_int, [_vp, C.c_int, _ip]),
     ("pecs_mlp_create", C.c_int, [C.c_int, _ip, C.c_ulonglong, C.POINTER(_vp)]),
     ("pecs_mlp_destroy", None, [_vp]),
     ("pecs_mlp_n_params", C.c_int, [_vp, C.POINTER(C.c_longlong)]),

@@ -297,7 +297,8 @@ def reference_params(n_refine: int = 4, degree: int = 1, **kw) -> Params:
 def default_options(precision: int = PREC_FP64, use_graphs: bool = True, leaf_cells: int = 8,
                     ir_max_iters: int = 0, device: int = 0, host_setup_only: bool = False,
                     panel_chunk: int = 0, panel_min_ctas: int = 0,
-                    autotune: bool = True, gpu_factor_min_front: int = 0) -> F.pecs_options:
+                    autotune: bool = True, gpu_factor_min_front: int = 0,
+                    flow_sweep: int = 0, increment_solves: bool = False) -> F.pecs_options:
     o = F.pecs_options()
     lib().pecs_default_options(C.byref(o))
     o.precision = precision
@@ -310,6 +311,8 @@ def default_options(precision: int = PREC_FP64, use_graphs: bool = True, leaf_ce
     o.panel_min_ctas = panel_min_ctas
     o.autotune = int(autotune)
     o.gpu_factor_min_front = gpu_factor_min_front
+    o.flow_sweep = flow_sweep
+    o.increment_solves = int(increment_solves)
     return o
 
 
@@ -323,14 +326,15 @@ class Context:
     def __init__(self, params: Sequence[Params] | Params, precision: int = PREC_FP64,
                  use_graphs: bool = True, leaf_cells: int = 8, ir_max_iters: int = 0,
                  device: int = 0, host_setup_only: bool = False, panel_chunk: int = 0,
-                 panel_min_ctas: int = 0, autotune: bool = True, gpu_factor_min_front: int = 0):
+                 panel_min_ctas: int = 0, autotune: bool = True, gpu_factor_min_front: int = 0,
+                 flow_sweep: int = 0, increment_solves: bool = False):
         if isinstance(params, Params):
             params = [params]
         self.params = list(params)
         arr = (F.pecs_params * len(self.params))(*[p.to_c() for p in self.params])
         opt = default_options(precision, use_graphs, leaf_cells, ir_max_iters, device,
                               host_setup_only, panel_chunk, panel_min_ctas, autotune,
-                              gpu_factor_min_front)
+                              gpu_factor_min_front, flow_sweep, increment_solves)
         h = C.c_void_p()
         check(lib().pecs_create(arr, len(self.params), C.byref(opt), C.byref(h)))
         self._h = h

@@ -139,6 +139,40 @@ __global__ void k_scatter_sum_il(const float* __restrict__ x32, const float* __r
   }
 }
 
+// dst[d * R + k] = src[k][d] as an FP32 pair (the previous step's solution,
+// interleaved for the residual of an increment solve)
+__global__ void k_gather_pairs_il(const double* const* __restrict__ src, float2* __restrict__ dst, int n, int R) {
+  __shared__ double t[32][33];
+  const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k = k0 + kk, d = d0 + threadIdx.x;
+    t[kk][threadIdx.x] = (k < R && d < n) ? src[k][d] : 0.0;
+  }
+  __syncthreads();
+  for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
+    const int d = d0 + dd, k = k0 + threadIdx.x;
+    if (d < n && k < R) dst[(size_t)d * R + k] = d2ff(t[threadIdx.x][dd]);
+  }
+}
+
+// dst_k[d] = old_k[d] + (double) d32[d * R + k]: the previous step's solution
+// plus the increment an increment solve found
+__global__ void k_scatter_delta_il(const float* __restrict__ d32, const double* const* __restrict__ old,
+                                   double* const* __restrict__ dst, int n, int R, const int* __restrict__ mask,
+                                   int nf) {
+  __shared__ float t[32][33];
+  const int d0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int dd = threadIdx.y; dd < 32; dd += blockDim.y) {
+    const int d = d0 + dd, k = k0 + threadIdx.x;
+    t[dd][threadIdx.x] = (d < n && k < R) ? d32[(size_t)d * R + k] : 0.f;
+  }
+  __syncthreads();
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k = k0 + kk, d = d0 + threadIdx.x;
+    if (k < R && d < n && (!mask || mask[k / nf])) dst[k][d] = old[k][d] + f2d_exact(t[threadIdx.x][kk]);
+  }
+}
+
 // x = (double) x32 + (double) d32
 __global__ void k_sum_il(const float* __restrict__ x32, const float* __restrict__ d32,
                          double* __restrict__ x, size_t n) {
@@ -476,6 +510,7 @@ struct Engine {
   DBuf<double> t_phi, t_qw, t_fphi, t_fw, t_psix, t_psiy, t_phiP, t_mref;
   DBuf<float> tf_phi, tf_qw, tf_fphi, tf_fw, tf_psix, tf_psiy;
   DBuf<double> t_drift_x, t_drift_y;
+  DBuf<float2> t_drift_x_ff, t_drift_y_ff, t_mref_ff;
   DBuf<int> t_drift_cx, t_drift_cy;
   DBuf<double> t_charge;
   Tables T{};
@@ -556,8 +591,11 @@ struct Engine {
   int launches_per_step() const {
     const int lc = bank_c.kernel_launches_per_solve(), lp = bank_p.kernel_launches_per_solve();
     const int sc = il[0].n_sets, sp = il[1].n_sets;
-    return 1 + lc * (1 + ir_iters(0)) + sc * set_launches_per_solve(0) + 1 + lp * (1 + ir_iters(1)) +
-           sp * set_launches_per_solve(1) + 3;
+    // increment solves: gather, gather of the previous solution, residual and
+    // scatter per set, one sweep
+    const bool dc = delta_solves() && il_f32(0), dp = delta_solves() && il_f32(1);
+    return 1 + (dc ? lc + 4 * sc : lc * (1 + ir_iters(0)) + sc * set_launches_per_solve(0)) + 1 +
+           (dp ? lp + 4 * sp : lp * (1 + ir_iters(1)) + sp * set_launches_per_solve(1)) + 3;
   }
   // algorithmic bytes of one application of a bank to all of its right-hand
   // sides: every stored factor entry once, plus the vectors (b read, y write +
@@ -688,7 +726,42 @@ struct Engine {
   // x = A^-1 b for every right-hand side of a bank, in the interleaved layout:
   // gather the instance-major RHS vectors, sweep (+ refinement), scatter the
   // solutions into state[target].
-  void solve_bank_il(const FactorBank& bank, int which, int target, cudaStream_t s) {
+  // Increment solves (time steps of the mixed mode with increment_solves):
+  // r = b - K u_prev with u_prev the previous step's solution (state buffer
+  // 1 - target) in FP32 pairs, one FP32 sweep d = K32^-1 r, u = u_prev + d.
+  // The error of d relative to the exact increment is that of one FP32 solve,
+  // so it shrinks with the step's change and vanishes at the fixed point,
+  // where r = 0: the steady state is that of the FP64 system.
+  bool delta_solves() const {
+    return opt.increment_solves > 0 && opt.precision == PECS_PREC_FP32_MIXED;
+  }
+  void solve_bank_delta(const FactorBank& bank, int which, int target, cudaStream_t s) {
+    IlBank& I = il[which];
+    const dim3 tb(32, 8);
+    for (int si = 0; si < I.n_sets; ++si) {
+      IlSet& S_ = I.set[si];
+      const dim3 g((S_.n + 31) / 32, (S_.R + 31) / 32);
+      k_gather_il<<<g, tb, 0, s>>>(S_.src.p, S_.B.p, nullptr, S_.n, S_.R);
+      PECS_CUDA(cudaGetLastError());
+      k_gather_pairs_il<<<g, tb, 0, s>>>(S_.dst[1 - target].p, S_.Xs.p, S_.n, S_.R);
+      PECS_CUDA(cudaGetLastError());
+      launch_residual_df(csr_df.m[S_.mat], S_.B.p, S_.Xs.p, S_.Rr32.p, S_.n, S_.R, s);
+    }
+    bank_sweep(bank, which, true, s);
+    for (int si = 0; si < I.n_sets; ++si) {
+      IlSet& S_ = I.set[si];
+      const dim3 g((S_.n + 31) / 32, (S_.R + 31) / 32);
+      k_scatter_delta_il<<<g, tb, 0, s>>>(S_.D32.p, S_.dst[1 - target].p, S_.dst[target].p, S_.n, S_.R,
+                                          scatter_mask, S_.R / n_inst);
+      PECS_CUDA(cudaGetLastError());
+    }
+  }
+
+  void solve_bank_il(const FactorBank& bank, int which, int target, cudaStream_t s, bool delta = false) {
+    if (delta && il_f32(which) && target != cur) {
+      solve_bank_delta(bank, which, target, s);
+      return;
+    }
     IlBank& I = il[which];
     const dim3 tb(32, 8);
     const bool f32 = il_f32(which);
@@ -897,16 +970,26 @@ struct Engine {
     build_il(0, carrier_set_fields(), bank_c);
     build_il(1, {{4}}, bank_p);
     if (opt.autotune) {
-      // panel banks: per level, the fastest tiling for these right-hand sides
+      // panel banks: per level, the fastest tiling for these right-hand sides,
+      // then the flow sweep if it is faster still
       for (int which = 0; which < 2; ++which) {
         FactorBank& bk = which == 0 ? bank_c : bank_p;
         if (!bk.panel()) continue;
         if (il_f32(which))
-          bk.autotune(il_view_f(which, false), il[which].max_R, st);
+          bk.autotune(il_view_f(which, false), il[which].max_R, st, 3, opt.flow_sweep);
         else
-          bk.autotune(il_view(which, false), il[which].max_R, st);
+          bk.autotune(il_view(which, false), il[which].max_R, st, 3, opt.flow_sweep);
       }
       PECS_CUDA(cudaStreamSynchronize(st));
+    } else if (opt.flow_sweep > 0) {
+      for (int which = 0; which < 2; ++which) {
+        FactorBank& bk = which == 0 ? bank_c : bank_p;
+        if (!bk.panel()) continue;
+        if (il_f32(which))
+          bk.force_flow(il_view_f(which, false), il[which].max_R);
+        else
+          bk.force_flow(il_view(which, false), il[which].max_R);
+      }
     }
     // steady-state buffers
     partial.alloc((size_t)n_inst * 5 * kRedChunks);
@@ -1025,9 +1108,23 @@ struct Engine {
       for (int b = 0; b < n1; ++b)
         for (int q = 0; q < Q; ++q) chg[(size_t)a * n1 + b] += pt.phi[a * Q + q] * ct.phi[b * Q + q] * ct.qw[q];
     t_charge.upload(chg);
+    // FP32 pairs (hi rounded to nearest, lo the rounded remainder) for the
+    // mixed path
+    auto ff = [](const std::vector<double>& v) {
+      std::vector<float2> o(v.size());
+      for (size_t k = 0; k < v.size(); ++k) {
+        const float hi = (float)v[k];
+        o[k] = make_float2(hi, (float)(v[k] - (double)hi));
+      }
+      return o;
+    };
+    t_drift_x_ff.upload(ff(dx));
+    t_drift_y_ff.upload(ff(dy));
+    t_mref_ff.upload(ff(mref));
     T = Tables{t_phi.p,  t_qw.p,  t_fphi.p,  t_fw.p,   t_psix.p,  t_psiy.p, t_phiP.p,
                t_mref.p, tf_phi.p, tf_qw.p, tf_fphi.p, tf_fw.p, tf_psix.p, tf_psiy.p,
-               t_drift_x.p, t_drift_y.p, t_drift_cx.p, t_drift_cy.p, t_charge.p};
+               t_drift_x.p, t_drift_y.p, t_drift_cx.p, t_drift_cy.p, t_charge.p,
+               t_drift_x_ff.p, t_drift_y_ff.p, t_mref_ff.p};
   }
 
   void upload_regions() {
@@ -1162,7 +1259,7 @@ struct Engine {
 
   void stage_carrier_rhs(cudaStream_t s, const int* act) { launch_carrier_rhs(s, act); }
   void stage_solve_carriers(cudaStream_t s, const int* act) {
-    solve_bank_il(bank_c, 0, nxt(), s);
+    solve_bank_il(bank_c, 0, nxt(), s, delta_solves());
     carriers_advanced = true;
   }
   void stage_poisson_rhs(cudaStream_t s, const int* act) {
@@ -1170,7 +1267,7 @@ struct Engine {
   }
   void stage_solve_poisson(cudaStream_t s, const int* act) {
     const int target = carriers_advanced ? nxt() : cur;
-    solve_bank_il(bank_p, 1, target, s);
+    solve_bank_il(bank_p, 1, target, s, delta_solves() && carriers_advanced);
     if (carriers_advanced) {
       cur = nxt();
       carriers_advanced = false;
@@ -1692,6 +1789,10 @@ int pecs_get_info(pecs_ctx* ctx, pecs_info* info) {
       info->initialize_launches = e.initialize_launches();
       info->tuned_sweep_ms[0] = e.bank_c.tuned_ms();
       info->tuned_sweep_ms[1] = e.bank_p.tuned_ms();
+      info->flow_rpl[0] = e.bank_c.flow_rpl();
+      info->flow_rpl[1] = e.bank_p.flow_rpl();
+      info->flow_top[0] = e.bank_c.flow_top();
+      info->flow_top[1] = e.bank_p.flow_top();
     }
   })
 }
@@ -2294,6 +2395,20 @@ int pecs_debug_time_levels(pecs_ctx* ctx, int which, int reps, double* ms, int c
     })
   }();
   return rc == PECS_OK ? n : rc;
+}
+
+int pecs_debug_flow_stall(pecs_ctx* ctx, int which, int* flag) {
+  PECS_TRY({
+    if (!ctx || !flag || (which != 0 && which != 1)) throw PecsError(PECS_E_ARG, "invalid arguments");
+    Engine& e = ctx->e;
+    need_device(e);
+    const FactorBank& B = which == 0 ? e.bank_c : e.bank_p;
+    if (B.flow_rpl() == 0) throw PecsError(PECS_E_STATE, "the bank does not use the flow sweep");
+    B.debug_arm_flow_stall();
+    e.bank_sweep(B, which, false, e.st);
+    PECS_CUDA(cudaStreamSynchronize(e.st));
+    *flag = B.flow_error(true);
+  })
 }
 
 // diagnostic: apply the host copy of the factors (no GPU involved)

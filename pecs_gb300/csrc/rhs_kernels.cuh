@@ -40,6 +40,9 @@ struct Tables {
   const int *drift_cx, *drift_cy;  // their RT indices, nrt/2 each
   // Poisson charge matrix sum_q phiP_a phi_b w_q on the unit square, nphi x n1
   const double* charge;
+  // FP32-pair copies (hi, lo) of the drift tensors and the mass matrix for the
+  // mixed-precision path
+  const float2 *drift_x_ff, *drift_y_ff, *mref_ff;
 };
 
 struct RegionDev {
@@ -106,14 +109,16 @@ __device__ __forceinline__ const float* tab<float>(const double*, const float* f
 // grid: x over (cells of both regions) * 2 carriers, y over instances.
 // Tq is the arithmetic type of the quadrature terms (SRH, interface, Schottky,
 // and in the FP64 path the drift).  Tq = double is the FP64 path.  Tq = float
-// is the mixed path: the constant part, (1/dt) M u^{n-1} and the drift term
-// of the current equations, (q/eps) u D, stay FP64 -- the drift is large
-// (|D|/h relative to the density terms) and its rounding would leave a
-// per-step noise of ~eps32 |D| dt / h in the densities, above a 1e-8
-// steady-state criterion; it is evaluated as the bilinear form
-// sum_bc T_abc u_b D_c with precomputed tensors -- while the small
-// recombination and interface terms run on the FP32 pipe (GB300 issues FP32
-// FMAs ~60x faster than FP64).
+// is the mixed path: (1/dt) M u^{n-1} and the drift term of the current
+// equations, (q/eps) u D, keep ~47-bit accuracy -- the drift is large (|D|/h
+// relative to the density terms) and its rounding would leave a per-step
+// noise of ~eps32 |D| dt / h in the densities, above a 1e-8 steady-state
+// criterion -- but run in FP32-pair arithmetic on the FP32 pipe (fp_bits.cuh;
+// inputs split on the integer pipe), the drift as the bilinear form
+// sum_bc T_abc u_b D_c with precomputed tensors; the small recombination and
+// interface terms run in plain FP32, and only the final additions to the
+// constant part are FP64 (GB300 issues FP32 operations ~60x faster than FP64,
+// conversions included).
 template <int K, int KP, typename Tq>
 __global__ void __launch_bounds__(128)
     k_carrier_rhs(Tables T, RegionDev semi, RegionDev elec, int n_regions, FieldPtrs F,
@@ -156,21 +161,21 @@ __global__ void __launch_bounds__(128)
   const double* Pv = F.u[4] + (size_t)i * F.nd[4];
   Tq Dd[nrt];
 #pragma unroll
-  for (int b = 0; b < nrt; ++b) Dd[b] = (Tq)Pv[R.rt[c * nrt + b]];
+  for (int b = 0; b < nrt; ++b) Dd[b] = to_q<Tq>(Pv[R.rt[c * nrt + b]]);
   const double2 h = R.h[c];
   const double hxhy = h.x * h.y;
-  const Tq hxhy_q = (Tq)hxhy;
+  const Tq hxhy_q = to_q<Tq>(hxhy);
   const Tq charge = which ? Tq(1) : Tq(-1);
-  const Tq inv_eps = (Tq)R.inv_eps;
+  const Tq inv_eps = to_q<Tq>(R.inv_eps);
   // quadrature-term accumulators: [Jx (n1) | Jy (n1) | u (n1)]
   Tq r[3 * n1];
-  double drift64[2 * n1];  // mixed path: FP64 drift of the current rows
+  float2 drift_ff[2 * n1];  // mixed path: FP32-pair drift of the current rows
 #pragma unroll
-  for (int a = 0; a < 2 * n1; ++a) drift64[a] = 0.0;
+  for (int a = 0; a < 2 * n1; ++a) drift_ff[a] = make_float2(0.f, 0.f);
 #pragma unroll
   for (int a = 0; a < 3 * n1; ++a) r[a] = Tq(0);
   const bool srh = in_semi && P.srh;
-  const Tq ni = (Tq)P.n_i, taun = (Tq)P.tau_n, taup = (Tq)P.tau_p;
+  const Tq ni = to_q<Tq>(P.n_i), taun = to_q<Tq>(P.tau_n), taup = to_q<Tq>(P.tau_p);
 #pragma unroll 1
   for (int q = 0; q < Q; ++q) {
     const Tq JxW = qw[q] * hxhy_q;
@@ -201,33 +206,30 @@ __global__ void __launch_bounds__(128)
       r[2 * n1 + a] += ph * Rq;
     }
   }
+  float2 uff[n1];  // mixed path: the own density in FP32 pairs
   if constexpr (!std::is_same<Tq, double>::value) {
-    // FP64 drift of the current equations: (q/eps) hx hy sum_bj T_abj u_b D_j,
-    // with the products u_b D_j formed once (n1 * nrt/2 per component)
-    constexpr int NC = nrt / 2;
-    double px[n1 * NC], py[n1 * NC];
 #pragma unroll
+    for (int a = 0; a < n1; ++a) uff[a] = d2ff(uown[a]);
+    // drift of the current equations: (q/eps) hx hy sum_bj T_abj u_b D_j, each
+    // product u_b D_j formed once and added into every row a
+    constexpr int NC = nrt / 2;
+#pragma unroll 1
     for (int j = 0; j < NC; ++j) {
-      const double dx = Pv[R.rt[c * nrt + T.drift_cx[j]]];
-      const double dy = Pv[R.rt[c * nrt + T.drift_cy[j]]];
+      const float2 dx = d2ff(Pv[R.rt[c * nrt + T.drift_cx[j]]]);
+      const float2 dy = d2ff(Pv[R.rt[c * nrt + T.drift_cy[j]]]);
 #pragma unroll
       for (int b = 0; b < n1; ++b) {
-        px[b * NC + j] = uown[b] * dx;
-        py[b * NC + j] = uown[b] * dy;
+        const float2 px = ff_mul(uff[b], dx), py = ff_mul(uff[b], dy);
+#pragma unroll
+        for (int a = 0; a < n1; ++a) {
+          drift_ff[a] = ff_fma(T.drift_x_ff[(a * n1 + b) * NC + j], px, drift_ff[a]);
+          drift_ff[n1 + a] = ff_fma(T.drift_y_ff[(a * n1 + b) * NC + j], py, drift_ff[n1 + a]);
+        }
       }
     }
-    const double sc = (which ? 1.0 : -1.0) * R.inv_eps * hxhy;
+    const float2 sc = d2ff((which ? 1.0 : -1.0) * R.inv_eps * hxhy);
 #pragma unroll
-    for (int a = 0; a < n1; ++a) {
-      double sx = 0.0, sy = 0.0;
-#pragma unroll
-      for (int t = 0; t < n1 * NC; ++t) {
-        sx += T.drift_x[a * n1 * NC + t] * px[t];
-        sy += T.drift_y[a * n1 * NC + t] * py[t];
-      }
-      drift64[a] = sc * sx;
-      drift64[n1 + a] = sc * sy;
-    }
+    for (int a = 0; a < 2 * n1; ++a) drift_ff[a] = ff_mul(sc, drift_ff[a]);
   }
   // interface Robin transfer (SolarCell.cpp:1265-1347, 1630-1716)
   const int4 bid = R.bid[c];
@@ -237,8 +239,8 @@ __global__ void __launch_bounds__(128)
     const double* o1p = F.u[O.field1] + (size_t)i * F.nd[O.field1] + 2 * O.nc * n1 + pc * n1;
     const double* o2p = F.u[O.field1 + 1] + (size_t)i * F.nd[O.field1 + 1] + 2 * O.nc * n1 + pc * n1;
     const int ff = R.iface_face, pf = R.partner_face;
-    const Tq flen = (Tq)((ff == 0 || ff == 1) ? h.y : h.x);
-    const Tq ket = (Tq)P.k_et, kht = (Tq)P.k_ht;
+    const Tq flen = to_q<Tq>((ff == 0 || ff == 1) ? h.y : h.x);
+    const Tq ket = to_q<Tq>(P.k_et), kht = to_q<Tq>(P.k_ht);
 #pragma unroll 1
     for (int q = 0; q < nq; ++q) {
       Tq a1 = 0, a2 = 0, b1 = 0, b2 = 0;
@@ -254,8 +256,8 @@ __global__ void __launch_bounds__(128)
       // semiconductor-side values n, p and electrolyte-side r, o
       const Tq n = in_semi ? a1 : b1, p = in_semi ? a2 : b2;
       const Tq rr = in_semi ? b1 : a1, oo = in_semi ? b2 : a2;
-      const Tq ne = (Tq)iface_ne[(size_t)i * n_iface * nq + ii * nq + q];
-      const Tq pe = (Tq)iface_pe[(size_t)i * n_iface * nq + ii * nq + q];
+      const Tq ne = to_q<Tq>(iface_ne[(size_t)i * n_iface * nq + ii * nq + q]);
+      const Tq pe = to_q<Tq>(iface_pe[(size_t)i * n_iface * nq + ii * nq + q]);
       const Tq Jf = fw[q] * flen;
       const Tq tn = -ket * (n - ne) * oo * Jf;
       const Tq tp = kht * (p - pe) * rr * Jf;
@@ -273,21 +275,22 @@ __global__ void __launch_bounds__(128)
 #pragma unroll 1
     for (int fc = 0; fc < 4; ++fc) {
       if (bids[fc] != 3) continue;
-      const Tq flen = (Tq)((fc == 0 || fc == 1) ? h.y : h.x);
+      const Tq flen = to_q<Tq>((fc == 0 || fc == 1) ? h.y : h.x);
       for (int q = 0; q < nq; ++q) {
         Tq val = 0;
 #pragma unroll
         for (int a = 0; a < n1; ++a) val += fphi[(fc * n1 + a) * nq + q] * (which ? u2[a] : u1[a]);
         const size_t o = (size_t)i * nc * 4 * nq + (size_t)(c * 4 + fc) * nq + q;
         const Tq Jf = fw[q] * flen;
-        const Tq coef = which ? (Tq)P.s_p * (val - (Tq)sch_pe[o]) * Jf
-                              : -(Tq)P.s_n * (val - (Tq)sch_ne[o]) * Jf;
+        const Tq coef = which ? to_q<Tq>(P.s_p) * (val - to_q<Tq>(sch_pe[o])) * Jf
+                              : -to_q<Tq>(P.s_n) * (val - to_q<Tq>(sch_ne[o])) * Jf;
 #pragma unroll
         for (int a = 0; a < n1; ++a) r[2 * n1 + a] += fphi[(fc * n1 + a) * nq + q] * coef;
       }
     }
   }
-  // constant part + (1/dt) M u^{n-1} in FP64, then the quadrature terms
+  // constant part + (1/dt) M u^{n-1} (FP64, or FP32 pairs in the mixed path),
+  // then the quadrature terms
   const double* bcp = F.bc[f] + (size_t)i * nd;
   double* outp = F.out[f] + (size_t)i * nd;
 #pragma unroll
@@ -298,15 +301,27 @@ __global__ void __launch_bounds__(128)
       if constexpr (std::is_same<Tq, double>::value)
         outp[o] = bcp[o] + (double)r[comp * n1 + a];
       else
-        outp[o] = bcp[o] + drift64[comp * n1 + a];
+        outp[o] = bcp[o] + ff2d(drift_ff[comp * n1 + a]);
     }
+  if constexpr (std::is_same<Tq, double>::value) {
 #pragma unroll
-  for (int a = 0; a < n1; ++a) {
-    double s = 0.0;
+    for (int a = 0; a < n1; ++a) {
+      double s = 0.0;
 #pragma unroll
-    for (int b = 0; b < n1; ++b) s += T.mref[a * n1 + b] * uown[b];
-    const size_t o = (size_t)2 * nc * n1 + c * n1 + a;
-    outp[o] = bcp[o] + s * hxhy * R.inv_dt + from_q<Tq>(r[2 * n1 + a]);
+      for (int b = 0; b < n1; ++b) s += T.mref[a * n1 + b] * uown[b];
+      const size_t o = (size_t)2 * nc * n1 + c * n1 + a;
+      outp[o] = bcp[o] + s * hxhy * R.inv_dt + from_q<Tq>(r[2 * n1 + a]);
+    }
+  } else {
+    const float2 md = d2ff(hxhy * R.inv_dt);
+#pragma unroll
+    for (int a = 0; a < n1; ++a) {
+      float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int b = 0; b < n1; ++b) s = ff_fma(T.mref_ff[a * n1 + b], uff[b], s);
+      const size_t o = (size_t)2 * nc * n1 + c * n1 + a;
+      outp[o] = bcp[o] + ff2d(ff_add(ff_mul(s, md), r[2 * n1 + a]));
+    }
   }
 }
 

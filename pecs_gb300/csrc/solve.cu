@@ -1,5 +1,7 @@
 // Level-scheduled multifrontal solve kernels and their host-side plan (solve.cuh).
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 
@@ -548,10 +550,12 @@ __device__ __forceinline__ void sts(T* p, const VR (&v)[N]) {
 // The item record carries everything about its node (sizes, offsets, the
 // node's child-map range), and the node's index metadata is staged once, so
 // the chain of dependent loads per item is: record -> metadata -> copies.
+// nbuf = 2: the staging buffers are doubled and chunk c + 1 is copied while
+// chunk c is multiplied (items with more than one chunk).
 template <typename T>
 __host__ __device__ constexpr size_t panel_smem_bytes(int ds_rows, int rc, int kc, int ri_max,
-                                                      int sc_rows, int meta_ints) {
-  return ((size_t)ds_rows * rc + (size_t)kc * ri_max + (size_t)sc_rows * rc) * sizeof(T) +
+                                                      int sc_rows, int meta_ints, int nbuf = 1) {
+  return (size_t)nbuf * ((size_t)ds_rows * rc + (size_t)kc * ri_max + (size_t)sc_rows * rc) * sizeof(T) +
          (size_t)meta_ints * sizeof(int);
 }
 
@@ -567,6 +571,13 @@ __device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
 
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 
@@ -590,15 +601,35 @@ __device__ __forceinline__ void stage_row(T* dst, const T* src, bool ok) {
   }
 }
 
-template <typename T, int RPL, bool FWD, typename SVT>
-__global__ void __launch_bounds__(kSolveThreads)
-    k_panel(BankView B, SVT S, const PanelItem* __restrict__ items, int kc_cap, int ds_rows,
-            int ri_max, int sc_rows, int max_s, int max_f, int cm_cap, T* __restrict__ partials,
-            int* __restrict__ counters, int parts_ld, int ychunks) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+template <typename T>
+__device__ __forceinline__ T quiet_nan() {
+  if constexpr (sizeof(T) == 4)
+    return __int_as_float(0x7fc00000);
+  else
+    return __longlong_as_double(0x7ff8000000000000ll);
+}
+
+// Staging shape of a panel launch (its shared-memory layout): staged block
+// columns per chunk, staged right-hand-side rows, the tallest row tile, staged
+// child-update rows per chunk, and the index metadata sizes.
+struct PanelShape {
+  int kc_cap, ds_rows, ri_max, sc_rows, max_s, max_f, cm_cap;
+  int nbuf;  // staging buffers (2: the next chunk is copied during this one's products)
+};
+
+// One panel item (rows [r0, r1) of one node) applied to the right-hand-side
+// chunk starting at rc0 (chunk index `chunk`).  wait_inputs() is called by
+// every thread once the block tile's copies are in flight and before any
+// vector is read; it returns false when the inputs could not be waited for,
+// and the item then writes NaN (the solve's results are flagged non-finite).
+// main_done() is called once the item no longer reads its inputs.
+template <typename T, int RPL, bool FWD, typename SVT, typename Wait, typename Done>
+__device__ __forceinline__ void panel_tile(const BankView& B, const SVT& S, const PanelItem& I, int rc0,
+                                           int chunk, const PanelShape& P, T* __restrict__ partials,
+                                           int* __restrict__ counters, int parts_ld, int ychunks,
+                                           unsigned char* smem_raw, Wait wait_inputs, Done main_done) {
   constexpr int RC = 32 * RPL;
   constexpr int NW = kSolveThreads / 32;
-  const PanelItem I = items[blockIdx.x];
   const int r0 = I.a.y, r1 = I.a.z, ri = I.a.w;
   const int s = I.b.x, m = I.b.y, f = s + m, w_off = I.b.w;
   const auto st = S.set[I.b.z];
@@ -606,8 +637,9 @@ __global__ void __launch_bounds__(kSolveThreads)
   static_assert(std::is_same<typename std::remove_cv<typename std::remove_pointer<decltype(st.y)>::type>::type,
                              T>::value, "sweep vectors must have the block's type");
   const int R = st.nrhs;
-  const int rc0 = blockIdx.y * RC;
   if (rc0 >= R) return;
+  const int max_s = P.max_s, max_f = P.max_f, cm_cap = P.cm_cap, ri_max = P.ri_max;
+  const int ds_rows = P.ds_rows, sc_rows = P.sc_rows;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int rl = rc0 + lane * RPL;  // first right-hand side of this lane
   const bool lane_ok = rl < R;      // R is a multiple of RPL
@@ -617,17 +649,24 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int nrows = r1 - r0;
   const int wpr = 32 / ri;  // warps sharing a row group (column parts)
   const int g = warp / wpr, part = warp % wpr;
-  // split-K: this CTA covers columns [k_lo, k_hi) of a tile split in n_parts
+  // split-K: this CTA covers columns [k_lo, k_hi) of a tile split in n_parts;
+  // an unsplit item may carry its own (smaller) chunk width in e.x
   const bool split = I.e.z >= 0;
   const int k_lo = split ? I.e.x : 0, k_hi = split ? I.e.y : K;
-  T* Ds = reinterpret_cast<T*>(smem_raw);  // [ds_rows][RC], ds_rows >= 32 when ri < 32
-  T* Gs = Ds + (size_t)ds_rows * RC;        // [kc_cap][ri]
-  T* Sc = Gs + (size_t)kc_cap * ri_max;     // [sc_rows][RC] child-update rows of a chunk
+  const int kc_cap = (!split && I.e.x > 0) ? min(I.e.x, P.kc_cap) : P.kc_cap;
+  bool bad = false;
+  const int nbuf = P.nbuf;
+  // staging buffers, nbuf of each: Ds [ds_rows][RC] (nbuf * ds_rows >= 32 when
+  // ri < 32: the column-part reduction reuses them), Gs [kc_cap][ri], Sc
+  // [sc_rows][RC] child-update rows of a chunk
+  T* Ds0 = reinterpret_cast<T*>(smem_raw);
+  T* Gs0 = Ds0 + (size_t)nbuf * ds_rows * RC;
+  T* Sc0 = Gs0 + (size_t)nbuf * P.kc_cap * ri_max;
   // index metadata of the whole node:
   //   forward:  src_s[s] = own rows; cp_s[f + 1] = child-update ranges per front
   //             position (relative to the node's first entry); cm_s = child rows
   //   backward: src_s[f] = own rows (y) / ~update rows (x)
-  int* src_s = reinterpret_cast<int*>(Sc + (size_t)sc_rows * RC);
+  int* src_s = reinterpret_cast<int*>(Sc0 + (size_t)nbuf * sc_rows * RC);
   int* cp_s = src_s + (FWD ? max_s : max_f);
   int* cm_s = cp_s + max_f + 1;
   const int cbase = I.d.y, ncm = I.d.z;
@@ -650,26 +689,34 @@ __global__ void __launch_bounds__(kSolveThreads)
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int q = 0; q < RPL; ++q) acc[i][q] = T(0);
-  for (int k0 = k_lo; k0 < k_hi; k0 += kc_cap) {
+  // (A) asynchronous copies of one chunk into buffer b: block tile (read-only,
+  // may start before the inputs are waited for), then right-hand-side rows and
+  // child-update rows
+  const int ri_log = 31 - __clz(ri);  // ri is a power of two
+  auto stage_block = [&](int k0, int b) {
     const int kc = min(kc_cap, k_hi - k0);
-    // (A) asynchronous copies: block tile, right-hand-side rows, child rows
+    T* Gs = Gs0 + (size_t)b * P.kc_cap * ri_max;
+    const T* Mk = M + (size_t)k0 * ld + r0;
     for (int idx = tid; idx < kc * ri; idx += kSolveThreads) {
-      const int k = idx / ri, i = idx - k * ri;
+      const int k = idx >> ri_log, i = idx & (ri - 1);
       if (i < nrows)
-        cp_async<sizeof(T)>(Gs + idx, M + (size_t)(k0 + k) * ld + r0 + i);
+        cp_async<sizeof(T)>(Gs + idx, Mk + (size_t)k * ld + i);
       else
         Gs[idx] = T(0);
     }
-    if (k0 == k_lo) pdl_wait();  // vectors below are written by the previous level
+  };
+  auto stage_rows = [&](int k0, int b) {
+    const int kc = min(kc_cap, k_hi - k0);
+    T* Ds = Ds0 + (size_t)b * ds_rows * RC;
     for (int k = warp; k < kc; k += NW) {
       const int sr = src_s[k0 + k];
       const T* src = FWD ? st.b + (size_t)sr * R
                          : (sr >= 0 ? st.y + (size_t)sr * R : st.x + (size_t)(~sr) * R);
       stage_row<T, RPL>(Ds + (size_t)k * RC + lane * RPL, src + rl, lane_ok);
     }
-    int cb = 0;
     if (FWD) {
-      cb = cp_s[k0];
+      T* Sc = Sc0 + (size_t)b * sc_rows * RC;
+      const int cb = cp_s[k0];
       const int ne = cp_s[k0 + kc] - cb;  // <= sc_rows (plan)
       for (int e = warp; e < ne; e += NW) {
         const int c = cb + e;
@@ -677,10 +724,30 @@ __global__ void __launch_bounds__(kSolveThreads)
         stage_row<T, RPL>(Sc + (size_t)e * RC + lane * RPL, st.w + (size_t)wi * R + rl, lane_ok);
       }
     }
-    cp_async_wait_all();
+    cp_async_commit();
+  };
+  if (k_lo < k_hi) stage_block(k_lo, 0);
+  bad = !wait_inputs();  // vectors below are written by earlier work
+  if (k_lo < k_hi) stage_rows(k_lo, 0);
+  int chunk_i = 0;
+  for (int k0 = k_lo; k0 < k_hi; k0 += kc_cap, ++chunk_i) {
+    const int kc = min(kc_cap, k_hi - k0);
+    const int b = nbuf == 2 ? (chunk_i & 1) : 0;
+    const bool more = k0 + kc_cap < k_hi;
+    if (more && nbuf == 2) {
+      stage_block(k0 + kc_cap, b ^ 1);
+      stage_rows(k0 + kc_cap, b ^ 1);
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_group<0>();
+    }
     __syncthreads();
+    T* Ds = Ds0 + (size_t)b * ds_rows * RC;
+    const T* Gs = Gs0 + (size_t)b * P.kc_cap * ri_max;
     if (FWD) {
       // (B) subtract the children's updates from the staged right-hand sides
+      const T* Sc = Sc0 + (size_t)b * sc_rows * RC;
+      const int cb = cp_s[k0];
       for (int k = warp; k < kc; k += NW) {
         const int p = k0 + k;
         const int e0 = cp_s[p] - cb, e1 = cp_s[p + 1] - cb;
@@ -698,21 +765,32 @@ __global__ void __launch_bounds__(kSolveThreads)
       __syncthreads();
     }
     // (C) register tiles
+    const T* Gp = Gs + 4 * g;
+    const T* Dp = Ds + lane * RPL;
+#pragma unroll 4
     for (int k = part; k < kc; k += wpr) {
       T gv[4], dv[RPL];
-      lds<T, 4>(Gs + k * ri + 4 * g, gv);
-      lds<T, RPL>(Ds + (size_t)k * RC + lane * RPL, dv);
+      lds<T, 4>(Gp + k * ri, gv);
+      lds<T, RPL>(Dp + (size_t)k * RC, dv);
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int q = 0; q < RPL; ++q) acc[i][q] += gv[i] * dv[q];
     }
-    __syncthreads();
+    __syncthreads();  // buffer b is restaged two chunks later (one, single-buffered)
+    if (more && nbuf == 1) {
+      stage_block(k0 + kc_cap, 0);
+      stage_rows(k0 + kc_cap, 0);
+    }
   }
-  pdl_trigger();
+  main_done();
   // row i of the item -> its destination
   auto emit = [&](int i, T (&v)[RPL]) {
     const int row = r0 + i;
+    if (bad) {
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) v[q] = quiet_nan<T>();
+    }
     if (FWD) {
       if (row < s) {
         st_rhs<RPL>(st.y + (size_t)src_s[row] * R + rl, v);
@@ -747,7 +825,7 @@ __global__ void __launch_bounds__(kSolveThreads)
         if (4 * g + i < nrows) finish(4 * g + i, acc[i]);
     }
   } else {
-    T* red = Ds;  // [wpr][ri][RC] = 32 * RC values
+    T* red = Ds0;  // [wpr][ri][RC] = 32 * RC values
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -773,7 +851,7 @@ __global__ void __launch_bounds__(kSolveThreads)
   __shared__ int ticket;
   __threadfence();
   __syncthreads();
-  int* ctr = counters + (size_t)I.e.z * ychunks + blockIdx.y;
+  int* ctr = counters + (size_t)I.e.z * ychunks + chunk;
   if (tid == 0) ticket = atomicAdd(ctr, 1);
   __syncthreads();
   if (ticket != I.e.w - 1) return;
@@ -794,6 +872,21 @@ __global__ void __launch_bounds__(kSolveThreads)
   if (tid == 0) *ctr = 0;
 }
 
+template <typename T, int RPL, bool FWD, typename SVT>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_panel(BankView B, SVT S, const PanelItem* __restrict__ items, PanelShape P, T* __restrict__ partials,
+            int* __restrict__ counters, int parts_ld, int ychunks) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const PanelItem I = items[blockIdx.x];
+  panel_tile<T, RPL, FWD, SVT>(
+      B, S, I, (int)blockIdx.y * 32 * RPL, (int)blockIdx.y, P, partials, counters, parts_ld, ychunks, smem_raw,
+      [] {
+        pdl_wait();
+        return true;
+      },
+      [] { pdl_trigger(); });
+}
+
 // Leaf levels: a warp per node (all of its rows) and right-hand-side chunk,
 // eight independent nodes per CTA and no CTA barrier.  A level qualifies when
 // its nodes are small (at most kWarpMaxK columns and kWarpMaxRows rows) and,
@@ -811,27 +904,25 @@ __host__ __device__ constexpr size_t panel_warp_bytes(int max_k, int rows_pad, i
           15) & ~(size_t)15;
 }
 
-template <typename T, int RPL, bool FWD, typename SVT>
-__global__ void __launch_bounds__(kSolveThreads)
-    k_panel_warp(BankView B, SVT S, const PanelItem* __restrict__ items, int n_items, int max_k,
-                 int rows_pad) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// One leaf-level node applied by one warp to the right-hand-side chunk at rc0;
+// `base` is the warp's shared-memory slice.  wait_inputs() (every lane) is
+// called once the block's copies are in flight and before any vector is read;
+// false: the inputs could not be waited for and the node writes NaN.
+template <typename T, int RPL, bool FWD, typename SVT, typename Wait, typename Done>
+__device__ __forceinline__ void panel_warp_node(const BankView& B, const SVT& S, const PanelItem& I, int rc0,
+                                                int max_k, int rows_pad, unsigned char* base, Wait wait_inputs,
+                                                Done main_done) {
   constexpr int RC = 32 * RPL;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int idx = blockIdx.x * kWarpNodesPerCta + warp;
-  if (idx >= n_items) return;
-  const PanelItem I = items[idx];
+  const int lane = threadIdx.x & 31;
   const int s = I.b.x, m = I.b.y, f = s + m, w_off = I.b.w;
   const auto st = S.set[I.b.z];
   const int R = st.nrhs;
-  const int rc0 = blockIdx.y * RC;
   if (rc0 >= R) return;
   const int rl = rc0 + lane * RPL;
   const bool lane_ok = rl < R;
   const int K = FWD ? s : f;
   const int rows = FWD ? f : s;  // = the leading dimension of the block
   const T* M = static_cast<const T*>(FWD ? B.G : B.H) + (((long long)I.c.y << 32) | (unsigned)I.c.x);
-  unsigned char* base = smem_raw + (size_t)warp * panel_warp_bytes<T>(max_k, rows_pad, RC);
   T* Ds = reinterpret_cast<T*>(base);        // [max_k][RC]
   T* Gs = Ds + (size_t)max_k * RC;           // [max_k][rows_pad]
   int* src_s = reinterpret_cast<int*>(Gs + (size_t)max_k * rows_pad);  // [max_k]
@@ -848,7 +939,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       Gs[e] = T(0);
   }
   __syncwarp();
-  pdl_wait();  // vectors below are written by the previous level
+  const bool bad = !wait_inputs();  // vectors below are written by earlier work
   for (int k = 0; k < K; ++k) {
     const int sr = src_s[k];
     const T* src = FWD ? st.b + (size_t)sr * R
@@ -857,7 +948,7 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
   cp_async_wait_all();
   __syncwarp();
-  pdl_trigger();
+  main_done();
   if (!lane_ok) return;
   for (int r4 = 0; r4 < rows; r4 += 4) {
     T acc[4][RPL];
@@ -874,6 +965,12 @@ __global__ void __launch_bounds__(kSolveThreads)
 #pragma unroll
         for (int q = 0; q < RPL; ++q) acc[i][q] += gv[i] * dv[q];
     }
+    if (bad) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) acc[i][q] = quiet_nan<T>();
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int row = r4 + i;
@@ -888,6 +985,160 @@ __global__ void __launch_bounds__(kSolveThreads)
       }
     }
   }
+}
+
+template <typename T, int RPL, bool FWD, typename SVT>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_panel_warp(BankView B, SVT S, const PanelItem* __restrict__ items, int n_items, int max_k,
+                 int rows_pad) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5;
+  const int idx = blockIdx.x * kWarpNodesPerCta + warp;
+  if (idx >= n_items) return;
+  const PanelItem I = items[idx];
+  panel_warp_node<T, RPL, FWD, SVT>(
+      B, S, I, (int)blockIdx.y * 32 * RPL, max_k, rows_pad,
+      smem_raw + (size_t)warp * panel_warp_bytes<T>(max_k, rows_pad, 32 * RPL),
+      [] {
+        pdl_wait();
+        return true;
+      },
+      [] { pdl_trigger(); });
+}
+
+// ---- flow sweeps -------------------------------------------------------------
+// One persistent launch per sweep direction instead of one launch per tree
+// level.  The direction's work entries are listed in topological order
+// (forward: by height, backward: by depth); every CTA repeatedly takes the
+// next entry from a ticket counter and, before reading any vector, waits until
+// the entry's node has its inputs: forward, every item of its children has
+// finished (their update rows are written); backward, every item of its
+// parent has finished (the parent finished only after its own parent, so all
+// ancestors' solution rows are written).  An entry only ever waits on entries
+// with smaller tickets, which CTAs already running hold, so the sweep always
+// progresses whatever the number of resident CTAs.  Finished items add one to
+// a per-node counter with release semantics; waits read it with acquire
+// semantics.  Each direction's launch zeroes the other direction's counters
+// and ticket, so consecutive sweeps start from zero without extra launches.
+// Vectors produced inside a launch are whole 128-byte lines per row (checked
+// on the host), so no line read from L1 can be stale.
+struct FlowView {
+  const int4* entries;  // (0: one CTA item / 1: up to 8 warp items, first item, item count, RHS chunk)
+  const PanelItem* items;
+  const int4* sync;     // per item: (wait counter or -1, wait target, signal counter or -1, 0)
+  int* ctr;             // this direction's per-node counters
+  int* other_ctr;       // the other direction's (zeroed here)
+  int n_ctr;
+  int* queue;           // this direction's ticket counter
+  int* other_queue;
+  int* err;             // set to 1 when a wait runs out
+  int n_entries;
+};
+
+// Polls of one wait before it gives up (with 64 ns sleeps and a global load
+// each: tens to hundreds of milliseconds, against a whole sweep of well under
+// a millisecond).
+constexpr unsigned kFlowPollLimit = 1u << 18;
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_release_gpu(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait for *ctr >= target; false (and the error flag set) when the
+// poll limit runs out.
+__device__ __noinline__ bool flow_wait(const int* ctr, int target, int* err) {
+  if (ld_acquire_gpu(ctr) >= target) return true;
+  for (unsigned n = 0; n < kFlowPollLimit; ++n) {
+    __nanosleep(64);
+    if (ld_acquire_gpu(ctr) >= target) return true;
+  }
+  atomicExch(err, 1);
+  return false;
+}
+
+template <typename T, int RPL, bool FWD, typename SVT>
+__global__ void __launch_bounds__(kSolveThreads, 3)
+    k_panel_flow(BankView B, SVT S, FlowView F, PanelShape P, int warp_max_k, int warp_rows_pad) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_ticket, s_ok;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = blockIdx.x * kSolveThreads + tid; i < F.n_ctr; i += gridDim.x * kSolveThreads) F.other_ctr[i] = 0;
+  if (blockIdx.x == 0 && tid == 0) *F.other_queue = 0;
+  // The next ticket is taken while the current entry runs, and an entry's
+  // completion is signalled (by lane 0 of the warp that owns it) after the
+  // barrier that starts the next one, so neither round trip sits between
+  // two entries.
+  int pending = -1;  // lane 0: the counter this warp still has to signal
+  if (tid == 0) s_ticket = atomicAdd(F.queue, 1);
+  for (;;) {
+    __syncthreads();
+    const int t = s_ticket;
+    if (lane == 0 && pending >= 0) red_release_gpu(F.ctr + pending, 1);
+    pending = -1;
+    __syncthreads();  // every thread has read s_ticket
+    if (t >= F.n_entries) break;
+    if (tid == 0) s_ticket = atomicAdd(F.queue, 1);
+    const int4 e = F.entries[t];
+    const int rc0 = e.w * 32 * RPL;
+    if (e.x == 0) {
+      const int4 sy = F.sync[e.y];
+      panel_tile<T, RPL, FWD, SVT>(
+          B, S, F.items[e.y], rc0, e.w, P, nullptr, nullptr, 0, 0, smem_raw,
+          [&] {
+            if (tid == 0) s_ok = sy.x < 0 || flow_wait(F.ctr + sy.x, sy.y, F.err);
+            __syncthreads();
+            return s_ok != 0;
+          },
+          [] {});
+      if (tid == 0) pending = sy.z;
+    } else if (warp < e.z) {
+      const int ii = e.y + warp;
+      const int4 sy = F.sync[ii];
+      panel_warp_node<T, RPL, FWD, SVT>(
+          B, S, F.items[ii], rc0, warp_max_k, warp_rows_pad,
+          smem_raw + (size_t)warp * panel_warp_bytes<T>(warp_max_k, warp_rows_pad, 32 * RPL),
+          [&] {
+            int ok = 1;
+            if (lane == 0) ok = sy.x < 0 || flow_wait(F.ctr + sy.x, sy.y, F.err);
+            return __shfl_sync(0xffffffffu, ok, 0) != 0;
+          },
+          [] {});
+      __syncwarp();
+      if (lane == 0) pending = sy.z;
+    }
+  }
+}
+
+constexpr size_t kFlowSmem = 96 * 1024;    // flow launches: leaf-warp slices within this
+constexpr size_t kFlowScBytes = 32 * 1024;  // flow launches: staged child-update rows per chunk
+constexpr int kFlowCmMax = 1024;            // flow launches: staged child-map entries per node
+
+template <typename T, typename SVT>
+const void* flow_kernel(int rpl, bool forward) {
+  if (forward)
+    return rpl == 1 ? (const void*)k_panel_flow<T, 1, true, SVT>
+                    : (rpl == 2 ? (const void*)k_panel_flow<T, 2, true, SVT> : (const void*)k_panel_flow<T, 4, true, SVT>);
+  return rpl == 1 ? (const void*)k_panel_flow<T, 1, false, SVT>
+                  : (rpl == 2 ? (const void*)k_panel_flow<T, 2, false, SVT> : (const void*)k_panel_flow<T, 4, false, SVT>);
+}
+
+template <typename T, int RPL, typename SVT>
+void launch_flow(bool forward, const BankView& B, const SVT& S, const FlowPlan& FP, const FlowView& F,
+                 cudaStream_t st) {
+  const PanelShape shape{FP.kc_cap, FP.ds_rows, FP.ri_max, FP.sc_rows, FP.max_s, FP.max_f, FP.cm_cap, FP.nbuf};
+  if (forward)
+    k_panel_flow<T, RPL, true, SVT><<<FP.grid, kSolveThreads, FP.smem, st>>>(B, S, F, shape, FP.warp_max_k,
+                                                                            FP.warp_rows_pad);
+  else
+    k_panel_flow<T, RPL, false, SVT><<<FP.grid, kSolveThreads, FP.smem, st>>>(B, S, F, shape, FP.warp_max_k,
+                                                                             FP.warp_rows_pad);
+  PECS_CUDA(cudaGetLastError());
 }
 
 // Tile shape of one level for nrhs right-hand sides: the longest row tiles and
@@ -925,12 +1176,13 @@ void launch_panel(bool forward, const BankView& B, const SVT& S, const PanelPlan
   int ci = 0;
   while (ci + 1 < kPanelKcSteps && (kPanelKc[ci] > kcap || kPanelKc[ci + 1] >= std::max(1, L.max_k))) ++ci;
   size_t smem = 0;
-  int kc = 1, ds_rows = 32, sc_rows = 0;
+  int kc = 1, ds_rows = 32, sc_rows = 0, nbuf = 1;
   for (;; ++ci) {
     kc = std::min(kPanelKc[ci], std::max(1, L.max_k));
-    ds_rows = P.min_ri < 32 ? std::max(kc, 32) : kc;
+    nbuf = 1;  // level launches: single-buffered (measured faster: more CTAs per SM)
+    ds_rows = P.min_ri < 32 ? std::max(kc, 32 / nbuf) : kc;
     sc_rows = forward ? L.sc_rows[ci] : 0;
-    smem = panel_smem_bytes<T>(ds_rows, RC, kc, P.max_ri, sc_rows, meta);
+    smem = panel_smem_bytes<T>(ds_rows, RC, kc, P.max_ri, sc_rows, meta, nbuf);
     if (smem <= kPanelSmem || ci + 1 == kPanelKcSteps) break;
   }
   if (smem > kPanelSmem) throw PecsError(PECS_E_ARG, "panel staging exceeds shared memory");
@@ -946,14 +1198,13 @@ void launch_panel(bool forward, const BankView& B, const SVT& S, const PanelPlan
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   T* parts = reinterpret_cast<T*>(L.partials.p);
+  const PanelShape shape{kc, ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap, nbuf};
   if (forward)
-    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_panel<T, RPL, true, SVT>, B, S, (const PanelItem*)P.items.p, kc,
-                                 ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap, parts,
-                                 L.counters.p, parts_ld, ychunks));
+    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_panel<T, RPL, true, SVT>, B, S, (const PanelItem*)P.items.p, shape,
+                                 parts, L.counters.p, parts_ld, ychunks));
   else
-    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_panel<T, RPL, false, SVT>, B, S, (const PanelItem*)P.items.p, kc,
-                                 ds_rows, P.max_ri, sc_rows, L.max_s, L.max_f, L.cm_cap, parts,
-                                 L.counters.p, parts_ld, ychunks));
+    PECS_CUDA(cudaLaunchKernelEx(&cfg, k_panel<T, RPL, false, SVT>, B, S, (const PanelItem*)P.items.p, shape,
+                                 parts, L.counters.p, parts_ld, ychunks));
 }
 
 template <typename T, typename SVT>
@@ -1072,6 +1323,149 @@ void launch_panel_level(bool forward, const BankView& B, const SVT& S, const Pan
 }
 }  // namespace
 
+FlowPlanHost plan_flow(const FlowNodes& nd, bool forward, int top, int rpl, int max_nrhs, int kc_max, int esz,
+                       int n_sm) {
+  FlowPlanHost H;
+  const int n_nodes = (int)nd.s.size();
+  const std::vector<std::vector<int>>& lv_all = forward ? nd.by_height : nd.by_depth;
+  // the covered levels in ticket order (forward: the highest heights, from
+  // the lowest of them up; backward: depths 0 .. top-1)
+  const int L = (int)lv_all.size();
+  top = std::min(std::max(top, 1), L);
+  const std::vector<std::vector<int>> lv(forward ? lv_all.begin() + (L - top) : lv_all.begin(),
+                                         forward ? lv_all.end() : lv_all.begin() + top);
+  const int RC = 32 * rpl;
+  H.n_chunks = (std::max(1, max_nrhs) + RC - 1) / RC;
+  kc_max = std::max(1, kc_max);
+  const int sc_cap = std::max(8, (int)(kFlowScBytes / ((size_t)RC * esz)));
+  auto warp_bytes = [&](int k, int r) {
+    return esz == 8 ? panel_warp_bytes<double>(k, r, RC) : panel_warp_bytes<float>(k, r, RC);
+  };
+  auto rows_of = [&](int g) { return forward ? nd.s[g] + nd.m[g] : nd.s[g]; };
+  // per level: leaf warps (small nodes, forward without children, the warp
+  // slices within budget) or CTA row tiles (32 rows, fewer where a level has
+  // too few tiles to fill the GPU)
+  std::vector<int> warp_level(lv.size(), 0), cap_level(lv.size(), 32);
+  int wk = 0, wr = 0;
+  for (size_t l = 0; l < lv.size(); ++l) {
+    bool leaf = true;
+    int mk = 0, mr = 0;
+    for (int g : lv[l]) {
+      const int f = nd.s[g] + nd.m[g];
+      const int rows = rows_of(g), k = forward ? nd.s[g] : f;
+      const bool kids = nd.cmap_ptr[nd.cm_off[g] + f] > nd.cmap_ptr[nd.cm_off[g]];
+      if (k > kWarpMaxK || rows > kWarpMaxRows || (forward && kids)) leaf = false;
+      mk = std::max(mk, k);
+      mr = std::max(mr, rows);
+    }
+    const int nk = std::max(wk, mk), nr = std::max(wr, (mr + 3) & ~3);
+    if (leaf && kWarpNodesPerCta * warp_bytes(nk, nr) <= kFlowSmem) {
+      warp_level[l] = 1;
+      wk = nk;
+      wr = nr;
+      continue;
+    }
+    int cap = 32;
+    while (cap > 4) {
+      long long t = 0;
+      for (int g : lv[l]) t += (rows_of(g) + cap - 1) / cap;
+      if (t * H.n_chunks >= n_sm) break;
+      cap /= 2;
+    }
+    cap_level[l] = cap;
+  }
+  H.warp_max_k = wk;
+  H.warp_rows_pad = wr;
+  // items per node (signals per chunk), then the items with their waits
+  std::vector<int> nsig(n_nodes, 0), per_node(n_nodes, 1);
+  for (size_t l = 0; l < lv.size(); ++l)
+    for (int g : lv[l]) {
+      const int rows = rows_of(g);
+      if (warp_level[l]) {
+        nsig[g] = 1;
+        per_node[g] = rows;
+      } else {
+        const int cap = cap_level[l];
+        const int nit = (rows + cap - 1) / cap;
+        per_node[g] = (rows + nit - 1) / nit;
+        nsig[g] = (rows + per_node[g] - 1) / per_node[g];
+      }
+    }
+  std::vector<int> kid_sig(n_nodes, 0);
+  for (int g = 0; g < n_nodes; ++g)
+    if (nd.parent[g] >= 0) kid_sig[nd.parent[g]] += nsig[g];
+  int min_ri = 32, max_k_tiles = 0;
+  for (size_t l = 0; l < lv.size(); ++l) {
+    const size_t first = H.items.size();
+    for (int g : lv[l]) {
+      const int s = nd.s[g], m = nd.m[g], f = s + m;
+      const int rows = rows_of(g);
+      const long long off = forward ? nd.goff[g] : nd.hoff[g];
+      const int cb = nd.cmap_ptr[nd.cm_off[g]];
+      const int ncm = nd.cmap_ptr[nd.cm_off[g] + f] - cb;
+      const int p = nd.parent[g];
+      const int4 sy = forward ? make_int4(kid_sig[g] > 0 ? g : -1, kid_sig[g] * H.n_chunks, p, 0)
+                              : make_int4(p, p >= 0 ? nsig[p] * H.n_chunks : 0, g, 0);
+      PanelItem it;
+      it.b = make_int4(s, m, nd.node_set[g], nd.w_off[g]);
+      it.c = make_int4((int)(off & 0xffffffffll), (int)(off >> 32), nd.own_off[g], nd.upd_off[g]);
+      if (warp_level[l]) {
+        it.a = make_int4(g, 0, rows, 32);
+        it.d = make_int4(nd.cm_off[g], cb, 0, 0);
+        it.e = make_int4(0, 0, -1, 1);
+        H.items.push_back(it);
+        H.sync.push_back(sy);
+        continue;
+      }
+      // the widest chunk (<= kc_max columns) whose child-update rows fit
+      int kc = kc_max, rows_sc = 0;
+      for (;; kc /= 2) {
+        rows_sc = 0;
+        if (forward) {
+          const int* cp = nd.cmap_ptr.data() + nd.cm_off[g];
+          for (int k0 = 0; k0 < s; k0 += kc) rows_sc = std::max(rows_sc, cp[std::min(k0 + kc, s)] - cp[k0]);
+        }
+        if (rows_sc <= sc_cap || kc == 1) break;
+      }
+      H.kc_cap = std::max(H.kc_cap, kc);
+      max_k_tiles = std::max(max_k_tiles, forward ? s : f);
+      H.sc_rows = std::max(H.sc_rows, rows_sc);
+      H.max_s = std::max(H.max_s, s);
+      H.max_f = std::max(H.max_f, f);
+      H.cm_cap = std::max(H.cm_cap, std::min(ncm, kFlowCmMax));
+      const int per = per_node[g];
+      int ri = 4;
+      while (ri < per) ri *= 2;
+      H.ri_max = std::max(H.ri_max, ri);
+      min_ri = std::min(min_ri, ri);
+      it.d = make_int4(nd.cm_off[g], cb, ncm, 0);
+      it.e = make_int4(kc, 0, -1, 1);  // no split; this node's chunk width
+      for (int r0 = 0; r0 < rows; r0 += per) {
+        it.a = make_int4(g, r0, std::min(rows, r0 + per), ri);
+        H.items.push_back(it);
+        H.sync.push_back(sy);
+      }
+    }
+    // entries: the level's items, each for every chunk (consecutive, so the
+    // chunks of one tile share its block in L2); leaf warps in groups
+    for (size_t i = first; i < H.items.size();) {
+      const int n = warp_level[l] ? (int)std::min<size_t>(kWarpNodesPerCta, H.items.size() - i) : 1;
+      for (int c = 0; c < H.n_chunks; ++c) H.entries.push_back(make_int4(warp_level[l], (int)i, n, c));
+      i += n;
+    }
+  }
+  H.nbuf = max_k_tiles > H.kc_cap ? 2 : 1;  // items of several chunks: double-buffered staging
+  H.ds_rows = min_ri < 32 ? std::max(H.kc_cap, 32 / H.nbuf) : H.kc_cap;
+  const int meta = forward ? H.max_s + H.max_f + 1 + H.cm_cap : H.max_f;
+  const size_t tile_smem =
+      esz == 8 ? panel_smem_bytes<double>(H.ds_rows, RC, H.kc_cap, H.ri_max, H.sc_rows, meta, H.nbuf)
+               : panel_smem_bytes<float>(H.ds_rows, RC, H.kc_cap, H.ri_max, H.sc_rows, meta, H.nbuf);
+  const size_t warp_smem = wk == 0 ? 0 : kWarpNodesPerCta * warp_bytes(wk, wr);
+  H.smem = std::max(tile_smem, warp_smem);
+  H.ok = H.smem <= kPanelSmem;
+  return H;
+}
+
 BankView FactorBank::view() const {
   BankView v;
   v.s = s_.p;
@@ -1093,6 +1487,13 @@ BankView FactorBank::view() const {
 }
 
 int FactorBank::kernel_launches_per_solve() const {
+  if (flow_sel_ >= 0) {
+    const int top = flow_cfg_[flow_sel_].top;
+    int n = 2;
+    for (size_t l = 0; l + top < pfwd_.size(); ++l) n += pfwd_[l].tiles[0].n_items > 0;
+    for (size_t l = top; l < pbwd_.size(); ++l) n += pbwd_[l].tiles[0].n_items > 0;
+    return n;
+  }
   int n = 0;
   for (auto& l : pfwd_) n += l.tiles[0].n_items > 0;
   for (auto& l : pbwd_) n += l.tiles[0].n_items > 0;
@@ -1345,6 +1746,7 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
             P.n_items = (int)items.size();
             P.max_ri = max_ri;
             P.min_ri = min_ri;
+            for (const PanelItem& it : items) P.max_span = std::max(P.max_span, it.e.y - it.e.x);
             P.items.upload(items);
             out[l].split_tiles = tiles;
             const int ych = (parts_ld_ + 31) / 32;
@@ -1417,6 +1819,7 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
           P.n_items = (int)items.size();
           P.max_ri = max_ri;
           P.min_ri = min_ri;
+          P.max_span = max_k;
           P.items.upload(items);
         }
       }
@@ -1429,6 +1832,80 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
       set_panel_smem_limit<double, IlSetsView>();
     else
       set_panel_smem_limit<float, IlSetsViewF>();
+    // flow plans: both directions, 1, 2 and 4 right-hand sides per lane
+    n_nodes_ = (int)hs.size();
+    std::vector<int> parent(n_nodes_, -1);
+    {
+      int b0 = 0;
+      for (int fi = 0; fi < n_sets_; ++fi) {
+        const MfFactor& F = *factors[fi];
+        for (int j = 0; j < (int)F.nodes.size(); ++j)
+          for (int c : F.nodes[j].children) parent[b0 + c] = b0 + j;
+        b0 += (int)F.nodes.size();
+      }
+    }
+    flow_state_.alloc(2 * (size_t)n_nodes_ + 3);
+    flow_state_.zero();
+    stall_node_ = -1;
+    for (int g = 0; g < (int)factors[0]->nodes.size() && stall_node_ < 0; ++g)
+      if (parent[g] < 0 && !factors[0]->nodes[g].children.empty()) stall_node_ = g;
+    int n_sm = 0, dev = 0;
+    PECS_CUDA(cudaGetDevice(&dev));
+    PECS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    FlowNodes nodes{hs, hm, node_set, w_off, own_off, upd_off, cm_off, cmap_ptr, goff, hoff, parent, {}, {}};
+    for (auto& l : fl) nodes.by_height.push_back(l.nodes);
+    for (auto& l : bl) nodes.by_depth.push_back(l.nodes);
+    const int esz = prec_ == PECS_PREC_FP64 ? 8 : 4;
+    flow_cfg_.clear();
+    flow_sel_ = -1;
+    const int n_levels = (int)std::max(fl.size(), bl.size());
+    std::vector<int> tops{n_levels};
+    for (int t : {7, 5, 3})
+      if (t < n_levels) tops.push_back(t);
+    for (int top : tops) {
+      for (int kc : {64, 32}) {
+        for (int rpl : {1, 2, 4}) {
+          FlowConfig cfg;
+          cfg.top = top;
+          cfg.kc = std::min(kc, tune_.chunk);
+          cfg.rpl = rpl;
+          bool ok = true;
+          for (int d = 0; d < 2 && ok; ++d) {
+            FlowPlan& FP = cfg.plan[d];
+            FlowPlanHost H = plan_flow(nodes, d == 0, top, rpl, max_nrhs, cfg.kc, esz, n_sm);
+            if (!H.ok) {
+              ok = false;
+              break;
+            }
+            FP.top = top;
+            FP.rpl = rpl;
+            FP.n_chunks = H.n_chunks;
+            FP.kc_cap = H.kc_cap;
+            FP.nbuf = H.nbuf;
+            FP.ds_rows = H.ds_rows;
+            FP.ri_max = H.ri_max;
+            FP.sc_rows = H.sc_rows;
+            FP.max_s = H.max_s;
+            FP.max_f = H.max_f;
+            FP.cm_cap = H.cm_cap;
+            FP.warp_max_k = H.warp_max_k;
+            FP.warp_rows_pad = H.warp_rows_pad;
+            FP.smem = H.smem;
+            FP.n_entries = (int)H.entries.size();
+            FP.items.upload(H.items);
+            FP.sync.upload(H.sync);
+            FP.entries.upload(H.entries);
+            const void* fn = esz == 8 ? flow_kernel<double, IlSetsView>(rpl, d == 0)
+                                      : flow_kernel<float, IlSetsViewF>(rpl, d == 0);
+            PECS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmem));
+            int per_sm = 0;
+            PECS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSolveThreads, FP.smem));
+            FP.grid = std::max(1, std::min(FP.n_entries, std::max(1, per_sm) * n_sm));
+          }
+          if (ok) flow_cfg_.push_back(std::move(cfg));
+        }
+      }
+    }
     return;
   }
   make(fl, true, fwd_);
@@ -1502,8 +1979,80 @@ int FactorBank::panel_rpl(const SVT& sets, int max_nrhs) const {
   return rpl;
 }
 
+int FactorBank::flow_error(bool clear) const {
+  if (!panel_ || flow_state_.n == 0) return 0;
+  int e = 0;
+  int* p = flow_state_.p + 2 * (size_t)n_nodes_ + 2;
+  PECS_CUDA(cudaMemcpy(&e, p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (clear) PECS_CUDA(cudaMemset(p, 0, sizeof(int)));
+  return e;
+}
+
+void FactorBank::debug_arm_flow_stall() const {
+  if (!panel_ || flow_state_.n == 0 || stall_node_ < 0) throw PecsError(PECS_E_STATE, "no flow sweep to stall");
+  PECS_CUDA(cudaDeviceSynchronize());
+  const int v = -(1 << 30);
+  PECS_CUDA(cudaMemcpy(flow_state_.p + stall_node_, &v, sizeof(int), cudaMemcpyHostToDevice));
+}
+
+// A flow configuration applies when its plans cover these right-hand sides
+// and every sweep vector row is a whole number of 128-byte lines at a 128-byte
+// aligned address (rows written inside the launch never share a line with
+// another).
+template <typename SVT>
+bool FactorBank::flow_ok(const SVT& sets, int max_nrhs, int cfg) const {
+  using T = typename std::conditional<std::is_same<SVT, IlSetsViewF>::value, float, double>::type;
+  if (!panel_ || cfg < 0 || cfg >= (int)flow_cfg_.size()) return false;
+  if ((prec_ == PECS_PREC_FP64) != (sizeof(T) == 8)) return false;
+  const FlowConfig& C = flow_cfg_[cfg];
+  const int rpl = C.rpl;
+  if (C.plan[0].n_entries == 0 || C.plan[1].n_entries == 0) return false;
+  if ((max_nrhs + 32 * rpl - 1) / (32 * rpl) != C.plan[0].n_chunks) return false;
+  if (panel_rpl(sets, max_nrhs) < rpl) return false;
+  auto al = [](const void* p) { return ((uintptr_t)p & 127u) == 0; };
+  for (int si = 0; si < n_sets_; ++si) {
+    const auto& v = sets.set[si];
+    if (v.nrhs > max_nrhs || v.nrhs % rpl != 0 || ((size_t)v.nrhs * sizeof(T)) % 128 != 0) return false;
+    if (!al(v.b) || !al(v.y) || !al(v.w) || !al(v.x)) return false;
+  }
+  return true;
+}
+
+// Hybrid sweep: level launches for the levels below the configuration's top
+// levels, then one flow launch per direction over those, then level launches
+// again (backward) for the rest.
+template <typename SVT>
+void FactorBank::solve_flow(const SVT& sets, int max_nrhs, int cfg, cudaStream_t st) const {
+  using T = typename std::conditional<std::is_same<SVT, IlSetsViewF>::value, float, double>::type;
+  const BankView B = view();
+  const FlowConfig& C = flow_cfg_[cfg];
+  const int lrpl = panel_rpl(sets, max_nrhs);
+  int* base = flow_state_.p;
+  int* ctr[2] = {base, base + n_nodes_};
+  int* queue[2] = {base + 2 * (size_t)n_nodes_, base + 2 * (size_t)n_nodes_ + 1};
+  int* err = base + 2 * (size_t)n_nodes_ + 2;
+  for (size_t l = 0; l + C.top < pfwd_.size(); ++l)
+    launch_panel_level<T, SVT>(true, B, sets, pfwd_[l], max_nrhs, lrpl, tune_, parts_ld_, st);
+  for (int d = 0; d < 2; ++d) {
+    const FlowPlan& FP = C.plan[d];
+    const FlowView F{FP.entries.p, FP.items.p, FP.sync.p, ctr[d], ctr[1 - d], n_nodes_,
+                     queue[d],     queue[1 - d], err,     FP.n_entries};
+    switch (C.rpl) {
+      case 1: launch_flow<T, 1, SVT>(d == 0, B, sets, FP, F, st); break;
+      case 2: launch_flow<T, 2, SVT>(d == 0, B, sets, FP, F, st); break;
+      default: launch_flow<T, 4, SVT>(d == 0, B, sets, FP, F, st); break;
+    }
+  }
+  for (size_t l = C.top; l < pbwd_.size(); ++l)
+    launch_panel_level<T, SVT>(false, B, sets, pbwd_[l], max_nrhs, lrpl, tune_, parts_ld_, st);
+}
+
 template <typename SVT>
 void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) const {
+  if (flow_sel_ >= 0 && flow_ok(sets, max_nrhs, flow_sel_)) {
+    solve_flow(sets, max_nrhs, flow_sel_, st);
+    return;
+  }
   const int rpl = panel_rpl(sets, max_nrhs);
   const BankView B = view();
   for (int pass = 0; pass < 2; ++pass) {
@@ -1524,17 +2073,52 @@ void FactorBank::solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) con
 // cache state the real sweep gives it.  The sweep's values are meaningless
 // while tuning; callers solve again before using any result.
 template <typename SVT>
-void FactorBank::autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, int reps) {
+void FactorBank::force_flow_impl(const SVT& sets, int max_nrhs) {
+  // every level in the flow launch, the widest chunks and the most
+  // right-hand sides per lane that apply
+  int best = -1;
+  for (int c = 0; c < (int)flow_cfg_.size(); ++c) {
+    const FlowConfig& C = flow_cfg_[c];
+    if (!flow_ok(sets, max_nrhs, c) || C.top != flow_cfg_[0].top) continue;
+    if (best < 0 || C.kc > flow_cfg_[best].kc || (C.kc == flow_cfg_[best].kc && C.rpl > flow_cfg_[best].rpl))
+      best = c;
+  }
+  flow_sel_ = best;
+}
+
+void FactorBank::force_flow(const IlSetsViewF& sets, int max_nrhs) {
+  force_flow_impl(sets, max_nrhs);
+  release_unused_flow();
+}
+void FactorBank::force_flow(const IlSetsView& sets, int max_nrhs) {
+  force_flow_impl(sets, max_nrhs);
+  release_unused_flow();
+}
+
+void FactorBank::release_unused_flow() {
+  for (int c = 0; c < (int)flow_cfg_.size(); ++c) {
+    if (c == flow_sel_) continue;
+    for (FlowPlan& P : flow_cfg_[c].plan) {
+      P.items.release();
+      P.sync.release();
+      P.entries.release();
+      P.n_entries = 0;
+    }
+  }
+}
+
+template <typename SVT>
+void FactorBank::autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, int reps, int flow_mode) {
   using T = typename std::conditional<std::is_same<SVT, IlSetsViewF>::value, float, double>::type;
   const int rpl = panel_rpl(sets, max_nrhs);
   cudaEvent_t e0, e1;
   PECS_CUDA(cudaEventCreate(&e0));
   PECS_CUDA(cudaEventCreate(&e1));
-  const int per_sweep = kernel_launches_per_solve();
   for (int pass = 0; pass < 2; ++pass)
     for (PanelPlan& L : pass == 0 ? pfwd_ : pbwd_)
       L.tuned = panel_default_option<T>(L, max_nrhs, rpl, tune_, parts_ld_);
   auto time_sweep = [&]() {
+    const int per_sweep = kernel_launches_per_solve();
     float best = 1e30f;
     solve_panel(sets, max_nrhs, st);  // warm-up
     tune_launches_ += per_sweep;
@@ -1573,6 +2157,30 @@ void FactorBank::autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, 
       L.tuned = best;
     }
   }
+  // the flow sweep (one persistent launch per direction) at each valid
+  // right-hand-sides-per-lane count, against the tuned level sweep
+  int best_flow = -1;
+  float best_flow_ms = 1e30f;
+  for (int c = 0; c < (int)flow_cfg_.size() && flow_mode >= 0; ++c) {
+    if (!flow_ok(sets, max_nrhs, c)) continue;
+    flow_sel_ = c;
+    const float ms = time_sweep();
+    flow_sel_ = -1;
+    if (std::getenv("PECS_TUNE_LOG"))  // diagnostic: every flow configuration's sweep time
+      std::fprintf(stderr, "flow top %d kc %d rpl %d: %.4f ms (levels %.4f ms)\n", flow_cfg_[c].top,
+                   flow_cfg_[c].kc, flow_cfg_[c].rpl, ms, best_sweep);
+    if (flow_error() != 0)
+      throw PecsError(PECS_E_CUDA, "flow sweep: a wait for a node's inputs ran out");
+    if (ms < best_flow_ms) {
+      best_flow_ms = ms;
+      best_flow = c;
+    }
+  }
+  if (best_flow >= 0 && (flow_mode > 0 || best_flow_ms < best_sweep)) {
+    best_sweep = best_flow_ms;
+    flow_sel_ = best_flow;
+  }
+  release_unused_flow();
   tuned_ms_ = best_sweep;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -1607,14 +2215,14 @@ std::vector<double> FactorBank::time_levels(const IlSetsViewF& sets, int max_nrh
   return ms;
 }
 
-void FactorBank::autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps) {
+void FactorBank::autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps, int flow_mode) {
   if (!panel_ || prec_ == PECS_PREC_FP64) throw PecsError(PECS_E_STATE, "autotune needs an FP32 panel bank");
-  autotune_panel(sets, max_nrhs, st, reps);
+  autotune_panel(sets, max_nrhs, st, reps, flow_mode);
 }
 
-void FactorBank::autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps) {
+void FactorBank::autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps, int flow_mode) {
   if (!panel_ || prec_ != PECS_PREC_FP64) throw PecsError(PECS_E_STATE, "autotune needs an FP64 panel bank");
-  autotune_panel(sets, max_nrhs, st, reps);
+  autotune_panel(sets, max_nrhs, st, reps, flow_mode);
 }
 
 void FactorBank::solve(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st) const {

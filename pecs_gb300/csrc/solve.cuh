@@ -111,6 +111,7 @@ struct PanelTiles {
   int n_items = 0;
   int max_ri = 4;   // largest rows-per-tile of the items
   int min_ri = 32;  // smallest (< 32: column parts reduce in shared memory)
+  int max_span = 0; // most columns one item covers (> the chunk width: double-buffered staging)
   DBuf<PanelItem> items;
 };
 
@@ -135,6 +136,61 @@ struct PanelPlan {
   int warp_rows = 0;  // leaf levels: most rows of a node
   PanelOption tuned;  // the autotuner's choice (kind -1: heuristic)
 };
+
+// A flow sweep of one direction (one persistent launch; solve.cu): work
+// entries in topological order, the items they name, and per item the node
+// counter it waits on (with its target) and the one it signals.
+struct FlowPlan {
+  int top = 0;       // tree levels it covers, from the root side (the rest: level launches)
+  int rpl = 0;       // right-hand sides per lane (32 * rpl per chunk)
+  int n_chunks = 0;  // right-hand-side chunks the entries cover
+  int n_entries = 0;
+  int kc_cap = 0, ds_rows = 0, ri_max = 0, sc_rows = 0, max_s = 1, max_f = 1, cm_cap = 0, nbuf = 1;
+  int warp_max_k = 0, warp_rows_pad = 0;
+  size_t smem = 0;
+  int grid = 0;      // persistent CTAs (resident capacity, at most one per entry)
+  DBuf<int4> entries, sync;
+  DBuf<PanelItem> items;
+};
+
+// Host description of the factor tree a flow plan is built from (bank-wide
+// node numbering; per node: sizes, RHS set, offsets, child-map pointer and
+// parent, and the nodes of each height and depth).
+struct FlowNodes {
+  const std::vector<int>& s;
+  const std::vector<int>& m;
+  const std::vector<int>& node_set;
+  const std::vector<int>& w_off;
+  const std::vector<int>& own_off;
+  const std::vector<int>& upd_off;
+  const std::vector<int>& cm_off;
+  const std::vector<int>& cmap_ptr;
+  const std::vector<long long>& goff;
+  const std::vector<long long>& hoff;
+  const std::vector<int>& parent;
+  std::vector<std::vector<int>> by_height, by_depth;
+};
+
+// A flow plan before upload: the launch shape, the items with their waits and
+// signals ((wait counter or -1, target, signal counter or -1, 0)), and the
+// entries in ticket order ((kind, first item, item count, RHS chunk)).
+struct FlowPlanHost {
+  bool ok = false;  // false: its staging does not fit in shared memory
+  int n_chunks = 0;
+  int kc_cap = 1, ds_rows = 1, ri_max = 4, sc_rows = 0, max_s = 1, max_f = 1, cm_cap = 0, nbuf = 1;
+  int warp_max_k = 0, warp_rows_pad = 0;
+  size_t smem = 0;
+  std::vector<PanelItem> items;
+  std::vector<int4> sync, entries;
+};
+
+// Builds one direction's flow plan over the `top` tree levels nearest the root
+// (forward: the highest heights; backward: the smallest depths; top >= the
+// level count: all of them) for rpl right-hand sides per lane and at most
+// max_nrhs right-hand sides per set (host only; esz: bytes per value; kc_max:
+// staged block columns per chunk; n_sm: multiprocessors to fill).
+FlowPlanHost plan_flow(const FlowNodes& nd, bool forward, int top, int rpl, int max_nrhs, int kc_max, int esz,
+                       int n_sm);
 
 struct LevelPlan {
   int n_large = 0, n_thin = 0;
@@ -172,9 +228,25 @@ class FactorBank {
   // Panel banks: choose each level's tiling option by timing whole sweeps on
   // these right-hand sides (the sweep's outputs are garbage afterwards).
   // tuned_ms(): the tuned sweep's time.
-  void autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps = 3);
-  void autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps = 3);
+  // flow_mode: 0 = the flow sweep when it times faster than the tuned levels,
+  // 1 = the fastest flow sweep wherever one applies, -1 = levels only.
+  void autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps = 3, int flow_mode = 0);
+  void autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps = 3, int flow_mode = 0);
+  // Untuned banks: the flow sweep with the most right-hand sides per lane that
+  // applies to these sets (the level sweep if none does).
+  void force_flow(const IlSetsViewF& sets, int max_nrhs);
+  void force_flow(const IlSetsView& sets, int max_nrhs);
   double tuned_ms() const { return tuned_ms_; }
+  // Panel banks: right-hand sides per lane of the flow sweep in use (0: every
+  // level its own launch), and the tree levels it covers from the root side.
+  int flow_rpl() const { return flow_sel_ < 0 ? 0 : flow_cfg_[flow_sel_].rpl; }
+  int flow_top() const { return flow_sel_ < 0 ? 0 : flow_cfg_[flow_sel_].top; }
+  // 1 if a flow sweep's wait ran out since the bank was built or the flag was
+  // last cleared (that sweep's results were written as NaN); synchronises
+  int flow_error(bool clear = false) const;
+  // Diagnostic: the next forward flow sweep finds the first factor's root
+  // counter far below its target, so that root's waits run out.
+  void debug_arm_flow_stall() const;
   // Diagnostic: device time of each level launch of one sweep (forward levels,
   // then backward), CUDA events recorded between the launches, mean of reps
   // sweeps after one warm-up; the events keep consecutive levels from
@@ -201,11 +273,29 @@ class FactorBank {
   template <typename SVT>
   void solve_panel(const SVT& sets, int max_nrhs, cudaStream_t st) const;
   template <typename SVT>
-  void autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, int reps);
+  void autotune_panel(const SVT& sets, int max_nrhs, cudaStream_t st, int reps, int flow_mode);
+  template <typename SVT>
+  void force_flow_impl(const SVT& sets, int max_nrhs);
   template <typename SVT>
   int panel_rpl(const SVT& sets, int max_nrhs) const;
   double tuned_ms_ = 0.0;
   int tune_launches_ = 0;
+  // flow sweeps built at creation: levels covered from the root side x staged
+  // columns per chunk x right-hand sides per lane, both directions each
+  struct FlowConfig {
+    int top = 0, kc = 0, rpl = 0;
+    FlowPlan plan[2];  // forward, backward
+  };
+  std::vector<FlowConfig> flow_cfg_;
+  int flow_sel_ = -1;     // the configuration in use (-1: level launches only)
+  DBuf<int> flow_state_;  // [2][nodes] counters, 2 tickets, error flag
+  int n_nodes_ = 0;
+  int stall_node_ = -1;  // the first factor's root (debug_arm_flow_stall)
+  void release_unused_flow();
+  template <typename SVT>
+  bool flow_ok(const SVT& sets, int max_nrhs, int cfg) const;
+  template <typename SVT>
+  void solve_flow(const SVT& sets, int max_nrhs, int cfg, cudaStream_t st) const;
   BankView view() const;
   template <typename SV>
   void solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const;

@@ -1,0 +1,72 @@
+"""Increment solves (pecs_options.increment_solves, mixed precision): each
+time step's FP32-factor solves compute the increment from the previous step's
+solution -- residual b - K u_prev in FP32 pairs, one FP32 sweep -- instead of
+a sweep and a refinement sweep from zero.  The fixed point is the FP64
+system's; trajectories stay within the mixed mode's bounds of FP64; the
+benchmark's 1e-8 criterion stops at the same step counts."""
+import numpy as np
+import pytest
+
+import oracle
+import pecs_gb300 as pg
+from helpers import rel_err, to_lib
+from test_gpu_parity import _panel_instances
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctxs(Ps):
+    mk = lambda **kw: pg.Context([to_lib(P) for P in Ps], **kw)
+    return (mk(), mk(precision=pg.PREC_FP32_MIXED),
+            mk(precision=pg.PREC_FP32_MIXED, increment_solves=True))
+
+
+def test_increment_solves_launch_count_and_trajectory(pecs_lib):
+    """40 instances (80 carrier and 40 Poisson right-hand sides: both banks
+    on FP32 panel sweeps): one sweep per solve instead of two, and the state
+    after 20 steps as close to FP64 as the refined mixed mode's bound."""
+    Ps = _panel_instances(40, oracle.half_cell_params(n_refine=3))
+    ref, mx, inc = _ctxs(Ps)
+    a, b = mx.info(), inc.info()
+    assert b.launches_per_step < a.launches_per_step
+    for c in (ref, mx, inc):
+        c.initialize()
+        c.step(20)
+    for f in ref.fields():
+        e_mx = max(rel_err(mx.get_state(f, i), ref.get_state(f, i)) for i in range(40))
+        e_inc = max(rel_err(inc.get_state(f, i), ref.get_state(f, i)) for i in range(40))
+        print("after 20 steps", f, "mixed", e_mx, "increment", e_inc)
+        assert e_inc < 1e-6, (f, e_inc)
+
+
+def test_increment_solves_reach_the_fp64_fixed_point(pecs_lib):
+    """6000 steps (past the point where FP64 changes by < 1e-10 per step):
+    the increment solves' fixed point equals the FP64 one to 1e-9 in every
+    field and in the interface current."""
+    base = oracle.half_cell_params(n_refine=3)
+    Ps = _panel_instances(40, base)
+    ref, mx, inc = _ctxs(Ps)
+    for c in (ref, mx, inc):
+        c.initialize()
+        c.step(6000)
+    cur64, cur_inc, cur_mx = ref.interface_current(), inc.interface_current(), mx.interface_current()
+    for f in ref.fields():
+        e_inc = max(rel_err(inc.get_state(f, i), ref.get_state(f, i)) for i in range(40))
+        e_mx = max(rel_err(mx.get_state(f, i), ref.get_state(f, i)) for i in range(40))
+        print("fixed point", f, "mixed", e_mx, "increment", e_inc)
+        assert e_inc < 1e-9, (f, e_inc)
+    e_cur = np.max(np.abs(cur_inc - cur64) / np.abs(cur64))
+    print("current", e_cur, np.max(np.abs(cur_mx - cur64) / np.abs(cur64)))
+    assert e_cur < 1e-9
+
+
+def test_increment_solves_stop_with_fp64_at_the_benchmark_criterion(pecs_lib):
+    Ps = _panel_instances(40, oracle.half_cell_params(n_refine=3))
+    ref, _, inc = _ctxs(Ps)
+    steps = {}
+    for name, c in (("fp64", ref), ("inc", inc)):
+        c.initialize()
+        steps[name], _ = c.run_to_steady_state(5000, 1e-8, check_every=50)
+    d = np.abs(np.asarray(steps["inc"], float) - np.asarray(steps["fp64"], float))
+    print("step differences", d.max(), np.median(steps["fp64"]))
+    assert np.all(d <= 0.05 * np.asarray(steps["fp64"], float) + 2)

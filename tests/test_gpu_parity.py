@@ -369,3 +369,32 @@ def test_bench_mesh_batched_fp64_and_mixed(pecs_lib, bench_mesh_oracle):
     bound = {"densities": 1e-6, "potential": 1e-5, "D": 1e-5, "current": 1e-5, "J": 1e-4}
     for k, v in w.items():
         assert v < bound[k], (k, w)
+
+
+@pytest.mark.parametrize("P", [oracle.half_cell_params(n_refine=3),
+                               INSULATED_SCHOTTKY,
+                               oracle.half_cell_params(n_refine=2, degree=2),
+                               oracle.half_cell_params(n_refine=2, degree=2, poisson_pairing=1)],
+                         ids=["halfcell_r3", "insulated_schottky", "halfcell_r2_k2", "halfcell_r2_k2_rt2"])
+def test_mixed_carrier_rhs_against_oracle(pecs_lib, P):
+    """The mixed mode's carrier right-hand side on a state 10 FP64 steps along
+    the trajectory, against the oracle's FP64 one: the current rows (constant
+    part + drift, FP32-pair arithmetic) to 1e-12 of the row scale, the density
+    rows (+ (1/dt) M u in FP32 pairs + FP32 recombination and interface
+    terms) to 1e-8 of the row scale."""
+    pb = oracle.Problem(P)
+    st, _, _ = pb.run(10)
+    ctx = _ctx(P, precision=pg.PREC_FP32_MIXED)
+    ctx.initialize()
+    for name, v in st.items():
+        ctx.set_state(FIELD_OF[name], v)
+    ctx.assemble_carrier_rhs()
+    rhs = pb.carrier_rhs(st)
+    for name, v in rhs.items():
+        got = ctx.get_rhs(FIELD_OF[name])
+        third = len(v) // 3
+        cur, dens = slice(0, 2 * third), slice(2 * third, None)
+        e_cur = np.max(np.abs(got[cur] - v[cur])) / np.max(np.abs(v[cur]))
+        e_den = np.max(np.abs(got[dens] - v[dens])) / np.max(np.abs(v[dens]))
+        print(name, e_cur, e_den)
+        assert e_cur < 1e-12 and e_den < 1e-8, (name, e_cur, e_den)
