@@ -11,7 +11,9 @@ dataset exists for this model): seeded parameter draws.
 
 Default (full) mode, one bench step = 64 held-out points:
   value   learned + batched: the points streamed through 64 slots of one
-          context in FP32-mixed precision, each warm-started by the neural
+          context in FP32-mixed precision with increment solves (one FP32
+          sweep per solve on the residual against the previous step; the
+          same fixed point as refined solves), each warm-started by the neural
           operator (first-step-residual fallback), timed with CUDA events on
           the library's stream, parameters uploaded per refill, L2 flushed.
   e2e     64 further points through the public C ABI (pecs_sweep_stream) with
@@ -75,6 +77,9 @@ def parse():
     ap.add_argument("--batch-inst", type=int, default=64)
     ap.add_argument("--leaf-cells", type=int, default=8,
                     help="nested-dissection leaf size in cells (the solve tree's height)")
+    ap.add_argument("--increment", type=int, choices=[0, 1], default=1,
+                    help="mixed precision: time steps solve for the increment from the previous "
+                         "step (one FP32 sweep per solve, same fixed point); 0 = refined solves")
     ap.add_argument("--flow", type=int, choices=[-1, 0, 1], default=0,
                     help="batched solve sweeps: 1 = one persistent launch per direction, "
                          "-1 = one launch per tree level, 0 = whichever the autotuner times faster")
@@ -350,7 +355,7 @@ def run_profile_sweep(args):
     pg.build()
     prec = {"fp64": pg.PREC_FP64, "fp32ir": pg.PREC_FP32_IR, "mixed": pg.PREC_FP32_MIXED}[args.precision]
     ctx = pg.Context(workload_params(args, 0), precision=prec, leaf_cells=args.leaf_cells,
-                     flow_sweep=args.flow)
+                     flow_sweep=args.flow, increment_solves=bool(args.increment))
     which = 0 if args.profile_sweep == "carrier" else 1
     info = ctx.info()
     ms = ctx.time_solve(which, reps=1)
@@ -383,7 +388,7 @@ def run_plain(args):
     prec = {"fp64": pg.PREC_FP64, "fp32ir": pg.PREC_FP32_IR, "mixed": pg.PREC_FP32_MIXED}[args.precision]
     params = workload_params(args, rank)
     ctx = pg.Context(params, precision=prec, device=local, use_graphs=args.profile_steps == 0,
-                     flow_sweep=args.flow)
+                     flow_sweep=args.flow, increment_solves=bool(args.increment))
     info = ctx.info()
     if args.profile_steps:
         ctx.initialize()
@@ -610,7 +615,8 @@ def run_full(args):
     thetas = L.sample(per_rank * world, seed=777)[rank * per_rank:(rank + 1) * per_rank]
     th_w, th_t, th_e = thetas[:n_w], thetas[n_w:n_w + n_t], thetas[n_w + n_t:]
     ctx = pg.Context([L.instance_params(t, base) for t in thetas[:B]], precision=pg.PREC_FP32_MIXED,
-                     device=local, leaf_cells=args.leaf_cells, flow_sweep=args.flow)
+                     device=local, leaf_cells=args.leaf_cells, flow_sweep=args.flow,
+                     increment_solves=bool(args.increment))
     info = ctx.info()
     trained_here = None
     if os.path.exists(args.model):

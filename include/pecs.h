@@ -139,9 +139,9 @@ typedef struct pecs_options {
   int increment_solves; /* PECS_PREC_FP32_MIXED: time steps solve for the increment from the
                            previous step's solution -- the residual b - K u_prev in FP32 pairs,
                            one FP32 sweep, u = u_prev + increment -- instead of a sweep and a
-                           refinement sweep from zero; the fixed point is the FP64 system's
-                           (the residual vanishes there).  Initial and refill solves keep
-                           the refinement.  (1 = on, 0 = default: off) */
+                           refinement sweep from zero; the residual vanishes at the fixed
+                           point, which is therefore the refined mixed mode's.  Initial and
+                           refill solves keep the refinement.  (1 = on, 0 = default: off) */
 } pecs_options;
 
 typedef struct pecs_info {

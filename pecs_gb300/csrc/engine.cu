@@ -169,7 +169,10 @@ __global__ void k_scatter_delta_il(const float* __restrict__ d32, const double* 
   __syncthreads();
   for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
     const int k = k0 + kk, d = d0 + threadIdx.x;
-    if (k < R && d < n && (!mask || mask[k / nf])) dst[k][d] = old[k][d] + f2d_exact(t[threadIdx.x][kk]);
+    // FP32-pair sum converted with integer operations (FP64 additions are
+    // the scarce resource on GB300): the state keeps ~47 bits of the update
+    if (k < R && d < n && (!mask || mask[k / nf]))
+      dst[k][d] = ff2d_i32(ff_add(d2ff(old[k][d]), t[threadIdx.x][kk]));
   }
 }
 
@@ -195,6 +198,18 @@ __global__ void k_widen_il(const float* __restrict__ x32, double* __restrict__ x
 __device__ __forceinline__ float2 as_pair(float2 v) { return v; }
 __device__ __forceinline__ float2 as_pair(float v) { return make_float2(v, 0.f); }
 
+// b - (sh + sl): for a float residual (the next sweep's input) entirely in
+// FP32 pairs, b split on the integer pipe; for a double residual in FP64
+template <typename RT>
+__device__ __forceinline__ RT df_residual(double b, float sh, float sl) {
+  if constexpr (sizeof(RT) == 4) {
+    const float2 t = ff_add(d2ff(b), make_float2(-sh, -sl));
+    return t.x + t.y;
+  } else {
+    return b - ((double)sh + (double)sl);
+  }
+}
+
 template <typename X, typename RT>
 __global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const X* __restrict__ xs,
                                  RT* __restrict__ r, int n, int R) {
@@ -213,7 +228,7 @@ __global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const X*
     sl += e + pe;
   }
   const size_t o = (size_t)row * R + k;
-  r[o] = (RT)(b[o] - ((double)sh + (double)sl));
+  r[o] = df_residual<RT>(b[o], sh, sl);
 }
 
 // Four right-hand sides per lane (128 per warp, R a multiple of 4): the row's
@@ -233,8 +248,8 @@ __device__ __forceinline__ void ld_pairs4(const float2* p, float2 (&v)[4]) {
   v[2] = make_float2(t1.x, t1.y);
   v[3] = make_float2(t1.z, t1.w);
 }
-__device__ __forceinline__ void st4(float* p, const double (&v)[4]) {
-  *reinterpret_cast<float4*>(p) = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+__device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
 }
 __device__ __forceinline__ void st4(double* p, const double (&v)[4]) {
   reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
@@ -267,9 +282,9 @@ __global__ void k_residual_df_il4(CsrDf A, const double* __restrict__ b, const X
   const size_t o = (size_t)row * R + k;
   const double2 b0 = reinterpret_cast<const double2*>(b + o)[0], b1 = reinterpret_cast<const double2*>(b + o)[1];
   const double bb[4] = {b0.x, b0.y, b1.x, b1.y};
-  double v[4];
+  RT v[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) v[q] = bb[q] - ((double)sh[q] + (double)sl[q]);
+  for (int q = 0; q < 4; ++q) v[q] = df_residual<RT>(bb[q], sh[q], sl[q]);
   st4(r + o, v);
 }
 
@@ -731,7 +746,7 @@ struct Engine {
   // 1 - target) in FP32 pairs, one FP32 sweep d = K32^-1 r, u = u_prev + d.
   // The error of d relative to the exact increment is that of one FP32 solve,
   // so it shrinks with the step's change and vanishes at the fixed point,
-  // where r = 0: the steady state is that of the FP64 system.
+  // where r = 0: the steady state is that of the refined solves.
   bool delta_solves() const {
     return opt.increment_solves > 0 && opt.precision == PECS_PREC_FP32_MIXED;
   }

@@ -14,25 +14,29 @@
 
 namespace pecs {
 
+// The bit fields are handled in 32-bit halves (__double2hiint /
+// __double2loint / __hiloint2double): 64-bit integer shifts and bit counts
+// also occupy the narrow FP64 unit on GB300 (measured with ncu: FP64-pipe
+// activity followed them), 32-bit integer operations do not.
+
 // exact float -> double
 __device__ __forceinline__ double f2d_exact(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xFFu;
+  if ((u << 1) == 0u) return __hiloint2double((int)u, 0);  // +-0
   if (e == 0u || e == 0xFFu) return (double)f;
-  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
-                                  ((unsigned long long)(e + (1023u - 127u)) << 52) |
-                                  ((unsigned long long)(u & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)bits);
+  const unsigned m = u & 0x7FFFFFu;
+  const unsigned hi = (u & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
+  return __hiloint2double((int)hi, (int)(m << 29));
 }
 
 // double -> float rounded toward zero (relative error < 2^-23); for sums of
 // squares, where the rounding mode does not matter
 __device__ __forceinline__ float d2f_trunc(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7FFull) - 1023 + 127;
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
   if (e <= 0 || e >= 0xFF) return (float)x;  // zero, tiny, huge, inf, nan
-  const unsigned u = ((unsigned)(b >> 63) << 31) | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7FFFFFull);
-  return __uint_as_float(u);
+  return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
 }
 
 // ---- FP32-pair ("double-float") arithmetic --------------------------------
@@ -41,29 +45,70 @@ __device__ __forceinline__ float d2f_trunc(double x) {
 // classic error-free transformations: TwoSum (Knuth), FastTwoSum (Dekker;
 // |a| >= |b|) and the product error through a fused multiply-add.
 
-// binary64 -> pair: hi = x truncated to 24 bits (integer pipe), lo = the next
-// 24 bits of x (truncated), both built from x's bit fields; values whose
-// exponent puts lo outside the normal float range (and zeros, infinities,
-// NaNs) take the regular conversion
+// binary64 -> pair: hi = x truncated to 24 bits, lo = the next 24 bits of x
+// (truncated), both built from x's bit fields on the integer pipe; |x| below
+// 2^-126 becomes 0 and a lo below the normal float range is dropped (absolute
+// errors under 2^-126), values above 2^127 take the regular conversion
 __device__ __forceinline__ float2 d2ff(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7FFull) - 1023;
-  if (e < -70 || e > 126) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu) - 1023;
+  if (e < -126) return make_float2(__uint_as_float(sign), 0.f);  // zero, or below 2^-126: 0
+  if (e > 126) {  // huge, infinity, NaN
     const float h = (float)x;
     return make_float2(h, (float)(x - (double)h));
   }
-  const float hi = d2f_trunc(x);
-  const unsigned m = (unsigned)(b & 0x1FFFFFFFull);  // the 29 bits below hi's mantissa
-  if (m == 0u) return make_float2(hi, 0.f);
-  const int lead = 31 - __clz(m);                     // m = 1.f * 2^lead
+  const float fh = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+  const unsigned m = lo & 0x1FFFFFFFu;  // the 29 bits below hi's mantissa
+  if (m == 0u) return make_float2(fh, 0.f);
+  const int lead = 31 - __clz(m);       // m = 1.f * 2^lead
+  const int ex = e - 52 + lead + 127;   // lo = m * 2^(e - 52)
+  if (ex <= 0) return make_float2(fh, 0.f);  // lo below the normal range: dropped
   const unsigned mant = lead > 23 ? (m >> (lead - 23)) : (m << (23 - lead));
-  const unsigned ex = (unsigned)(e - 52 + lead + 127);  // lo = m * 2^(e - 52)
-  const float lo = __uint_as_float(((unsigned)(b >> 63) << 31) | (ex << 23) | (mant & 0x7FFFFFu));
-  return make_float2(hi, lo);
+  return make_float2(fh, __uint_as_float(sign | ((unsigned)ex << 23) | (mant & 0x7FFFFFu)));
 }
 
 // pair -> binary64 (the two exact widenings and one FP64 addition)
 __device__ __forceinline__ double ff2d(float2 a) { return f2d_exact(a.x) + f2d_exact(a.y); }
+
+// pair -> binary64 with 32-bit integer operations only: hi's 24-bit
+// significand is placed at bits 52..29 of a 53-bit integer held in two
+// words, lo's significand aligned to it (bits below 2^(e_hi - 52) dropped) is
+// added or subtracted with carry, and one shift renormalises (|lo| <= ulp(hi),
+// so the sum moves by less than a factor of two).  Within one unit in the
+// last place of the exact sum; subnormal, infinite and NaN halves take ff2d.
+__device__ __forceinline__ double ff2d_i32(float2 a) {
+  const unsigned uh = __float_as_uint(a.x), ul = __float_as_uint(a.y);
+  const int eh = (int)((uh >> 23) & 0xFFu), el = (int)((ul >> 23) & 0xFFu);
+  if ((ul << 1) == 0u) return f2d_exact(a.x);
+  if (eh == 0 || eh == 0xFF || el == 0xFF) return ff2d(a);
+  if (el == 0) return f2d_exact(a.x);  // subnormal lo: below hi's last place
+  const int sh = 29 - (eh - el);       // lo's significand in units of 2^(eh - 179)
+  if (sh < -24) return f2d_exact(a.x);
+  const unsigned ml = (ul & 0x7FFFFFu) | 0x800000u;
+  const unsigned L = sh >= 0 ? (ml << sh) : (ml >> -sh);
+  const unsigned mh = (uh & 0x7FFFFFu) | 0x800000u;
+  unsigned AH = mh >> 3, AL = mh << 29;  // mh * 2^29
+  if ((uh ^ ul) >> 31) {
+    AH -= (AL < L) ? 1u : 0u;
+    AL -= L;
+  } else {
+    const unsigned t = AL + L;
+    AH += (t < AL) ? 1u : 0u;
+    AL = t;
+  }
+  int e = eh - 127;
+  if (AH >= (1u << 21)) {  // carried into bit 53
+    AL = (AL >> 1) | (AH << 31);
+    AH >>= 1;
+    ++e;
+  } else if (AH < (1u << 20)) {  // borrowed below bit 52
+    AH = (AH << 1) | (AL >> 31);
+    AL <<= 1;
+    --e;
+  }
+  return __hiloint2double((int)((uh & 0x80000000u) | ((unsigned)(e + 1023) << 20) | (AH & 0xFFFFFu)), (int)AL);
+}
 
 __device__ __forceinline__ float2 ff_fast_two_sum(float a, float b) {
   const float s = a + b;

@@ -163,8 +163,7 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
   for (int b = 0; b < nrt; ++b) Dd[b] = to_q<Tq>(Pv[R.rt[c * nrt + b]]);
   const double2 h = R.h[c];
-  const double hxhy = h.x * h.y;
-  const Tq hxhy_q = to_q<Tq>(hxhy);
+  const Tq hxhy_q = std::is_same<Tq, double>::value ? (Tq)(h.x * h.y) : to_q<Tq>(h.x) * to_q<Tq>(h.y);
   const Tq charge = which ? Tq(1) : Tq(-1);
   const Tq inv_eps = to_q<Tq>(R.inv_eps);
   // quadrature-term accumulators: [Jx (n1) | Jy (n1) | u (n1)]
@@ -227,7 +226,8 @@ __global__ void __launch_bounds__(128)
         }
       }
     }
-    const float2 sc = d2ff((which ? 1.0 : -1.0) * R.inv_eps * hxhy);
+    float2 sc = ff_mul(ff_mul(d2ff(R.inv_eps), d2ff(h.x)), d2ff(h.y));
+    if (!which) sc = make_float2(-sc.x, -sc.y);
 #pragma unroll
     for (int a = 0; a < 2 * n1; ++a) drift_ff[a] = ff_mul(sc, drift_ff[a]);
   }
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(128)
       if constexpr (std::is_same<Tq, double>::value)
         outp[o] = bcp[o] + (double)r[comp * n1 + a];
       else
-        outp[o] = bcp[o] + ff2d(drift_ff[comp * n1 + a]);
+        outp[o] = ff2d_i32(ff_add(d2ff(bcp[o]), drift_ff[comp * n1 + a]));
     }
   if constexpr (std::is_same<Tq, double>::value) {
 #pragma unroll
@@ -310,17 +310,17 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
       for (int b = 0; b < n1; ++b) s += T.mref[a * n1 + b] * uown[b];
       const size_t o = (size_t)2 * nc * n1 + c * n1 + a;
-      outp[o] = bcp[o] + s * hxhy * R.inv_dt + from_q<Tq>(r[2 * n1 + a]);
+      outp[o] = bcp[o] + s * (h.x * h.y) * R.inv_dt + from_q<Tq>(r[2 * n1 + a]);
     }
   } else {
-    const float2 md = d2ff(hxhy * R.inv_dt);
+    const float2 md = ff_mul(ff_mul(d2ff(h.x), d2ff(h.y)), d2ff(R.inv_dt));
 #pragma unroll
     for (int a = 0; a < n1; ++a) {
       float2 s = make_float2(0.f, 0.f);
 #pragma unroll
       for (int b = 0; b < n1; ++b) s = ff_fma(T.mref_ff[a * n1 + b], uff[b], s);
       const size_t o = (size_t)2 * nc * n1 + c * n1 + a;
-      outp[o] = bcp[o] + ff2d(ff_add(ff_mul(s, md), r[2 * n1 + a]));
+      outp[o] = ff2d_i32(ff_add(ff_add(d2ff(bcp[o]), ff_mul(s, md)), r[2 * n1 + a]));
     }
   }
 }
