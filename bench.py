@@ -71,9 +71,11 @@ def parse():
     ap.add_argument("--ref-procs", type=int, default=0,
                     help="--impl reference: oracle processes (0 = one per host core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", choices=["full", "plain"], default="full",
+    ap.add_argument("--mode", choices=["full", "plain", "ragged"], default="full",
                     help="full: learned warm start + 64-instance batches (FP32-mixed) with the "
-                         "plain FP64 path measured beside it; plain: one configuration only")
+                         "plain FP64 path measured beside it; plain: one configuration only; "
+                         "ragged: 64 instances of refinement 5-7 and degree 1-2 in FP64, "
+                         "one context per mesh group")
     ap.add_argument("--batch-inst", type=int, default=64)
     ap.add_argument("--leaf-cells", type=int, default=8,
                     help="nested-dissection leaf size in cells (the solve tree's height)")
@@ -344,7 +346,75 @@ def main():
         return run_profile_sweep(args)
     if args.mode == "full" and not args.profile_steps:
         return run_full(args)
+    if args.mode == "ragged":
+        return run_ragged(args)
     return run_plain(args)
+
+
+def ragged_points(n, seed):
+    """Uneven I-V points: refinement uniform on {5, 6, 7}, LDG degree on {1, 2},
+    bias U[-0.5, 0.5], G0 U[0.5, 2], alpha U[1, 10], tau log-uniform [0.1, 10]."""
+    import numpy as np
+    import pecs_gb300 as pg
+    rng = np.random.default_rng(seed)
+    pts = []
+    for _ in range(n):
+        tau = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
+        pts.append(pg.half_cell(n_refine=int(rng.integers(5, 8)), degree=int(rng.integers(1, 3)),
+                                phi_app=float(rng.uniform(-0.5, 0.5)), G0=float(rng.uniform(0.5, 2.0)),
+                                alpha=float(rng.uniform(1.0, 10.0)), tau_n=tau, tau_p=tau))
+    return pts
+
+
+def run_ragged(args):
+    """64 uneven points per rank (FP64) to steady state through
+    sweep.ragged_sweep: the points are grouped by mesh and each group is
+    streamed through its own context, the groups one after another; host
+    parameters in, steps and currents out.  One bench step = the 64 points;
+    the contexts' setup (factorisation, autotuning) is outside the timed
+    region, as for every other mode (it happens once per mesh)."""
+    import numpy as np
+    import torch
+
+    import pecs_gb300 as pg
+    from pecs_gb300.sweep import matrix_key
+
+    world, rank, local = dist_init(args)
+    pg.build()
+    n = args.batch_inst
+    groups = {}
+    for i, p in enumerate(ragged_points(n * world, 31)[rank * n:(rank + 1) * n]):
+        groups.setdefault(matrix_key(p), []).append(p)
+    ctxs = [(pts, pg.Context(pts, device=local)) for pts in groups.values()]
+    for pts, c in ctxs:        # warm-up: a few steps of every group
+        c.sweep_stream(pts, 3, 1e-30, 3)
+    barrier(world)
+    torch.cuda.synchronize()
+    per_group, t_all = [], 0.0
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for pts, c in ctxs:
+            tg = time.perf_counter()
+            steps, cur, _ = c.sweep_stream(pts, MAX_STEPS, TOL, CHECK_EVERY)
+            p0 = pts[0]
+            per_group.append({"refine": int(round(np.log2(p0.ny))), "degree": p0.degree, "points": len(pts),
+                              "seconds": time.perf_counter() - tg, "median_steps": float(np.median(steps)),
+                              "capped": int(np.sum(steps >= MAX_STEPS))})
+        torch.cuda.synchronize()
+        t_all = time.perf_counter() - t0
+    t_all = max_over_ranks(t_all, world)
+    if rank == 0:
+        line = {"metric": "I-V points/sec to steady state", "value": n * world / t_all,
+                "unit": "I-V points/s", "n_gpus": world, "steps": 1, "warmup": 1,
+                "ms_per_step": t_all * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": f"{n} uneven half-cell points per GPU: refinement 5-7, LDG degree 1-2, "
+                                       f"FP64, to rel. change <= {TOL} (<= {MAX_STEPS} steps), one context "
+                                       "per mesh group, groups one after another",
+                           "groups": per_group, "timing": "host wall clock around the public API calls"},
+                "clocks": clk.summary()}
+        print(json.dumps(line))
+    return 0
 
 
 def run_profile_sweep(args):
@@ -486,7 +556,9 @@ def run_plain(args):
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": {"fp64": "f64", "fp32ir": "f32 factors + f64 refinement",
-                  "mixed": "f32 factors/quadrature + double-float refinement"}[args.precision],
+                  "mixed": ("f32 factors/quadrature, double-float residuals, increment solves"
+                            if args.increment else
+                            "f32 factors/quadrature + double-float refinement")}[args.precision],
         "data": "synthetic",
         "config": {"workload": f"half cell 2x{2**args.refine}x{2**args.refine}, LDG k=1, "
                                f"RT0xDGQ0 Poisson, dt=1e-3, to rel. change <= {TOL} "
@@ -697,8 +769,10 @@ def run_full(args):
         "metric": "I-V points/sec to steady state", "value": value, "unit": "I-V points/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 factors/sweeps + double-float refinement (learned+batched); "
-                                      "f64 plain",
+        "vs_baseline": None,
+        "dtype": ("f32 factors/sweeps, double-float residuals and mass/drift terms, increment solves "
+                  if args.increment else
+                  "f32 factors/sweeps + double-float refinement ") + "(learned+batched); f64 plain",
         "data": "synthetic",
         "config": {"workload": f"learned+batched: held-out I-V points streamed through {B} slots on the half "
                                f"cell 2x{2**args.refine}x{2**args.refine}, LDG k=1, RT0xDGQ0 Poisson, dt=1e-3, "

@@ -120,7 +120,7 @@ __device__ __forceinline__ const float* tab<float>(const double*, const float* f
 // constant part are FP64 (GB300 issues FP32 operations ~60x faster than FP64,
 // conversions included).
 template <int K, int KP, typename Tq>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, (K == 1 && sizeof(Tq) == 4) ? 8 : 1)
     k_carrier_rhs(Tables T, RegionDev semi, RegionDev elec, int n_regions, FieldPtrs F,
                   const InstDev* __restrict__ inst, const double* __restrict__ iface_ne,
                   const double* __restrict__ iface_pe, int n_iface, const double* __restrict__ sch_ne,

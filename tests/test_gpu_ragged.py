@@ -35,3 +35,43 @@ def test_ragged_sweep_matches_single_instances(pecs_lib):
         for f in ctx.fields():
             b = ctx.get_state(f, 0)
             assert np.linalg.norm(fields[i][f] - b) <= 1e-13 * np.linalg.norm(b), (i, f)
+
+
+def config3_points(n=64, seed=11):
+    """Config 3's draws: refinement uniform on {5, 6, 7}, LDG degree on {1, 2},
+    bias U[-0.5, 0.5], G0 U[0.5, 2], alpha U[1, 10], tau log-uniform [0.1, 10]."""
+    rng = np.random.default_rng(seed)
+    pts = []
+    for _ in range(n):
+        tau = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
+        pts.append(pg.half_cell(n_refine=int(rng.integers(5, 8)), degree=int(rng.integers(1, 3)),
+                                phi_app=float(rng.uniform(-0.5, 0.5)), G0=float(rng.uniform(0.5, 2.0)),
+                                alpha=float(rng.uniform(1.0, 10.0)), tau_n=tau, tau_p=tau))
+    return pts
+
+
+def test_config3_ragged_batch_levels_5_to_7(pecs_lib):
+    """Config 3's shape: 64 instances with refinement levels 5-7 and degrees
+    1-2 in FP64, each mesh group streamed through its own context (every
+    stage one launch per group).  After 10 steps (the step cap) one instance
+    of every group equals the same instance marched alone -- padded with
+    copies to its group's slot count, so the same kernels run -- to 1e-13."""
+    pts = config3_points()
+    steps, cur, fields = ragged_sweep(pts, slots=64, max_steps=10, tol=1e-30, check_every=5,
+                                      want_fields=True)
+    assert np.all(steps == 10)
+    groups = {}
+    for i, p in enumerate(pts):
+        groups.setdefault(matrix_key(p), []).append(i)
+    assert len(groups) == 6
+    for key, idx in groups.items():
+        i = idx[len(idx) // 2]
+        ctx = pg.Context([pts[i]] * len(idx))
+        ctx.initialize()
+        ctx.step(10)
+        for f in ctx.fields():
+            b = ctx.get_state(f, 0)
+            assert np.linalg.norm(fields[i][f] - b) <= 1e-13 * np.linalg.norm(b), (key, f)
+        c = ctx.interface_current()[0]
+        assert abs(cur[i] - c) <= 1e-12 * abs(c)
+        ctx.close()
