@@ -130,12 +130,13 @@ typedef struct pecs_options {
   int gpu_factor_min_front; /* factorisation: fronts with at least this many rows are
                                factored in FP64 on the GPU (0 = default 1024; < 0 = all
                                on the host); host_setup_only contexts factor on the host */
-  int flow_sweep;      /* panel solve kernels: one persistent launch per sweep direction,
-                          nodes started as soon as their children (forward) or parent
-                          (backward) finish, instead of one launch per tree level
-                          (0 = default: when the autotuner times it faster; 1 = wherever
-                          a flow plan applies; -1 = never).  A flow plan applies to banks
-                          whose sweep vector rows are whole 128-byte lines */
+  int flow_sweep;      /* solve sweeps: one persistent launch per sweep direction, nodes
+                          started as soon as their children (forward) or parent (backward)
+                          finish, instead of one launch per tree level (0 = default: when
+                          the autotuner times it faster; 1 = wherever a flow plan applies;
+                          -1 = never).  Panel banks: a flow plan applies where the sweep
+                          vector rows are whole 128-byte lines; few-right-hand-side banks:
+                          up to 16 (FP64: 8) right-hand sides per set */
   int increment_solves; /* PECS_PREC_FP32_MIXED: time steps solve for the increment from the
                            previous step's solution -- the residual b - K u_prev in FP32 pairs,
                            one FP32 sweep, u = u_prev + increment -- instead of a sweep and a
@@ -162,7 +163,8 @@ typedef struct pecs_info {
   int flow_rpl[2];         /* carrier / Poisson sweeps: right-hand sides per lane of the flow
                               sweep in use (0: one launch per tree level) */
   int flow_top[2];         /* carrier / Poisson sweeps: tree levels (from the root side) the
-                              flow launches cover; the others are launched level by level */
+                              flow launches cover (0: none); the others are launched level
+                              by level */
 } pecs_info;
 
 typedef struct pecs_ctx pecs_ctx;

@@ -1006,6 +1006,17 @@ struct Engine {
           bk.force_flow(il_view(which, false), il[which].max_R);
       }
     }
+    // few-right-hand-side banks: the flow sweep when it times faster (or as
+    // flow_sweep forces)
+    if (opt.autotune || opt.flow_sweep != 0) {
+      for (int which = 0; which < 2; ++which) {
+        FactorBank& bk = which == 0 ? bank_c : bank_p;
+        if (bk.panel()) continue;
+        bk.tune_rows_flow(il_view(which, false), il[which].max_R, st,
+                          opt.autotune ? opt.flow_sweep : (opt.flow_sweep > 0 ? 1 : -1));
+      }
+      PECS_CUDA(cudaStreamSynchronize(st));
+    }
     // steady-state buffers
     partial.alloc((size_t)n_inst * 5 * kRedChunks);
     partial.zero();
@@ -2418,7 +2429,7 @@ int pecs_debug_flow_stall(pecs_ctx* ctx, int which, int* flag) {
     Engine& e = ctx->e;
     need_device(e);
     const FactorBank& B = which == 0 ? e.bank_c : e.bank_p;
-    if (B.flow_rpl() == 0) throw PecsError(PECS_E_STATE, "the bank does not use the flow sweep");
+    if (B.flow_rpl() == 0 && !B.rows_flow()) throw PecsError(PECS_E_STATE, "the bank does not use the flow sweep");
     B.debug_arm_flow_stall();
     e.bank_sweep(B, which, false, e.st);
     PECS_CUDA(cudaStreamSynchronize(e.st));

@@ -19,6 +19,34 @@ namespace {
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
+// Polls of one wait before it gives up (with 64 ns sleeps and a global load
+// each: tens to hundreds of milliseconds, against a whole sweep of well under
+// a millisecond).
+constexpr unsigned kFlowPollLimit = 1u << 18;
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_release_gpu(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait for *ctr >= target; false (and the error flag set) when the
+// poll limit runs out.
+__device__ __noinline__ bool flow_wait(const int* ctr, int target, int* err) {
+  if (ld_acquire_gpu(ctr) >= target) return true;
+  for (unsigned n = 0; n < kFlowPollLimit; ++n) {
+    __nanosleep(64);
+    if (ld_acquire_gpu(ctr) >= target) return true;
+  }
+  atomicExch(err, 1);
+  return false;
+}
+
+
 // Loads RB consecutive staged values (16-byte aligned) with vector loads.
 template <typename T, int RB>
 __device__ __forceinline__ void load_rhs(const T* p, T (&v)[RB]) {
@@ -57,6 +85,11 @@ __device__ __forceinline__ double getb(const SetView& s, int r, int d) { return 
 __device__ __forceinline__ double gety(const SetView& s, int r, int d) { return s.y[r][d]; }
 __device__ __forceinline__ double getx(const SetView& s, int r, int d) { return s.x[r][d]; }
 __device__ __forceinline__ double getw(const SetView& s, int r, int d) { return s.w[r][d]; }
+// L2-coherent reads (ld.global.cg) of vectors written inside the same launch
+// (flow sweeps: other CTAs' update and solution rows, which share cache lines
+// with rows this SM may have read earlier)
+__device__ __forceinline__ double getw_cg(const SetView& s, int r, int d) { return __ldcg(s.w[r] + d); }
+__device__ __forceinline__ double getx_cg(const SetView& s, int r, int d) { return __ldcg(s.x[r] + d); }
 __device__ __forceinline__ void puty(const SetView& s, int r, int d, double v) { s.y[r][d] = v; }
 __device__ __forceinline__ void putx(const SetView& s, int r, int d, double v) { s.x[r][d] = v; }
 __device__ __forceinline__ void putw(const SetView& s, int r, int d, double v) { s.w[r][d] = v; }
@@ -72,6 +105,12 @@ __device__ __forceinline__ double getx(const IlSetView& s, int r, int d) {
 __device__ __forceinline__ double getw(const IlSetView& s, int r, int d) {
   return s.w[(size_t)d * s.nrhs + r];
 }
+__device__ __forceinline__ double getw_cg(const IlSetView& s, int r, int d) {
+  return __ldcg(s.w + (size_t)d * s.nrhs + r);
+}
+__device__ __forceinline__ double getx_cg(const IlSetView& s, int r, int d) {
+  return __ldcg(s.x + (size_t)d * s.nrhs + r);
+}
 __device__ __forceinline__ void puty(const IlSetView& s, int r, int d, double v) {
   s.y[(size_t)d * s.nrhs + r] = v;
 }
@@ -83,17 +122,17 @@ __device__ __forceinline__ void putw(const IlSetView& s, int r, int d, double v)
 }
 
 // Sum of the children's update entries that land on front position p.
-template <typename SVi>
+template <bool CG, typename SVi>
 __device__ __forceinline__ double gather_updates(const BankView& B, const SVi& st, int r, int c0,
                                                  int c1) {
   double v = 0.0;
-  for (int c = c0; c < c1; ++c) v += getw(st, r, B.cmap_idx[c]);
+  for (int c = c0; c < c1; ++c) v += CG ? getw_cg(st, r, B.cmap_idx[c]) : getw(st, r, B.cmap_idx[c]);
   return v;
 }
 
 // Forward sweep, large node: CTA computes rows [r0, r1) of Gf * d.
-template <typename T, int RB, typename SV>
-__device__ void fwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
+template <typename T, int RB, typename SV, bool CG = false>
+__device__ void fwd_large(const BankView& B, const SV& S, int4 it, T* sm, int chunk) {
   const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j];
   const auto& st = S.set[B.node_set[j]];
@@ -103,8 +142,8 @@ __device__ void fwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
   const int wo = B.w_off[j];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   {
-    // one chunk of RB right-hand sides per blockIdx.y
-    const int rb = blockIdx.y * RB;
+    // one chunk of RB right-hand sides (blockIdx.y in the level kernels)
+    const int rb = chunk * RB;
     if (rb >= st.nrhs) return;
     const int nr = min(RB, st.nrhs - rb);
     for (int p = threadIdx.x; p < s; p += blockDim.x) {
@@ -113,7 +152,7 @@ __device__ void fwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
 #pragma unroll
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
-        if (r < nr) v = getb(st, rb + r, gd) - gather_updates(B, st, rb + r, c0, c1);
+        if (r < nr) v = getb(st, rb + r, gd) - gather_updates<CG>(B, st, rb + r, c0, c1);
         sm[r * s + p] = (T)v;  // RHS-major: lanes of a warp read consecutive columns
       }
     }
@@ -158,7 +197,7 @@ __device__ void fwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
               puty(st, rb + r, own[row], (double)acc[r]);
             } else {
               const int t = row - s;
-              const double cu = gather_updates(B, st, rb + r, cptr[row], cptr[row + 1]);
+              const double cu = gather_updates<CG>(B, st, rb + r, cptr[row], cptr[row + 1]);
               putw(st, rb + r, wo + t, cu + (double)acc[r]);
             }
           }
@@ -174,8 +213,8 @@ __device__ void fwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
 // column-major, so lane `row` reads Gf[c][row] for c = 0..s-1: consecutive
 // lanes read consecutive addresses and every lane has s independent loads in
 // flight; no cross-lane reduction.  A warp item covers rows [r0, r1).
-template <typename T, int RB, typename SV>
-__device__ void fwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
+template <typename T, int RB, typename SV, bool CG = false>
+__device__ void fwd_thin(const BankView& B, const SV& S, int4 it, T* sm, int chunk) {
   const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j], m = B.m[j], f = s + m;
   const auto& st = S.set[B.node_set[j]];
@@ -185,8 +224,8 @@ __device__ void fwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
   const int wo = B.w_off[j];
   const int lane = threadIdx.x & 31;
   {
-    // one chunk of RB right-hand sides per blockIdx.y
-    const int rb = blockIdx.y * RB;
+    // one chunk of RB right-hand sides (blockIdx.y in the level kernels)
+    const int rb = chunk * RB;
     if (rb >= st.nrhs) return;
     const int nr = min(RB, st.nrhs - rb);
     for (int p = lane; p < s; p += 32) {
@@ -195,7 +234,7 @@ __device__ void fwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
 #pragma unroll
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
-        if (r < nr) v = getb(st, rb + r, gd) - gather_updates(B, st, rb + r, c0, c1);
+        if (r < nr) v = getb(st, rb + r, gd) - gather_updates<CG>(B, st, rb + r, c0, c1);
         sm[p * RB + r] = (T)v;
       }
     }
@@ -221,7 +260,7 @@ __device__ void fwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
         const int c0 = cptr[row], c1 = cptr[row + 1];
 #pragma unroll
         for (int r = 0; r < RB; ++r)
-          if (r < nr) putw(st, rb + r, wo + row - s, gather_updates(B, st, rb + r, c0, c1) + (double)acc[r]);
+          if (r < nr) putw(st, rb + r, wo + row - s, gather_updates<CG>(B, st, rb + r, c0, c1) + (double)acc[r]);
       }
     }
     __syncwarp();
@@ -229,8 +268,8 @@ __device__ void fwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
 }
 
 // Backward sweep, large node: rows [r0, r1) of Hb * [y_own ; x_upd].
-template <typename T, int RB, typename SV>
-__device__ void bwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
+template <typename T, int RB, typename SV, bool CG = false>
+__device__ void bwd_large(const BankView& B, const SV& S, int4 it, T* sm, int chunk) {
   const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j], m = B.m[j], f = s + m;
   const auto& st = S.set[B.node_set[j]];
@@ -239,15 +278,15 @@ __device__ void bwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
   const T* H = static_cast<const T*>(B.H) + B.hoff[j];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   {
-    // one chunk of RB right-hand sides per blockIdx.y
-    const int rb = blockIdx.y * RB;
+    // one chunk of RB right-hand sides (blockIdx.y in the level kernels)
+    const int rb = chunk * RB;
     if (rb >= st.nrhs) return;
     const int nr = min(RB, st.nrhs - rb);
     for (int p = threadIdx.x; p < f; p += blockDim.x) {
 #pragma unroll
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
-        if (r < nr) v = (p < s) ? gety(st, rb + r, own[p]) : getx(st, rb + r, upd[p - s]);
+        if (r < nr) v = (p < s) ? gety(st, rb + r, own[p]) : (CG ? getx_cg(st, rb + r, upd[p - s]) : getx(st, rb + r, upd[p - s]));
         sm[r * f + p] = (T)v;
       }
     }
@@ -295,8 +334,8 @@ __device__ void bwd_large(const BankView& B, const SV& S, int4 it, T* sm) {
 }
 
 // Backward sweep, thin node (s + m <= kThinCols): Hb stored column-major.
-template <typename T, int RB, typename SV>
-__device__ void bwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
+template <typename T, int RB, typename SV, bool CG = false>
+__device__ void bwd_thin(const BankView& B, const SV& S, int4 it, T* sm, int chunk) {
   const int j = it.x, r0 = it.y, r1 = it.z;
   const int s = B.s[j], m = B.m[j], f = s + m;
   const auto& st = S.set[B.node_set[j]];
@@ -305,15 +344,15 @@ __device__ void bwd_thin(const BankView& B, const SV& S, int4 it, T* sm) {
   const T* H = static_cast<const T*>(B.H) + B.hoff[j];
   const int lane = threadIdx.x & 31;
   {
-    // one chunk of RB right-hand sides per blockIdx.y
-    const int rb = blockIdx.y * RB;
+    // one chunk of RB right-hand sides (blockIdx.y in the level kernels)
+    const int rb = chunk * RB;
     if (rb >= st.nrhs) return;
     const int nr = min(RB, st.nrhs - rb);
     for (int p = lane; p < f; p += 32) {
 #pragma unroll
       for (int r = 0; r < RB; ++r) {
         double v = 0.0;
-        if (r < nr) v = (p < s) ? gety(st, rb + r, own[p]) : getx(st, rb + r, upd[p - s]);
+        if (r < nr) v = (p < s) ? gety(st, rb + r, own[p]) : (CG ? getx_cg(st, rb + r, upd[p - s]) : getx(st, rb + r, upd[p - s]));
         sm[p * RB + r] = (T)v;
       }
     }
@@ -348,11 +387,11 @@ __global__ void __launch_bounds__(kSolveThreads)
   pdl_trigger();  // the next level may start launching once every CTA here has started
   pdl_wait();     // every access below may read the previous level's results
   if ((int)blockIdx.x < n_large) {
-    fwd_large<T, RB, SV>(B, S, items[blockIdx.x], sm);
+    fwd_large<T, RB, SV>(B, S, items[blockIdx.x], sm, (int)blockIdx.y);
   } else {
     const int wib = threadIdx.x >> 5;
     const int idx = ((int)blockIdx.x - n_large) * (kSolveThreads / 32) + wib;
-    if (idx < n_thin) fwd_thin<T, RB, SV>(B, S, thin[idx], sm + wib * kThinCols * RB);
+    if (idx < n_thin) fwd_thin<T, RB, SV>(B, S, thin[idx], sm + wib * kThinCols * RB, (int)blockIdx.y);
   }
 }
 
@@ -365,11 +404,11 @@ __global__ void __launch_bounds__(kSolveThreads)
   pdl_trigger();
   pdl_wait();
   if ((int)blockIdx.x < n_large) {
-    bwd_large<T, RB, SV>(B, S, items[blockIdx.x], sm);
+    bwd_large<T, RB, SV>(B, S, items[blockIdx.x], sm, (int)blockIdx.y);
   } else {
     const int wib = threadIdx.x >> 5;
     const int idx = ((int)blockIdx.x - n_large) * (kSolveThreads / 32) + wib;
-    if (idx < n_thin) bwd_thin<T, RB, SV>(B, S, thin[idx], sm + wib * kThinCols * RB);
+    if (idx < n_thin) bwd_thin<T, RB, SV>(B, S, thin[idx], sm + wib * kThinCols * RB, (int)blockIdx.y);
   }
 }
 
@@ -399,6 +438,103 @@ void launch_level(bool forward, const BankView& B, const SV& S, const LevelPlan&
   else
     PECS_CUDA(cudaLaunchKernelEx(&cfg, k_backward<T, RB, SV>, B, S, (const int4*)L.items.p, L.n_large,
                                  (const int4*)L.thin.p, L.n_thin));
+}
+
+// The output rows of one item (RHS chunk `chunk`) set to NaN by threads
+// t0 = 0 .. nt-1: a flow item whose wait ran out, so that the solve's results
+// are flagged non-finite.
+template <int RB, bool FWD, typename SV>
+__device__ void poison_rows(const BankView& B, const SV& S, int4 it, int chunk, int t0, int nt) {
+  const int j = it.x, r0 = it.y, r1 = it.z;
+  const int s = B.s[j];
+  const auto& st = S.set[B.node_set[j]];
+  const int* own = B.own_idx + B.own_off[j];
+  const int rb = chunk * RB;
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  for (int e = t0; e < (r1 - r0) * RB; e += nt) {
+    const int row = r0 + e / RB, r = rb + e % RB;
+    if (r >= st.nrhs) continue;
+    if (!FWD)
+      putx(st, r, own[row], nan);
+    else if (row < s)
+      puty(st, r, own[row], nan);
+    else
+      putw(st, r, B.w_off[j] + row - s, nan);
+  }
+}
+
+// Flow sweep of the few-right-hand-side path: one persistent launch per
+// direction over the level plans' items -- wide-node row chunks (kind 0, a
+// CTA) and groups of up to eight thin-node row chunks (kind 1, a warp each)
+// -- in topological order, with the panel flow sweep's tickets, per-node
+// counters, bounded waits, deferred release signals and reset of the other
+// direction's counters (see k_panel_flow).  Vectors written inside the
+// launch are read with ld.global.cg: their rows (8 or 16 bytes per dof)
+// share cache lines.
+struct RowsFlowView {
+  const int4* entries;  // (kind, first item, item count, RHS chunk)
+  const int4* items;    // (node, row0, row1, 0)
+  const int4* sync;     // (wait counter or -1, target, signal counter or -1, 0)
+  int* ctr;
+  int* other_ctr;
+  int n_ctr;
+  int* queue;
+  int* other_queue;
+  int* err;
+  int n_entries;
+};
+
+template <typename T, int RB, bool FWD, typename SV>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_rows_flow(BankView B, SV S, RowsFlowView F) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  __shared__ int s_ticket, s_ok;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = blockIdx.x * kSolveThreads + tid; i < F.n_ctr; i += gridDim.x * kSolveThreads) F.other_ctr[i] = 0;
+  if (blockIdx.x == 0 && tid == 0) *F.other_queue = 0;
+  int pending = -1;
+  if (tid == 0) s_ticket = atomicAdd(F.queue, 1);
+  for (;;) {
+    __syncthreads();
+    const int t = s_ticket;
+    if (lane == 0 && pending >= 0) red_release_gpu(F.ctr + pending, 1);
+    pending = -1;
+    __syncthreads();
+    if (t >= F.n_entries) break;
+    if (tid == 0) s_ticket = atomicAdd(F.queue, 1);
+    const int4 e = F.entries[t];
+    if (e.x == 0) {
+      const int4 sy = F.sync[e.y];
+      if (tid == 0) s_ok = sy.x < 0 || flow_wait(F.ctr + sy.x, sy.y, F.err);
+      __syncthreads();
+      if (s_ok) {
+        if (FWD)
+          fwd_large<T, RB, SV, true>(B, S, F.items[e.y], sm, e.w);
+        else
+          bwd_large<T, RB, SV, true>(B, S, F.items[e.y], sm, e.w);
+      } else {
+        poison_rows<RB, FWD, SV>(B, S, F.items[e.y], e.w, tid, kSolveThreads);
+      }
+      if (tid == 0) pending = sy.z;
+    } else if (warp < e.z) {
+      const int4 sy = F.sync[e.y + warp];
+      int ok = 1;
+      if (lane == 0) ok = sy.x < 0 || flow_wait(F.ctr + sy.x, sy.y, F.err);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (ok) {
+        T* wsm = sm + warp * kThinCols * RB;
+        if (FWD)
+          fwd_thin<T, RB, SV, true>(B, S, F.items[e.y + warp], wsm, e.w);
+        else
+          bwd_thin<T, RB, SV, true>(B, S, F.items[e.y + warp], wsm, e.w);
+      } else {
+        poison_rows<RB, FWD, SV>(B, S, F.items[e.y + warp], e.w, lane, 32);
+      }
+      __syncwarp();
+      if (lane == 0) pending = sy.z;
+    }
+  }
 }
 
 template <typename T, int RB>
@@ -1035,33 +1171,6 @@ struct FlowView {
   int n_entries;
 };
 
-// Polls of one wait before it gives up (with 64 ns sleeps and a global load
-// each: tens to hundreds of milliseconds, against a whole sweep of well under
-// a millisecond).
-constexpr unsigned kFlowPollLimit = 1u << 18;
-
-__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void red_release_gpu(int* p, int v) {
-  asm volatile("red.release.gpu.global.add.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
-}
-
-// Bounded wait for *ctr >= target; false (and the error flag set) when the
-// poll limit runs out.
-__device__ __noinline__ bool flow_wait(const int* ctr, int target, int* err) {
-  if (ld_acquire_gpu(ctr) >= target) return true;
-  for (unsigned n = 0; n < kFlowPollLimit; ++n) {
-    __nanosleep(64);
-    if (ld_acquire_gpu(ctr) >= target) return true;
-  }
-  atomicExch(err, 1);
-  return false;
-}
-
 template <typename T, int RPL, bool FWD, typename SVT>
 __global__ void __launch_bounds__(kSolveThreads, 3)
     k_panel_flow(BankView B, SVT S, FlowView F, PanelShape P, int warp_max_k, int warp_rows_pad) {
@@ -1487,6 +1596,7 @@ BankView FactorBank::view() const {
 }
 
 int FactorBank::kernel_launches_per_solve() const {
+  if (rows_flow_on_) return 2;
   if (flow_sel_ >= 0) {
     const int top = flow_cfg_[flow_sel_].top;
     int n = 2;
@@ -1629,9 +1739,12 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
   // level plans: uniform work units so a level's time is not set by one long
   // item.  Thin nodes (cols <= kThinCols): warp items of <= kThinRows rows.
   // Wide nodes: CTA items of <= kWideRows rows (kWideRows/8 rows per warp).
+  std::vector<std::vector<int4>> keep_items[2], keep_thin[2];  // host copies for the flow plans
   auto make = [&](const std::vector<LevelNodes>& lv, bool forward, std::vector<LevelPlan>& out) {
     out.clear();
     out.resize(lv.size());
+    keep_items[forward ? 0 : 1].assign(lv.size(), {});
+    keep_thin[forward ? 0 : 1].assign(lv.size(), {});
     for (size_t l = 0; l < lv.size(); ++l) {
       std::vector<int4> items, thin;
       int max_cols = 0;
@@ -1670,6 +1783,8 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
       out[l].max_cols = max_cols;
       out[l].items.upload(items);
       out[l].thin.upload(thin);
+      keep_items[forward ? 0 : 1][l] = items;
+      keep_thin[forward ? 0 : 1][l] = thin;
     }
   };
   if (panel) {
@@ -1910,6 +2025,59 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
   }
   make(fl, true, fwd_);
   make(bl, false, bwd_);
+  // flow plans over the same items: per node the number of its items (its
+  // signals), waits on the children's (forward) or the parent's (backward)
+  {
+    const int n_nodes = (int)hs.size();
+    n_nodes_ = n_nodes;
+    std::vector<int> parent(n_nodes, -1);
+    int b0 = 0;
+    for (int fi = 0; fi < n_sets_; ++fi) {
+      const MfFactor& F = *factors[fi];
+      for (int j = 0; j < (int)F.nodes.size(); ++j)
+        for (int c : F.nodes[j].children) parent[b0 + c] = b0 + j;
+      b0 += (int)F.nodes.size();
+    }
+    flow_state_.alloc(2 * (size_t)n_nodes + 3);
+    flow_state_.zero();
+    rows_flow_on_ = false;
+    stall_node_ = -1;
+    for (int g = 0; g < (int)factors[0]->nodes.size() && stall_node_ < 0; ++g)
+      if (parent[g] < 0 && !factors[0]->nodes[g].children.empty()) stall_node_ = g;
+    for (int d = 0; d < 2; ++d) {
+      std::vector<int> nsig(n_nodes, 0), kid_sig(n_nodes, 0);
+      for (size_t l = 0; l < keep_items[d].size(); ++l) {
+        for (const int4& it : keep_items[d][l]) ++nsig[it.x];
+        for (const int4& it : keep_thin[d][l]) ++nsig[it.x];
+      }
+      for (int g = 0; g < n_nodes; ++g)
+        if (parent[g] >= 0) kid_sig[parent[g]] += nsig[g];
+      std::vector<int4> items, sync, entries;
+      auto push = [&](const int4& it) {
+        const int g = it.x, pa = parent[g];
+        items.push_back(it);
+        sync.push_back(d == 0 ? make_int4(kid_sig[g] > 0 ? g : -1, kid_sig[g], pa, 0)
+                              : make_int4(pa, pa >= 0 ? nsig[pa] : 0, g, 0));
+      };
+      for (size_t l = 0; l < keep_items[d].size(); ++l) {
+        for (const int4& it : keep_items[d][l]) {
+          entries.push_back(make_int4(0, (int)items.size(), 1, 0));
+          push(it);
+        }
+        const std::vector<int4>& th = keep_thin[d][l];
+        for (size_t i = 0; i < th.size(); i += kSolveThreads / 32) {
+          const int n = (int)std::min<size_t>(kSolveThreads / 32, th.size() - i);
+          entries.push_back(make_int4(1, (int)items.size(), n, 0));
+          for (int k = 0; k < n; ++k) push(th[i + k]);
+        }
+      }
+      RowsFlowPlan& P = rows_flow_plan_[d];
+      P.n_entries = (int)entries.size();
+      P.entries.upload(entries);
+      P.items.upload(items);
+      P.sync.upload(sync);
+    }
+  }
   max_cols_ = 0;
   for (auto& l : fwd_) max_cols_ = std::max(max_cols_, l.max_cols);
   for (auto& l : bwd_) max_cols_ = std::max(max_cols_, l.max_cols);
@@ -1936,12 +2104,109 @@ void FactorBank::build(const std::vector<const MfFactor*>& factors, int precisio
   }
 }
 
-template <typename SV>
-void FactorBank::solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const {
-  const BankView B = view();
+int FactorBank::solve_rb(int max_nrhs) const {
   int rb = max_nrhs <= 1 ? 1 : (max_nrhs <= 2 ? 2 : (max_nrhs <= 4 ? 4 : (max_nrhs <= 8 ? 8 : 16)));
   if (prec_ == PECS_PREC_FP64) rb = std::min(rb, 8);  // FP64: register budget
-  rb = std::min(rb, max_rb_);
+  return std::min(rb, max_rb_);
+}
+
+template <typename T, int RB, typename SV>
+void launch_rows_flow(const BankView& B, const SV& S, const RowsFlowView& Ff, const RowsFlowView& Fb,
+                      size_t smem, cudaStream_t st) {
+  const void* fns[2] = {(const void*)k_rows_flow<T, RB, true, SV>, (const void*)k_rows_flow<T, RB, false, SV>};
+  int dev = 0, n_sm = 0;
+  PECS_CUDA(cudaGetDevice(&dev));
+  PECS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  for (int d = 0; d < 2; ++d) {
+    PECS_CUDA(cudaFuncSetAttribute(fns[d], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap));
+    int per_sm = 0;
+    PECS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[d], kSolveThreads, smem));
+    const RowsFlowView& F = d == 0 ? Ff : Fb;
+    const int grid = std::max(1, std::min(F.n_entries, std::max(1, per_sm) * n_sm));
+    if (d == 0)
+      k_rows_flow<T, RB, true, SV><<<grid, kSolveThreads, smem, st>>>(B, S, F);
+    else
+      k_rows_flow<T, RB, false, SV><<<grid, kSolveThreads, smem, st>>>(B, S, F);
+    PECS_CUDA(cudaGetLastError());
+  }
+}
+
+template <typename SV>
+void FactorBank::solve_rows_flow(const SV& sets, int max_nrhs, cudaStream_t st) const {
+  const BankView B = view();
+  const int rb = solve_rb(max_nrhs);
+  const size_t esz = prec_ == PECS_PREC_FP64 ? 8 : 4;
+  const size_t smem = std::max(((size_t)max_cols_ + kSolveThreads / 32) * rb * esz,
+                               (size_t)(kSolveThreads / 32) * kThinCols * rb * esz);
+  int* base = flow_state_.p;
+  int* ctr[2] = {base, base + n_nodes_};
+  int* queue[2] = {base + 2 * (size_t)n_nodes_, base + 2 * (size_t)n_nodes_ + 1};
+  int* err = base + 2 * (size_t)n_nodes_ + 2;
+  RowsFlowView F[2];
+  for (int d = 0; d < 2; ++d) {
+    const RowsFlowPlan& P = rows_flow_plan_[d];
+    F[d] = RowsFlowView{P.entries.p, P.items.p, P.sync.p, ctr[d], ctr[1 - d], n_nodes_,
+                        queue[d],    queue[1 - d], err,   P.n_entries};
+  }
+  auto go = [&](auto tag) {
+    using T = decltype(tag);
+    switch (rb) {
+      case 1: launch_rows_flow<T, 1, SV>(B, sets, F[0], F[1], smem, st); break;
+      case 2: launch_rows_flow<T, 2, SV>(B, sets, F[0], F[1], smem, st); break;
+      case 4: launch_rows_flow<T, 4, SV>(B, sets, F[0], F[1], smem, st); break;
+      case 8: launch_rows_flow<T, 8, SV>(B, sets, F[0], F[1], smem, st); break;
+      default: launch_rows_flow<T, 16, SV>(B, sets, F[0], F[1], smem, st); break;
+    }
+  };
+  if (prec_ == PECS_PREC_FP64)
+    go(double{});
+  else
+    go(float{});
+}
+
+void FactorBank::tune_rows_flow(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int flow_mode, int reps) {
+  rows_flow_on_ = false;
+  if (panel_ || flow_mode < 0 || max_nrhs > solve_rb(max_nrhs) || rows_flow_plan_[0].n_entries == 0) return;
+  if (flow_mode > 0) {
+    rows_flow_on_ = true;
+    return;
+  }
+  cudaEvent_t e0, e1;
+  PECS_CUDA(cudaEventCreate(&e0));
+  PECS_CUDA(cudaEventCreate(&e1));
+  auto time = [&](bool flow) {
+    rows_flow_on_ = flow;
+    solve(sets, max_nrhs, st);  // warm-up
+    float best = 1e30f;
+    for (int r = 0; r < reps; ++r) {
+      PECS_CUDA(cudaEventRecord(e0, st));
+      solve(sets, max_nrhs, st);
+      PECS_CUDA(cudaEventRecord(e1, st));
+      PECS_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      PECS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best = std::min(best, ms);
+    }
+    return best;
+  };
+  const float lev = time(false), flo = time(true);
+  if (flow_error() != 0) throw PecsError(PECS_E_CUDA, "flow sweep: a wait for a node's inputs ran out");
+  if (std::getenv("PECS_TUNE_LOG"))
+    std::fprintf(stderr, "rows flow: %.4f ms (levels %.4f ms)\n", flo, lev);
+  rows_flow_on_ = flo < lev;
+  tuned_ms_ = std::min(flo, lev);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+}
+
+template <typename SV>
+void FactorBank::solve_impl(const SV& sets, int max_nrhs, cudaStream_t st) const {
+  if (rows_flow_on_ && max_nrhs <= solve_rb(max_nrhs)) {
+    solve_rows_flow(sets, max_nrhs, st);
+    return;
+  }
+  const BankView B = view();
+  const int rb = solve_rb(max_nrhs);
   for (const LevelPlan& L : fwd_) {
     if (prec_ == PECS_PREC_FP64)
       launch_rb<double, SV>(rb, true, B, sets, L, max_nrhs, st);
@@ -1980,7 +2245,7 @@ int FactorBank::panel_rpl(const SVT& sets, int max_nrhs) const {
 }
 
 int FactorBank::flow_error(bool clear) const {
-  if (!panel_ || flow_state_.n == 0) return 0;
+  if (flow_state_.n == 0) return 0;
   int e = 0;
   int* p = flow_state_.p + 2 * (size_t)n_nodes_ + 2;
   PECS_CUDA(cudaMemcpy(&e, p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1989,7 +2254,7 @@ int FactorBank::flow_error(bool clear) const {
 }
 
 void FactorBank::debug_arm_flow_stall() const {
-  if (!panel_ || flow_state_.n == 0 || stall_node_ < 0) throw PecsError(PECS_E_STATE, "no flow sweep to stall");
+  if (flow_state_.n == 0 || stall_node_ < 0) throw PecsError(PECS_E_STATE, "no flow sweep to stall");
   PECS_CUDA(cudaDeviceSynchronize());
   const int v = -(1 << 30);
   PECS_CUDA(cudaMemcpy(flow_state_.p + stall_node_, &v, sizeof(int), cudaMemcpyHostToDevice));

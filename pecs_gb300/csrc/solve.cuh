@@ -192,6 +192,13 @@ struct FlowPlanHost {
 FlowPlanHost plan_flow(const FlowNodes& nd, bool forward, int top, int rpl, int max_nrhs, int kc_max, int esz,
                        int n_sm);
 
+// The flow sweep of the few-right-hand-side path (one direction): the level
+// plans' wide and thin items in topological order (solve.cu, k_rows_flow).
+struct RowsFlowPlan {
+  int n_entries = 0;
+  DBuf<int4> entries, items, sync;
+};
+
 struct LevelPlan {
   int n_large = 0, n_thin = 0;
   DBuf<int4> items;   // wide nodes: (node, row0, row1, 0), one CTA each
@@ -232,6 +239,11 @@ class FactorBank {
   // 1 = the fastest flow sweep wherever one applies, -1 = levels only.
   void autotune(const IlSetsViewF& sets, int max_nrhs, cudaStream_t st, int reps = 3, int flow_mode = 0);
   void autotune(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int reps = 3, int flow_mode = 0);
+  // Few-right-hand-side banks: time the level sweep against the flow sweep on
+  // these sets (a few sweeps each; outputs are garbage afterwards) and keep
+  // the faster (flow_mode 0), the flow sweep (1) or the levels (-1).
+  void tune_rows_flow(const IlSetsView& sets, int max_nrhs, cudaStream_t st, int flow_mode = 0, int reps = 3);
+  bool rows_flow() const { return rows_flow_on_; }
   // Untuned banks: the flow sweep with the most right-hand sides per lane that
   // applies to these sets (the level sweep if none does).
   void force_flow(const IlSetsViewF& sets, int max_nrhs);
@@ -240,7 +252,9 @@ class FactorBank {
   // Panel banks: right-hand sides per lane of the flow sweep in use (0: every
   // level its own launch), and the tree levels it covers from the root side.
   int flow_rpl() const { return flow_sel_ < 0 ? 0 : flow_cfg_[flow_sel_].rpl; }
-  int flow_top() const { return flow_sel_ < 0 ? 0 : flow_cfg_[flow_sel_].top; }
+  int flow_top() const {
+    return rows_flow_on_ ? (int)fwd_.size() : (flow_sel_ < 0 ? 0 : flow_cfg_[flow_sel_].top);
+  }
   // 1 if a flow sweep's wait ran out since the bank was built or the flag was
   // last cleared (that sweep's results were written as NaN); synchronises
   int flow_error(bool clear = false) const;
@@ -291,6 +305,11 @@ class FactorBank {
   DBuf<int> flow_state_;  // [2][nodes] counters, 2 tickets, error flag
   int n_nodes_ = 0;
   int stall_node_ = -1;  // the first factor's root (debug_arm_flow_stall)
+  RowsFlowPlan rows_flow_plan_[2];
+  bool rows_flow_on_ = false;
+  int solve_rb(int max_nrhs) const;
+  template <typename SV>
+  void solve_rows_flow(const SV& sets, int max_nrhs, cudaStream_t st) const;
   void release_unused_flow();
   template <typename SVT>
   bool flow_ok(const SVT& sets, int max_nrhs, int cfg) const;

@@ -82,3 +82,44 @@ def test_flow_wait_runs_out_and_is_reported(pecs_lib):
             x = ctx.get_state(f, i)
             assert np.all(np.isfinite(x))
             assert rel_err(x, lev.get_state(f, i)) < 1e-12
+
+
+@pytest.mark.parametrize("P", [oracle.half_cell_params(n_refine=5), oracle.half_cell_params(n_refine=3, degree=2)],
+                         ids=["ref5_k1", "ref3_k2"])
+def test_rows_flow_fp64_single_instance_matches_levels_and_oracle(pecs_lib, P):
+    """The plain single-instance FP64 path (two carrier and one Poisson
+    right-hand sides: the few-RHS kernels) with its sweeps as one persistent
+    launch per direction: equal to the level launches to 1e-12 and to the
+    oracle's trajectory within the step tolerance."""
+    lib_p = to_lib(P)
+    flow = pg.Context(lib_p, flow_sweep=1)
+    lev = pg.Context(lib_p, flow_sweep=-1)
+    assert flow.info().flow_top[0] > 0 and flow.info().solve_launches[0] == 2
+    assert lev.info().flow_top[0] == 0
+    for c in (flow, lev):
+        c.initialize()
+        c.step(10)
+    for f in flow.fields():
+        assert rel_err(flow.get_state(f), lev.get_state(f)) < 1e-12, f
+    st, _, _ = oracle.Problem(P).run(10)
+    _compare_state(flow, st, STEP_TOL)
+
+
+def test_rows_flow_wait_runs_out_and_is_reported(pecs_lib):
+    """As test_flow_wait_runs_out_and_is_reported, for the few-RHS flow sweep:
+    the stalled root's rows are written as NaN, the flag is raised, and the
+    context's next trajectory equals the level path's."""
+    lib_p = to_lib(oracle.half_cell_params(n_refine=4))
+    ctx = pg.Context(lib_p, flow_sweep=1)
+    lev = pg.Context(lib_p, flow_sweep=-1)
+    ctx.initialize()
+    flag = C.c_int(-1)
+    pg._ffi.check(pg.lib().pecs_debug_flow_stall(ctx._h, 0, C.byref(flag)))
+    assert flag.value == 1
+    for c in (ctx, lev):
+        c.initialize()
+        c.step(3)
+    for f in ctx.fields():
+        x = ctx.get_state(f)
+        assert np.all(np.isfinite(x))
+        assert rel_err(x, lev.get_state(f)) < 1e-12
