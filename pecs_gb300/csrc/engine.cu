@@ -210,9 +210,12 @@ __device__ __forceinline__ RT df_residual(double b, float sh, float sl) {
   }
 }
 
+// b: interleaved right-hand sides, or (bt non-null) a table of per-RHS
+// vectors read in place (one 8-byte load per lane; saves the transposing
+// gather of an increment solve)
 template <typename X, typename RT>
-__global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const X* __restrict__ xs,
-                                 RT* __restrict__ r, int n, int R) {
+__global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const double* const* __restrict__ bt,
+                                 const X* __restrict__ xs, RT* __restrict__ r, int n, int R) {
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int k = blockIdx.y * 32 + (threadIdx.x & 31);
   if (row >= n || k >= R) return;
@@ -228,7 +231,7 @@ __global__ void k_residual_df_il(CsrDf A, const double* __restrict__ b, const X*
     sl += e + pe;
   }
   const size_t o = (size_t)row * R + k;
-  r[o] = df_residual<RT>(b[o], sh, sl);
+  r[o] = df_residual<RT>(bt ? bt[k][row] : b[o], sh, sl);
 }
 
 // Four right-hand sides per lane (128 per warp, R a multiple of 4): the row's
@@ -257,8 +260,8 @@ __device__ __forceinline__ void st4(double* p, const double (&v)[4]) {
 }
 
 template <typename X, typename RT>
-__global__ void k_residual_df_il4(CsrDf A, const double* __restrict__ b, const X* __restrict__ xs,
-                                  RT* __restrict__ r, int n, int R) {
+__global__ void k_residual_df_il4(CsrDf A, const double* __restrict__ b, const double* const* __restrict__ bt,
+                                  const X* __restrict__ xs, RT* __restrict__ r, int n, int R) {
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int k = blockIdx.y * 128 + (threadIdx.x & 31) * 4;
   if (row >= n || k >= R) return;
@@ -280,8 +283,14 @@ __global__ void k_residual_df_il4(CsrDf A, const double* __restrict__ b, const X
     }
   }
   const size_t o = (size_t)row * R + k;
-  const double2 b0 = reinterpret_cast<const double2*>(b + o)[0], b1 = reinterpret_cast<const double2*>(b + o)[1];
-  const double bb[4] = {b0.x, b0.y, b1.x, b1.y};
+  double bb[4];
+  if (bt) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) bb[q] = bt[k + q][row];
+  } else {
+    const double2 b0 = reinterpret_cast<const double2*>(b + o)[0], b1 = reinterpret_cast<const double2*>(b + o)[1];
+    bb[0] = b0.x, bb[1] = b0.y, bb[2] = b1.x, bb[3] = b1.y;
+  }
   RT v[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) v[q] = df_residual<RT>(bb[q], sh[q], sl[q]);
@@ -289,11 +298,12 @@ __global__ void k_residual_df_il4(CsrDf A, const double* __restrict__ b, const X
 }
 
 template <typename X, typename RT>
-void launch_residual_df(const CsrDf& A, const double* b, const X* xs, RT* r, int n, int R, cudaStream_t s) {
+void launch_residual_df(const CsrDf& A, const double* b, const X* xs, RT* r, int n, int R, cudaStream_t s,
+                        const double* const* bt = nullptr) {
   if (R % 4 == 0 && R >= 96)
-    k_residual_df_il4<X, RT><<<dim3((n + 7) / 8, (R + 127) / 128), 256, 0, s>>>(A, b, xs, r, n, R);
+    k_residual_df_il4<X, RT><<<dim3((n + 7) / 8, (R + 127) / 128), 256, 0, s>>>(A, b, bt, xs, r, n, R);
   else
-    k_residual_df_il<X, RT><<<dim3((n + 7) / 8, (R + 31) / 32), 256, 0, s>>>(A, b, xs, r, n, R);
+    k_residual_df_il<X, RT><<<dim3((n + 7) / 8, (R + 31) / 32), 256, 0, s>>>(A, b, bt, xs, r, n, R);
   PECS_CUDA(cudaGetLastError());
 }
 
@@ -606,11 +616,11 @@ struct Engine {
   int launches_per_step() const {
     const int lc = bank_c.kernel_launches_per_solve(), lp = bank_p.kernel_launches_per_solve();
     const int sc = il[0].n_sets, sp = il[1].n_sets;
-    // increment solves: gather, gather of the previous solution, residual and
+    // increment solves: gather of the previous solution, residual and
     // scatter per set, one sweep
     const bool dc = delta_solves() && il_f32(0), dp = delta_solves() && il_f32(1);
-    return 1 + (dc ? lc + 4 * sc : lc * (1 + ir_iters(0)) + sc * set_launches_per_solve(0)) + 1 +
-           (dp ? lp + 4 * sp : lp * (1 + ir_iters(1)) + sp * set_launches_per_solve(1)) + 3;
+    return 1 + (dc ? lc + 3 * sc : lc * (1 + ir_iters(0)) + sc * set_launches_per_solve(0)) + 1 +
+           (dp ? lp + 3 * sp : lp * (1 + ir_iters(1)) + sp * set_launches_per_solve(1)) + 3;
   }
   // algorithmic bytes of one application of a bank to all of its right-hand
   // sides: every stored factor entry once, plus the vectors (b read, y write +
@@ -756,11 +766,11 @@ struct Engine {
     for (int si = 0; si < I.n_sets; ++si) {
       IlSet& S_ = I.set[si];
       const dim3 g((S_.n + 31) / 32, (S_.R + 31) / 32);
-      k_gather_il<<<g, tb, 0, s>>>(S_.src.p, S_.B.p, nullptr, S_.n, S_.R);
-      PECS_CUDA(cudaGetLastError());
       k_gather_pairs_il<<<g, tb, 0, s>>>(S_.dst[1 - target].p, S_.Xs.p, S_.n, S_.R);
       PECS_CUDA(cudaGetLastError());
-      launch_residual_df(csr_df.m[S_.mat], S_.B.p, S_.Xs.p, S_.Rr32.p, S_.n, S_.R, s);
+      // the right-hand sides are read in place from the per-instance vectors
+      launch_residual_df(csr_df.m[S_.mat], (const double*)nullptr, S_.Xs.p, S_.Rr32.p, S_.n, S_.R, s,
+                         (const double* const*)S_.src.p);
     }
     bank_sweep(bank, which, true, s);
     for (int si = 0; si < I.n_sets; ++si) {
