@@ -380,18 +380,46 @@ def warm_start_vectors(ctx: Context, op: NeuralOperator, thetas: np.ndarray, bas
     return init_n, init_p, fallback, (vn, vp)
 
 
+TAU = NAMES.index("tau")
+
+
+def lifetime_order(thetas: np.ndarray) -> np.ndarray:
+    """Longest carrier lifetime first: the order in which a streamed sweep
+    should take the points so that the slots finish together.  A point's
+    slowest decaying mode -- recombination, set by tau -- sets its step count
+    (on 256 held-out draws log tau correlates 0.70 with the warm-started
+    steps, the other five parameters and the first-step relative change at
+    most 0.21); starting the long points first is the longest-processing-time
+    rule of list scheduling (simulated on those draws for 192 points through
+    64 slots: makespan 9293 steps against 9823 in random order)."""
+    return np.argsort(-thetas[:, TAU], kind="stable")
+
+
 def stream_warm_sweep(ctx: Context, op: Optional[NeuralOperator], thetas: np.ndarray, base: Params,
-                      max_steps=5000, tol=1e-8, check_every=50, want_fields: bool = False):
+                      max_steps=5000, tol=1e-8, check_every=50, want_fields: bool = False,
+                      order: bool = True):
     """All rows of ``thetas`` to steady state in one streamed sweep through
     ctx's slots (pecs_sweep_stream), warm-started by ``op`` (None: standard
-    initial condition).  Returns (steps incl. the two probe steps of a
-    warm-started point, fallback flags, currents, fields or None)."""
-    params = [instance_params(t, base) for t in thetas]
+    initial condition); order: stream the points longest lifetime first
+    (lifetime_order).  Returns, in the rows' order, (steps incl. the two probe
+    steps of a warm-started point, fallback flags, currents, fields or None;
+    fields as one array per field with the points' vectors one after another)."""
+    n = thetas.shape[0]
+    perm = lifetime_order(thetas) if order else np.arange(n)
+    th = thetas[perm]
+    params = [instance_params(t, base) for t in th]
     if op is None:
         steps, cur, fin = ctx.sweep_stream(params, max_steps, tol, check_every, want_fields=want_fields)
-        return steps, np.ones(len(params), dtype=bool), cur, fin
-    init_n, init_p, fallback, keep = warm_start_vectors(ctx, op, thetas, base)
-    steps, cur, fin = ctx.sweep_stream(params, max_steps, tol, check_every, init_n=init_n, init_p=init_p,
-                                       want_fields=want_fields)
-    del keep
-    return steps + 2, fallback, cur, fin
+        fallback = np.ones(n, dtype=bool)
+    else:
+        init_n, init_p, fallback, keep = warm_start_vectors(ctx, op, th, base)
+        steps, cur, fin = ctx.sweep_stream(params, max_steps, tol, check_every, init_n=init_n, init_p=init_p,
+                                           want_fields=want_fields)
+        del keep
+        steps = steps + 2
+    inv = np.empty(n, dtype=np.int64)
+    inv[perm] = np.arange(n)
+    if fin is not None:
+        for f, a in fin.items():
+            fin[f] = a.reshape(n, -1)[inv].reshape(-1)
+    return steps[inv], np.asarray(fallback)[inv], cur[inv], fin

@@ -110,3 +110,31 @@ def test_committed_model_file_is_consistent():
     assert d["mean"].shape == d["scale"].shape == (n_out,)
     assert d["basis"].shape == (n_out, int(d["rank"])) and d["cscale"].shape == (int(d["rank"]),)
     assert np.all(d["scale"] > 0) and np.all(d["cscale"] > 0)
+
+
+def test_stream_order_longest_lifetime_first_results_in_row_order():
+    """stream_warm_sweep hands the points to the stream longest carrier
+    lifetime first and returns every result in the caller's row order."""
+    import pecs_gb300 as pg
+    th = L.sample(10, seed=3)
+
+    class FakeStream:
+        def sweep_stream(self, params, max_steps, tol, check_every, init_n=None, init_p=None,
+                         want_fields=False):
+            taus = np.array([p.tau_n for p in params])
+            assert np.all(np.diff(taus) <= 0)  # longest lifetime first
+            fin = {0: np.repeat(taus, 3), 4: np.repeat(-taus, 2)} if want_fields else None
+            return (taus * 100).astype(np.int32), taus.copy(), fin
+
+    steps, fb, cur, fin = L.stream_warm_sweep(FakeStream(), None, th, pg.half_cell(n_refine=2),
+                                              want_fields=True)
+    assert np.allclose(cur, th[:, 4])
+    assert np.array_equal(steps, (th[:, 4] * 100).astype(np.int32))
+    assert np.allclose(fin[0].reshape(10, 3), th[:, 4:5]) and np.allclose(fin[4].reshape(10, 2), -th[:, 4:5])
+    assert np.all(fb)
+    # order=False keeps the rows' order
+    class Plain(FakeStream):
+        def sweep_stream(self, params, *a, **k):
+            return np.arange(len(params), dtype=np.int32), np.zeros(len(params)), None
+    s2, _, _, _ = L.stream_warm_sweep(Plain(), None, th, pg.half_cell(n_refine=2), order=False)
+    assert np.array_equal(s2, np.arange(10))
