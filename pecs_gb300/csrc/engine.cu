@@ -1483,10 +1483,10 @@ struct Engine {
       if (!err.empty()) throw PecsError(PECS_E_ARG, err);
     }
     std::vector<int> mask(n_inst, 0);
+    for (size_t t = 0; t < slots.size(); ++t) S->inst[slots[t]] = P[t];
+    S->compute_instances_at(slots);
     for (size_t t = 0; t < slots.size(); ++t) {
       const int i = slots[t];
-      S->inst[i] = P[t];
-      S->compute_instance(i);
       mask[i] = 1;
       auto put = [&](DBuf<double>& d, const std::vector<double>& v) {
         if (v.empty()) return;

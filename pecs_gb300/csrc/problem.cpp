@@ -4,6 +4,7 @@
 #include "dense.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -702,7 +703,23 @@ void Setup::compute_instances(const std::vector<pecs_params>& p) {
   schottky_ne.assign(ninst, {});
   schottky_pe.assign(ninst, {});
   for (int fld = 0; fld < 4; ++fld) init[fld].assign(ninst, {});
-  for (int s = 0; s < ninst; ++s) compute_instance(s);
+  std::vector<int> all(ninst);
+  for (int s = 0; s < ninst; ++s) all[s] = s;
+  compute_instances_at(all);
+}
+
+// The listed instances' data on the host threads (each instance writes only
+// its own slots and reads the shared setup, so the results do not depend on
+// the thread count); instances are handed out one at a time.
+void Setup::compute_instances_at(const std::vector<int>& slots) {
+  const int n = (int)slots.size();
+  if (n == 0) return;
+  const unsigned hc = std::thread::hardware_concurrency();
+  const int nt = std::max(1, std::min(n, (int)(hc ? hc : 1)));
+  std::atomic<int> next{0};
+  dense::run_threads(nt, [&](int) {
+    for (int t = next.fetch_add(1); t < n; t = next.fetch_add(1)) compute_instance(slots[t]);
+  });
 }
 
 void Setup::compute_instance(int s) {

@@ -83,6 +83,8 @@ struct Setup {
   void compute_instances(const std::vector<pecs_params>& p);
   // recompute the per-instance data of instance s from inst[s]
   void compute_instance(int s);
+  // the same for several instances, on the host threads
+  void compute_instances_at(const std::vector<int>& slots);
 };
 
 // Validates a parameter set; returns an empty string when it is usable.
