@@ -1485,6 +1485,9 @@ struct Engine {
     std::vector<int> mask(n_inst, 0);
     for (size_t t = 0; t < slots.size(); ++t) S->inst[slots[t]] = P[t];
     S->compute_instances_at(slots);
+    // host sources of the copies below stay alive until the synchronisation
+    // at the end (the per-instance vectors, ips, mask)
+    std::vector<InstDev> ips(slots.size());
     for (size_t t = 0; t < slots.size(); ++t) {
       const int i = slots[t];
       mask[i] = 1;
@@ -1505,8 +1508,8 @@ struct Engine {
         put(sch_pe, S->schottky_pe[i]);
       }
       const pecs_params& p = S->inst[i];
-      const InstDev ip{p.k_et, p.k_ht, p.tau_n, p.tau_p, p.n_i, p.s_n, p.s_p, p.srh, 0};
-      PECS_CUDA(cudaMemcpyAsync(inst.p + i, &ip, sizeof(InstDev), cudaMemcpyHostToDevice, st));
+      ips[t] = InstDev{p.k_et, p.k_ht, p.tau_n, p.tau_p, p.n_i, p.s_n, p.s_p, p.srh, 0};
+      PECS_CUDA(cudaMemcpyAsync(inst.p + i, &ips[t], sizeof(InstDev), cudaMemcpyHostToDevice, st));
       for (int f = 0; f < 4; ++f) {
         if (!nd[f]) continue;
         const double* src = init_dev[f].p + (size_t)i * nd[f];
@@ -1515,8 +1518,6 @@ struct Engine {
         PECS_CUDA(cudaMemcpyAsync(state[cur][f].p + (size_t)i * nd[f], src, (size_t)nd[f] * 8,
                                   cudaMemcpyDeviceToDevice, st));
       }
-      // host data of this slot must stay alive until the copies ran
-      PECS_CUDA(cudaStreamSynchronize(st));
     }
     PECS_CUDA(cudaMemcpyAsync(refill_mask.p, mask.data(), n_inst * 4, cudaMemcpyHostToDevice, st));
     scatter_mask = refill_mask.p;

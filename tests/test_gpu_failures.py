@@ -90,15 +90,17 @@ def test_poisoned_predictions_fall_back_to_the_standard_start(pecs_lib):
     thetas = L.sample(4, seed=77)
     ctx = pg.Context([base] * 4)
     lay = L.Layout.of(ctx)
+    # order=False: the stand-in operator poisons rows by their position in
+    # the batch it is given, so the points keep the rows' order
     steps_p, _, cur_p, fin = L.stream_warm_sweep(ctx, None, thetas, base, 3000, 1e-8, 25,
-                                                 want_fields=True)
+                                                 want_fields=True, order=False)
     nd = lay.nd_carrier
     gn = torch.from_numpy(fin[pg.FIELD_N].reshape(4, nd)[3].copy()).cuda()
     gp = torch.from_numpy(fin[pg.FIELD_P].reshape(4, nd)[3].copy()).cuda()
     gn[:lay.u_off] = 0.0       # a prediction carries densities only
     gp[:lay.u_off] = 0.0
     op = _PoisonedOperator(gn, gp)
-    steps_w, fb, cur_w, _ = L.stream_warm_sweep(ctx, op, thetas, base, 3000, 1e-8, 25)
+    steps_w, fb, cur_w, _ = L.stream_warm_sweep(ctx, op, thetas, base, 3000, 1e-8, 25, order=False)
     assert list(fb) == [True, True, True, False]
     for k in range(3):   # fallbacks: exactly the plain march, plus the two probe steps
         assert steps_w[k] == steps_p[k] + 2
@@ -108,3 +110,16 @@ def test_poisoned_predictions_fall_back_to_the_standard_start(pecs_lib):
     steps_b, fb_b, cur_b = L.warm_started_sweep(ctx, op, thetas, base, 3000, 1e-8, 25)
     assert list(fb_b) == [True, True, True, False]
     assert np.all(np.isfinite(cur_b))
+
+
+def test_lifetime_order_changes_only_the_schedule(pecs_lib):
+    """Streaming the points longest lifetime first changes which slot runs
+    which point and when, not the points' results: the same steps and
+    currents, in the caller's row order, as the rows' own order."""
+    base = _base()
+    thetas = L.sample(8, seed=78)
+    ctx = pg.Context([base] * 4)
+    s0, f0, c0, _ = L.stream_warm_sweep(ctx, None, thetas, base, 3000, 1e-8, 25, order=False)
+    s1, f1, c1, _ = L.stream_warm_sweep(ctx, None, thetas, base, 3000, 1e-8, 25, order=True)
+    assert np.array_equal(s0, s1) and np.array_equal(f0, f1)
+    assert np.allclose(c1, c0, rtol=1e-13, atol=0.0)
