@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <thread>
+#include <condition_variable>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -1474,8 +1476,11 @@ struct Engine {
   // uploaded slice by slice), their initial state (standard, or the given
   // device densities for electrons / holes), then one Poisson solve whose
   // results are written to these slots only.
+  // pre: the slots' per-instance data already computed (a streamed sweep's
+  // background preparation), moved in; empty: computed here
   void refill(const std::vector<int>& slots, const std::vector<pecs_params>& P,
-              const std::vector<const double*>& init_n, const std::vector<const double*>& init_p) {
+              const std::vector<const double*>& init_n, const std::vector<const double*>& init_p,
+              std::vector<Setup::InstanceData>* pre = nullptr) {
     {
       std::vector<pecs_params> chk(P);
       chk.insert(chk.begin(), S->inst[0]);
@@ -1484,7 +1489,11 @@ struct Engine {
     }
     std::vector<int> mask(n_inst, 0);
     for (size_t t = 0; t < slots.size(); ++t) S->inst[slots[t]] = P[t];
-    S->compute_instances_at(slots);
+    if (pre) {
+      for (size_t t = 0; t < slots.size(); ++t) S->store_instance(slots[t], std::move((*pre)[t]));
+    } else {
+      S->compute_instances_at(slots);
+    }
     // host sources of the copies below stay alive until the synchronisation
     // at the end (the per-instance vectors, ips, mask)
     std::vector<InstDev> ips(slots.size());
@@ -1544,17 +1553,81 @@ struct Engine {
     check_every += check_every & 1;
     std::vector<int> slot_point(n_inst, -1);
     int next = 0;
+    // The points after the first fill have their per-instance data (the
+    // constant right-hand sides, projected initial states: host work of a
+    // few milliseconds each) prepared by a host thread in stream order while
+    // the GPU marches, at most n_inst points ahead of the refills.
+    struct Prefetch {
+      std::vector<Setup::InstanceData> data;
+      std::vector<char> ready;
+      std::mutex mu;
+      std::condition_variable cv;
+      int consumed = 0;
+      bool stop = false;
+      std::thread worker;
+      ~Prefetch() {
+        {
+          std::lock_guard<std::mutex> g(mu);
+          stop = true;
+        }
+        cv.notify_all();
+        if (worker.joinable()) worker.join();
+      }
+    } pf;
+    pf.data.resize(n_points);
+    pf.ready.assign(n_points, 0);
+    const int n_first = std::min(n_inst, n_points);
+    if (n_points > n_first) {
+      const unsigned hc = std::thread::hardware_concurrency();
+      const int threads = std::max(1, (int)(hc ? hc : 1));
+      const Setup* Sc = S.get();
+      pf.worker = std::thread([&pf, Sc, params, n_first, n_points, threads, this]() {
+        for (int q = n_first; q < n_points; ++q) {
+          {
+            std::unique_lock<std::mutex> lk(pf.mu);
+            pf.cv.wait(lk, [&] { return pf.stop || q - pf.consumed < n_inst; });
+            if (pf.stop) return;
+          }
+          Setup::InstanceData d;
+          try {
+            Sc->compute_instance_data(params[q], d, threads);
+          } catch (...) {
+            // left unready: the refill computes this point itself
+            std::lock_guard<std::mutex> g(pf.mu);
+            pf.ready[q] = 2;
+            pf.cv.notify_all();
+            continue;
+          }
+          std::lock_guard<std::mutex> g(pf.mu);
+          pf.data[q] = std::move(d);
+          pf.ready[q] = 1;
+          pf.cv.notify_all();
+        }
+      });
+    }
     auto take = [&](std::vector<int>& slots) {
       std::vector<pecs_params> P;
       std::vector<const double*> in, ip;
+      std::vector<Setup::InstanceData> pre;
+      bool all_pre = next >= n_first;
       for (int i : slots) {
         slot_point[i] = next;
         P.push_back(params[next]);
         in.push_back(init_n ? init_n[next] : nullptr);
         ip.push_back(init_p ? init_p[next] : nullptr);
+        if (next >= n_first) {
+          std::unique_lock<std::mutex> lk(pf.mu);
+          pf.cv.wait(lk, [&] { return pf.ready[next] != 0; });
+          if (pf.ready[next] == 1)
+            pre.push_back(std::move(pf.data[next]));
+          else
+            all_pre = false;
+          pf.consumed = next + 1;
+          pf.cv.notify_all();
+        }
         ++next;
       }
-      refill(slots, P, in, ip);
+      refill(slots, P, in, ip, all_pre && pre.size() == slots.size() ? &pre : nullptr);
     };
     // first fill: every slot the points can occupy; idle slots are inactive
     std::vector<int> first;

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <numeric>
 #include <sstream>
@@ -711,23 +712,58 @@ void Setup::compute_instances(const std::vector<pecs_params>& p) {
 // The listed instances' data on the host threads (each instance writes only
 // its own slots and reads the shared setup, so the results do not depend on
 // the thread count); instances are handed out one at a time.
+// Fewer instances than threads (a streamed sweep refilling a slot or two):
+// each instance's cell loops are split over the threads instead.
 void Setup::compute_instances_at(const std::vector<int>& slots) {
   const int n = (int)slots.size();
   if (n == 0) return;
   const unsigned hc = std::thread::hardware_concurrency();
-  const int nt = std::max(1, std::min(n, (int)(hc ? hc : 1)));
+  const int hw = std::max(1, (int)(hc ? hc : 1));
+  if (n < hw) {
+    for (int t = 0; t < n; ++t) compute_instance(slots[t], hw);
+    return;
+  }
   std::atomic<int> next{0};
-  dense::run_threads(nt, [&](int) {
+  dense::run_threads(hw, [&](int) {
     for (int t = next.fetch_add(1); t < n; t = next.fetch_add(1)) compute_instance(slots[t]);
   });
 }
 
-void Setup::compute_instance(int s) {
+namespace {
+// fn(first, last) over [0, n) in `threads` contiguous ranges (one when small)
+void par_range(int n, int threads, const std::function<void(int, int)>& fn) {
+  if (threads <= 1 || n < 512) {
+    fn(0, n);
+    return;
+  }
+  const int chunk = (n + threads - 1) / threads;
+  dense::run_threads(threads, [&](int t) {
+    const int a = t * chunk, b = std::min(n, a + chunk);
+    if (a < b) fn(a, b);
+  });
+}
+}  // namespace
+
+void Setup::compute_instance(int s, int threads) {
+  InstanceData d;
+  compute_instance_data(inst[s], d, threads);
+  store_instance(s, std::move(d));
+}
+
+void Setup::store_instance(int s, InstanceData&& d) {
+  for (int f = 0; f < 5; ++f) bconst[f][s] = std::move(d.bconst[f]);
+  for (int f = 0; f < 4; ++f) init[f][s] = std::move(d.init[f]);
+  iface_ne[s] = std::move(d.iface_ne);
+  iface_pe[s] = std::move(d.iface_pe);
+  schottky_ne[s] = std::move(d.schottky_ne);
+  schottky_pe[s] = std::move(d.schottky_pe);
+}
+
+void Setup::compute_instance_data(const pecs_params& Pi, InstanceData& d, int threads) const {
   const int nloc = n_rt + n_phi;
   std::vector<double> g1, w1;
   gauss01(k + 1, g1, w1);
   {
-    const pecs_params& Pi = inst[s];
     for (int reg = 0; reg < (full ? 2 : 1); ++reg) {
       const CarrierSystem& CS = reg == 0 ? semi : elec;
       const Grid& g = CS.grid;
@@ -735,7 +771,9 @@ void Setup::compute_instance(int s) {
       for (int cc = 0; cc < 2; ++cc) {
         int fld = 2 * reg + cc;
         std::vector<double> b(CS.ndofs, 0.0);
-        for (int K = 0; K < nc; ++K) {
+        // every cell writes only its own rows of b
+        par_range(nc, threads, [&](int K0, int K1) {
+        for (int K = K0; K < K1; ++K) {
           double x0, y0, hx, hy;
           g.geom(K, x0, y0, hx, hy);
           double diam = std::sqrt(hx * hx + hy * hy);
@@ -770,7 +808,8 @@ void Setup::compute_instance(int s) {
             }
           }
         }
-        bconst[fld][s] = std::move(b);
+        });
+        d.bconst[fld] = std::move(b);
         // initial conditions: L2 projection with QGauss(k+1) (SolarCell.cpp:1996-2021)
         std::vector<double> u(CS.ndofs, 0.0);
         {
@@ -785,7 +824,8 @@ void Setup::compute_instance(int s) {
                 for (int qx_ = 0; qx_ < nq; ++qx_)
                   Mref[a * n1 + bb] += L[qx_][a % m] * L[qy_][a / m] * L[qx_][bb % m] * L[qy_][bb / m] *
                                        w1[qx_] * w1[qy_];
-          for (int K = 0; K < nc; ++K) {
+          par_range(nc, threads, [&](int K0, int K1) {
+          for (int K = K0; K < K1; ++K) {
             double x0, y0, hx, hy;
             g.geom(K, x0, y0, hx, hy);
             std::vector<double> rhs(n1, 0.0);
@@ -819,8 +859,9 @@ void Setup::compute_instance(int s) {
             }
             for (int a = 0; a < n1; ++a) u[2 * nc * n1 + K * n1 + a] = c[a];
           }
+          });
         }
-        init[fld][s] = std::move(u);
+        d.init[fld] = std::move(u);
       }
     }
     // Poisson constant part: doping on semiconductor cells + Dirichlet potential
@@ -859,7 +900,7 @@ void Setup::compute_instance(int s) {
     }
     for (int d = 0; d < pois.ndofs; ++d)
       if (pois.constrained[d]) bP[d] = 0.0;
-    bconst[4][s] = std::move(bP);
+    d.bconst[4] = std::move(bP);
     // interface equilibria at the semiconductor face qp
     if (full) {
       std::vector<double> ne(iface_semi.size() * nq1), pe(iface_semi.size() * nq1);
@@ -872,8 +913,8 @@ void Setup::compute_instance(int s) {
           pe[t * nq1 + q] = carrier_bc(Pi, 1, X, Y);
         }
       }
-      iface_ne[s] = std::move(ne);
-      iface_pe[s] = std::move(pe);
+      d.iface_ne = std::move(ne);
+      d.iface_pe = std::move(pe);
     }
     if (has_schottky) {
       const Grid& gs = semi.grid;
@@ -894,8 +935,8 @@ void Setup::compute_instance(int s) {
           }
         }
       }
-      schottky_ne[s] = std::move(ne);
-      schottky_pe[s] = std::move(pe);
+      d.schottky_ne = std::move(ne);
+      d.schottky_pe = std::move(pe);
     }
   }
 }

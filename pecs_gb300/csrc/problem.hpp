@@ -81,8 +81,17 @@ struct Setup {
 
   explicit Setup(const std::vector<pecs_params>& p);
   void compute_instances(const std::vector<pecs_params>& p);
-  // recompute the per-instance data of instance s from inst[s]
-  void compute_instance(int s);
+  // recompute the per-instance data of instance s from inst[s] (its cell
+  // loops split over `threads` host threads)
+  void compute_instance(int s, int threads = 1);
+  // the per-instance data of one parameter set, computed apart from the
+  // slots (reads only the shared setup: safe beside other threads' calls),
+  // and its move into slot s
+  struct InstanceData {
+    std::vector<double> bconst[5], init[4], iface_ne, iface_pe, schottky_ne, schottky_pe;
+  };
+  void compute_instance_data(const pecs_params& p, InstanceData& d, int threads = 1) const;
+  void store_instance(int s, InstanceData&& d);
   // the same for several instances, on the host threads
   void compute_instances_at(const std::vector<int>& slots);
 };
