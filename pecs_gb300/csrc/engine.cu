@@ -1577,6 +1577,7 @@ struct Engine {
     pf.data.resize(n_points);
     pf.ready.assign(n_points, 0);
     const int n_first = std::min(n_inst, n_points);
+    pf.consumed = n_first;  // the first fill computes its points itself
     if (n_points > n_first) {
       const unsigned hc = std::thread::hardware_concurrency();
       const int threads = std::max(1, (int)(hc ? hc : 1));
