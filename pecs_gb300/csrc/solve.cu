@@ -1,4 +1,6 @@
-// Level-scheduled multifrontal solve kernels and their host-side plan (solve.cuh).
+// Multifrontal solve kernels and their host-side plans (solve.cuh): one
+// launch per tree level (few-right-hand-side and panel kernels), or one
+// persistent dataflow launch per direction (flow sweeps) over the same items.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>

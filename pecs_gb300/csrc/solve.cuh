@@ -1,4 +1,5 @@
-// Level-scheduled application of multifrontal LU factors on the GPU.
+// Application of multifrontal LU factors on the GPU, level by level or as a
+// dataflow sweep (flow plans below).
 //
 // A FactorBank holds one or more factors (mf.hpp) concatenated node-wise.  Each
 // factor is bound to a "RHS set": a list of right-hand sides that share the
