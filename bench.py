@@ -74,9 +74,12 @@ def parse():
     ap.add_argument("--mode", choices=["full", "plain", "ragged"], default="full",
                     help="full: learned warm start + 64-instance batches (FP32-mixed) with the "
                          "plain FP64 path measured beside it; plain: one configuration only; "
-                         "ragged: 64 instances of refinement 5-7 and degree 1-2 in FP64, "
-                         "one context per mesh group")
+                         "ragged: 64 instances of refinement 5-7 and degree 1-2 (--precision, "
+                         "default FP64), one context per mesh group")
     ap.add_argument("--batch-inst", type=int, default=64)
+    ap.add_argument("--concurrent", type=int, choices=[0, 1], default=0,
+                    help="ragged mode: run the mesh groups' sweeps at the same time (one host "
+                         "thread and CUDA stream per group) instead of one after another")
     ap.add_argument("--leaf-cells", type=int, default=8,
                     help="nested-dissection leaf size in cells (the solve tree's height)")
     ap.add_argument("--increment", type=int, choices=[0, 1], default=1,
@@ -367,14 +370,18 @@ def ragged_points(n, seed):
 
 
 def run_ragged(args):
-    """64 uneven points per rank (FP64) to steady state through
-    sweep.ragged_sweep: the points are grouped by mesh and each group is
-    streamed through its own context, the groups one after another; host
-    parameters in, steps and currents out.  One bench step = the 64 points;
-    the contexts' setup (factorisation, autotuning) is outside the timed
-    region, as for every other mode (it happens once per mesh)."""
+    """64 uneven points per rank to steady state through the public API: the
+    points are grouped by mesh and each group is streamed through its own
+    context (pecs_sweep_stream), the groups one after another or, with
+    --concurrent 1, all at once (one host thread and CUDA stream per group,
+    as sweep.ragged_sweep(concurrent=True)); host parameters in, steps and
+    currents out.  --precision fp64 (default) or mixed (with --increment).
+    One bench step = the 64 points; the contexts' setup (factorisation,
+    autotuning) is outside the timed region, as for every other mode (it
+    happens once per mesh)."""
     import numpy as np
     import torch
+    from concurrent.futures import ThreadPoolExecutor
 
     import pecs_gb300 as pg
     from pecs_gb300.sweep import matrix_key
@@ -382,35 +389,50 @@ def run_ragged(args):
     world, rank, local = dist_init(args)
     pg.build()
     n = args.batch_inst
+    prec = {"fp64": pg.PREC_FP64, "fp32ir": pg.PREC_FP32_IR, "mixed": pg.PREC_FP32_MIXED}[args.precision]
     groups = {}
     for i, p in enumerate(ragged_points(n * world, 31)[rank * n:(rank + 1) * n]):
         groups.setdefault(matrix_key(p), []).append(p)
-    ctxs = [(pts, pg.Context(pts, device=local)) for pts in groups.values()]
+    ctxs = [(pts, pg.Context(pts, device=local, precision=prec, increment_solves=bool(args.increment)))
+            for pts in groups.values()]
     for pts, c in ctxs:        # warm-up: a few steps of every group
         c.sweep_stream(pts, 3, 1e-30, 3)
     barrier(world)
     torch.cuda.synchronize()
-    per_group, t_all = [], 0.0
+    t0 = 0.0
+
+    def run_group(pc):
+        pts, c = pc
+        tg = time.perf_counter()
+        steps, cur, _ = c.sweep_stream(pts, MAX_STEPS, TOL, CHECK_EVERY)
+        p0 = pts[0]
+        return {"refine": int(round(np.log2(p0.ny))), "degree": p0.degree, "points": len(pts),
+                "seconds": time.perf_counter() - tg, "ends_at_s": time.perf_counter() - t0,
+                "median_steps": float(np.median(steps)), "capped": int(np.sum(steps >= MAX_STEPS))}
+
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
-        for pts, c in ctxs:
-            tg = time.perf_counter()
-            steps, cur, _ = c.sweep_stream(pts, MAX_STEPS, TOL, CHECK_EVERY)
-            p0 = pts[0]
-            per_group.append({"refine": int(round(np.log2(p0.ny))), "degree": p0.degree, "points": len(pts),
-                              "seconds": time.perf_counter() - tg, "median_steps": float(np.median(steps)),
-                              "capped": int(np.sum(steps >= MAX_STEPS))})
+        if args.concurrent:
+            with ThreadPoolExecutor(max_workers=len(ctxs)) as pool:
+                per_group = list(pool.map(run_group, ctxs))
+        else:
+            per_group = [run_group(pc) for pc in ctxs]
         torch.cuda.synchronize()
         t_all = time.perf_counter() - t0
     t_all = max_over_ranks(t_all, world)
     if rank == 0:
+        mixed = args.precision == "mixed"
+        how = ("FP32 factors, increment solves" if mixed and args.increment else
+               "FP32 factors, refined solves" if mixed else args.precision.upper())
         line = {"metric": "I-V points/sec to steady state", "value": n * world / t_all,
                 "unit": "I-V points/s", "n_gpus": world, "steps": 1, "warmup": 1,
                 "ms_per_step": t_all * 1e3, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "vs_baseline": None, "dtype": "f32+f32-pair" if mixed else "f64", "data": "synthetic",
                 "config": {"workload": f"{n} uneven half-cell points per GPU: refinement 5-7, LDG degree 1-2, "
-                                       f"FP64, to rel. change <= {TOL} (<= {MAX_STEPS} steps), one context "
-                                       "per mesh group, groups one after another",
+                                       f"{how}, to rel. change <= {TOL} (<= {MAX_STEPS} steps), one context "
+                                       "per mesh group, " + ("groups at the same time, one host thread and "
+                                                             "stream each" if args.concurrent else
+                                                             "groups one after another"),
                            "groups": per_group, "timing": "host wall clock around the public API calls"},
                 "clocks": clk.summary()}
         print(json.dumps(line))

@@ -1799,8 +1799,12 @@ struct pecs_lu {
 // pecs_lu_factor: fronts with at least this many rows go to the GPU
 static std::atomic<int> g_lu_gpu_min_front{1024};
 
+// Also makes the context's GPU the calling thread's current device: a context
+// may be driven from any host thread (one per context in a concurrent ragged
+// sweep), and a thread's current device starts at 0.
 static void need_device(Engine& e) {
   if (e.host_only) throw PecsError(PECS_E_STATE, "context was created with host_setup_only");
+  PECS_CUDA(cudaSetDevice(e.opt.device));
 }
 
 extern "C" {

@@ -65,13 +65,21 @@ def matrix_key(p) -> tuple:
 
 
 def ragged_sweep(points: Sequence, slots: int = 64, precision: int = None, max_steps: int = 5000,
-                 tol: float = 1e-8, check_every: int = 50, want_fields: bool = False, **ctx_kw):
+                 tol: float = 1e-8, check_every: int = 50, want_fields: bool = False,
+                 concurrent: bool = False, **ctx_kw):
     """I-V points of uneven size (different refinement levels, degrees or other
     matrix-defining parameters) to steady state: the points are grouped by
     their meshes and fixed matrices, and each group is streamed through one
     context of at most ``slots`` slots (pecs_sweep_stream).  Results come back
     in the order of ``points``: (steps, currents, fields or None), fields as
-    one array per point and field."""
+    one array per point and field.
+
+    ``concurrent``: every group's context is created first (one after
+    another: setup uses all host threads), then the groups' sweeps run at the
+    same time, one host thread per group, each on its context's own CUDA
+    stream, so that small meshes fill the SMs a large mesh leaves idle.  The
+    results are those of the groups run one after another: each context's
+    kernels and step sequence are the same either way."""
     import numpy as np
 
     from .api import PREC_FP64, Context
@@ -82,14 +90,40 @@ def ragged_sweep(points: Sequence, slots: int = 64, precision: int = None, max_s
     steps = np.zeros(len(points), dtype=np.int64)
     cur = np.zeros(len(points))
     fields = [None] * len(points) if want_fields else None
-    for idx in groups.values():
-        pts = [points[i] for i in idx]
-        ctx = Context(pts[:min(slots, len(pts))], precision=prec, **ctx_kw)
-        s, c, fin = ctx.sweep_stream(pts, max_steps, tol, check_every, want_fields=want_fields)
+
+    def finish(idx, ctx, res):
+        s, c, fin = res
         for k, i in enumerate(idx):
             steps[i] = s[k]
             cur[i] = c[k]
             if want_fields:
                 fields[i] = {f: fin[f][k * ctx.ndofs[f]:(k + 1) * ctx.ndofs[f]].copy() for f in fin}
-        ctx.close()
+
+    def make(idx):
+        pts = [points[i] for i in idx]
+        return pts, Context(pts[:min(slots, len(pts))], precision=prec, **ctx_kw)
+
+    if not concurrent:
+        for idx in groups.values():
+            pts, ctx = make(idx)
+            try:
+                finish(idx, ctx, ctx.sweep_stream(pts, max_steps, tol, check_every, want_fields=want_fields))
+            finally:
+                ctx.close()
+        return steps, cur, fields
+
+    from concurrent.futures import ThreadPoolExecutor
+    made = []
+    try:
+        for idx in groups.values():
+            made.append((idx,) + make(idx))
+        with ThreadPoolExecutor(max_workers=len(made)) as pool:
+            futs = [pool.submit(ctx.sweep_stream, pts, max_steps, tol, check_every, want_fields=want_fields)
+                    for _, pts, ctx in made]
+            results = [f.result() for f in futs]
+        for (idx, _, ctx), res in zip(made, results):
+            finish(idx, ctx, res)
+    finally:
+        for _, _, ctx in made:
+            ctx.close()
     return steps, cur, fields

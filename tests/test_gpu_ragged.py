@@ -75,3 +75,49 @@ def test_config3_ragged_batch_levels_5_to_7(pecs_lib):
         c = ctx.interface_current()[0]
         assert abs(cur[i] - c) <= 1e-12 * abs(c)
         ctx.close()
+
+
+def _small_ragged_points(seed):
+    rng = np.random.default_rng(seed)
+    pts = []
+    for _ in range(10):
+        pts.append(pg.half_cell(n_refine=int(rng.integers(2, 4)), degree=int(rng.integers(1, 3)),
+                                phi_app=float(rng.uniform(-0.5, 0.5)), G0=float(rng.uniform(0.5, 2.0))))
+    return pts
+
+
+def test_concurrent_ragged_sweep_equals_serial(pecs_lib):
+    """The groups' sweeps at the same time (one host thread and stream per
+    context) end where the groups run one after another end: same steps,
+    currents to 1e-12, fields to 1e-13 (two contexts of a group may time
+    different tilings at creation, nothing else differs)."""
+    pts = _small_ragged_points(5)
+    kw = dict(slots=3, max_steps=400, tol=1e-6, check_every=10, want_fields=True)
+    s0, c0, f0 = ragged_sweep(pts, **kw)
+    s1, c1, f1 = ragged_sweep(pts, concurrent=True, **kw)
+    assert np.array_equal(s0, s1)
+    assert np.all(np.abs(c1 - c0) <= 1e-12 * np.abs(c0))
+    for i in range(len(pts)):
+        for f, v in f0[i].items():
+            assert np.linalg.norm(f1[i][f] - v) <= 1e-13 * np.linalg.norm(v), (i, f)
+
+
+def test_mixed_increment_ragged_sweep_within_1e6_of_fp64(pecs_lib):
+    """Uneven points (refinement 2-3, degrees 1 and 2) to the benchmark's
+    steady-state criterion with FP32 factors and increment solves, groups at
+    the same time, against the FP64 ragged sweep: currents and every field
+    within 1e-6, steps to steady state within 5% + 2."""
+    pts = _small_ragged_points(9)
+    kw = dict(slots=4, max_steps=5000, tol=1e-8, check_every=10, want_fields=True)
+    s64, c64, f64 = ragged_sweep(pts, **kw)
+    smx, cmx, fmx = ragged_sweep(pts, precision=pg.PREC_FP32_MIXED, increment_solves=True,
+                                 concurrent=True, **kw)
+    assert np.all(s64 < 5000)
+    e_cur = np.abs(cmx - c64) / np.abs(c64)
+    print("steps fp64", s64, "mixed", smx, "current errors", e_cur)
+    assert np.all(e_cur < 1e-6)
+    assert np.all(np.abs(smx - s64) <= 0.05 * s64 + 2)
+    for i in range(len(pts)):
+        for f, v in f64[i].items():
+            e = np.linalg.norm(fmx[i][f] - v) / np.linalg.norm(v)
+            assert e < 1e-6, (i, pts[i].ny, pts[i].degree, f, e)

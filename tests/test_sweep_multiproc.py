@@ -153,3 +153,62 @@ def test_gloo_two_ranks_build_library_contexts(pecs_lib):
             np.testing.assert_array_equal(a, b)
     # the instances really differ (each rank computed different data)
     assert not np.array_equal(want[0], want[-1])
+
+
+class _FakeContext:
+    """Stands in for pecs_gb300.api.Context in ragged_sweep: steps, current
+    and a two-entry field per point derived from the point's parameters."""
+    made, closed = [], []
+    fail_degree = None
+
+    def __init__(self, pts, precision=None, **kw):
+        self.ndofs = {0: 2}
+        _FakeContext.made.append(self)
+
+    def sweep_stream(self, pts, max_steps, tol, check_every, want_fields=False):
+        import time
+
+        import numpy as np
+        time.sleep(0.01)
+        if _FakeContext.fail_degree is not None and pts[0].degree == _FakeContext.fail_degree:
+            raise RuntimeError("group failed")
+        steps = np.array([int(round(p.phi_app * 1000)) for p in pts])
+        cur = np.array([p.G0 for p in pts])
+        fin = {0: np.concatenate([[p.G0, p.ny] for p in pts])} if want_fields else None
+        return steps, cur, fin
+
+    def close(self):
+        _FakeContext.closed.append(self)
+
+
+def test_ragged_sweep_concurrent_groups_on_host(pecs_lib, monkeypatch):
+    """Grouping, result order and clean-up of ragged_sweep, serial and
+    concurrent, with a fake context: the same results in point order either
+    way, every context closed, and a group's error raised after all the
+    contexts are closed."""
+    import numpy as np
+
+    import pecs_gb300 as pg
+    import pecs_gb300.api as api
+    from pecs_gb300.sweep import ragged_sweep
+    monkeypatch.setattr(api, "Context", _FakeContext)
+    pts = [pg.half_cell(n_refine=2 + i % 2, degree=1 + (i // 2) % 2, phi_app=0.01 * i, G0=1.0 + i)
+           for i in range(11)]
+    res = {}
+    for conc in (False, True):
+        _FakeContext.made, _FakeContext.closed = [], []
+        res[conc] = ragged_sweep(pts, slots=2, want_fields=True, concurrent=conc)
+        assert len(_FakeContext.made) == 4 and len(_FakeContext.closed) == 4
+    for conc in (False, True):
+        steps, cur, fields = res[conc]
+        assert list(steps) == [10 * i for i in range(11)]
+        assert list(cur) == [1.0 + i for i in range(11)]
+        assert [list(f[0]) for f in fields] == [[1.0 + i, p.ny] for i, p in enumerate(pts)]
+    _FakeContext.made, _FakeContext.closed = [], []
+    _FakeContext.fail_degree = 2
+    try:
+        with pytest.raises(RuntimeError, match="group failed"):
+            ragged_sweep(pts, concurrent=True)
+    finally:
+        _FakeContext.fail_degree = None
+    assert len(_FakeContext.closed) == len(_FakeContext.made) == 4
