@@ -117,7 +117,7 @@ def ragged_sweep(points: Sequence, slots: int = 64, precision: int = None, max_s
     try:
         for idx in groups.values():
             made.append((idx,) + make(idx))
-        with ThreadPoolExecutor(max_workers=len(made)) as pool:
+        with ThreadPoolExecutor(max_workers=max(1, len(made))) as pool:
             futs = [pool.submit(ctx.sweep_stream, pts, max_steps, tol, check_every, want_fields=want_fields)
                     for _, pts, ctx in made]
             results = [f.result() for f in futs]

@@ -204,6 +204,9 @@ def test_ragged_sweep_concurrent_groups_on_host(pecs_lib, monkeypatch):
         assert list(steps) == [10 * i for i in range(11)]
         assert list(cur) == [1.0 + i for i in range(11)]
         assert [list(f[0]) for f in fields] == [[1.0 + i, p.ny] for i, p in enumerate(pts)]
+    for conc in (False, True):
+        steps, cur, fields = ragged_sweep([], want_fields=True, concurrent=conc)
+        assert len(steps) == len(cur) == len(fields) == 0
     _FakeContext.made, _FakeContext.closed = [], []
     _FakeContext.fail_degree = 2
     try:
