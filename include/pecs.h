@@ -20,6 +20,11 @@
  * calling thread.  No call aborts the process.  Host buffers are owned by the
  * caller and copied; device memory is owned by the library.  Contexts are
  * independent; calls on one context must not overlap from several threads.
+ * Any host thread may call into a context: every call that uses the GPU first
+ * makes the context's device (pecs_options.device) the thread's current one,
+ * and each context runs on its own stream, so contexts driven from separate
+ * threads run at the same time (as the reference's four concurrent carrier
+ * solves do, SolarCell.cpp:1763-1781).
  */
 #ifndef PECS_H
 #define PECS_H
